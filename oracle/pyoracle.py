@@ -1,0 +1,214 @@
+"""ctypes binding of the CPU oracle (oracle/oracle.cpp).  TEST INFRASTRUCTURE ONLY.
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
+import this module; the engine itself never does.  ``build()`` compiles the oracle
+with the host compiler into ``oracle/_build/liboracle.so``.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+SOURCES = [
+    os.path.join(HERE, "oracle.cpp"),
+    os.path.join(ROOT, "cantera_gb300", "csrc", "mechanism.cpp"),
+    os.path.join(ROOT, "cantera_gb300", "csrc", "yaml_lite.cpp"),
+]
+NSTAT = 9
+STAT_NAMES = ["steps", "rhs_evals", "newton_iters", "lin_setups", "jac_evals",
+              "err_test_fails", "conv_fails", "last_order", "status"]
+
+
+def build(force=False):
+    """Compile the oracle (-ffp-contract=off so x86 and Arm agree bit for bit)."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    newest = max(os.path.getmtime(s) for s in SOURCES + [os.path.join(HERE, "oracle.h")])
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+           "-o", LIB] + SOURCES + ["-lpthread"]
+    subprocess.check_call(cmd)
+    return LIB
+
+
+class BdfOpts(ctypes.Structure):
+    _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double),
+                ("max_steps", ctypes.c_int32), ("max_order", ctypes.c_int32),
+                ("analytic_jacobian", ctypes.c_int32), ("lu_fp32", ctypes.c_int32),
+                ("max_time_step", ctypes.c_double), ("jac_reuse", ctypes.c_int32)]
+
+
+def opts(rtol=1e-9, atol=1e-15, max_steps=20000, max_order=5, analytic=False,
+         lu_fp32=False, max_time_step=0.0, jac_reuse=None):
+    """Integrator options.  Defaults follow the reference ReactorNet (rtol 1e-9, atol 1e-15,
+    20000 steps per advance, order 5, difference-quotient Jacobian kept between setups)."""
+    if jac_reuse is None:
+        jac_reuse = not analytic
+    return BdfOpts(rtol, atol, max_steps, max_order, int(analytic), int(lu_fp32), max_time_step,
+                   int(jac_reuse))
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        D = ctypes.POINTER(ctypes.c_double)
+        I32 = ctypes.c_int32
+        L.or_mech_load.restype = I32
+        L.or_mech_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        L.or_last_error.restype = ctypes.c_char_p
+        L.or_rates_batch.argtypes = [I32, I32, D, D, D, D, I32, ctypes.POINTER(I32),
+                                     ctypes.POINTER(I32), D, I32]
+        L.or_advance_batch.argtypes = [I32, I32, D, D, D, ctypes.c_double,
+                                       ctypes.POINTER(BdfOpts), D, D,
+                                       ctypes.POINTER(ctypes.c_int64), D, I32]
+        L.or_advance_trajectory.argtypes = [I32, ctypes.c_double, ctypes.c_double, D, I32, D,
+                                            ctypes.POINTER(BdfOpts), D,
+                                            ctypes.POINTER(ctypes.c_int64)]
+        L.or_ignition_by_steps.argtypes = [I32, ctypes.c_double, ctypes.c_double, D,
+                                           ctypes.c_double, ctypes.POINTER(BdfOpts), D,
+                                           ctypes.POINTER(ctypes.c_int64)]
+        L.or_thermo.argtypes = [I32, ctypes.c_double, D, D, D]
+        L.or_rates.argtypes = [I32, ctypes.c_double, ctypes.c_double, D, D, D, D, D, D, D]
+        L.or_ddci.argtypes = [I32, ctypes.c_double, ctypes.c_double, D, I32, D]
+        L.or_reactor_rhs.argtypes = [I32, ctypes.c_double, D, D]
+        L.or_equivalence_ratio.argtypes = [I32, ctypes.c_double, D, D, D]
+        L.or_mole_to_mass.argtypes = [I32, D, D]
+        L.or_molecular_weights.argtypes = [I32, D]
+        L.or_species_index.argtypes = [I32, ctypes.c_char_p]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _c(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Mech:
+    """A mechanism loaded into the oracle."""
+
+    def __init__(self, path, phase=""):
+        L = lib()
+        self.h = L.or_mech_load(path.encode(), phase.encode())
+        if self.h < 0:
+            raise RuntimeError(L.or_last_error().decode())
+        K = ctypes.c_int32()
+        R = ctypes.c_int32()
+        L.or_mech_sizes(self.h, ctypes.byref(K), ctypes.byref(R))
+        self.K, self.R = K.value, R.value
+        self.mw = np.zeros(self.K)
+        L.or_molecular_weights(self.h, _p(self.mw))
+
+    def species_index(self, name):
+        return lib().or_species_index(self.h, name.encode())
+
+    def composition(self, spec):
+        """'H2:2, O2:1' -> normalised array over species (mole basis)."""
+        x = np.zeros(self.K)
+        for item in spec.split(","):
+            n, v = item.split(":")
+            k = self.species_index(n.strip())
+            if k < 0:
+                raise KeyError(n)
+            x[k] += float(v)
+        return x / x.sum()
+
+    def mole_to_mass(self, X):
+        Y = np.zeros(self.K)
+        lib().or_mole_to_mass(self.h, _p(_c(X)), _p(Y))
+        return Y
+
+    def equivalence_ratio(self, phi, fuel, oxidizer):
+        Y = np.zeros(self.K)
+        lib().or_equivalence_ratio(self.h, phi, _p(_c(self.composition(fuel))),
+                                   _p(_c(self.composition(oxidizer))), _p(Y))
+        return Y
+
+    def thermo(self, T):
+        cp, h, s = np.zeros(self.K), np.zeros(self.K), np.zeros(self.K)
+        lib().or_thermo(self.h, T, _p(cp), _p(h), _p(s))
+        return cp, h, s
+
+    def rates(self, T, P, Y):
+        out = {k: np.zeros(self.R) for k in ("kf", "rkc", "ropf", "ropr", "ropnet")}
+        wdot = np.zeros(self.K)
+        lib().or_rates(self.h, T, P, _p(_c(Y)), _p(out["kf"]), _p(out["rkc"]), _p(out["ropf"]),
+                       _p(out["ropr"]), _p(out["ropnet"]), _p(wdot))
+        out["wdot"] = wdot
+        return out
+
+    def ddci(self, T, P, Y, mode=0):
+        J = np.zeros((self.K, self.K))
+        lib().or_ddci(self.h, T, P, _p(_c(Y)), mode, _p(J))
+        return J
+
+    def rates_batch(self, T, P, Y_sm, mode=1, pattern=None, threads=None):
+        """Species-major batch: Y_sm [K][n].  Returns wdot [K][n] (and jac [nnz][n])."""
+        n = len(T)
+        threads = threads or os.cpu_count()
+        wdot = np.zeros((self.K, n))
+        jac = None
+        cp = ri = None
+        if pattern is not None:
+            colptr, rowidx = pattern
+            cp = np.ascontiguousarray(colptr, dtype=np.int32)
+            ri = np.ascontiguousarray(rowidx, dtype=np.int32)
+            jac = np.zeros((len(ri), n))
+        I = ctypes.POINTER(ctypes.c_int32)
+        lib().or_rates_batch(self.h, n, _p(_c(T)), _p(_c(P)), _p(_c(Y_sm)), _p(wdot), mode,
+                             cp.ctypes.data_as(I) if cp is not None else None,
+                             ri.ctypes.data_as(I) if ri is not None else None,
+                             _p(jac) if jac is not None else None, threads)
+        return wdot, jac
+
+    def reactor_rhs(self, P, y):
+        ydot = np.zeros(self.K + 2)
+        lib().or_reactor_rhs(self.h, P, _p(_c(y)), _p(ydot))
+        return ydot
+
+    def advance_batch(self, T0, P, Y0, t_end, o=None, threads=None):
+        """Reactor-major Y0 [n][K].  Returns T [n], Y [n][K], stats [n][9], tign [n]."""
+        n = len(T0)
+        o = o or opts()
+        threads = threads or os.cpu_count()
+        T = np.zeros(n)
+        Y = np.zeros((n, self.K))
+        st = np.zeros((n, NSTAT), dtype=np.int64)
+        tig = np.zeros(n)
+        lib().or_advance_batch(self.h, n, _p(_c(T0)), _p(_c(P)), _p(_c(Y0)), t_end,
+                               ctypes.byref(o), _p(T), _p(Y),
+                               st.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _p(tig), threads)
+        return T, Y, st, tig
+
+    def trajectory(self, T0, P, Y0, times, o=None):
+        o = o or opts()
+        times = _c(times)
+        out = np.zeros((len(times), self.K + 1))
+        st = np.zeros(NSTAT, dtype=np.int64)
+        rc = lib().or_advance_trajectory(self.h, T0, P, _p(_c(Y0)), len(times), _p(times),
+                                         ctypes.byref(o), _p(out),
+                                         st.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+        return out, st, rc
+
+    def ignition_by_steps(self, T0, P, Y0, dT=500.0, o=None):
+        o = o or opts()
+        t = ctypes.c_double()
+        st = np.zeros(NSTAT, dtype=np.int64)
+        rc = lib().or_ignition_by_steps(self.h, T0, P, _p(_c(Y0)), dT, ctypes.byref(o),
+                                        ctypes.byref(t),
+                                        st.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+        return t.value, st, rc
