@@ -1,0 +1,281 @@
+"""cantera_gb300 - a GB300-native batched engine for Cantera's reactor hot path.
+
+Python mirror of the C ABI in ``include/gbchem.h`` (library ``_build/libgbchem.so``),
+shaped like the Cantera objects it stands in for:
+
+* :class:`Solution` - ``ct.Solution(yaml, phase)`` for an ideal-gas mechanism, with the
+  batched kinetics getters ``net_production_rates`` and ``net_production_rates_ddCi``
+  (Cantera ``Kinetics.net_production_rates`` / ``net_production_rates_ddCi``,
+  interfaces/cython/cantera/kinetics.py:456-461,928-940) over many states at once.
+* :class:`ReactorNet` - ``ct.ReactorNet`` over ``IdealGasConstPressureReactor`` objects
+  (interfaces/cython/cantera/reactor.py:1781-1827), batched: one object advances n
+  independent reactors with ``advance(t)``; ``rtol``/``atol``/``max_steps`` setters and
+  ``solver_stats`` follow ReactorNet's names.
+
+Arrays are species-major (``Y[k, s]``).  numpy arrays are copied to and from the GPU
+inside each call; CUDA torch tensors are passed to the engine as device pointers.
+There is no CPU fallback: without the library or a CUDA device every call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = ["Solution", "ReactorNet", "library", "DATA_DIR", "GBError"]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DATA_DIR = os.path.join(HERE, "data")
+LIB_PATH = os.path.join(HERE, "_build", "libgbchem.so")
+GB_ERR = -999
+GB_DEVICE_POINTERS = 1
+STAT_NAMES = ["steps", "rhs_evals", "newton_iters", "lin_setups", "jac_evals",
+              "err_test_fails", "conv_fails", "last_order"]
+STATUS_NAMES = {0: "ok", 1: "max steps", 2: "error-test failures", 3: "convergence failures",
+                4: "non-finite state", 5: "step size too small"}
+
+
+class GBError(RuntimeError):
+    """An engine call returned GB_ERR; the message is the engine's."""
+
+
+class NetOptions(ctypes.Structure):
+    _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double),
+                ("max_steps", ctypes.c_int32), ("max_order", ctypes.c_int32),
+                ("max_time_step", ctypes.c_double), ("lu_precision", ctypes.c_int32),
+                ("warps_per_block", ctypes.c_int32), ("use_graph", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def library():
+    """Load the engine library (building it first if its sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH) or os.environ.get("GBCHEM_REBUILD"):
+        from . import build as _build
+        _build.build()
+    L = ctypes.CDLL(LIB_PATH)
+    I32, D, P = ctypes.c_int32, ctypes.c_double, ctypes.c_void_p
+    sig = {
+        "gb_mech_load": (I32, [ctypes.c_char_p, ctypes.c_char_p]),
+        "gb_mech_del": (I32, [I32]),
+        "gb_mech_n_species": (I32, [I32]),
+        "gb_mech_n_reactions": (I32, [I32]),
+        "gb_mech_species_name": (I32, [I32, I32, I32, ctypes.c_char_p]),
+        "gb_mech_species_index": (I32, [I32, ctypes.c_char_p]),
+        "gb_mech_molecular_weights": (I32, [I32, I32, P]),
+        "gb_kin_net_production_rates": (I32, [I32, I32, P, P, P, I32, P, I32]),
+        "gb_kin_jac_nnz": (I32, [I32]),
+        "gb_kin_jac_pattern": (I32, [I32, I32, P, I32, P]),
+        "gb_kin_net_production_rates_ddCi": (I32, [I32, I32, P, P, P, I32, P, P, I32]),
+        "gb_net_default_options": (None, [ctypes.POINTER(NetOptions)]),
+        "gb_net_new": (I32, [I32, I32, ctypes.POINTER(NetOptions)]),
+        "gb_net_del": (I32, [I32]),
+        "gb_net_set_state": (I32, [I32, P, P, P, I32]),
+        "gb_net_advance": (I32, [I32, D]),
+        "gb_net_time": (D, [I32]),
+        "gb_net_get_state": (I32, [I32, P, P, I32]),
+        "gb_net_get_status": (I32, [I32, P]),
+        "gb_net_solver_stats": (I32, [I32, P]),
+        "gb_net_ignition_times": (I32, [I32, P]),
+        "gb_get_error": (I32, [I32, ctypes.c_char_p]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc == GB_ERR:
+        buf = ctypes.create_string_buffer(4096)
+        library().gb_get_error(4096, buf)
+        raise GBError(buf.value.decode())
+    return rc
+
+
+def _is_torch_cuda(a):
+    return type(a).__module__.startswith("torch") and getattr(a, "is_cuda", False)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if _is_torch_cuda(a):
+        return ctypes.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _host(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.shape != shape:
+        a = a.reshape(shape)
+    return a
+
+
+class Solution:
+    """An ideal-gas mechanism loaded into the engine (``ct.Solution(yaml, phase)``)."""
+
+    def __init__(self, infile, name=""):
+        path = infile
+        if not os.path.exists(path):
+            cand = os.path.join(DATA_DIR, infile)
+            if os.path.exists(cand):
+                path = cand
+        self._h = _check(library().gb_mech_load(path.encode(), name.encode()))
+        L = library()
+        self.n_species = _check(L.gb_mech_n_species(self._h))
+        self.n_reactions = _check(L.gb_mech_n_reactions(self._h))
+        buf = ctypes.create_string_buffer(256)
+        self.species_names = []
+        for k in range(self.n_species):
+            _check(L.gb_mech_species_name(self._h, k, 256, buf))
+            self.species_names.append(buf.value.decode())
+        self.molecular_weights = np.zeros(self.n_species)
+        _check(L.gb_mech_molecular_weights(self._h, self.n_species, _ptr(self.molecular_weights)))
+        nnz = _check(L.gb_kin_jac_nnz(self._h))
+        self.jac_colptr = np.zeros(self.n_species + 1, dtype=np.int32)
+        self.jac_rowidx = np.zeros(nnz, dtype=np.int32)
+        _check(L.gb_kin_jac_pattern(self._h, self.n_species + 1, _ptr(self.jac_colptr), nnz,
+                                     _ptr(self.jac_rowidx)))
+
+    def species_index(self, name):
+        k = library().gb_mech_species_index(self._h, name.encode())
+        if k < 0:
+            raise KeyError(name)
+        return k
+
+    @property
+    def jac_nnz(self):
+        return len(self.jac_rowidx)
+
+    def _args(self, T, P, Y):
+        if _is_torch_cuda(T):
+            n = T.shape[0]
+            return n, T, P, Y, GB_DEVICE_POINTERS
+        T = _host(T)
+        n = T.shape[0]
+        P = _host(np.broadcast_to(np.asarray(P, dtype=np.float64), (n,)))
+        Y = _host(Y, (self.n_species, n))
+        return n, T, P, Y, 0
+
+    def net_production_rates(self, T, P, Y, out=None):
+        """wdot[K, n] (kmol/m^3/s) for n states; Y is species-major [K, n]."""
+        n, T, P, Y, flags = self._args(T, P, Y)
+        if out is None:
+            if flags:
+                import torch
+                out = torch.empty((self.n_species, n), dtype=torch.float64, device=T.device)
+            else:
+                out = np.empty((self.n_species, n))
+        _check(library().gb_kin_net_production_rates(self._h, n, _ptr(T), _ptr(P), _ptr(Y),
+                                                      self.n_species * n, _ptr(out), flags))
+        return out
+
+    def net_production_rates_ddCi(self, T, P, Y, vals=None, wdot=None):
+        """d(wdot)/d(c) values [nnz, n] on the pattern (jac_colptr, jac_rowidx)."""
+        n, T, P, Y, flags = self._args(T, P, Y)
+        if vals is None:
+            if flags:
+                import torch
+                vals = torch.empty((self.jac_nnz, n), dtype=torch.float64, device=T.device)
+            else:
+                vals = np.empty((self.jac_nnz, n))
+        _check(library().gb_kin_net_production_rates_ddCi(self._h, n, _ptr(T), _ptr(P), _ptr(Y),
+                                                           self.jac_nnz, _ptr(vals), _ptr(wdot), flags))
+        return vals
+
+    def dense_ddCi(self, vals, s):
+        """Dense K x K d(wdot)/dc of state s from pattern values."""
+        J = np.zeros((self.n_species, self.n_species))
+        v = vals[:, s] if not _is_torch_cuda(vals) else vals[:, s].cpu().numpy()
+        for c in range(self.n_species):
+            for p in range(self.jac_colptr[c], self.jac_colptr[c + 1]):
+                J[self.jac_rowidx[p], c] = v[p]
+        return J
+
+    def __del__(self):
+        try:
+            if _lib is not None:
+                _lib.gb_mech_del(self._h)
+        except Exception:
+            pass
+
+
+class ReactorNet:
+    """n independent constant-pressure ideal-gas reactors advanced together."""
+
+    def __init__(self, solution, T, P, Y, rtol=1e-9, atol=1e-15, max_steps=20000, max_order=5,
+                 max_time_step=0.0, lu_precision=64, warps_per_block=0, use_graph=False):
+        L = library()
+        self.solution = solution
+        o = NetOptions()
+        L.gb_net_default_options(ctypes.byref(o))
+        o.rtol, o.atol, o.max_steps, o.max_order = rtol, atol, max_steps, max_order
+        o.max_time_step, o.lu_precision = max_time_step, lu_precision
+        o.warps_per_block, o.use_graph = warps_per_block, int(use_graph)
+        n = T.shape[0] if _is_torch_cuda(T) else np.asarray(T).shape[0]
+        self.n = n
+        self._h = _check(L.gb_net_new(solution._h, n, ctypes.byref(o)))
+        self.set_state(T, P, Y)
+
+    def set_state(self, T, P, Y):
+        n, T, P, Y, flags = self.solution._args(T, P, Y)
+        if n != self.n:
+            raise ValueError("expected %d reactors" % self.n)
+        _check(library().gb_net_set_state(self._h, _ptr(T), _ptr(P), _ptr(Y), flags))
+
+    def advance(self, t):
+        """Advance every reactor to time t; returns the number of failed reactors."""
+        return _check(library().gb_net_advance(self._h, float(t)))
+
+    @property
+    def time(self):
+        return library().gb_net_time(self._h)
+
+    def get_state(self, T=None, Y=None):
+        """Temperatures [n] and mass fractions [K, n] at the current time."""
+        flags = GB_DEVICE_POINTERS if _is_torch_cuda(T) else 0
+        if T is None:
+            T = np.empty(self.n)
+            Y = np.empty((self.solution.n_species, self.n))
+        _check(library().gb_net_get_state(self._h, _ptr(T), _ptr(Y), flags))
+        return T, Y
+
+    @property
+    def T(self):
+        return self.get_state()[0]
+
+    @property
+    def Y(self):
+        return self.get_state()[1]
+
+    @property
+    def status(self):
+        s = np.empty(self.n, dtype=np.int32)
+        _check(library().gb_net_get_status(self._h, _ptr(s)))
+        return s
+
+    @property
+    def solver_stats(self):
+        """Per-reactor counters as a dict of arrays (CVodesIntegrator::solverStats names)."""
+        st = np.empty((self.n, 8), dtype=np.int64)
+        _check(library().gb_net_solver_stats(self._h, _ptr(st)))
+        return {k: st[:, i] for i, k in enumerate(STAT_NAMES)}
+
+    @property
+    def ignition_times(self):
+        t = np.empty(self.n)
+        _check(library().gb_net_ignition_times(self._h, _ptr(t)))
+        return t
+
+    def __del__(self):
+        try:
+            if _lib is not None:
+                _lib.gb_net_del(self._h)
+        except Exception:
+            pass

@@ -1,0 +1,634 @@
+// capi.cu - host side of the engine and its C ABI (include/gbchem.h).
+//
+// Handles index process-wide tables, as Cantera's CLib Cabinet does
+// (interfaces/clib/src/Cabinet.h); every entry point catches exceptions and turns
+// them into GB_ERR plus a thread-local message (interfaces/clib/src/clib_utils.h:32-52).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gbchem.h"
+#include "devmech.h"
+#include "kernels.h"
+#include "mechanism.h"
+
+using namespace gbchem;
+
+namespace {
+
+thread_local std::string g_error;
+
+struct CudaError : std::runtime_error {
+    explicit CudaError(const std::string& m) : std::runtime_error(m) {}
+};
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Device buffer with RAII.
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { if (p) cudaFree(p); }
+    void ensure(size_t b) {
+        if (b <= bytes) return;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        ck(cudaMalloc(&p, std::max<size_t>(b, 256)), "cudaMalloc");
+        bytes = b;
+    }
+    template <class T> T* as() const { return (T*)p; }
+};
+
+// Arena builder for the packed mechanism: appends arrays with 32-byte alignment.
+struct Arena {
+    std::vector<char> data;
+    template <class T> size_t add(const std::vector<T>& v) {
+        size_t off = (data.size() + 31) & ~size_t(31);
+        data.resize(off + v.size() * sizeof(T) + 32);
+        if (!v.empty()) std::memcpy(data.data() + off, v.data(), v.size() * sizeof(T));
+        return off;
+    }
+};
+
+struct MechEntry {
+    Mechanism m;
+    DBuf arena;
+    DevMech dm{};
+    std::vector<int32_t> jcPtr, jrIdx;
+    cudaStream_t stream = nullptr;
+    int smCount = 0;
+    // kinetics workspace
+    DBuf dT, dP, dY, dW, dJ, dCounter;
+    ~MechEntry() { if (stream) cudaStreamDestroy(stream); }
+};
+
+struct NetEntry {
+    int mech;
+    int n;
+    gb_net_options opts;
+    double time = 0.0;
+    int warpsPerBlock = 0, blocks = 0, ld = 0, warpDoubles = 0, recStride = 0;
+    DBuf dP, dT, dY, dRec, dStats, dStatus, dTign, dCounter, dOrder;
+    bool haveOrder = false;
+    cudaGraphExec_t graph = nullptr;
+    double graphTout = -1.0;
+    ~NetEntry() { if (graph) cudaGraphExecDestroy(graph); }
+};
+
+std::mutex g_mu;
+std::vector<std::unique_ptr<MechEntry>> g_mechs;
+std::vector<std::unique_ptr<NetEntry>> g_nets;
+
+MechEntry& mech(int32_t h) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (h < 0 || h >= (int32_t)g_mechs.size() || !g_mechs[h]) throw std::runtime_error("invalid mechanism handle " + std::to_string(h));
+    return *g_mechs[h];
+}
+NetEntry& net(int32_t h) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (h < 0 || h >= (int32_t)g_nets.size() || !g_nets[h]) throw std::runtime_error("invalid reactor network handle " + std::to_string(h));
+    return *g_nets[h];
+}
+
+template <class F> int32_t guarded(F&& f) {
+    try {
+        return f();
+    } catch (std::exception& e) {
+        g_error = e.what();
+        return GB_ERR;
+    } catch (...) {
+        g_error = "unknown error";
+        return GB_ERR;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Mechanism -> device layout
+// ---------------------------------------------------------------------------
+void packDevMech(MechEntry& e) {
+    const Mechanism& m = e.m;
+    const int K = m.K, R = m.R;
+    if (K > kMaxSpecies) throw std::runtime_error("mechanism has more species than the GPU path supports");
+    std::vector<double> rmw(K), nasa((size_t)K * kNasaStride, 0.0);
+    for (int k = 0; k < K; k++) {
+        rmw[k] = 1.0 / m.mw[k];
+        nasa[(size_t)k * kNasaStride] = m.nasaTmid[k];
+        for (int j = 0; j < 7; j++) {
+            nasa[(size_t)k * kNasaStride + 1 + j] = m.nasaLow[7 * k + j];
+            nasa[(size_t)k * kNasaStride + 8 + j] = m.nasaHigh[7 * k + j];
+        }
+    }
+    std::vector<int4> rinfo(R), rk(R), pk(R);
+    std::vector<D4> rarr(R);
+    std::vector<int> sidePtr(1, 0), sideK;
+    std::vector<double> sideNu, sideOrd;
+    std::vector<D4> fo1, fo2;
+    std::vector<int> rsPtr(1, 0), rsK;
+    std::vector<double> rsNu;
+    std::vector<std::map<int, double>> net(R);
+    for (int i = 0; i < R; i++) {
+        int flags = m.kind[i] & kKindMask;
+        if (m.reversible[i]) flags |= kRevBit;
+        flags |= (m.reacBucket[i] & 7) << kRBucketShift;
+        flags |= (m.prodBucket[i] & 7) << kPBucketShift;
+        int fo = -1;
+        if (m.kind[i] == kLindemann || m.kind[i] == kTroe) {
+            fo = (int)fo1.size();
+            fo1.push_back(D4{m.A0[i], m.b0[i], m.Ea0R[i], m.troe[4 * i]});
+            fo2.push_back(D4{m.troe[4 * i + 1], m.troe[4 * i + 2], m.troe[4 * i + 3], m.kind[i] == kTroe ? 1.0 : 0.0});
+        }
+        rinfo[i] = int4{flags, m.tbOfRxn[i], fo, 0};
+        rarr[i] = D4{m.A[i], m.b[i], m.EaR[i], m.dn[i]};
+        auto expand = [&](const int32_t* ks, const double* nus, int n) {
+            int4 e4{-1, -1, -1, 0};
+            int cnt = 0;
+            int* slot[3] = {&e4.x, &e4.y, &e4.z};
+            for (int j = 0; j < n; j++)
+                for (int r = 0; r < (int)nus[j] && cnt < 3; r++) *slot[cnt++] = ks[j];
+            e4.w = cnt;
+            return e4;
+        };
+        rk[i] = expand(&m.reacK[m.reacPtr[i]], &m.reacNu[m.reacPtr[i]], m.reacPtr[i + 1] - m.reacPtr[i]);
+        pk[i] = expand(&m.prodK[m.prodPtr[i]], &m.prodNu[m.prodPtr[i]], m.prodPtr[i + 1] - m.prodPtr[i]);
+        for (int j = m.reacPtr[i]; j < m.reacPtr[i + 1]; j++) {
+            sideK.push_back(m.reacK[j]); sideNu.push_back(m.reacNu[j]); sideOrd.push_back(m.reacOrder[j]);
+            net[i][m.reacK[j]] -= m.reacNu[j];
+        }
+        sidePtr.push_back((int)sideK.size());
+        for (int j = m.prodPtr[i]; j < m.prodPtr[i + 1]; j++) {
+            sideK.push_back(m.prodK[j]); sideNu.push_back(m.prodNu[j]); sideOrd.push_back(m.prodNu[j]);
+            net[i][m.prodK[j]] += m.prodNu[j];
+        }
+        sidePtr.push_back((int)sideK.size());
+        for (auto& kv : net[i])
+            if (kv.second != 0.0) { rsK.push_back(kv.first); rsNu.push_back(kv.second); }
+        rsPtr.push_back((int)rsK.size());
+    }
+    // species gather lists (net coefficients)
+    std::vector<std::vector<std::pair<int, double>>> bySpecies(K);
+    for (int i = 0; i < R; i++)
+        for (int q = rsPtr[i]; q < rsPtr[i + 1]; q++) bySpecies[rsK[q]].push_back({i, rsNu[q]});
+    std::vector<int> spPtr(1, 0), spRxn;
+    std::vector<double> spNu;
+    for (int k = 0; k < K; k++) {
+        for (auto& pr : bySpecies[k]) { spRxn.push_back(pr.first); spNu.push_back(pr.second); }
+        spPtr.push_back((int)spRxn.size());
+    }
+    // third bodies
+    std::vector<int> tbRxn(m.tbRxn.begin(), m.tbRxn.end()), tbMA(m.tbMassAction.begin(), m.tbMassAction.end());
+    std::vector<int> tbPtr(m.tbPtr.begin(), m.tbPtr.end()), tbK(m.tbSpecies.begin(), m.tbSpecies.end());
+    std::vector<double> tbDef(m.tbDefault), tbE(m.tbEffMinusDefault);
+    // Jacobian columns: dependencies of each reaction through mass action and the
+    // non-default part of its third-body efficiencies
+    std::vector<std::vector<std::pair<int, double>>> cols(K);
+    for (int i = 0; i < R; i++) {
+        std::map<int, double> deps;
+        for (int j = m.reacPtr[i]; j < m.reacPtr[i + 1]; j++) deps[m.reacK[j]] += 0.0;
+        if (m.reversible[i])
+            for (int j = m.prodPtr[i]; j < m.prodPtr[i + 1]; j++) deps[m.prodK[j]] += 0.0;
+        int t = m.tbOfRxn[i];
+        if (t >= 0)
+            for (int q = m.tbPtr[t]; q < m.tbPtr[t + 1]; q++)
+                if (m.tbEffMinusDefault[q] != 0.0) deps[m.tbSpecies[q]] = m.tbEffMinusDefault[q];
+        for (auto& kv : deps) cols[kv.first].push_back({i, kv.second});
+    }
+    std::vector<int> colPtr(1, 0), colRxn;
+    std::vector<double> colE;
+    std::vector<long> work(K, 0);
+    for (int j = 0; j < K; j++) {
+        for (auto& pr : cols[j]) {
+            colRxn.push_back(pr.first);
+            colE.push_back(pr.second);
+            work[j] += 1 + (rsPtr[pr.first + 1] - rsPtr[pr.first]);
+        }
+        colPtr.push_back((int)colRxn.size());
+    }
+    // balance columns over 32 lanes: heaviest first onto the least-loaded lane
+    std::vector<int> order(K);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+    std::vector<std::vector<int>> laneList(32);
+    std::vector<long> load(32, 0);
+    for (int j : order) {
+        int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        laneList[l].push_back(j);
+        load[l] += work[j];
+    }
+    std::vector<int> laneColPtr(1, 0), laneCols;
+    for (int l = 0; l < 32; l++) {
+        for (int j : laneList[l]) laneCols.push_back(j);
+        laneColPtr.push_back((int)laneCols.size());
+    }
+    // dense default-efficiency part
+    std::vector<int> gsPtr(1, 0), gsTb;
+    std::vector<double> gsCoef;
+    {
+        std::vector<std::vector<std::pair<int, double>>> gl(K);
+        for (int t = 0; t < m.nThirdBody(); t++) {
+            if (m.tbDefault[t] == 0.0) continue;
+            int i = m.tbRxn[t];
+            for (int q = rsPtr[i]; q < rsPtr[i + 1]; q++) gl[rsK[q]].push_back({t, rsNu[q] * m.tbDefault[t]});
+        }
+        for (int k = 0; k < K; k++) {
+            for (auto& pr : gl[k]) { gsTb.push_back(pr.first); gsCoef.push_back(pr.second); }
+            gsPtr.push_back((int)gsTb.size());
+        }
+    }
+    // output pattern
+    jacobianPattern(m, e.jcPtr, e.jrIdx);
+    std::vector<int> jpCol(e.jrIdx.size());
+    for (int c = 0; c < K; c++)
+        for (int q = e.jcPtr[c]; q < e.jcPtr[c + 1]; q++) jpCol[q] = c;
+    std::vector<int> jcPtr(e.jcPtr.begin(), e.jcPtr.end()), jrIdx(e.jrIdx.begin(), e.jrIdx.end());
+
+    Arena a;
+    size_t o_mw = a.add(m.mw), o_rmw = a.add(rmw), o_nasa = a.add(nasa);
+    size_t o_rinfo = a.add(rinfo), o_rarr = a.add(rarr), o_rk = a.add(rk), o_pk = a.add(pk);
+    size_t o_sidePtr = a.add(sidePtr), o_sideK = a.add(sideK), o_sideNu = a.add(sideNu), o_sideOrd = a.add(sideOrd);
+    size_t o_rsPtr = a.add(rsPtr), o_rsK = a.add(rsK), o_rsNu = a.add(rsNu);
+    size_t o_fo1 = a.add(fo1), o_fo2 = a.add(fo2);
+    size_t o_tbRxn = a.add(tbRxn), o_tbDef = a.add(tbDef), o_tbMA = a.add(tbMA), o_tbPtr = a.add(tbPtr),
+           o_tbK = a.add(tbK), o_tbE = a.add(tbE);
+    size_t o_spPtr = a.add(spPtr), o_spRxn = a.add(spRxn), o_spNu = a.add(spNu);
+    size_t o_colPtr = a.add(colPtr), o_colRxn = a.add(colRxn), o_colE = a.add(colE);
+    size_t o_lcp = a.add(laneColPtr), o_lc = a.add(laneCols);
+    size_t o_gsPtr = a.add(gsPtr), o_gsTb = a.add(gsTb), o_gsCoef = a.add(gsCoef);
+    size_t o_jcPtr = a.add(jcPtr), o_jrIdx = a.add(jrIdx), o_jpCol = a.add(jpCol);
+    e.arena.ensure(a.data.size());
+    ck(cudaMemcpy(e.arena.p, a.data.data(), a.data.size(), cudaMemcpyHostToDevice), "upload mechanism");
+    char* b = e.arena.as<char>();
+    DevMech& d = e.dm;
+    d.K = K; d.R = R; d.N = K + 1; d.NF = (int)fo1.size(); d.NTB = m.nThirdBody(); d.nnz = (int)jrIdx.size();
+    d.Pref = m.Pref; d.Rgas = gasConstant();
+    d.mw = (const double*)(b + o_mw); d.rmw = (const double*)(b + o_rmw); d.nasa = (const double*)(b + o_nasa);
+    d.rinfo = (const int4*)(b + o_rinfo); d.rarr = (const D4*)(b + o_rarr);
+    d.rk = (const int4*)(b + o_rk); d.pk = (const int4*)(b + o_pk);
+    d.sidePtr = (const int*)(b + o_sidePtr); d.sideK = (const int*)(b + o_sideK);
+    d.sideNu = (const double*)(b + o_sideNu); d.sideOrd = (const double*)(b + o_sideOrd);
+    d.rsPtr = (const int*)(b + o_rsPtr); d.rsK = (const int*)(b + o_rsK); d.rsNu = (const double*)(b + o_rsNu);
+    d.fo1 = (const D4*)(b + o_fo1); d.fo2 = (const D4*)(b + o_fo2);
+    d.tbRxn = (const int*)(b + o_tbRxn); d.tbDef = (const double*)(b + o_tbDef); d.tbMA = (const int*)(b + o_tbMA);
+    d.tbPtr = (const int*)(b + o_tbPtr); d.tbK = (const int*)(b + o_tbK); d.tbE = (const double*)(b + o_tbE);
+    d.spPtr = (const int*)(b + o_spPtr); d.spRxn = (const int*)(b + o_spRxn); d.spNu = (const double*)(b + o_spNu);
+    d.colPtr = (const int*)(b + o_colPtr); d.colRxn = (const int*)(b + o_colRxn); d.colE = (const double*)(b + o_colE);
+    d.laneColPtr = (const int*)(b + o_lcp); d.laneCols = (const int*)(b + o_lc);
+    d.gsPtr = (const int*)(b + o_gsPtr); d.gsTb = (const int*)(b + o_gsTb); d.gsCoef = (const double*)(b + o_gsCoef);
+    d.jcPtr = (const int*)(b + o_jcPtr); d.jrIdx = (const int*)(b + o_jrIdx); d.jpCol = (const int*)(b + o_jpCol);
+}
+
+int maxSmemPerBlock() {
+    int dev = 0, v = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    ck(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device attribute");
+    return v;
+}
+
+// Copy n*count doubles to a device buffer unless they are already on the device.
+const double* stage(const double* src, size_t count, DBuf& buf, bool device, cudaStream_t s) {
+    if (device) return src;
+    buf.ensure(count * sizeof(double));
+    ck(cudaMemcpyAsync(buf.p, src, count * sizeof(double), cudaMemcpyHostToDevice, s), "copy to device");
+    return buf.as<double>();
+}
+
+int32_t runRates(int32_t h, int32_t n, const double* T, const double* P, const double* Y, double* wdot,
+                 double* vals, int32_t flags) {
+    MechEntry& e = mech(h);
+    if (n < 0) throw std::runtime_error("negative number of states");
+    if (n == 0) return 0;
+    const bool dev = (flags & GB_DEVICE_POINTERS) != 0;
+    const int K = e.m.K;
+    cudaStream_t s = e.stream;
+    const double* dT = stage(T, n, e.dT, dev, s);
+    const double* dP = stage(P, n, e.dP, dev, s);
+    const double* dY = stage(Y, (size_t)K * n, e.dY, dev, s);
+    double* dW = nullptr;
+    double* dJ = nullptr;
+    if (wdot) {
+        if (dev) dW = wdot;
+        else { e.dW.ensure((size_t)K * n * 8); dW = e.dW.as<double>(); }
+    }
+    if (vals) {
+        if (dev) dJ = vals;
+        else { e.dJ.ensure((size_t)e.dm.nnz * n * 8); dJ = e.dJ.as<double>(); }
+    }
+    e.dCounter.ensure(sizeof(int));
+    ck(cudaMemsetAsync(e.dCounter.p, 0, sizeof(int), s), "memset");
+    RatesParams p{};
+    p.m = e.dm; p.n = n; p.T = dT; p.P = dP; p.Y = dY; p.wdot = dW; p.jac = dJ;
+    p.counter = e.dCounter.as<int>();
+    p.warpDoubles = ratesWarpDoubles(e.dm);
+    int wpb = std::max(1, std::min(8, maxSmemPerBlock() / (p.warpDoubles * 8)));
+    int blocksPerSm = std::max(1, (228 * 1024) / (p.warpDoubles * 8 * wpb));
+    int blocks = std::min(e.smCount * blocksPerSm, (n + wpb - 1) / wpb);
+    ck(launchRates(p, blocks, wpb, s), "rates kernel launch");
+    if (wdot && !dev) ck(cudaMemcpyAsync(wdot, dW, (size_t)K * n * 8, cudaMemcpyDeviceToHost, s), "copy wdot");
+    if (vals && !dev) ck(cudaMemcpyAsync(vals, dJ, (size_t)e.dm.nnz * n * 8, cudaMemcpyDeviceToHost, s), "copy jac");
+    ck(cudaStreamSynchronize(s), "rates kernel");
+    return 0;
+}
+
+void netLaunch(NetEntry& ne, MechEntry& me, double t0, double tout) {
+    BdfParams p{};
+    p.m = me.dm; p.n = ne.n; p.t0 = t0; p.tout = tout;
+    p.rtol = ne.opts.rtol; p.atol = ne.opts.atol;
+    p.hmaxInv = ne.opts.max_time_step > 0 ? 1.0 / ne.opts.max_time_step : 0.0;
+    p.maxSteps = ne.opts.max_steps; p.maxOrder = ne.opts.max_order;
+    p.P = ne.dP.as<double>(); p.T = ne.dT.as<double>(); p.Y = ne.dY.as<double>();
+    p.rec = ne.dRec.as<double>(); p.recStride = ne.recStride;
+    p.stats = ne.dStats.as<long long>(); p.status = ne.dStatus.as<int>(); p.tign = ne.dTign.as<double>();
+    p.counter = ne.dCounter.as<int>(); p.order = ne.haveOrder ? ne.dOrder.as<int>() : nullptr;
+    p.ld = ne.ld; p.warpDoubles = ne.warpDoubles;
+    ck(cudaMemsetAsync(ne.dCounter.p, 0, sizeof(int), me.stream), "memset");
+    ck(launchBdf(p, ne.blocks, ne.warpsPerBlock, ne.opts.lu_precision == 32, me.stream), "integrator launch");
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t gb_get_error(int32_t buflen, char* buf) {
+    if (buf && buflen > 0) {
+        std::strncpy(buf, g_error.c_str(), (size_t)buflen - 1);
+        buf[buflen - 1] = '\0';
+    }
+    return (int32_t)g_error.size();
+}
+
+int32_t gb_mech_load(const char* path, const char* phase) {
+    return guarded([&]() -> int32_t {
+        if (!path) throw std::runtime_error("null path");
+        auto e = std::make_unique<MechEntry>();
+        e->m = loadMechanism(path, phase ? phase : "");
+        int dev = 0;
+        ck(cudaGetDevice(&dev), "cudaGetDevice");
+        ck(cudaDeviceGetAttribute(&e->smCount, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+        ck(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
+        packDevMech(*e);
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_mechs.push_back(std::move(e));
+        return (int32_t)g_mechs.size() - 1;
+    });
+}
+
+int32_t gb_mech_del(int32_t h) {
+    return guarded([&]() -> int32_t {
+        mech(h);
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_mechs[h].reset();
+        return 0;
+    });
+}
+
+int32_t gb_mech_n_species(int32_t h) { return guarded([&]() -> int32_t { return mech(h).m.K; }); }
+int32_t gb_mech_n_reactions(int32_t h) { return guarded([&]() -> int32_t { return mech(h).m.R; }); }
+
+int32_t gb_mech_species_name(int32_t h, int32_t k, int32_t buflen, char* buf) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        if (k < 0 || k >= e.m.K) throw std::runtime_error("species index out of range");
+        const std::string& s = e.m.speciesNames[k];
+        if (buf && buflen > 0) {
+            std::strncpy(buf, s.c_str(), (size_t)buflen - 1);
+            buf[buflen - 1] = '\0';
+        }
+        return (int32_t)s.size();
+    });
+}
+
+int32_t gb_mech_species_index(int32_t h, const char* name) {
+    return guarded([&]() -> int32_t { return mech(h).m.speciesIndex(name ? name : ""); });
+}
+
+int32_t gb_mech_molecular_weights(int32_t h, int32_t buflen, double* mw) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        if (buflen < e.m.K) throw std::runtime_error("buffer too small for molecular weights");
+        std::copy(e.m.mw.begin(), e.m.mw.end(), mw);
+        return 0;
+    });
+}
+
+int32_t gb_kin_net_production_rates(int32_t h, int32_t n, const double* T, const double* P, const double* Y,
+                                    int32_t bufLen, double* wdot, int32_t flags) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        if ((int64_t)bufLen < (int64_t)e.m.K * n) throw std::runtime_error("wdot buffer too small: need K*n");
+        if (!T || !P || !Y || !wdot) throw std::runtime_error("null array argument");
+        return runRates(h, n, T, P, Y, wdot, nullptr, flags);
+    });
+}
+
+int32_t gb_kin_jac_nnz(int32_t h) {
+    return guarded([&]() -> int32_t { return (int32_t)mech(h).jrIdx.size(); });
+}
+
+int32_t gb_kin_jac_pattern(int32_t h, int32_t ncolptr, int32_t* colptr, int32_t nnz, int32_t* rowidx) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        if (ncolptr < (int32_t)e.jcPtr.size() || nnz < (int32_t)e.jrIdx.size())
+            throw std::runtime_error("pattern buffers too small");
+        std::copy(e.jcPtr.begin(), e.jcPtr.end(), colptr);
+        std::copy(e.jrIdx.begin(), e.jrIdx.end(), rowidx);
+        return 0;
+    });
+}
+
+int32_t gb_kin_net_production_rates_ddCi(int32_t h, int32_t n, const double* T, const double* P, const double* Y,
+                                         int32_t nnz, double* vals, double* wdot, int32_t flags) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        if (nnz < (int32_t)e.jrIdx.size()) throw std::runtime_error("nnz smaller than the Jacobian pattern");
+        if (!T || !P || !Y || !vals) throw std::runtime_error("null array argument");
+        return runRates(h, n, T, P, Y, wdot, vals, flags);
+    });
+}
+
+void gb_net_default_options(gb_net_options* o) {
+    if (!o) return;
+    o->rtol = 1e-9;
+    o->atol = 1e-15;
+    o->max_steps = 20000;
+    o->max_order = 5;
+    o->max_time_step = 0.0;
+    o->lu_precision = 64;
+    o->warps_per_block = 0;
+    o->use_graph = 0;
+}
+
+int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
+    return guarded([&]() -> int32_t {
+        MechEntry& me = mech(h);
+        if (n <= 0) throw std::runtime_error("a reactor network needs n > 0 reactors");
+        auto ne = std::make_unique<NetEntry>();
+        ne->mech = h;
+        ne->n = n;
+        if (opts) ne->opts = *opts;
+        else gb_net_default_options(&ne->opts);
+        if (ne->opts.lu_precision != 32 && ne->opts.lu_precision != 64)
+            throw std::runtime_error("lu_precision must be 32 or 64");
+        if (ne->opts.max_order < 1 || ne->opts.max_order > 5) throw std::runtime_error("max_order must be 1..5");
+        if (!(ne->opts.rtol > 0) || !(ne->opts.atol > 0)) throw std::runtime_error("tolerances must be positive");
+        const int N = me.dm.N;
+        const bool fp32 = ne->opts.lu_precision == 32;
+        ne->ld = fp32 ? (N % 2 == 0 ? N + 1 : N) : (N % 2 == 0 ? N + 1 : N);
+        ne->warpDoubles = bdfWarpDoubles(me.dm, ne->ld, fp32);
+        ne->recStride = bdfRecordStride(N);
+        const int smemMax = maxSmemPerBlock();
+        int fit = smemMax / (ne->warpDoubles * 8);
+        if (fit < 1) throw std::runtime_error("mechanism too large for one warp's shared memory");
+        int wpb = ne->opts.warps_per_block > 0 ? ne->opts.warps_per_block : std::min(fit, 8);
+        wpb = std::min(wpb, fit);
+        ne->warpsPerBlock = wpb;
+        int blocksPerSm = std::max(1, (228 * 1024) / (ne->warpDoubles * 8 * wpb));
+        ne->blocks = std::min(me.smCount * blocksPerSm, (n + wpb - 1) / wpb);
+        const int K = me.m.K;
+        ne->dP.ensure((size_t)n * 8);
+        ne->dT.ensure((size_t)n * 8);
+        ne->dY.ensure((size_t)K * n * 8);
+        ne->dRec.ensure((size_t)n * ne->recStride * 8);
+        ne->dStats.ensure((size_t)n * 8 * 8);
+        ne->dStatus.ensure((size_t)n * 4);
+        ne->dTign.ensure((size_t)n * 8);
+        ne->dCounter.ensure(sizeof(int));
+        ck(cudaMemset(ne->dRec.p, 0, (size_t)n * ne->recStride * 8), "memset");
+        ck(cudaMemset(ne->dStats.p, 0, (size_t)n * 64), "memset");
+        ck(cudaMemset(ne->dStatus.p, 0, (size_t)n * 4), "memset");
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_nets.push_back(std::move(ne));
+        return (int32_t)g_nets.size() - 1;
+    });
+}
+
+int32_t gb_net_del(int32_t h) {
+    return guarded([&]() -> int32_t {
+        net(h);
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_nets[h].reset();
+        return 0;
+    });
+}
+
+int32_t gb_net_set_state(int32_t h, const double* T, const double* P, const double* Y, int32_t flags) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        MechEntry& me = mech(ne.mech);
+        if (!T || !P || !Y) throw std::runtime_error("null array argument");
+        const int K = me.m.K, n = ne.n;
+        auto kind = (flags & GB_DEVICE_POINTERS) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+        cudaStream_t s = me.stream;
+        ck(cudaMemcpyAsync(ne.dT.p, T, (size_t)n * 8, kind, s), "copy T");
+        ck(cudaMemcpyAsync(ne.dP.p, P, (size_t)n * 8, kind, s), "copy P");
+        ck(cudaMemcpyAsync(ne.dY.p, Y, (size_t)K * n * 8, kind, s), "copy Y");
+        ck(cudaMemsetAsync(ne.dRec.p, 0, (size_t)n * ne.recStride * 8, s), "reset records");
+        ck(cudaMemsetAsync(ne.dStats.p, 0, (size_t)n * 64, s), "reset stats");
+        ck(cudaMemsetAsync(ne.dStatus.p, 0, (size_t)n * 4, s), "reset status");
+        // queue order: hottest reactors first (they take the most steps), so the
+        // longest integrations start early and the tail of the queue is short
+        std::vector<double> hT(n);
+        if (flags & GB_DEVICE_POINTERS) ck(cudaMemcpyAsync(hT.data(), T, (size_t)n * 8, cudaMemcpyDeviceToHost, s), "copy T");
+        else std::copy(T, T + n, hT.begin());
+        ck(cudaStreamSynchronize(s), "set state");
+        std::vector<int> ord(n);
+        std::iota(ord.begin(), ord.end(), 0);
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return hT[a] > hT[b]; });
+        ne.dOrder.ensure((size_t)n * 4);
+        ck(cudaMemcpy(ne.dOrder.p, ord.data(), (size_t)n * 4, cudaMemcpyHostToDevice), "copy order");
+        ne.haveOrder = true;
+        ne.time = 0.0;
+        return 0;
+    });
+}
+
+int32_t gb_net_advance(int32_t h, double t) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        MechEntry& me = mech(ne.mech);
+        if (t < ne.time) throw std::runtime_error("cannot integrate backwards in time");
+        if (t == ne.time) return 0;
+        cudaStream_t s = me.stream;
+        if (ne.opts.use_graph) {
+            if (!ne.graph || ne.graphTout != t) {
+                if (ne.graph) { cudaGraphExecDestroy(ne.graph); ne.graph = nullptr; }
+                cudaGraph_t g;
+                ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+                netLaunch(ne, me, ne.time, t);
+                ck(cudaStreamEndCapture(s, &g), "end capture");
+                ck(cudaGraphInstantiate(&ne.graph, g, 0), "graph instantiate");
+                cudaGraphDestroy(g);
+                ne.graphTout = t;
+            }
+            ck(cudaGraphLaunch(ne.graph, s), "graph launch");
+        } else {
+            netLaunch(ne, me, ne.time, t);
+        }
+        ck(cudaStreamSynchronize(s), "integrator");
+        ne.time = t;
+        std::vector<int> st(ne.n);
+        ck(cudaMemcpy(st.data(), ne.dStatus.p, (size_t)ne.n * 4, cudaMemcpyDeviceToHost), "copy status");
+        int bad = 0;
+        for (int v : st) bad += (v != 0);
+        return bad;
+    });
+}
+
+double gb_net_time(int32_t h) {
+    try {
+        return net(h).time;
+    } catch (std::exception& e) {
+        g_error = e.what();
+        return -999.999;
+    }
+}
+
+int32_t gb_net_get_state(int32_t h, double* T, double* Y, int32_t flags) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        MechEntry& me = mech(ne.mech);
+        auto kind = (flags & GB_DEVICE_POINTERS) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        if (T) ck(cudaMemcpy(T, ne.dT.p, (size_t)ne.n * 8, kind), "copy T");
+        if (Y) ck(cudaMemcpy(Y, ne.dY.p, (size_t)me.m.K * ne.n * 8, kind), "copy Y");
+        return 0;
+    });
+}
+
+int32_t gb_net_get_status(int32_t h, int32_t* status) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        ck(cudaMemcpy(status, ne.dStatus.p, (size_t)ne.n * 4, cudaMemcpyDeviceToHost), "copy status");
+        return 0;
+    });
+}
+
+int32_t gb_net_solver_stats(int32_t h, int64_t* stats) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        ck(cudaMemcpy(stats, ne.dStats.p, (size_t)ne.n * 64, cudaMemcpyDeviceToHost), "copy stats");
+        return 0;
+    });
+}
+
+int32_t gb_net_ignition_times(int32_t h, double* tign) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        ck(cudaMemcpy(tign, ne.dTign.p, (size_t)ne.n * 8, cudaMemcpyDeviceToHost), "copy tign");
+        return 0;
+    });
+}
+
+}  // extern "C"

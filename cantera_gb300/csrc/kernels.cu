@@ -1,0 +1,846 @@
+// kernels.cu - GPU kernels of the engine: batched net production rates and their
+// concentration Jacobian, and the batched BDF reactor integrator.
+//
+// Both kernels are persistent: a grid sized to fill every SM, one state (reactor) per
+// warp at a time, and a device-side work counter from which a warp takes its next state
+// as soon as it finishes the previous one.  Reactors of very different stiffness
+// (igniting next to inert) therefore never leave warps idle until the queue runs dry.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.h"
+#include "kinetics.cuh"
+
+namespace gbchem {
+
+// =============================================================================
+// Rates and d(wdot)/dc over a batch of states (Kinetics::getNetProductionRates,
+// Kinetics::netProductionRates_ddCi)
+// =============================================================================
+__global__ void __launch_bounds__(256) k_rates(RatesParams p) {
+    extern __shared__ double smem[];
+    const DevMech& m = p.m;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    double* base = smem + (size_t)warp * p.warpDoubles;
+    KinScratch s;
+    const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF);
+    s.carve(base, m.K, m.R, m.NTB, m.NF);
+    double* Yl = base + kinD;
+    double* gk = Yl + m.K;
+    double* Jc = gk + m.K;
+    const int ld = m.K + 1;
+    KinState st;
+    for (;;) {
+        int idx = 0;
+        if (lane == 0) idx = atomicAdd(p.counter, 1);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= p.n) break;
+        for (int k = lane; k < m.K; k += 32) Yl[k] = p.Y[(size_t)k * p.n + idx];
+        double T = p.T[idx], P = p.P[idx];
+        __syncwarp();
+        warpState(m, T, P, Yl, s, st, lane);
+        __syncwarp();
+        warpRates<true>(m, s, st, lane);
+        if (p.wdot)
+            for (int k = lane; k < m.K; k += 32) p.wdot[(size_t)k * p.n + idx] = s.wdot[k];
+        if (p.jac) {
+            for (int q = lane; q < m.K * ld; q += 32) Jc[q] = 0.0;
+            __syncwarp();
+            warpJacC<double>(m, s, Jc, ld, lane);
+            warpDenseG(m, s, gk, lane);
+            for (int q = lane; q < m.nnz; q += 32) {
+                int r = m.jrIdx[q], c = m.jpCol[q];
+                p.jac[(size_t)q * p.n + idx] = Jc[(size_t)r * ld + c] + gk[r];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// =============================================================================
+// Batched BDF integrator (the CVODES algorithm as the reference configures it:
+// src/numerics/CVodesIntegrator.cpp:281-529, src/zeroD/ReactorNet.cpp:164-169)
+// =============================================================================
+namespace {
+constexpr int QMAX = 5;
+constexpr double BIAS1 = 6.0, BIAS2 = 6.0, BIAS3 = 10.0, ADDON = 1e-6;
+constexpr double ETA_FIX_MAX = 1.5;
+constexpr double ETA_MAX_FIRST = 1e4, ETA_MAX_EARLY = 10.0, ETA_MAX_GENERAL = 10.0;
+constexpr int SMALL_NST = 10;
+constexpr double ETA_MIN_EF = 0.1, ETA_MAX_EF = 0.2, ETA_CF = 0.25;
+constexpr int SMALL_NEF = 2, MXNEF1 = 3, MXNEF = 7, MXNCF = 10;
+constexpr int MAXCOR = 3;
+constexpr double NLSCOEF = 0.1, CRDOWN = 0.3, RDIV = 2.0;
+constexpr int MSBP = 20;
+constexpr double DGMAX = 0.3;
+constexpr double UROUND = 2.220446049250313e-16;
+enum { ST_OK = 0, ST_MAX_STEPS = 1, ST_ERR_FAIL = 2, ST_CONV_FAIL = 3, ST_NONFINITE = 4, ST_H_TOO_SMALL = 5 };
+enum { NLS_OK = 0, NLS_RECOVER = 1 };
+
+// scalar slots of the per-reactor record (after zn[QMAX+1][N])
+enum {
+    R_TN = 0, R_H, R_HSCALE, R_HPRIME, R_ETA, R_ETAMAX, R_TAU = 6, R_TQ = 13, R_GAMMAP = 19, R_CRATE,
+    R_SAVEDTQ5, R_IGN = 22, R_Q = 30, R_QPRIME, R_QWAIT, R_NST, R_NSTLP, R_NSAMP, R_FLAGS, R_STATUS,
+    R_L = 38, R_NSCAL = 44
+};
+enum { F_HASPREV = 1, F_HASRIGHT = 2, F_AWAIT = 4, F_INIT = 8 };
+}  // namespace
+
+struct BdfScal {
+    double tn, h, hscale, hprime, eta, etamax, gamma, gammap, gamrat, crate, acnrm, saved_tq5;
+    double tau[QMAX + 2], tq[6], l[QMAX + 1];
+    int q, qprime, qwait, L, nst, nstlp;
+    bool haveLU;
+    // ignition marker
+    double ls_t, ls_v, pv_t, pv_v, bs_t, bs_v, nx_t, nx_v;
+    int nsamp, flags, status0;
+    long long nrhs, nni, nsetups, nje, netf, ncfn;
+};
+
+struct BdfWarp {
+    const DevMech* m;
+    int N, Nnorm, lane, ld;
+    double P, rtol, atol, hmaxInv;
+    int maxOrder;
+    KinScratch s;
+    KinState st;
+    double *zn, *ewt, *acor, *y, *ftemp, *tempv, *v1, *v2;
+    int* piv;
+
+    __device__ double wrms(const double* v) const {
+        double a = 0.0;
+        for (int i = lane; i < N; i += 32) { double x = v[i] * ewt[i]; a += x * x; }
+        return sqrt(warpSum(a) / Nnorm);
+    }
+    __device__ double* Z(int j) const { return zn + (size_t)j * N; }
+    __device__ void setEwt(const double* yv) {
+        for (int i = lane; i < N; i += 32) ewt[i] = 1.0 / (rtol * fabs(yv[i]) + atol);
+        __syncwarp();
+    }
+    // reactor right-hand side; returns true when every derivative is finite
+    __device__ bool rhs(const double* z, double* zdot, BdfScal& S) {
+        const DevMech& mm = *m;
+        S.nrhs++;
+        warpState(mm, z[0], P, z + 1, s, st, lane);
+        __syncwarp();
+        warpRates<true>(mm, s, st, lane);
+        double ph = 0.0, pc = 0.0;
+        for (int k = lane; k < mm.K; k += 32) {
+            ph += s.wdot[k] * s.hRT[k];
+            pc += s.c[k] * s.cpR[k];
+        }
+        double hw = warpSum(ph);
+        double cpmass = mm.Rgas * (warpSum(pc) / st.rho);
+        double dTdt = -(hw * st.RT) / (st.rho * cpmass);
+        bool ok = isfinite(dTdt);
+        if (lane == 0) zdot[0] = dTdt;
+        for (int k = lane; k < mm.K; k += 32) {
+            double v = s.wdot[k] * mm.mw[k] / st.rho;
+            zdot[1 + k] = v;
+            ok = ok && isfinite(v);
+        }
+        __syncwarp();
+        return __all_sync(0xffffffffu, ok);
+    }
+
+    // Newton matrix M = I - gamma*J (J analytic in the species columns, one-sided
+    // difference in T), factored in place.  Returns false if J is not finite or M singular.
+    template <typename MT>
+    __device__ bool setup(MT* M, BdfScal& S) {
+        const DevMech& mm = *m;
+        const int K = mm.K;
+        // the kinetics scratch holds the state of y (the last rhs call was at y)
+        for (int q = lane; q < N * ld; q += 32) M[q] = (MT)0;
+        __syncwarp();
+        warpJacC<MT>(mm, s, M + ld + 1, ld, lane);
+        // v1 = X (mole fractions); v2[k] = (Jc X)_k; later hJ
+        for (int k = lane; k < K; k += 32) v1[k] = s.c[k] / st.ctot;
+        __syncwarp();
+        for (int k = lane; k < K; k += 32) {
+            const MT* row = M + (size_t)(1 + k) * ld + 1;
+            double a = 0.0;
+            for (int l = 0; l < K; l++) a += (double)row[l] * v1[l];
+            v2[k] = a;
+        }
+        double pcp = 0.0;
+        for (int k = lane; k < K; k += 32) pcp += v1[k] * s.cpR[k];
+        const double cpmix = warpSum(pcp);
+        __syncwarp();
+        // column pass: hJ_j, the transformed species block, and the T row
+        double phj = 0.0;
+        for (int j = lane; j < K; j += 32) {
+            double a = 0.0;
+            for (int k = 0; k < K; k++) a += s.hRT[k] * (double)M[(size_t)(1 + k) * ld + 1 + j];
+            tempv[j] = a;   // hJ_j (tempv is free during setup)
+            phj += a * v1[j];
+        }
+        const double hJX = warpSum(phj);
+        const double rho = st.rho, mmw = st.mmw;
+        const double D = rho * mm.Rgas * (cpmix / mmw);
+        const double G = ftemp[0];
+        __syncwarp();
+        for (int j = lane; j < K; j += 32) {
+            double Wj = mm.mw[j];
+            for (int k = 0; k < K; k++) {
+                double Wk = mm.mw[k];
+                MT* p = M + (size_t)(1 + k) * ld + 1 + j;
+                *p = (MT)((Wk / Wj) * ((double)*p - v2[k]) + s.wdot[k] * Wk * mmw / (rho * Wj));
+            }
+            double dH = (rho / Wj) * st.RT * (tempv[j] - hJX);
+            double dD = (rho * mm.Rgas / Wj) * (s.cpR[j] - cpmix);
+            M[1 + j] = (MT)(-(dH + G * dD) / D);
+        }
+        __syncwarp();
+        // T column: one-sided difference
+        const double T0 = y[0];
+        const double dT = sqrt(UROUND) * fmax(1.0, fabs(T0));
+        for (int i = lane; i < N; i += 32) tempv[i] = y[i];
+        __syncwarp();
+        if (lane == 0) tempv[0] = T0 + dT;
+        __syncwarp();
+        bool ok = rhs(tempv, v1, S);
+        for (int i = lane; i < N; i += 32) M[(size_t)i * ld] = (MT)((v1[i] - ftemp[i]) / dT);
+        __syncwarp();
+        // M = I - gamma*J
+        const double g = S.gamma;
+        bool fin = true;
+        for (int q = lane; q < N * ld; q += 32) {
+            double v = -g * (double)M[q];
+            fin = fin && isfinite(v);
+            M[q] = (MT)v;
+        }
+        __syncwarp();
+        for (int i = lane; i < N; i += 32) M[(size_t)i * ld + i] = (MT)((double)M[(size_t)i * ld + i] + 1.0);
+        __syncwarp();
+        ok = __all_sync(0xffffffffu, ok && fin);
+        S.nje++;
+        S.nsetups++;
+        if (!ok) return false;
+        return luFactor(M);
+    }
+
+    template <typename MT>
+    __device__ bool luFactor(MT* a) {
+        bool nonsingular = true;
+        for (int k = 0; k < N; k++) {
+            // pivot: largest |a[i][k]|, lowest row index on ties
+            double bv = -1.0;
+            int bi = N;
+            for (int i = k + lane; i < N; i += 32) {
+                double v = fabs((double)a[(size_t)i * ld + k]);
+                if (v > bv) { bv = v; bi = i; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+            }
+            if (lane == 0) piv[k] = bi;
+            if (!(bv > 0.0)) { nonsingular = false; bi = k; }
+            if (bi != k) {
+                for (int j = lane; j < N; j += 32) {
+                    MT t = a[(size_t)k * ld + j];
+                    a[(size_t)k * ld + j] = a[(size_t)bi * ld + j];
+                    a[(size_t)bi * ld + j] = t;
+                }
+            }
+            __syncwarp();
+            if (!nonsingular) break;
+            const MT inv = (MT)1 / a[(size_t)k * ld + k];
+            for (int i = k + 1 + lane; i < N; i += 32) a[(size_t)i * ld + k] *= inv;
+            __syncwarp();
+            for (int j = k + 1 + lane; j < N; j += 32) {
+                const MT u = a[(size_t)k * ld + j];
+                for (int i = k + 1; i < N; i++) a[(size_t)i * ld + j] -= a[(size_t)i * ld + k] * u;
+            }
+            __syncwarp();
+        }
+        return nonsingular;
+    }
+
+    template <typename MT>
+    __device__ void luSolve(const MT* a, double* b) {
+        if (lane == 0)
+            for (int k = 0; k < N; k++) {
+                int p = piv[k];
+                if (p != k) { double t = b[k]; b[k] = b[p]; b[p] = t; }
+            }
+        __syncwarp();
+        // keep the working vector in the factor's precision
+        for (int k = 0; k < N; k++) {
+            MT bk = (MT)b[k];
+            for (int i = k + 1 + lane; i < N; i += 32) b[i] = (double)((MT)b[i] - a[(size_t)i * ld + k] * bk);
+            __syncwarp();
+        }
+        for (int k = N - 1; k >= 0; k--) {
+            MT bk = (MT)b[k] / a[(size_t)k * ld + k];
+            __syncwarp();
+            if (lane == 0) b[k] = (double)bk;
+            for (int i = lane; i < k; i += 32) b[i] = (double)((MT)b[i] - a[(size_t)i * ld + k] * bk);
+            __syncwarp();
+        }
+    }
+
+    __device__ void predict(BdfScal& S) {
+        S.tn += S.h;
+        for (int k = 1; k <= S.q; k++)
+            for (int j = S.q; j >= k; j--) {
+                double* a = Z(j - 1);
+                const double* b = Z(j);
+                for (int i = lane; i < N; i += 32) a[i] += b[i];
+            }
+        __syncwarp();
+    }
+    __device__ void restore(BdfScal& S, double saved_t) {
+        S.tn = saved_t;
+        for (int k = 1; k <= S.q; k++)
+            for (int j = S.q; j >= k; j--) {
+                double* a = Z(j - 1);
+                const double* b = Z(j);
+                for (int i = lane; i < N; i += 32) a[i] -= b[i];
+            }
+        __syncwarp();
+    }
+    __device__ void rescale(BdfScal& S) {
+        double f = S.eta;
+        for (int j = 1; j <= S.q; j++) {
+            double* a = Z(j);
+            for (int i = lane; i < N; i += 32) a[i] *= f;
+            f *= S.eta;
+        }
+        __syncwarp();
+        S.h = S.hscale * S.eta;
+        S.hscale = S.h;
+    }
+    __device__ void setCoefficients(BdfScal& S) {
+        for (int i = 0; i <= QMAX; i++) S.l[i] = 0.0;
+        S.l[0] = S.l[1] = 1.0;
+        double xi_inv = 1.0, xistar_inv = 1.0, alpha0 = -1.0, alpha0_hat = -1.0, hsum = S.h;
+        const int q = S.q;
+        if (q > 1) {
+            for (int j = 2; j < q; j++) {
+                hsum += S.tau[j - 1];
+                xi_inv = S.h / hsum;
+                alpha0 -= 1.0 / j;
+                for (int i = j; i >= 1; i--) S.l[i] += S.l[i - 1] * xi_inv;
+            }
+            alpha0 -= 1.0 / q;
+            xistar_inv = -S.l[1] - alpha0;
+            hsum += S.tau[q - 1];
+            xi_inv = S.h / hsum;
+            alpha0_hat = -S.l[1] - xi_inv;
+            for (int i = q; i >= 1; i--) S.l[i] += S.l[i - 1] * xistar_inv;
+        }
+        double A1 = 1.0 - alpha0_hat + alpha0;
+        double A2 = 1.0 + q * A1;
+        S.tq[2] = fabs(A1 / (alpha0 * A2));
+        S.tq[5] = fabs(A2 * xistar_inv / (S.l[q] * xi_inv));
+        if (S.qwait == 1) {
+            if (q > 1) {
+                double C = xistar_inv / S.l[q];
+                double A3 = alpha0 + 1.0 / q;
+                double A4 = alpha0_hat + xi_inv;
+                double Cpinv = (1.0 - A4 + A3) / A3;
+                S.tq[1] = fabs(C * Cpinv);
+            } else {
+                S.tq[1] = 1.0;
+            }
+            double hs = hsum + S.tau[q];
+            double xi2 = S.h / hs;
+            double A5 = alpha0 - 1.0 / (q + 1);
+            double A6 = alpha0_hat - xi2;
+            double Cppinv = (1.0 - A6 + A5) / A2;
+            S.tq[3] = fabs(Cppinv / (xi2 * (q + 2) * A5));
+        }
+        S.tq[4] = NLSCOEF / S.tq[2];
+    }
+
+    template <typename MT>
+    __device__ int newton(MT* M, BdfScal& S, bool callSetup) {
+        const double rl1 = 1.0 / S.l[1];
+        bool jcur = false;
+        for (;;) {
+            for (int i = lane; i < N; i += 32) { y[i] = zn[i]; acor[i] = 0.0; }
+            __syncwarp();
+            if (!rhs(y, ftemp, S)) return NLS_RECOVER;
+            if (callSetup) {
+                callSetup = false;
+                bool ok = setup<MT>(M, S);
+                S.gammap = S.gamma;
+                S.gamrat = 1.0;
+                S.crate = 1.0;
+                S.nstlp = S.nst;
+                S.haveLU = ok;
+                jcur = true;
+                if (!ok) return NLS_RECOVER;
+            }
+            double delp = 0.0, del = 0.0;
+            int mm = 0;
+            bool retry = false;
+            const double* z1 = Z(1);
+            for (;;) {
+                S.nni++;
+                for (int i = lane; i < N; i += 32) tempv[i] = S.gamma * ftemp[i] - (rl1 * z1[i] + acor[i]);
+                __syncwarp();
+                luSolve<MT>(M, tempv);
+                if (S.gamrat != 1.0) {
+                    double f = 2.0 / (1.0 + S.gamrat);
+                    for (int i = lane; i < N; i += 32) tempv[i] *= f;
+                    __syncwarp();
+                }
+                del = wrms(tempv);
+                for (int i = lane; i < N; i += 32) { acor[i] += tempv[i]; y[i] = zn[i] + acor[i]; }
+                __syncwarp();
+                if (!isfinite(del)) { retry = !jcur; break; }
+                if (mm > 0) S.crate = fmax(CRDOWN * S.crate, del / delp);
+                double dcon = del * fmin(1.0, S.crate) / S.tq[4];
+                if (dcon <= 1.0) {
+                    S.acnrm = (mm == 0) ? del : wrms(acor);
+                    return NLS_OK;
+                }
+                mm++;
+                if (mm == MAXCOR || (mm >= 2 && del > RDIV * delp)) { retry = !jcur; break; }
+                delp = del;
+                if (!rhs(y, ftemp, S)) { retry = !jcur; break; }
+            }
+            if (retry && S.haveLU) { callSetup = true; continue; }
+            return NLS_RECOVER;
+        }
+    }
+
+    // Nordsieck order change (see the CPU restatement for the polynomial construction)
+    __device__ void decreaseOrder(BdfScal& S) {
+        double w[QMAX + 2] = {0, 0, 0, 0, 0, 0, 0};
+        w[2] = 1.0;
+        double hsum = 0.0;
+        for (int j = 1; j <= S.q - 2; j++) {
+            hsum += S.tau[j];
+            double xi = hsum / S.hscale;
+            for (int i = j + 2; i >= 2; i--) w[i] = w[i] * xi + w[i - 1];
+        }
+        const double* zq = Z(S.q);
+        for (int j = 2; j < S.q; j++) {
+            double* a = Z(j);
+            for (int i = lane; i < N; i += 32) a[i] -= w[j] * zq[i];
+        }
+        __syncwarp();
+        double* a = Z(S.q);
+        for (int i = lane; i < N; i += 32) a[i] = 0.0;
+        __syncwarp();
+    }
+    __device__ void increaseOrder(BdfScal& S, double lq_prev) {
+        double w[QMAX + 2] = {0, 0, 0, 0, 0, 0, 0};
+        w[2] = 1.0;
+        double hsum = 0.0;
+        for (int j = 1; j <= S.q - 1; j++) {
+            hsum += S.tau[j];
+            double xi = hsum / S.hscale;
+            for (int i = j + 2; i >= 2; i--) w[i] = w[i] * xi + w[i - 1];
+        }
+        const double c = lq_prev / (S.q + 1);
+        const double* sv = Z(QMAX);
+        for (int i = lane; i < N; i += 32) tempv[i] = c * sv[i];
+        __syncwarp();
+        for (int j = 2; j <= S.q; j++) {
+            double* a = Z(j);
+            for (int i = lane; i < N; i += 32) a[i] += w[j] * tempv[i];
+        }
+        double* top = Z(S.q + 1);
+        for (int i = lane; i < N; i += 32) top[i] = tempv[i];
+        __syncwarp();
+    }
+
+    __device__ void recordSample(BdfScal& S, double t, double v) {
+        if (S.flags & F_AWAIT) { S.nx_t = t; S.nx_v = v; S.flags = (S.flags & ~F_AWAIT) | F_HASRIGHT; }
+        if (S.nsamp == 0 || v > S.bs_v) {
+            S.pv_t = S.ls_t; S.pv_v = S.ls_v;
+            S.flags = (S.nsamp > 0) ? (S.flags | F_HASPREV) : (S.flags & ~F_HASPREV);
+            S.bs_t = t; S.bs_v = v;
+            S.flags = (S.flags | F_AWAIT) & ~F_HASRIGHT;
+        }
+        S.ls_t = t; S.ls_v = v;
+        S.nsamp++;
+    }
+    __device__ double ignitionTime(const BdfScal& S) const {
+        if (!(S.flags & F_HASPREV) || !(S.flags & F_HASRIGHT)) return S.bs_t;
+        double t0 = S.pv_t, t1 = S.bs_t, t2 = S.nx_t;
+        double s0 = (S.bs_v - S.pv_v) / (t1 - t0), s1 = (S.nx_v - S.bs_v) / (t2 - t1);
+        double curv = (s1 - s0) / (t2 - t0);
+        if (!(curv < 0)) return t1;
+        double tv = 0.5 * (t0 + t1) - s0 / (2.0 * curv);
+        return fmin(fmax(tv, t0), t2);
+    }
+
+    __device__ double initialStep(BdfScal& S, double tout) {
+        const double tdist = fabs(tout - S.tn);
+        const double tround = UROUND * fmax(fabs(S.tn), fabs(tout));
+        const double hlb = 100.0 * tround;
+        const double* z0 = Z(0);
+        const double* z1 = Z(1);
+        double hi = 0.0;
+        for (int i = lane; i < N; i += 32) hi = fmax(hi, fabs(z1[i]) / (0.1 * fabs(z0[i]) + atol));
+        double hub_inv = warpMax(hi);
+        double hub = 0.1 * tdist;
+        if (hub * hub_inv > 1.0) hub = 1.0 / hub_inv;
+        if (hub < hlb) return sqrt(hlb * hub);
+        double hg = sqrt(hlb * hub);
+        double hnew = hg;
+        for (int count = 1; count <= 4; count++) {
+            for (int i = lane; i < N; i += 32) y[i] = z0[i] + hg * z1[i];
+            __syncwarp();
+            if (!rhs(y, tempv, S)) { hg *= 0.2; continue; }
+            for (int i = lane; i < N; i += 32) tempv[i] = (tempv[i] - z1[i]) / hg;
+            __syncwarp();
+            double yddnrm = wrms(tempv);
+            hnew = (yddnrm * hub * hub > 2.0) ? sqrt(2.0 / yddnrm) : sqrt(hg * hub);
+            if (count == 4) break;
+            double hrat = hnew / hg;
+            if (hrat > 0.5 && hrat < 2.0) break;
+            if (count > 1 && hrat > 2.0) { hnew = hg; break; }
+            hg = hnew;
+        }
+        double h0 = 0.5 * hnew;
+        h0 = fmin(fmax(h0, hlb), hub);
+        if (hmaxInv > 0) h0 = fmin(h0, 1.0 / hmaxInv);
+        return h0;
+    }
+
+    __device__ void prepareNext(BdfScal& S, double dsm) {
+        if (S.etamax == 1.0) {
+            S.qwait = max(S.qwait, 2);
+            S.qprime = S.q;
+            S.hprime = S.h;
+            S.eta = 1.0;
+            S.etamax = (S.nst <= SMALL_NST) ? ETA_MAX_EARLY : ETA_MAX_GENERAL;
+            return;
+        }
+        const int L = S.L;
+        double etaq = 1.0 / (pow(BIAS2 * dsm, 1.0 / L) + ADDON);
+        if (S.qwait != 0) {
+            S.eta = etaq;
+            S.qprime = S.q;
+        } else {
+            S.qwait = 2;
+            double etaqm1 = 0.0, etaqp1 = 0.0;
+            if (S.q > 1) {
+                double ddn = wrms(Z(S.q)) * S.tq[1];
+                etaqm1 = 1.0 / (pow(BIAS1 * ddn, 1.0 / S.q) + ADDON);
+            }
+            if (S.q != maxOrder && S.saved_tq5 != 0.0) {
+                double cquot = (S.tq[5] / S.saved_tq5) * pow(S.h / S.tau[2], (double)L);
+                const double* sv = Z(QMAX);
+                for (int i = lane; i < N; i += 32) tempv[i] = acor[i] - cquot * sv[i];
+                __syncwarp();
+                double dup = wrms(tempv) * S.tq[3];
+                etaqp1 = 1.0 / (pow(BIAS3 * dup, 1.0 / (L + 1)) + ADDON);
+            }
+            double etam = fmax(etaqm1, fmax(etaq, etaqp1));
+            if (etam < ETA_FIX_MAX) {
+                S.eta = 1.0;
+                S.qprime = S.q;
+            } else if (etam == etaq) {
+                S.eta = etaq;
+                S.qprime = S.q;
+            } else if (etam == etaqm1) {
+                S.eta = etaqm1;
+                S.qprime = S.q - 1;
+            } else {
+                S.eta = etaqp1;
+                S.qprime = S.q + 1;
+                double* sv = Z(QMAX);
+                for (int i = lane; i < N; i += 32) sv[i] = acor[i];
+                __syncwarp();
+            }
+        }
+        if (S.eta < ETA_FIX_MAX) {
+            S.eta = 1.0;
+            S.qprime = S.q;
+        } else {
+            S.eta = fmin(S.eta, S.etamax);
+            if (hmaxInv > 0) S.eta /= fmax(1.0, fabs(S.h) * S.eta * hmaxInv);
+        }
+        S.hprime = S.h * S.eta;
+        S.etamax = (S.nst <= SMALL_NST) ? ETA_MAX_EARLY : ETA_MAX_GENERAL;
+    }
+
+    // one internal step; returns a status code
+    template <typename MT>
+    __device__ int step(MT* M, BdfScal& S) {
+        const double saved_t = S.tn;
+        int ncf = 0, nef = 0;
+        bool prevConvFail = false;
+        if (S.nst > 0) {
+            if (S.qprime != S.q) {
+                if (S.qprime == S.q + 1) increaseOrder(S, S.l[S.q]);
+                else decreaseOrder(S);
+                S.q = S.qprime;
+                S.L = S.q + 1;
+                S.qwait = S.L;
+            }
+            if (S.hprime != S.h) {
+                S.eta = S.hprime / S.h;
+                rescale(S);
+            }
+        }
+        setEwt(Z(0));
+        for (;;) {
+            predict(S);
+            setCoefficients(S);
+            S.gamma = S.h / S.l[1];
+            if (S.nst == 0) S.gammap = S.gamma;
+            S.gamrat = (S.nst > 0) ? S.gamma / S.gammap : 1.0;
+            bool callSetup = (S.nst == 0) || prevConvFail || (S.nst >= S.nstlp + MSBP) ||
+                             (fabs(S.gamrat - 1.0) > DGMAX) || !S.haveLU;
+            int nls = newton<MT>(M, S, callSetup);
+            if (nls != NLS_OK) {
+                S.ncfn++;
+                ncf++;
+                restore(S, saved_t);
+                if (ncf == MXNCF) return ST_CONV_FAIL;
+                S.eta = ETA_CF;
+                rescale(S);
+                prevConvFail = true;
+                S.etamax = 1.0;
+                if (fabs(S.h) < 10.0 * UROUND * fmax(1.0, fabs(S.tn))) return ST_H_TOO_SMALL;
+                continue;
+            }
+            double dsm = S.acnrm * S.tq[2];
+            if (dsm > 1.0) {
+                S.netf++;
+                nef++;
+                restore(S, saved_t);
+                if (nef == MXNEF) return ST_ERR_FAIL;
+                S.etamax = 1.0;
+                if (nef <= MXNEF1) {
+                    S.eta = 1.0 / (pow(BIAS2 * dsm, 1.0 / S.L) + ADDON);
+                    S.eta = fmax(ETA_MIN_EF, S.eta);
+                    if (nef >= SMALL_NEF) S.eta = fmin(S.eta, ETA_MAX_EF);
+                    rescale(S);
+                } else {
+                    S.eta = ETA_MIN_EF;
+                    S.h *= S.eta;
+                    S.hscale = S.h;
+                    S.qwait = 10;
+                    if (S.q > 1) { S.q = 1; S.L = 2; }
+                    if (!rhs(Z(0), tempv, S)) return ST_NONFINITE;
+                    double* z1 = Z(1);
+                    for (int i = lane; i < N; i += 32) z1[i] = S.h * tempv[i];
+                    for (int j = 2; j <= QMAX; j++) {
+                        double* a = Z(j);
+                        for (int i = lane; i < N; i += 32) a[i] = 0.0;
+                    }
+                    __syncwarp();
+                }
+                if (fabs(S.h) < 10.0 * UROUND * fmax(1.0, fabs(S.tn))) return ST_H_TOO_SMALL;
+                continue;
+            }
+            // accepted
+            S.nst++;
+            for (int i = S.q; i >= 2; i--) S.tau[i] = S.tau[i - 1];
+            if (S.q == 1 && S.nst > 1) S.tau[2] = S.tau[1];
+            S.tau[1] = S.h;
+            for (int j = 0; j <= S.q; j++) {
+                double* a = Z(j);
+                const double lj = S.l[j];
+                for (int i = lane; i < N; i += 32) a[i] += lj * acor[i];
+            }
+            __syncwarp();
+            S.qwait--;
+            if (S.qwait == 1 && S.q != QMAX) {
+                double* sv = Z(QMAX);
+                for (int i = lane; i < N; i += 32) sv[i] = acor[i];
+                __syncwarp();
+                S.saved_tq5 = S.tq[5];
+            }
+            recordSample(S, S.tn, zn[N] / S.h);
+            prepareNext(S, dsm);
+            return ST_OK;
+        }
+    }
+};
+
+template <typename MT>
+__global__ void __launch_bounds__(256) k_bdf(BdfParams p) {
+    extern __shared__ double smem[];
+    const DevMech& m = p.m;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    double* base = smem + (size_t)warp * p.warpDoubles;
+    BdfWarp W;
+    W.m = &m;
+    W.N = m.N;
+    W.Nnorm = m.N + 1;
+    W.lane = lane;
+    W.ld = p.ld;
+    W.rtol = p.rtol;
+    W.atol = p.atol;
+    W.hmaxInv = p.hmaxInv;
+    W.maxOrder = p.maxOrder;
+    const int N = m.N;
+    const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF);
+    W.s.carve(base, m.K, m.R, m.NTB, m.NF);
+    double* q = base + kinD;
+    W.zn = q; q += (QMAX + 1) * N;
+    W.ewt = q; q += N;
+    W.acor = q; q += N;
+    W.y = q; q += N;
+    W.ftemp = q; q += N;
+    W.tempv = q; q += N;
+    W.v1 = q; q += N;
+    W.v2 = q; q += N;
+    W.piv = (int*)q; q += (N + 1) / 2;
+    MT* M = (MT*)q;
+
+    for (;;) {
+        int idx = 0;
+        if (lane == 0) idx = atomicAdd(p.counter, 1);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= p.n) break;
+        const int r = p.order ? p.order[idx] : idx;
+        double* rec = p.rec + (size_t)r * p.recStride;
+        const double* rs = rec + (QMAX + 1) * N;
+        long long* stt = p.stats + (size_t)r * 8;
+        W.P = p.P[r];
+        BdfScal S;
+        const bool fresh = !(((int)rs[R_FLAGS]) & F_INIT);
+        if (fresh) {
+            // zn[0] = state, zn[1] = h*f(state)
+            double* z0 = W.zn;
+            if (lane == 0) z0[0] = p.T[r];
+            for (int k = lane; k < m.K; k += 32) z0[1 + k] = p.Y[(size_t)k * p.n + r];
+            for (int j = 1; j <= QMAX; j++)
+                for (int i = lane; i < N; i += 32) W.zn[(size_t)j * N + i] = 0.0;
+            __syncwarp();
+            S.tn = p.t0;
+            S.nrhs = S.nni = S.nsetups = S.nje = S.netf = S.ncfn = 0;
+            S.nst = 0; S.nstlp = 0;
+            S.haveLU = false;
+            S.flags = F_INIT; S.nsamp = 0;
+            S.ls_t = S.ls_v = S.pv_t = S.pv_v = S.bs_t = S.bs_v = S.nx_t = S.nx_v = 0.0;
+            for (int i = 0; i < QMAX + 2; i++) S.tau[i] = 0.0;
+            for (int i = 0; i < 6; i++) S.tq[i] = 0.0;
+            for (int i = 0; i <= QMAX; i++) S.l[i] = 0.0;
+            S.saved_tq5 = 0.0; S.crate = 1.0; S.gammap = 0.0; S.gamrat = 1.0; S.acnrm = 0.0;
+            W.setEwt(z0);
+            int status = ST_OK;
+            if (!W.rhs(z0, W.Z(1), S)) status = ST_NONFINITE;
+            if (status == ST_OK) {
+                double h0 = W.initialStep(S, p.tout);
+                double* z1 = W.Z(1);
+                for (int i = lane; i < N; i += 32) z1[i] *= h0;
+                __syncwarp();
+                S.h = S.hscale = S.hprime = h0;
+                S.eta = 1.0;
+                S.q = S.qprime = 1; S.L = 2; S.qwait = 2; S.etamax = ETA_MAX_FIRST;
+                S.tau[1] = h0;
+                W.recordSample(S, S.tn, z1[0] / h0);
+            } else {
+                S.h = S.hscale = S.hprime = 0.0;
+                S.q = S.qprime = 1; S.L = 2; S.qwait = 2; S.etamax = ETA_MAX_FIRST; S.eta = 1.0;
+            }
+            S.status0 = status;
+        } else {
+            for (int i = lane; i < (QMAX + 1) * N; i += 32) W.zn[i] = rec[i];
+            __syncwarp();
+            S.tn = rs[R_TN]; S.h = rs[R_H]; S.hscale = rs[R_HSCALE]; S.hprime = rs[R_HPRIME];
+            S.eta = rs[R_ETA]; S.etamax = rs[R_ETAMAX];
+            for (int i = 0; i < QMAX + 2; i++) S.tau[i] = rs[R_TAU + i];
+            for (int i = 0; i < 6; i++) S.tq[i] = rs[R_TQ + i];
+            for (int i = 0; i <= QMAX; i++) S.l[i] = rs[R_L + i];
+            S.gammap = rs[R_GAMMAP]; S.crate = rs[R_CRATE]; S.saved_tq5 = rs[R_SAVEDTQ5];
+            S.ls_t = rs[R_IGN + 0]; S.ls_v = rs[R_IGN + 1]; S.pv_t = rs[R_IGN + 2]; S.pv_v = rs[R_IGN + 3];
+            S.bs_t = rs[R_IGN + 4]; S.bs_v = rs[R_IGN + 5]; S.nx_t = rs[R_IGN + 6]; S.nx_v = rs[R_IGN + 7];
+            S.q = (int)rs[R_Q]; S.qprime = (int)rs[R_QPRIME]; S.qwait = (int)rs[R_QWAIT];
+            S.nst = (int)rs[R_NST]; S.nstlp = (int)rs[R_NSTLP]; S.nsamp = (int)rs[R_NSAMP];
+            S.flags = (int)rs[R_FLAGS];
+            S.L = S.q + 1;
+            S.haveLU = false;   // the factorisation is not kept between advance calls
+            S.gamrat = 1.0; S.acnrm = 0.0;
+            S.nrhs = stt[1]; S.nni = stt[2]; S.nsetups = stt[3]; S.nje = stt[4]; S.netf = stt[5]; S.ncfn = stt[6];
+            S.status0 = (int)rs[R_STATUS];
+        }
+        int status = S.status0;
+        long long count = 0;
+        while (status == ST_OK && S.tn < p.tout) {
+            if (count >= p.maxSteps) { status = ST_MAX_STEPS; break; }
+            status = W.step<MT>(M, S);
+            count++;
+        }
+        // output: interpolate to tout (or the last state on failure)
+        const double sfac = (status == ST_OK && S.h != 0.0) ? (p.tout - S.tn) / S.h : 0.0;
+        for (int i = lane; i < N; i += 32) {
+            double v = W.zn[(size_t)S.q * N + i];
+            for (int j = S.q - 1; j >= 0; j--) v = W.zn[(size_t)j * N + i] + sfac * v;
+            if (status != ST_OK) v = W.zn[i];
+            if (i == 0) p.T[r] = v;
+            else p.Y[(size_t)(i - 1) * p.n + r] = v;
+        }
+        // save the integrator record
+        for (int i = lane; i < (QMAX + 1) * N; i += 32) rec[i] = W.zn[i];
+        if (lane == 0) {
+            double* o = rec + (QMAX + 1) * N;
+            o[R_TN] = S.tn; o[R_H] = S.h; o[R_HSCALE] = S.hscale; o[R_HPRIME] = S.hprime;
+            o[R_ETA] = S.eta; o[R_ETAMAX] = S.etamax;
+            for (int i = 0; i < QMAX + 2; i++) o[R_TAU + i] = S.tau[i];
+            for (int i = 0; i < 6; i++) o[R_TQ + i] = S.tq[i];
+            for (int i = 0; i <= QMAX; i++) o[R_L + i] = S.l[i];
+            o[R_GAMMAP] = S.gammap; o[R_CRATE] = S.crate; o[R_SAVEDTQ5] = S.saved_tq5;
+            o[R_IGN + 0] = S.ls_t; o[R_IGN + 1] = S.ls_v; o[R_IGN + 2] = S.pv_t; o[R_IGN + 3] = S.pv_v;
+            o[R_IGN + 4] = S.bs_t; o[R_IGN + 5] = S.bs_v; o[R_IGN + 6] = S.nx_t; o[R_IGN + 7] = S.nx_v;
+            o[R_Q] = S.q; o[R_QPRIME] = S.qprime; o[R_QWAIT] = S.qwait; o[R_NST] = S.nst;
+            o[R_NSTLP] = S.nstlp; o[R_NSAMP] = S.nsamp; o[R_FLAGS] = S.flags; o[R_STATUS] = status;
+            stt[0] = S.nst; stt[1] = S.nrhs; stt[2] = S.nni; stt[3] = S.nsetups; stt[4] = S.nje;
+            stt[5] = S.netf; stt[6] = S.ncfn; stt[7] = S.q;
+            p.status[r] = status;
+            p.tign[r] = W.ignitionTime(S);
+        }
+        __syncwarp();
+    }
+}
+
+template __global__ void k_bdf<double>(BdfParams);
+template __global__ void k_bdf<float>(BdfParams);
+
+int bdfRecordStride(int N) { return (QMAX + 1) * N + R_NSCAL; }
+
+int bdfWarpDoubles(const DevMech& m, int ld, bool fp32) {
+    int N = m.N;
+    int kinD = 5 * m.K + 3 * m.R + 2 * m.NTB + m.NF;
+    int vec = (QMAX + 1) * N + 7 * N + (N + 1) / 2;
+    int mat = fp32 ? (N * ld + 1) / 2 : N * ld;
+    int tot = kinD + vec + mat;
+    return (tot + 1) & ~1;   // keep each warp's slice 16-byte aligned
+}
+
+int ratesWarpDoubles(const DevMech& m) {
+    int kinD = 5 * m.K + 3 * m.R + 2 * m.NTB + m.NF;
+    int tot = kinD + 2 * m.K + m.K * (m.K + 1);
+    return (tot + 1) & ~1;
+}
+
+cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
+    size_t smem = (size_t)p.warpDoubles * 8 * warpsPerBlock;
+    cudaError_t e = cudaFuncSetAttribute(k_rates, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_rates<<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream) {
+    size_t smem = (size_t)p.warpDoubles * 8 * warpsPerBlock;
+    cudaError_t e;
+    if (fp32) {
+        e = cudaFuncSetAttribute(k_bdf<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_bdf<float><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
+    } else {
+        e = cudaFuncSetAttribute(k_bdf<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_bdf<double><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace gbchem

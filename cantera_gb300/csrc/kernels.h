@@ -1,0 +1,48 @@
+// kernels.h - launch interface between the host library (capi.cu) and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "devmech.h"
+
+namespace gbchem {
+
+struct RatesParams {
+    DevMech m;
+    int n;
+    const double* T;
+    const double* P;
+    const double* Y;      // [K][n]
+    double* wdot;         // [K][n] or null
+    double* jac;          // [nnz][n] or null
+    int* counter;         // work counter (zeroed before launch)
+    int warpDoubles;      // shared-memory doubles per warp
+};
+
+struct BdfParams {
+    DevMech m;
+    int n;
+    double t0, tout;
+    double rtol, atol, hmaxInv;
+    int maxSteps, maxOrder;
+    const double* P;      // [n]
+    double* T;            // [n]   in: initial state of fresh reactors; out: T(tout)
+    double* Y;            // [K][n]
+    double* rec;          // [n][recStride] integrator records (flags 0 = fresh)
+    int recStride;
+    long long* stats;     // [n][8]
+    int* status;          // [n]
+    double* tign;         // [n]
+    int* counter;         // work counter (zeroed before launch)
+    const int* order;     // [n] queue order (null: identity)
+    int ld;               // leading dimension of the Newton matrix
+    int warpDoubles;
+};
+
+int bdfRecordStride(int N);
+int bdfWarpDoubles(const DevMech& m, int ld, bool fp32);
+int ratesWarpDoubles(const DevMech& m);
+cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
+cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream);
+
+}  // namespace gbchem

@@ -1,0 +1,314 @@
+// kinetics.cuh - warp-cooperative FP64 kinetics for one gas state per warp.
+//
+// One warp owns one state (T, P, Y[K]): lanes stride over species for thermo and the
+// production-rate gather, over reactions for the rate constants and rates of progress,
+// and over Jacobian columns for d(wdot)/dc.  Per-state scratch lives in the warp's slice
+// of shared memory.  Operation semantics follow the reference:
+//   NASA7                     include/cantera/thermo/NasaPoly1.h:103-122, NasaPoly2.h:105-112
+//   state (no normalisation)  src/thermo/Phase.cpp:362-372,501-505; IdealGasPhase.h:338-354
+//   chemical potentials       src/thermo/IdealGasPhase.cpp:59-66
+//   Kc and reverse rates      src/kinetics/BulkKinetics.cpp:465-484,562-569
+//   third bodies              include/cantera/kinetics/ThirdBodyCalc.h:75-92
+//   Arrhenius                 include/cantera/kinetics/Arrhenius.h:196-198
+//   falloff                   include/cantera/kinetics/Falloff.h:154-176; src/kinetics/Falloff.cpp:283-300
+//   mass action + sign rules  include/cantera/kinetics/StoichManager.h:131-480
+//   d(wdot)/dc                src/kinetics/BulkKinetics.cpp:712-811; StoichManager.h:164-168,227-236,300-312,406-430
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "devmech.h"
+
+namespace gbchem {
+
+__device__ __forceinline__ double warpSum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warpMax(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Per-state scratch in shared memory (sizes in doubles: K, K, K, K, K, R, R, R, NTB, NTB, NF).
+struct KinScratch {
+    double* c;      // concentrations [K]
+    double* cpR;    // cp/R [K]
+    double* hRT;    // h/RT [K]
+    double* g;      // g/RT + ln(P/Pref) [K]
+    double* wdot;   // [K]
+    double* rop;    // net rate of progress [R]
+    double* kfe;    // forward coefficient times [M] for mass-action three-body reactions [R]
+    double* rkc;    // 1/Kc (0 for irreversible) [R]
+    double* Mtb;    // third-body concentrations [NTB]
+    double* Qtb;    // d(rop)/d[M] per third-body reaction [NTB]
+    double* dlk;    // d ln k / d[M] of falloff reactions [NF]
+    __device__ static int doubles(int K, int R, int NTB, int NF) { return 5 * K + 3 * R + 2 * NTB + NF; }
+    __device__ void carve(double* p, int K, int R, int NTB, int NF) {
+        c = p; p += K; cpR = p; p += K; hRT = p; p += K; g = p; p += K; wdot = p; p += K;
+        rop = p; p += R; kfe = p; p += R; rkc = p; p += R;
+        Mtb = p; p += NTB; Qtb = p; p += NTB; dlk = p;
+    }
+};
+
+// Scalars of the current state, identical in every lane.
+struct KinState {
+    double T, P, RT, rho, mmw, ctot, lnT, recipT;
+};
+
+// mass-action product of one side (expanded species list e, count n = e.w) with the
+// StoichManager sign rules; `gen` selects the general power-law list (CN bucket).
+__device__ __forceinline__ double massAction(const DevMech& m, int bucket, int4 e, int side,
+                                             const double* c) {
+    if (bucket == 1) return c[e.x];
+    if (bucket == 2) {
+        double a = c[e.x], b = c[e.y];
+        return (a < 0 && b < 0) ? 0.0 : a * b;
+    }
+    if (bucket == 3) {
+        double a = c[e.x], b = c[e.y], d = c[e.z];
+        if ((a < 0 && (b < 0 || d < 0)) || (b < 0 && d < 0)) return 0.0;
+        return a * b * d;
+    }
+    double r = 1.0;
+    for (int q = m.sidePtr[side]; q < m.sidePtr[side + 1]; q++) {
+        double o = m.sideOrd[q];
+        if (o != 0.0) {
+            double x = c[m.sideK[q]];
+            if (x > 0.0) r *= pow(x, o);
+            else return 0.0;
+        }
+    }
+    return r;
+}
+
+// d(mass-action product)/dc_j with the StoichManager derivative rules.
+__device__ __forceinline__ double massActionDeriv(const DevMech& m, int bucket, int4 e, int side,
+                                                  const double* c, int j) {
+    if (bucket == 1) return (e.x == j) ? 1.0 : 0.0;
+    if (bucket == 2) {
+        double d = 0.0;
+        if (e.x == j && c[e.y] > 0) d += c[e.y];
+        if (e.y == j && c[e.x] > 0) d += c[e.x];
+        return d;
+    }
+    if (bucket == 3) {
+        double a = c[e.x], b = c[e.y], f = c[e.z], d = 0.0;
+        if (e.x == j && b > 0 && f > 0) d += b * f;
+        if (e.y == j && a > 0 && f > 0) d += a * f;
+        if (e.z == j && a > 0 && b > 0) d += a * b;
+        return d;
+    }
+    double d = 0.0;
+    int q0 = m.sidePtr[side], q1 = m.sidePtr[side + 1];
+    for (int q = q0; q < q1; q++) {
+        if (m.sideK[q] != j) continue;
+        double oi = m.sideOrd[q];
+        double x = c[j];
+        if (!(x > 0.0) || oi == 0.0) continue;
+        double prod = oi * pow(x, oi - 1.0);
+        for (int p = q0; p < q1; p++) {
+            if (p == q) continue;
+            double y = c[m.sideK[p]];
+            if (y > 0) prod *= pow(y, m.sideOrd[p]);
+            else { prod = 0.0; break; }
+        }
+        d += prod;
+    }
+    return d;
+}
+
+__device__ __forceinline__ double arrhenius(double A, double b, double EaR, double lnT, double recipT) {
+    return A * exp(b * lnT - EaR * recipT);
+}
+
+// Falloff rate k(T, M) and, optionally, d ln k / d M (analytic).
+__device__ __forceinline__ double falloff(D4 f1, D4 f2, double A, double b, double EaR,
+                                          const KinState& st, double M, double* dlnk_dM) {
+    double work = 0.0;
+    bool troe = f2.w != 0.0;
+    if (troe) {
+        double Fcent = (1.0 - f1.w) * exp(-st.T * f2.x) + f1.w * exp(-st.T * f2.y);
+        if (f2.z != 0.0) Fcent += exp(-f2.z / st.T);
+        work = log10(fmax(Fcent, 1e-300));
+    }
+    double klow = arrhenius(f1.x, f1.y, f1.z, st.lnT, st.recipT);
+    double khigh = arrhenius(A, b, EaR, st.lnT, st.recipT);
+    double dPr = klow / (khigh + 1e-300);
+    double pr = M * dPr;
+    double F = 1.0, dFdPr_over_F = 0.0;
+    if (troe) {
+        double lpr = log10(fmax(pr, 1e-300));
+        double cc = -0.4 - 0.67 * work;
+        double nn = 0.75 - 1.27 * work;
+        double u = lpr + cc;
+        double den = nn - 0.14 * u;
+        double f1v = u / den;
+        double q = 1.0 + f1v * f1v;
+        double lgf = work / q;
+        F = pow(10.0, lgf);
+        if (pr > 1e-300) dFdPr_over_F = (-work * 2.0 * f1v / (q * q) * (nn / (den * den))) / pr;
+    }
+    double k = pr * (F / (1.0 + pr)) * khigh;
+    if (dlnk_dM) {
+        // k = khigh * Pr/(1+Pr) * F(Pr): dk/dM = khigh*dPr*(F/(1+Pr)^2 + Pr/(1+Pr)*dF/dPr)
+        double s = 1.0 / (1.0 + pr);
+        double dk = khigh * dPr * (s * s * F + pr * s * F * dFdPr_over_F);
+        *dlnk_dM = (k != 0.0) ? dk / k : 0.0;
+    }
+    return k;
+}
+
+// Mixture state from (T, P, Y).  Y may alias any readable [K] array.
+__device__ __forceinline__ void warpState(const DevMech& m, double T, double P, const double* Y,
+                                          KinScratch& s, KinState& st, int lane) {
+    double part = 0.0;
+    for (int k = lane; k < m.K; k += 32) {
+        double ym = Y[k] * m.rmw[k];
+        s.c[k] = ym;
+        part += ym;
+    }
+    double sum = warpSum(part);
+    st.T = T;
+    st.P = P;
+    st.RT = T * m.Rgas;
+    st.mmw = 1.0 / sum;
+    st.rho = P * st.mmw / st.RT;
+    st.ctot = st.rho / st.mmw;
+    st.lnT = log(T);
+    st.recipT = 1.0 / T;
+    __syncwarp();
+    for (int k = lane; k < m.K; k += 32) s.c[k] *= st.rho;
+}
+
+// Species thermo + rates of progress + net production rates.  With `forJac`, also the
+// per-reaction data d(wdot)/dc needs (Qtb, dlk).
+template <bool forJac>
+__device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, int lane) {
+    const double lnPP = log(st.P / m.Pref);
+    for (int k = lane; k < m.K; k += 32) {
+        const double* a = m.nasa + (size_t)k * kNasaStride;
+        const double* p = (st.T <= a[0]) ? a + 1 : a + 8;
+        double T = st.T;
+        double t2 = T * T, t3 = t2 * T, t4 = t3 * T;
+        double ct0 = p[0], ct1 = p[1] * T, ct2 = p[2] * t2, ct3 = p[3] * t3, ct4 = p[4] * t4;
+        double cp = ct0 + ct1 + ct2 + ct3 + ct4;
+        double h = ct0 + 0.5 * ct1 + (1.0 / 3.0) * ct2 + 0.25 * ct3 + 0.2 * ct4 + p[5] * st.recipT;
+        double sR = ct0 * st.lnT + ct1 + 0.5 * ct2 + (1.0 / 3.0) * ct3 + 0.25 * ct4 + p[6];
+        s.cpR[k] = cp;
+        s.hRT[k] = h;
+        s.g[k] = (h - sR) + lnPP;
+    }
+    __syncwarp();
+    for (int t = lane; t < m.NTB; t += 32) {
+        double sum = 0.0;
+        for (int q = m.tbPtr[t]; q < m.tbPtr[t + 1]; q++) sum += m.tbE[q] * s.c[m.tbK[q]];
+        s.Mtb[t] = m.tbDef[t] * st.ctot + sum;
+    }
+    __syncwarp();
+    const double logStandConc = log(st.P / st.RT);
+    for (int i = lane; i < m.R; i += 32) {
+        int4 info = __ldg(&m.rinfo[i]);
+        D4 ar = m.rarr[i];
+        int kind = info.x & kKindMask;
+        double kf;
+        double dlnk = 0.0;
+        if (kind <= 1) {
+            kf = arrhenius(ar.x, ar.y, ar.z, st.lnT, st.recipT);
+        } else {
+            D4 f1 = m.fo1[info.z];
+            D4 f2 = m.fo2[info.z];
+            double M = s.Mtb[info.y];
+            kf = falloff(f1, f2, ar.x, ar.y, ar.z, st, M, forJac ? &dlnk : nullptr);
+            // the reference sets this derivative to zero unless k != 0 and [M] > 0
+            if (!(M > 0.0) || kf == 0.0) dlnk = 0.0;
+            if (forJac) s.dlk[info.z] = dlnk;
+        }
+        double kfe = (kind == 1) ? kf * s.Mtb[info.y] : kf;
+        int4 re = __ldg(&m.rk[i]);
+        int4 pe = __ldg(&m.pk[i]);
+        int rb = (info.x >> kRBucketShift) & 7, pb = (info.x >> kPBucketShift) & 7;
+        double rkc = 0.0;
+        double fwd = massAction(m, rb, re, 2 * i, s.c);
+        double rev = 0.0;
+        if (info.x & kRevBit) {
+            // Delta G / RT over the expanded species lists (products minus reactants)
+            double dG = 0.0;
+            if (pb != 0) {
+                dG = s.g[pe.x];
+                if (pe.w > 1) dG += s.g[pe.y];
+                if (pe.w > 2) dG += s.g[pe.z];
+            } else {
+                for (int q = m.sidePtr[2 * i + 1]; q < m.sidePtr[2 * i + 2]; q++) dG += m.sideNu[q] * s.g[m.sideK[q]];
+            }
+            double dr = 0.0;
+            if (rb != 0) {
+                dr = s.g[re.x];
+                if (re.w > 1) dr += s.g[re.y];
+                if (re.w > 2) dr += s.g[re.z];
+            } else {
+                for (int q = m.sidePtr[2 * i]; q < m.sidePtr[2 * i + 1]; q++) dr += m.sideNu[q] * s.g[m.sideK[q]];
+            }
+            dG -= dr;
+            rkc = fmin(exp(dG - ar.w * logStandConc), 1e300);
+            rev = massAction(m, pb, pe, 2 * i + 1, s.c);
+        }
+        double ropf = kfe * fwd;
+        double ropr = (kfe * rkc) * rev;
+        s.rop[i] = ropf - ropr;
+        if (forJac) {
+            s.kfe[i] = kfe;
+            s.rkc[i] = rkc;
+            if (kind == 1) s.Qtb[info.y] = kf * (fwd - rkc * rev);
+            else if (kind >= 2) s.Qtb[info.y] = kf * dlnk * (fwd - rkc * rev);
+        }
+    }
+    __syncwarp();
+    for (int k = lane; k < m.K; k += 32) {
+        double w = 0.0;
+        for (int q = m.spPtr[k]; q < m.spPtr[k + 1]; q++) w += m.spNu[q] * s.rop[m.spRxn[q]];
+        s.wdot[k] = w;
+    }
+    __syncwarp();
+}
+
+// d(wdot)/dc without the dense default-efficiency part: Jc[k*ld + j] (+)= ... for
+// k, j < K.  The dense part is g_k * (1 for every column); warpDenseG returns g in gout.
+// The caller zeroes Jc.  MT is the matrix element type (double or float).
+template <typename MT>
+__device__ void warpJacC(const DevMech& m, const KinScratch& s, MT* Jc, int ld, int lane) {
+    for (int q = m.laneColPtr[lane]; q < m.laneColPtr[lane + 1]; q++) {
+        int j = m.laneCols[q];
+        for (int e = m.colPtr[j]; e < m.colPtr[j + 1]; e++) {
+            int i = m.colRxn[e];
+            int4 info = __ldg(&m.rinfo[i]);
+            int rb = (info.x >> kRBucketShift) & 7, pb = (info.x >> kPBucketShift) & 7;
+            double kfe = s.kfe[i];
+            double dF = kfe * massActionDeriv(m, rb, __ldg(&m.rk[i]), 2 * i, s.c, j);
+            if (info.x & kRevBit) dF -= (kfe * s.rkc[i]) * massActionDeriv(m, pb, __ldg(&m.pk[i]), 2 * i + 1, s.c, j);
+            double ep = m.colE[e];
+            if (ep != 0.0) dF += ep * s.Qtb[info.y];
+            if (dF == 0.0) continue;
+            for (int r = m.rsPtr[i]; r < m.rsPtr[i + 1]; r++) {
+                MT* p = Jc + (size_t)m.rsK[r] * ld + j;
+                *p = (MT)((double)*p + m.rsNu[r] * dF);
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// g_k = sum over third-body reactions i with default efficiency d_i of S_net[k][i]*d_i*Q_i:
+// the part of d(wdot_k)/dc_j that is the same for every column j.
+__device__ __forceinline__ void warpDenseG(const DevMech& m, const KinScratch& s, double* gout, int lane) {
+    for (int k = lane; k < m.K; k += 32) {
+        double g = 0.0;
+        for (int q = m.gsPtr[k]; q < m.gsPtr[k + 1]; q++) g += m.gsCoef[q] * s.Qtb[m.gsTb[q]];
+        gout[k] = g;
+    }
+    __syncwarp();
+}
+
+}  // namespace gbchem

@@ -1,0 +1,114 @@
+/* gbchem.h - C ABI of the GB300 batched chemistry engine.
+ *
+ * A batched drop-in behind Cantera's hot path for many independent, constant-pressure,
+ * ideal-gas reactors.  The verbs and conventions mirror Cantera's generated C interface
+ * (CLib): int32 handles, an int32 status where 0 means success and GB_ERR (-999) an
+ * error whose message gb_get_error() returns, and no exception crossing the ABI
+ * (reference: interfaces/clib/include/cantera_clib/clib_defs.h ERR = -999;
+ * interfaces/clib/src/clib_utils.h:32-52 handleAllExceptions).
+ *
+ * Array layout: state batches are species-major, Y[k*n + s] for species k of state s
+ * (T[s], P[s] one value per state).  Pointers are host pointers unless `flags` has
+ * GB_DEVICE_POINTERS, in which case they are CUDA device pointers on the engine's
+ * device.  Every call returns after the GPU work it starts has finished.
+ *
+ * Threading: a handle is used by one host thread at a time; distinct handles may be
+ * used from distinct threads.  The last error message is kept per host thread.
+ */
+#ifndef GBCHEM_H
+#define GBCHEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB_ERR (-999)
+#define GB_DEVICE_POINTERS 1
+
+/* ---- mechanisms -------------------------------------------------------------------
+ * gb_mech_load replaces newSolution(yaml, phase, "none") (src/base/Solution.cpp:242-330)
+ * for ideal-gas phases with NASA7 thermo and elementary / three-body / Lindemann / Troe
+ * reactions.  Returns a handle >= 0 or GB_ERR. */
+int32_t gb_mech_load(const char* yaml_path, const char* phase_name);
+int32_t gb_mech_del(int32_t mech);
+int32_t gb_mech_n_species(int32_t mech);                  /* Kinetics::nTotalSpecies */
+int32_t gb_mech_n_reactions(int32_t mech);                /* Kinetics::nReactions */
+int32_t gb_mech_species_name(int32_t mech, int32_t k, int32_t buflen, char* buf);
+int32_t gb_mech_species_index(int32_t mech, const char* name);  /* -1 if absent */
+int32_t gb_mech_molecular_weights(int32_t mech, int32_t buflen, double* mw);
+
+/* ---- kinetics ----------------------------------------------------------------------
+ * Batched Kinetics::getNetProductionRates (src/kinetics/Kinetics.cpp:447-457; CLib
+ * kin_getNetProductionRates, interfaces/sourcegen/src/sourcegen/headers/ctkin.yaml:46).
+ * n states (T [K], P [Pa], unnormalised mass fractions Y[K][n]) -> wdot[K][n] kmol/m^3/s.
+ * bufLen must be >= K*n. */
+int32_t gb_kin_net_production_rates(int32_t mech, int32_t n, const double* T, const double* P,
+                                    const double* Y, int32_t bufLen, double* wdot, int32_t flags);
+
+/* Structural nonzeros of d(wdot)/d(c) as compressed sparse columns (colptr[K+1],
+ * rowidx[nnz], rows ascending in each column).  gb_kin_jac_nnz returns nnz. */
+int32_t gb_kin_jac_nnz(int32_t mech);
+int32_t gb_kin_jac_pattern(int32_t mech, int32_t ncolptr, int32_t* colptr, int32_t nnz, int32_t* rowidx);
+
+/* Batched Kinetics::netProductionRates_ddCi (src/kinetics/BulkKinetics.cpp:794-811;
+ * include/cantera/kinetics/Kinetics.h:1148): d(wdot_k)/d(c_j) at constant T and other
+ * concentrations, values vals[p*n + s] on the pattern above (p = slot).  The falloff
+ * [M]-dependence is differentiated analytically (the reference uses a one-sided
+ * difference with delta 1e-8).  wdot may be NULL; if not, wdot[K][n] is written too. */
+int32_t gb_kin_net_production_rates_ddCi(int32_t mech, int32_t n, const double* T, const double* P,
+                                         const double* Y, int32_t nnz, double* vals, double* wdot,
+                                         int32_t flags);
+
+/* ---- batched reactor network ------------------------------------------------------------
+ * gb_net_* replace ReactorNet over IdealGasConstPressureReactor (src/zeroD/ReactorNet.cpp:
+ * 37-357; CLib reactornet_advance, headers/ctreactornet.yaml:19-20): n independent reactors,
+ * each integrated by a variable-order (1..5) BDF method with modified Newton and a dense LU
+ * of I - gamma*J, per-reactor step and order control. */
+typedef struct {
+    double rtol;            /* ReactorNet::setRelativeTolerance; default 1e-9 */
+    double atol;            /* ReactorNet::setAbsoluteTolerance; default 1e-15 */
+    int32_t max_steps;      /* ReactorNet::setMaxSteps (per advance call); default 20000 */
+    int32_t max_order;      /* 1..5; default 5 */
+    double max_time_step;   /* ReactorNet::setMaxTimeStep; 0 = unlimited */
+    int32_t lu_precision;   /* 64: factor I - gamma*J in FP64; 32: in FP32 (residual, RHS,
+                               error norm and step control stay FP64) */
+    int32_t warps_per_block;/* reactors per thread block; 0 = autotuned */
+    int32_t use_graph;      /* 1: launch the advance through a captured CUDA graph */
+} gb_net_options;
+
+void gb_net_default_options(gb_net_options* opts);
+int32_t gb_net_new(int32_t mech, int32_t n, const gb_net_options* opts);
+int32_t gb_net_del(int32_t net);
+/* Set the initial state of every reactor and restart the integrators at time 0
+ * (IdealGasConstPressureReactor::getState; ReactorNet::reinitialize). */
+int32_t gb_net_set_state(int32_t net, const double* T, const double* P, const double* Y, int32_t flags);
+/* Advance every reactor to time t (ReactorNet::advance: step past t, interpolate back).
+ * Returns the number of reactors whose integration failed (status != 0), or GB_ERR. */
+int32_t gb_net_advance(int32_t net, double t);
+double gb_net_time(int32_t net);
+int32_t gb_net_get_state(int32_t net, double* T, double* Y, int32_t flags);
+
+/* Per-reactor status: 0 ok, 1 max steps, 2 repeated error-test failures, 3 repeated
+ * convergence failures, 4 non-finite state, 5 step size too small. */
+enum { GB_OK = 0, GB_MAX_STEPS = 1, GB_ERR_TEST_FAILS = 2, GB_CONV_FAILS = 3,
+       GB_NONFINITE = 4, GB_H_TOO_SMALL = 5 };
+int32_t gb_net_get_status(int32_t net, int32_t* status);
+
+/* Counters per reactor, stats[s*GB_NSTAT + i] (CVodesIntegrator::solverStats names). */
+enum { GB_STAT_STEPS = 0, GB_STAT_RHS, GB_STAT_NEWTON, GB_STAT_SETUPS, GB_STAT_JACS,
+       GB_STAT_ERRFAIL, GB_STAT_CONVFAIL, GB_STAT_ORDER, GB_NSTAT };
+int32_t gb_net_solver_stats(int32_t net, int64_t* stats);
+
+/* Time of the largest dT/dt seen at accepted steps since gb_net_set_state, refined by the
+ * vertex of the parabola through that step and its accepted neighbours. */
+int32_t gb_net_ignition_times(int32_t net, double* tign);
+
+/* Copy the most recent error message (thread-local) into buf; returns its length. */
+int32_t gb_get_error(int32_t buflen, char* buf);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBCHEM_H */
