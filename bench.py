@@ -1,0 +1,351 @@
+#!/usr/bin/env python3
+"""Benchmark: GRI-30 constant-pressure reactors advanced per second on one GB300.
+
+Workload (uneven stiffness): gri30.yaml, 65,536 independent ideal-gas constant-pressure
+reactors, T0 ~ U[700, 1800] K, P log-uniform in [1, 40] atm, CH4/air with equivalence
+ratio ~ U[0.5, 1.5] (seed 20261203 + 2), each advanced from t = 0 to 1e-2 s at rtol 1e-8,
+atol 1e-15 in one persistent launch with a device work queue.  Some reactors ignite, the
+cold ones stay nearly inert.  A "step" re-initialises every reactor and advances all of
+them to 1e-2 s.  Inputs are synthetic (no dataset is involved).
+
+Usage:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Under torchrun each rank takes a contiguous shard of the reactors (no collective on the
+data path); the time is the maximum over ranks.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GRI-30 reactors advanced/s on 1 GB300: FP64 BDF vs FP32-LU and NN+fallback @err"
+WL = dict(mechanism="gri30.yaml", phase="gri30", n=65536, t_end=1e-2, rtol=1e-8, atol=1e-15,
+          T0=(700.0, 1800.0), P_atm=(1.0, 40.0), phi=(0.5, 1.5), fuel="CH4:1",
+          oxidizer="O2:1, N2:3.76", seed=20261203 + 2)
+CPU_SAMPLE = 256          # reactors in the bounded CPU sample (a seeded subset of the workload)
+
+
+def workload_arrays(n, seed, eqr):
+    """T0 [n], P [n], Y0 [n, K] (reactor-major); eqr(phi) -> Y."""
+    rng = np.random.default_rng(seed)
+    T0 = rng.uniform(*WL["T0"], n)
+    P = 101325.0 * 10 ** rng.uniform(math.log10(WL["P_atm"][0]), math.log10(WL["P_atm"][1]), n)
+    phi = rng.uniform(*WL["phi"], n)
+    Y0 = np.array([eqr(p) for p in phi])
+    return T0, P, Y0
+
+
+def cpu_sample_indices(n, size, seed):
+    rng = np.random.default_rng(seed + 1000)
+    return np.sort(rng.choice(n, min(size, n), replace=False))
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                try:
+                    rows.append((float(f[1]), float(f[2]), f[5], f[6], f[7], f[8]))
+                except ValueError:
+                    pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(r[0] for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[2 + i].lower().startswith("active")})
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": rows[0][1], "reasons": reasons,
+                "samples": len(rows)}
+
+
+def flop_model(st, fp, N):
+    """FP64 operations per evaluation of each integrator component (FMA = 2 flops; exp and
+    log at their measured FMA-equivalent cost).  Returns a dict of per-unit FLOPs."""
+    E = 2.0 * fp["exp_fma"]
+    Lg = 2.0 * fp["log_fma"]
+    Pw = E + Lg
+    Dv = 8.0
+    K, R = st["K"], st["R"]
+    rhs = (3 * K + 20 + 25 * K + 3 * Lg + 2 * st["tb_entries"] + 2 * st["three_body"]
+           + R * (4 + E + 6)
+           + st["falloff"] * (4 + E + 14 + Dv)
+           + st["troe"] * (3 * E + 2 * Lg + Pw + 26)
+           + st["reversible"] * (10 + E)
+           + 2 * st["gather_entries"] + 4 * K + 10 + Dv)
+    jac = 6 * st["jac_col_entries"] + 2 * st["jac_scatter_entries"] + 10 * K * K + 10 * K + 3 * N * N
+    lu = (2.0 / 3.0) * N ** 3 + N * Dv
+    newton = 2 * N * N + 9 * N
+    step = 40 * N + 4 * E
+    return {"rhs": rhs, "jac": jac, "lu": lu, "newton": newton, "step": step}
+
+
+def algorithmic_flops(stats, fm, fp32_lu):
+    """Total FP64 FLOPs (and FP32 FLOPs for the mixed form) from per-reactor counters."""
+    nrhs = stats["rhs_evals"].sum()
+    nset = stats["lin_setups"].sum()
+    nni = stats["newton_iters"].sum()
+    nst = stats["steps"].sum()
+    f64 = nrhs * fm["rhs"] + nset * fm["jac"] + nst * fm["step"]
+    f32 = 0.0
+    if fp32_lu:
+        f32 = nset * fm["lu"] + nni * fm["newton"]
+    else:
+        f64 += nset * fm["lu"] + nni * fm["newton"]
+    return float(f64), float(f32)
+
+
+def read_traffic():
+    """DRAM bytes per launch of the integrator kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_bdf_gri30_uneven.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":")[1].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+def cpu_baseline(T0, P, Y0, idx, threads, kind="port"):
+    """The CPU restatement of the reference path on this host's cores: the reference's
+    ReactorNet settings (difference-quotient Jacobian kept between setups) on a bounded,
+    seeded sample of the same workload."""
+    from oracle import pyoracle as po
+    m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", WL["mechanism"]), WL["phase"])
+    o = po.opts(rtol=WL["rtol"], atol=WL["atol"], analytic=False, jac_reuse=True)
+    t0 = time.perf_counter()
+    T, Y, st, tig = m.advance_batch(T0[idx], P[idx], Y0[idx], WL["t_end"], o, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": len(idx) / dt, "unit": "reactors/s", "cores": threads, "kind": kind,
+            "sample": "%d seeded reactors of the workload (subset seed %d), oracle restatement of the "
+                      "reference path (not the reference binary), %d host threads, %.1f s"
+                      % (len(idx), WL["seed"] + 1000, threads, dt)}, (T, Y, st, tig)
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    from oracle import pyoracle as po
+    m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", WL["mechanism"]), WL["phase"])
+    T0, P, Y0 = workload_arrays(WL["n"], WL["seed"],
+                                lambda p: m.equivalence_ratio(p, WL["fuel"], WL["oxidizer"]))
+    threads = os.cpu_count()
+    idx = cpu_sample_indices(WL["n"], CPU_SAMPLE, WL["seed"])
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        cb, _ = cpu_baseline(T0, P, Y0, idx, threads)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = len(idx) * len(times) / tot
+    line = {"metric": METRIC, "value": value, "unit": "reactors/s", "impl": "reference",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "gri30 uneven stiffness: %d reactors to %g s (bounded sample of %d per step)"
+                       % (WL["n"], WL["t_end"], len(idx)), "rtol": WL["rtol"], "atol": WL["atol"]},
+            "cpu_baseline": dict(cb, value=value),
+            "e2e": {"value": value, "unit": "reactors/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=WL["n"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import cantera_gb300 as gb
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+    n_all = args.n
+    sol = gb.Solution(WL["mechanism"], WL["phase"])
+    K = sol.n_species
+    T0, P, Y0 = workload_arrays(n_all, WL["seed"],
+                                lambda p: sol.equivalence_ratio_mass_fractions(p, WL["fuel"], WL["oxidizer"]))
+    # contiguous shard of this rank
+    lo, hi = (n_all * rank) // ws, (n_all * (rank + 1)) // ws
+    n = hi - lo
+    Ts, Ps, Ys = T0[lo:hi].copy(), P[lo:hi].copy(), np.ascontiguousarray(Y0[lo:hi].T)
+    dT, dP, dY = (torch.tensor(a, device=dev) for a in (Ts, Ps, Ys))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > L2 (129 MB)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+
+    def maxover(x):
+        if not pg:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        return float(t.item())
+
+    fp = gb.measure_fp64()
+    fm = flop_model(sol.structure(), fp, K + 1)
+    results = {}
+    for variant, lu in (("fp64", 64), ("fp32_lu", 32)):
+        if variant == "fp32_lu" and args.no_fp32:
+            continue
+        net = gb.ReactorNet(sol, dT, dP, dY, rtol=WL["rtol"], atol=WL["atol"], lu_precision=lu, use_graph=True)
+        for _ in range(args.warmup if variant == "fp64" else 1):
+            net.set_state(dT, dP, dY)
+            net.advance(WL["t_end"])
+        barrier()
+        steps = args.steps if variant == "fp64" else 1
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        kernel_ms = 0.0
+        with Clocks(local) as clk:
+            for i in range(steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                ev[i][0].record()
+                net.set_state(dT, dP, dY)
+                bad = net.advance(WL["t_end"])
+                ev[i][1].record()
+                torch.cuda.synchronize()
+                kernel_ms += net.last_kernel_ms
+        barrier()
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+        ms_max = maxover(ms)
+        stats = net.solver_stats
+        f64, f32 = algorithmic_flops(stats, fm, lu == 32)
+        Tg, Yg = net.get_state()
+        results[variant] = {"ms": ms_max, "steps": steps, "kernel_ms": kernel_ms, "failed": int(bad),
+                            "f64": f64, "f32": f32, "clocks": clk.summary(), "T": Tg, "Y": Yg,
+                            "stats": {k: float(v.mean()) for k, v in stats.items()}}
+        del net
+
+    # end to end through the public API with host buffers: H2D of the initial state,
+    # the advance, D2H of the final state, every step
+    net = gb.ReactorNet(sol, Ts, Ps, Ys, rtol=WL["rtol"], atol=WL["atol"], lu_precision=64, use_graph=True)
+    Th = np.empty(n)
+    Yh = np.empty((K, n))
+    barrier()
+    e2e_ms = 0.0
+    e2e_steps = 1
+    for i in range(e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        net.set_state(Ts, Ps, Ys)
+        net.advance(WL["t_end"])
+        net.get_state(Th, Yh)
+        e2e_ms += 1e3 * (time.perf_counter() - t0)
+    barrier()
+    e2e_ms = maxover(e2e_ms)
+    del net
+
+    if rank != 0:
+        if pg:
+            pg.destroy_process_group()
+        return
+    r64 = results["fp64"]
+    value = n_all * r64["steps"] / (r64["ms"] / 1e3)
+    kernel_s = r64["kernel_ms"] / 1e3 / r64["steps"]
+    achieved = r64["f64"] / r64["steps"] / kernel_s / 1e12   # this rank's launches
+    peak = fp["gflops"] / 1e3
+    line = {"metric": METRIC, "value": value, "unit": "reactors/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r64["ms"] / r64["steps"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "gri30 uneven stiffness: %d reactors, T0 U[700,1800] K, P log-U[1,40] atm, "
+                                   "CH4/air phi U[0.5,1.5], to 1e-2 s" % n_all,
+                       "rtol": WL["rtol"], "atol": WL["atol"], "seed": WL["seed"],
+                       "l2": "flushed (256 MB write) before every timed step",
+                       "launch": "persistent kernel, device work queue, CUDA graph", "shards": ws},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": read_traffic(),
+                         "peak_source": "FP64 FMA rate measured live by this run (MEASURED_PEAKS.json has no FP64 figure)",
+                         "flops_per_reactor": r64["f64"] / r64["steps"] / n_all,
+                         "exp_fma_equiv": fp["exp_fma"], "log_fma_equiv": fp["log_fma"]},
+            "clocks": r64["clocks"], "gpu_launches": args.steps,
+            "solver_stats_mean": r64["stats"], "failed_reactors": r64["failed"],
+            "e2e": {"value": n_all * e2e_steps / (e2e_ms / 1e3), "unit": "reactors/s", "steps": e2e_steps,
+                    "h2d_bytes_per_step": n * (2 + K) * 8, "d2h_bytes_per_step": n * (1 + K) * 8}}
+    if "fp32_lu" in results:
+        r32 = results["fp32_lu"]
+        line["variants"] = {"fp32_lu": {"value": n_all * r32["steps"] / (r32["ms"] / 1e3), "unit": "reactors/s",
+                                        "ms_per_step": r32["ms"] / r32["steps"],
+                                        "solver_stats_mean": r32["stats"], "failed_reactors": r32["failed"],
+                                        "clocks": r32["clocks"]}}
+    if not args.no_cpu_baseline and ws == 1:
+        idx = cpu_sample_indices(n_all, CPU_SAMPLE, WL["seed"])
+        cb, (To, Yo, sto, tio) = cpu_baseline(T0, P, Y0, idx, os.cpu_count())
+        line["cpu_baseline"] = cb
+        err = {}
+        for vname, r in results.items():
+            Tg, Yg = r["T"][idx], r["Y"][:, idx].T
+            err[vname] = {"T_max_rel": float(np.max(np.abs(Tg - To) / To)),
+                          "Y_max_abs": float(np.max(np.abs(Yg - Yo))),
+                          "major_species_max_rel": float(np.max(np.abs(Yg - Yo)[Yo > 1e-3] / Yo[Yo > 1e-3]))}
+        line["error_vs_cpu_oracle"] = err
+    print(json.dumps(line))
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -76,11 +76,16 @@ def library():
         "gb_net_set_state": (I32, [I32, P, P, P, I32]),
         "gb_net_advance": (I32, [I32, D]),
         "gb_net_time": (D, [I32]),
+        "gb_net_last_advance_ms": (D, [I32]),
         "gb_net_get_state": (I32, [I32, P, P, I32]),
         "gb_net_get_status": (I32, [I32, P]),
         "gb_net_solver_stats": (I32, [I32, P]),
         "gb_net_ignition_times": (I32, [I32, P]),
         "gb_get_error": (I32, [I32, ctypes.c_char_p]),
+        "gb_mech_structure": (I32, [I32, I32, P]),
+        "gb_mech_equivalence_ratio": (I32, [I32, D, P, P, I32, P]),
+        "gb_measure_fp64": (I32, [P]),
+        "gb_check_exp": (I32, [I32, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -88,6 +93,13 @@ def library():
         f.argtypes = args
     _lib = L
     return L
+
+
+def measure_fp64():
+    """Device FP64 FMA rate (GFLOP/s) and exp / log cost in FMA-equivalents."""
+    r = np.zeros(3)
+    _check(library().gb_measure_fp64(_ptr(r)))
+    return {"gflops": float(r[0]), "exp_fma": float(r[1]), "log_fma": float(r[2])}
 
 
 def _check(rc):
@@ -143,11 +155,41 @@ class Solution:
         _check(L.gb_kin_jac_pattern(self._h, self.n_species + 1, _ptr(self.jac_colptr), nnz,
                                      _ptr(self.jac_rowidx)))
 
+    def structure(self):
+        """Structure counts used by the FP64 operation model of the benchmark."""
+        c = np.zeros(12, dtype=np.int64)
+        _check(library().gb_mech_structure(self._h, 12, _ptr(c)))
+        keys = ["K", "R", "reversible", "falloff", "troe", "three_body", "tb_entries",
+                "gather_entries", "jac_col_entries", "jac_scatter_entries", "reac_slots", "prod_slots"]
+        return dict(zip(keys, (int(v) for v in c)))
+
     def species_index(self, name):
         k = library().gb_mech_species_index(self._h, name.encode())
         if k < 0:
             raise KeyError(name)
         return k
+
+    def composition(self, spec):
+        """'CH4:1, O2:2' -> normalised mole fractions over the species."""
+        x = np.zeros(self.n_species)
+        for item in spec.split(","):
+            name, v = item.split(":")
+            x[self.species_index(name.strip())] += float(v)
+        return x / x.sum()
+
+    def mole_to_mass(self, X):
+        y = np.asarray(X, dtype=np.float64) * self.molecular_weights
+        return y / y.sum()
+
+    def equivalence_ratio_mass_fractions(self, phi, fuel, oxidizer):
+        """Mass fractions of the fuel/oxidizer mixture with equivalence ratio phi
+        (``ThermoPhase.set_equivalence_ratio(phi, fuel, oxidizer)``, molar basis)."""
+        Y = np.zeros(self.n_species)
+        f = np.ascontiguousarray(self.composition(fuel))
+        o = np.ascontiguousarray(self.composition(oxidizer))
+        _check(library().gb_mech_equivalence_ratio(self._h, float(phi), _ptr(f), _ptr(o),
+                                                   self.n_species, _ptr(Y)))
+        return Y
 
     @property
     def jac_nnz(self):
@@ -236,6 +278,11 @@ class ReactorNet:
     @property
     def time(self):
         return library().gb_net_time(self._h)
+
+    @property
+    def last_kernel_ms(self):
+        """Device time (ms) of the integrator launch of the last advance()."""
+        return library().gb_net_last_advance_ms(self._h)
 
     def get_state(self, T=None, Y=None):
         """Temperatures [n] and mass fractions [K, n] at the current time."""

@@ -87,7 +87,13 @@ struct NetEntry {
     bool haveOrder = false;
     cudaGraphExec_t graph = nullptr;
     double graphTout = -1.0;
-    ~NetEntry() { if (graph) cudaGraphExecDestroy(graph); }
+    cudaEvent_t evA = nullptr, evB = nullptr;
+    double lastMs = 0.0;
+    ~NetEntry() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (evA) cudaEventDestroy(evA);
+        if (evB) cudaEventDestroy(evB);
+    }
 };
 
 std::mutex g_mu;
@@ -133,6 +139,27 @@ void packDevMech(MechEntry& e) {
             nasa[(size_t)k * kNasaStride + 8 + j] = m.nasaHigh[7 * k + j];
         }
     }
+    // Device reaction order: falloff (Troe, then Lindemann), three-body, reversible, then
+    // irreversible reactions, and within each group those whose rate constant needs an
+    // exponential first.  A warp evaluates 32 consecutive reactions at a time, so grouping
+    // keeps its lanes on the same code path.  Results are per species and do not depend on
+    // this order (beyond summation order).
+    auto group = [&](int i) {
+        if (m.kind[i] == kTroe) return 0;
+        if (m.kind[i] == kLindemann) return 1;
+        if (m.kind[i] == kThreeBody) return 2;
+        return m.reversible[i] ? 3 : 4;
+    };
+    auto noExp = [&](int i) { return m.kind[i] <= kThreeBody && m.b[i] == 0.0 && m.EaR[i] == 0.0; };
+    std::vector<int> perm(R), inv(R);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) {
+        int ga = group(a), gb = group(b);
+        if (ga != gb) return ga < gb;
+        return (int)noExp(a) < (int)noExp(b);
+    });
+    for (int ni = 0; ni < R; ni++) inv[perm[ni]] = ni;
+
     std::vector<int4> rinfo(R), rk(R), pk(R);
     std::vector<D4> rarr(R);
     std::vector<int> sidePtr(1, 0), sideK;
@@ -141,7 +168,8 @@ void packDevMech(MechEntry& e) {
     std::vector<int> rsPtr(1, 0), rsK;
     std::vector<double> rsNu;
     std::vector<std::map<int, double>> net(R);
-    for (int i = 0; i < R; i++) {
+    for (int ni = 0; ni < R; ni++) {
+        const int i = perm[ni];
         int flags = m.kind[i] & kKindMask;
         if (m.reversible[i]) flags |= kRevBit;
         flags |= (m.reacBucket[i] & 7) << kRBucketShift;
@@ -152,8 +180,10 @@ void packDevMech(MechEntry& e) {
             fo1.push_back(D4{m.A0[i], m.b0[i], m.Ea0R[i], m.troe[4 * i]});
             fo2.push_back(D4{m.troe[4 * i + 1], m.troe[4 * i + 2], m.troe[4 * i + 3], m.kind[i] == kTroe ? 1.0 : 0.0});
         }
-        rinfo[i] = int4{flags, m.tbOfRxn[i], fo, 0};
-        rarr[i] = D4{m.A[i], m.b[i], m.EaR[i], m.dn[i]};
+        if (m.dn[i] == std::floor(m.dn[i]) && std::fabs(m.dn[i]) <= 3.0) flags |= kDnIntBit;
+        if (noExp(i)) flags |= kNoExpBit;
+        rinfo[ni] = int4{flags, m.tbOfRxn[i], fo, 0};
+        rarr[ni] = D4{m.A[i], m.b[i], m.EaR[i], m.dn[i]};
         auto expand = [&](const int32_t* ks, const double* nus, int n) {
             int4 e4{-1, -1, -1, 0};
             int cnt = 0;
@@ -163,19 +193,19 @@ void packDevMech(MechEntry& e) {
             e4.w = cnt;
             return e4;
         };
-        rk[i] = expand(&m.reacK[m.reacPtr[i]], &m.reacNu[m.reacPtr[i]], m.reacPtr[i + 1] - m.reacPtr[i]);
-        pk[i] = expand(&m.prodK[m.prodPtr[i]], &m.prodNu[m.prodPtr[i]], m.prodPtr[i + 1] - m.prodPtr[i]);
+        rk[ni] = expand(&m.reacK[m.reacPtr[i]], &m.reacNu[m.reacPtr[i]], m.reacPtr[i + 1] - m.reacPtr[i]);
+        pk[ni] = expand(&m.prodK[m.prodPtr[i]], &m.prodNu[m.prodPtr[i]], m.prodPtr[i + 1] - m.prodPtr[i]);
         for (int j = m.reacPtr[i]; j < m.reacPtr[i + 1]; j++) {
             sideK.push_back(m.reacK[j]); sideNu.push_back(m.reacNu[j]); sideOrd.push_back(m.reacOrder[j]);
-            net[i][m.reacK[j]] -= m.reacNu[j];
+            net[ni][m.reacK[j]] -= m.reacNu[j];
         }
         sidePtr.push_back((int)sideK.size());
         for (int j = m.prodPtr[i]; j < m.prodPtr[i + 1]; j++) {
             sideK.push_back(m.prodK[j]); sideNu.push_back(m.prodNu[j]); sideOrd.push_back(m.prodNu[j]);
-            net[i][m.prodK[j]] += m.prodNu[j];
+            net[ni][m.prodK[j]] += m.prodNu[j];
         }
         sidePtr.push_back((int)sideK.size());
-        for (auto& kv : net[i])
+        for (auto& kv : net[ni])
             if (kv.second != 0.0) { rsK.push_back(kv.first); rsNu.push_back(kv.second); }
         rsPtr.push_back((int)rsK.size());
     }
@@ -190,13 +220,15 @@ void packDevMech(MechEntry& e) {
         spPtr.push_back((int)spRxn.size());
     }
     // third bodies
-    std::vector<int> tbRxn(m.tbRxn.begin(), m.tbRxn.end()), tbMA(m.tbMassAction.begin(), m.tbMassAction.end());
+    std::vector<int> tbRxn(m.tbRxn.size()), tbMA(m.tbMassAction.begin(), m.tbMassAction.end());
+    for (size_t t = 0; t < tbRxn.size(); t++) tbRxn[t] = inv[m.tbRxn[t]];
     std::vector<int> tbPtr(m.tbPtr.begin(), m.tbPtr.end()), tbK(m.tbSpecies.begin(), m.tbSpecies.end());
     std::vector<double> tbDef(m.tbDefault), tbE(m.tbEffMinusDefault);
     // Jacobian columns: dependencies of each reaction through mass action and the
     // non-default part of its third-body efficiencies
     std::vector<std::vector<std::pair<int, double>>> cols(K);
-    for (int i = 0; i < R; i++) {
+    for (int ni = 0; ni < R; ni++) {
+        const int i = perm[ni];
         std::map<int, double> deps;
         for (int j = m.reacPtr[i]; j < m.reacPtr[i + 1]; j++) deps[m.reacK[j]] += 0.0;
         if (m.reversible[i])
@@ -205,7 +237,7 @@ void packDevMech(MechEntry& e) {
         if (t >= 0)
             for (int q = m.tbPtr[t]; q < m.tbPtr[t + 1]; q++)
                 if (m.tbEffMinusDefault[q] != 0.0) deps[m.tbSpecies[q]] = m.tbEffMinusDefault[q];
-        for (auto& kv : deps) cols[kv.first].push_back({i, kv.second});
+        for (auto& kv : deps) cols[kv.first].push_back({ni, kv.second});
     }
     std::vector<int> colPtr(1, 0), colRxn;
     std::vector<double> colE;
@@ -241,7 +273,7 @@ void packDevMech(MechEntry& e) {
         std::vector<std::vector<std::pair<int, double>>> gl(K);
         for (int t = 0; t < m.nThirdBody(); t++) {
             if (m.tbDefault[t] == 0.0) continue;
-            int i = m.tbRxn[t];
+            int i = inv[m.tbRxn[t]];
             for (int q = rsPtr[i]; q < rsPtr[i + 1]; q++) gl[rsK[q]].push_back({t, rsNu[q] * m.tbDefault[t]});
         }
         for (int k = 0; k < K; k++) {
@@ -424,6 +456,17 @@ int32_t gb_mech_molecular_weights(int32_t h, int32_t buflen, double* mw) {
     });
 }
 
+int32_t gb_mech_equivalence_ratio(int32_t h, double phi, const double* fuelX, const double* oxX,
+                                  int32_t buflen, double* Y) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        if (buflen < e.m.K) throw std::runtime_error("buffer too small for mass fractions");
+        if (!fuelX || !oxX || !Y) throw std::runtime_error("null array argument");
+        equivalenceRatioMassFractions(e.m, phi, fuelX, oxX, Y);
+        return 0;
+    });
+}
+
 int32_t gb_kin_net_production_rates(int32_t h, int32_t n, const double* T, const double* P, const double* Y,
                                     int32_t bufLen, double* wdot, int32_t flags) {
     return guarded([&]() -> int32_t {
@@ -431,6 +474,54 @@ int32_t gb_kin_net_production_rates(int32_t h, int32_t n, const double* T, const
         if ((int64_t)bufLen < (int64_t)e.m.K * n) throw std::runtime_error("wdot buffer too small: need K*n");
         if (!T || !P || !Y || !wdot) throw std::runtime_error("null array argument");
         return runRates(h, n, T, P, Y, wdot, nullptr, flags);
+    });
+}
+
+int32_t gb_mech_structure(int32_t h, int32_t ncounts, int64_t* counts) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        const Mechanism& m = e.m;
+        if (ncounts < 12) throw std::runtime_error("need 12 counts");
+        int64_t rev = 0, fo = 0, troe = 0, rslots = 0, pslots = 0;
+        for (int i = 0; i < m.R; i++) {
+            rev += m.reversible[i];
+            fo += (m.kind[i] == kLindemann || m.kind[i] == kTroe);
+            troe += (m.kind[i] == kTroe);
+            for (int j = m.reacPtr[i]; j < m.reacPtr[i + 1]; j++) rslots += (int64_t)m.reacNu[j];
+            for (int j = m.prodPtr[i]; j < m.prodPtr[i + 1]; j++) pslots += (int64_t)m.prodNu[j];
+        }
+        // gather / Jacobian list sizes are those of the packed device layout
+        std::vector<int> spPtr(e.m.K + 1), colPtr(e.m.K + 1), rsPtr(e.m.R + 1);
+        ck(cudaMemcpy(spPtr.data(), e.dm.spPtr, spPtr.size() * 4, cudaMemcpyDeviceToHost), "copy");
+        ck(cudaMemcpy(colPtr.data(), e.dm.colPtr, colPtr.size() * 4, cudaMemcpyDeviceToHost), "copy");
+        ck(cudaMemcpy(rsPtr.data(), e.dm.rsPtr, rsPtr.size() * 4, cudaMemcpyDeviceToHost), "copy");
+        std::vector<int> colRxn(colPtr.back());
+        if (!colRxn.empty())
+            ck(cudaMemcpy(colRxn.data(), e.dm.colRxn, colRxn.size() * 4, cudaMemcpyDeviceToHost), "copy");
+        int64_t scatter = 0;
+        for (int r : colRxn) scatter += rsPtr[r + 1] - rsPtr[r];
+        counts[0] = m.K; counts[1] = m.R; counts[2] = rev; counts[3] = fo; counts[4] = troe;
+        counts[5] = m.nThirdBody(); counts[6] = (int64_t)m.tbSpecies.size(); counts[7] = spPtr.back();
+        counts[8] = colPtr.back(); counts[9] = scatter; counts[10] = rslots; counts[11] = pslots;
+        return 0;
+    });
+}
+
+int32_t gb_measure_fp64(double* results) {
+    return guarded([&]() -> int32_t {
+        int dev = 0, sms = 0;
+        ck(cudaGetDevice(&dev), "cudaGetDevice");
+        ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+        ck(measureFp64(results, sms), "fp64 probe");
+        return 0;
+    });
+}
+
+int32_t gb_check_exp(int32_t n, const double* x, double* mine, double* lib) {
+    return guarded([&]() -> int32_t {
+        if (n < 0 || !x || !mine || !lib) throw std::runtime_error("bad arguments");
+        ck(checkExp(n, x, mine, lib), "exp check");
+        return 0;
     });
 }
 
@@ -506,6 +597,8 @@ int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
         ne->dStatus.ensure((size_t)n * 4);
         ne->dTign.ensure((size_t)n * 8);
         ne->dCounter.ensure(sizeof(int));
+        ck(cudaEventCreate(&ne->evA), "event");
+        ck(cudaEventCreate(&ne->evB), "event");
         ck(cudaMemset(ne->dRec.p, 0, (size_t)n * ne->recStride * 8), "memset");
         ck(cudaMemset(ne->dStats.p, 0, (size_t)n * 64), "memset");
         ck(cudaMemset(ne->dStatus.p, 0, (size_t)n * 4), "memset");
@@ -562,6 +655,7 @@ int32_t gb_net_advance(int32_t h, double t) {
         if (t < ne.time) throw std::runtime_error("cannot integrate backwards in time");
         if (t == ne.time) return 0;
         cudaStream_t s = me.stream;
+        ck(cudaEventRecord(ne.evA, s), "event record");
         if (ne.opts.use_graph) {
             if (!ne.graph || ne.graphTout != t) {
                 if (ne.graph) { cudaGraphExecDestroy(ne.graph); ne.graph = nullptr; }
@@ -577,7 +671,11 @@ int32_t gb_net_advance(int32_t h, double t) {
         } else {
             netLaunch(ne, me, ne.time, t);
         }
+        ck(cudaEventRecord(ne.evB, s), "event record");
         ck(cudaStreamSynchronize(s), "integrator");
+        float ms = 0.f;
+        ck(cudaEventElapsedTime(&ms, ne.evA, ne.evB), "event time");
+        ne.lastMs = ms;
         ne.time = t;
         std::vector<int> st(ne.n);
         ck(cudaMemcpy(st.data(), ne.dStatus.p, (size_t)ne.n * 4, cudaMemcpyDeviceToHost), "copy status");
@@ -590,6 +688,15 @@ int32_t gb_net_advance(int32_t h, double t) {
 double gb_net_time(int32_t h) {
     try {
         return net(h).time;
+    } catch (std::exception& e) {
+        g_error = e.what();
+        return -999.999;
+    }
+}
+
+double gb_net_last_advance_ms(int32_t h) {
+    try {
+        return net(h).lastMs;
     } catch (std::exception& e) {
         g_error = e.what();
         return -999.999;

@@ -24,6 +24,7 @@ constexpr int kRevBit = 1 << 3;     // reversible
 constexpr int kRBucketShift = 4;    // reactant StoichBucket (3 bits)
 constexpr int kPBucketShift = 7;    // product StoichBucket (3 bits)
 constexpr int kDnIntBit = 1 << 10;  // dn is an integer in [-3, 3]
+constexpr int kNoExpBit = 1 << 11;  // b = 0 and Ea = 0: k = A
 
 struct DevMech {
     int K, R, N, NF, NTB, nnz;

@@ -17,8 +17,10 @@ namespace gbchem {
 // Rates and d(wdot)/dc over a batch of states (Kinetics::getNetProductionRates,
 // Kinetics::netProductionRates_ddCi)
 // =============================================================================
-__global__ void __launch_bounds__(256) k_rates(RatesParams p) {
+__global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
     extern __shared__ double smem[];
+    __shared__ double s_tab[64];
+    loadExpTable(s_tab);
     const DevMech& m = p.m;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -26,6 +28,7 @@ __global__ void __launch_bounds__(256) k_rates(RatesParams p) {
     KinScratch s;
     const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF);
     s.carve(base, m.K, m.R, m.NTB, m.NF);
+    s.tab = s_tab;
     double* Yl = base + kinD;
     double* gk = Yl + m.K;
     double* Jc = gk + m.K;
@@ -89,7 +92,7 @@ enum { F_HASPREV = 1, F_HASRIGHT = 2, F_AWAIT = 4, F_INIT = 8 };
 
 struct BdfScal {
     double tn, h, hscale, hprime, eta, etamax, gamma, gammap, gamrat, crate, acnrm, saved_tq5;
-    double tau[QMAX + 2], tq[6], l[QMAX + 1];
+    double tau[QMAX + 2], tq[6], l[QMAX + 1];   // indexed only with compile-time indices (registers)
     int q, qprime, qwait, L, nst, nstlp;
     bool haveLU;
     // ignition marker
@@ -97,6 +100,16 @@ struct BdfScal {
     int nsamp, flags, status0;
     long long nrhs, nni, nsetups, nje, netf, ncfn;
 };
+
+// a[i] for a run-time i with every access at a compile-time index (keeps a[] in registers)
+template <int N>
+__device__ __forceinline__ double sel(const double (&a)[N], int i) {
+    double v = a[0];
+#pragma unroll
+    for (int k = 1; k < N; k++)
+        if (i == k) v = a[k];
+    return v;
+}
 
 struct BdfWarp {
     const DevMech* m;
@@ -315,31 +328,40 @@ struct BdfWarp {
         S.hscale = S.h;
     }
     __device__ void setCoefficients(BdfScal& S) {
+        const int q = S.q;
+#pragma unroll
         for (int i = 0; i <= QMAX; i++) S.l[i] = 0.0;
         S.l[0] = S.l[1] = 1.0;
         double xi_inv = 1.0, xistar_inv = 1.0, alpha0 = -1.0, alpha0_hat = -1.0, hsum = S.h;
-        const int q = S.q;
         if (q > 1) {
-            for (int j = 2; j < q; j++) {
-                hsum += S.tau[j - 1];
-                xi_inv = S.h / hsum;
-                alpha0 -= 1.0 / j;
-                for (int i = j; i >= 1; i--) S.l[i] += S.l[i - 1] * xi_inv;
+#pragma unroll
+            for (int j = 2; j < QMAX; j++) {
+                if (j < q) {
+                    hsum += S.tau[j - 1];
+                    xi_inv = S.h / hsum;
+                    alpha0 -= 1.0 / j;
+#pragma unroll
+                    for (int i = QMAX; i >= 1; i--)
+                        if (i <= j) S.l[i] += S.l[i - 1] * xi_inv;
+                }
             }
             alpha0 -= 1.0 / q;
             xistar_inv = -S.l[1] - alpha0;
-            hsum += S.tau[q - 1];
+            hsum += sel(S.tau, q - 1);
             xi_inv = S.h / hsum;
             alpha0_hat = -S.l[1] - xi_inv;
-            for (int i = q; i >= 1; i--) S.l[i] += S.l[i - 1] * xistar_inv;
+#pragma unroll
+            for (int i = QMAX; i >= 1; i--)
+                if (i <= q) S.l[i] += S.l[i - 1] * xistar_inv;
         }
+        const double lq = sel(S.l, q);
         double A1 = 1.0 - alpha0_hat + alpha0;
         double A2 = 1.0 + q * A1;
         S.tq[2] = fabs(A1 / (alpha0 * A2));
-        S.tq[5] = fabs(A2 * xistar_inv / (S.l[q] * xi_inv));
+        S.tq[5] = fabs(A2 * xistar_inv / (lq * xi_inv));
         if (S.qwait == 1) {
             if (q > 1) {
-                double C = xistar_inv / S.l[q];
+                double C = xistar_inv / lq;
                 double A3 = alpha0 + 1.0 / q;
                 double A4 = alpha0_hat + xi_inv;
                 double Cpinv = (1.0 - A4 + A3) / A3;
@@ -347,7 +369,7 @@ struct BdfWarp {
             } else {
                 S.tq[1] = 1.0;
             }
-            double hs = hsum + S.tau[q];
+            double hs = hsum + sel(S.tau, q);
             double xi2 = S.h / hs;
             double A5 = alpha0 - 1.0 / (q + 1);
             double A6 = alpha0_hat - xi2;
@@ -411,19 +433,33 @@ struct BdfWarp {
     }
 
     // Nordsieck order change (see the CPU restatement for the polynomial construction)
-    __device__ void decreaseOrder(BdfScal& S) {
-        double w[QMAX + 2] = {0, 0, 0, 0, 0, 0, 0};
+    // w(x) = x^2 prod_{j=1}^{nf}(x + xi_j): coefficients w[2..nf+2]
+    __device__ void orderPoly(const BdfScal& S, int nf, double (&w)[QMAX + 2]) const {
+#pragma unroll
+        for (int i = 0; i < QMAX + 2; i++) w[i] = 0.0;
         w[2] = 1.0;
         double hsum = 0.0;
-        for (int j = 1; j <= S.q - 2; j++) {
-            hsum += S.tau[j];
-            double xi = hsum / S.hscale;
-            for (int i = j + 2; i >= 2; i--) w[i] = w[i] * xi + w[i - 1];
+#pragma unroll
+        for (int j = 1; j <= QMAX - 1; j++) {
+            if (j <= nf) {
+                hsum += S.tau[j];
+                const double xi = hsum / S.hscale;
+#pragma unroll
+                for (int i = QMAX + 1; i >= 2; i--)
+                    if (i <= j + 2) w[i] = w[i] * xi + w[i - 1];
+            }
         }
+    }
+    __device__ void decreaseOrder(BdfScal& S) {
+        double w[QMAX + 2];
+        orderPoly(S, S.q - 2, w);
         const double* zq = Z(S.q);
-        for (int j = 2; j < S.q; j++) {
-            double* a = Z(j);
-            for (int i = lane; i < N; i += 32) a[i] -= w[j] * zq[i];
+#pragma unroll
+        for (int j = 2; j < QMAX; j++) {
+            if (j < S.q) {
+                double* a = Z(j);
+                for (int i = lane; i < N; i += 32) a[i] -= w[j] * zq[i];
+            }
         }
         __syncwarp();
         double* a = Z(S.q);
@@ -431,21 +467,18 @@ struct BdfWarp {
         __syncwarp();
     }
     __device__ void increaseOrder(BdfScal& S, double lq_prev) {
-        double w[QMAX + 2] = {0, 0, 0, 0, 0, 0, 0};
-        w[2] = 1.0;
-        double hsum = 0.0;
-        for (int j = 1; j <= S.q - 1; j++) {
-            hsum += S.tau[j];
-            double xi = hsum / S.hscale;
-            for (int i = j + 2; i >= 2; i--) w[i] = w[i] * xi + w[i - 1];
-        }
+        double w[QMAX + 2];
+        orderPoly(S, S.q - 1, w);
         const double c = lq_prev / (S.q + 1);
         const double* sv = Z(QMAX);
         for (int i = lane; i < N; i += 32) tempv[i] = c * sv[i];
         __syncwarp();
-        for (int j = 2; j <= S.q; j++) {
-            double* a = Z(j);
-            for (int i = lane; i < N; i += 32) a[i] += w[j] * tempv[i];
+#pragma unroll
+        for (int j = 2; j <= QMAX; j++) {
+            if (j <= S.q) {
+                double* a = Z(j);
+                for (int i = lane; i < N; i += 32) a[i] += w[j] * tempv[i];
+            }
         }
         double* top = Z(S.q + 1);
         for (int i = lane; i < N; i += 32) top[i] = tempv[i];
@@ -529,7 +562,12 @@ struct BdfWarp {
                 etaqm1 = 1.0 / (pow(BIAS1 * ddn, 1.0 / S.q) + ADDON);
             }
             if (S.q != maxOrder && S.saved_tq5 != 0.0) {
-                double cquot = (S.tq[5] / S.saved_tq5) * pow(S.h / S.tau[2], (double)L);
+                const double hr = S.h / S.tau[2];
+                double hp = hr;
+#pragma unroll
+                for (int i = 2; i <= QMAX + 1; i++)
+                    if (i <= L) hp *= hr;
+                double cquot = (S.tq[5] / S.saved_tq5) * hp;
                 const double* sv = Z(QMAX);
                 for (int i = lane; i < N; i += 32) tempv[i] = acor[i] - cquot * sv[i];
                 __syncwarp();
@@ -573,7 +611,7 @@ struct BdfWarp {
         bool prevConvFail = false;
         if (S.nst > 0) {
             if (S.qprime != S.q) {
-                if (S.qprime == S.q + 1) increaseOrder(S, S.l[S.q]);
+                if (S.qprime == S.q + 1) increaseOrder(S, sel(S.l, S.q));
                 else decreaseOrder(S);
                 S.q = S.qprime;
                 S.L = S.q + 1;
@@ -638,13 +676,18 @@ struct BdfWarp {
             }
             // accepted
             S.nst++;
-            for (int i = S.q; i >= 2; i--) S.tau[i] = S.tau[i - 1];
+#pragma unroll
+            for (int i = QMAX; i >= 2; i--)
+                if (i <= S.q) S.tau[i] = S.tau[i - 1];
             if (S.q == 1 && S.nst > 1) S.tau[2] = S.tau[1];
             S.tau[1] = S.h;
-            for (int j = 0; j <= S.q; j++) {
-                double* a = Z(j);
-                const double lj = S.l[j];
-                for (int i = lane; i < N; i += 32) a[i] += lj * acor[i];
+#pragma unroll
+            for (int j = 0; j <= QMAX; j++) {
+                if (j <= S.q) {
+                    double* a = Z(j);
+                    const double lj = S.l[j];
+                    for (int i = lane; i < N; i += 32) a[i] += lj * acor[i];
+                }
             }
             __syncwarp();
             S.qwait--;
@@ -662,8 +705,10 @@ struct BdfWarp {
 };
 
 template <typename MT>
-__global__ void __launch_bounds__(256) k_bdf(BdfParams p) {
+__global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
     extern __shared__ double smem[];
+    __shared__ double s_tab[64];
+    loadExpTable(s_tab);
     const DevMech& m = p.m;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -681,6 +726,7 @@ __global__ void __launch_bounds__(256) k_bdf(BdfParams p) {
     const int N = m.N;
     const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF);
     W.s.carve(base, m.K, m.R, m.NTB, m.NF);
+    W.s.tab = s_tab;
     double* q = base + kinD;
     W.zn = q; q += (QMAX + 1) * N;
     W.ewt = q; q += N;
@@ -807,7 +853,7 @@ int bdfRecordStride(int N) { return (QMAX + 1) * N + R_NSCAL; }
 
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32) {
     int N = m.N;
-    int kinD = 5 * m.K + 3 * m.R + 2 * m.NTB + m.NF;
+    int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF);
     int vec = (QMAX + 1) * N + 7 * N + (N + 1) / 2;
     int mat = fp32 ? (N * ld + 1) / 2 : N * ld;
     int tot = kinD + vec + mat;
@@ -815,7 +861,7 @@ int bdfWarpDoubles(const DevMech& m, int ld, bool fp32) {
 }
 
 int ratesWarpDoubles(const DevMech& m) {
-    int kinD = 5 * m.K + 3 * m.R + 2 * m.NTB + m.NF;
+    int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF);
     int tot = kinD + 2 * m.K + m.K * (m.K + 1);
     return (tot + 1) & ~1;
 }
@@ -841,6 +887,90 @@ cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp
         k_bdf<double><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
     }
     return cudaGetLastError();
+}
+
+// -----------------------------------------------------------------------------
+// FP64 probe: eight independent FMA chains per thread (enough to fill the pipe), and
+// chains of exp / log of varying arguments, over a grid that covers every SM.
+// -----------------------------------------------------------------------------
+__global__ void k_probe_fma(double* out, int iters, double a, double b) {
+    double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+           x7 = x0 + 7;
+    for (int i = 0; i < iters; i++) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+__global__ void k_probe_exp(double* out, int iters, int useLog) {
+    double s = 0, x = useLog ? 1.5 + threadIdx.x * 1e-4 : -1.0 - threadIdx.x * 1e-4;
+    for (int i = 0; i < iters; i++) {
+        s += useLog ? log(x) : exp(x);
+        x += 1e-7;
+        s += useLog ? log(x * 0.5) : exp(x * 0.5);
+        x += 1e-7;
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void k_check_exp(int n, const double* x, double* mine, double* lib) {
+    __shared__ double s_tab[64];
+    loadExpTable(s_tab);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        mine[i] = fexp(x[i], s_tab);
+        lib[i] = exp(x[i]);
+    }
+}
+
+cudaError_t checkExp(int n, const double* x, double* mine, double* lib) {
+    k_check_exp<<<256, 256>>>(n, x, mine, lib);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return cudaDeviceSynchronize();
+}
+
+cudaError_t measureFp64(double* results, int smCount) {
+    const int threads = 256, blocks = smCount * 8;
+    double* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, (size_t)threads * blocks * sizeof(double));
+    if (e != cudaSuccess) return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float ms = 0.f;
+    const int it = 4096;
+    double best = 0.0, bestExp = 1e30, bestLog = 1e30;
+    for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(a);
+        k_probe_fma<<<blocks, threads>>>(d, it, 1.0000001, 1e-9);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms, a, b);
+        double fmaPerS = 8.0 * it * threads * blocks / (ms * 1e-3);
+        best = fmax(best, fmaPerS);
+        cudaEventRecord(a);
+        k_probe_exp<<<blocks, threads>>>(d, it / 8, 0);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms, a, b);
+        double expPerS = 2.0 * (it / 8) * threads * blocks / (ms * 1e-3);
+        bestExp = fmin(bestExp, best / expPerS);
+        cudaEventRecord(a);
+        k_probe_exp<<<blocks, threads>>>(d, it / 8, 1);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms, a, b);
+        double logPerS = 2.0 * (it / 8) * threads * blocks / (ms * 1e-3);
+        bestLog = fmin(bestLog, best / logPerS);
+    }
+    e = cudaGetLastError();
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(d);
+    results[0] = 2.0 * best / 1e9;
+    results[1] = bestExp;
+    results[2] = bestLog;
+    return e;
 }
 
 }  // namespace gbchem

@@ -44,5 +44,8 @@ int bdfWarpDoubles(const DevMech& m, int ld, bool fp32);
 int ratesWarpDoubles(const DevMech& m);
 cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
 cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream);
+// FP64 throughput probe: returns {GFLOP/s of FMA, exp cost, log cost in FMA-equivalents}
+cudaError_t measureFp64(double* results, int smCount);
+cudaError_t checkExp(int n, const double* x, double* mine, double* lib);
 
 }  // namespace gbchem

@@ -32,6 +32,75 @@ __device__ __forceinline__ double warpMax(double v) {
     return v;
 }
 
+// ---------------------------------------------------------------------------
+// FP64 exponential (table-driven method of P. T. P. Tang, ACM TOMS 15(2), 1989):
+// x = (64 e + j) ln2/64 + r with |r| <= ln2/128, exp(x) = 2^e * 2^(j/64) * exp(r), exp(r)
+// by its Taylor polynomial to r^5 (truncation < 4e-17).  Ten FP64 operations against
+// about twenty for the library exp.  Arguments with |x| >= 700, infinities and NaN take
+// the library exp.  The 64-entry table 2^(j/64) (correctly rounded) sits in shared memory.
+// ---------------------------------------------------------------------------
+__device__ __constant__ double c_exp2tab[64] = {
+    1.0, 1.0108892860517005, 1.0218971486541166, 1.0330248790212284,
+    1.0442737824274138, 1.0556451783605572, 1.0671404006768237, 1.0787607977571199,
+    1.0905077326652577, 1.102382583307841, 1.1143867425958924, 1.1265216186082418,
+    1.1387886347566916, 1.1511892299529827, 1.1637248587775775, 1.1763969916502812,
+    1.189207115002721, 1.202156731452703, 1.215247359980469, 1.22848053610687,
+    1.241857812073484, 1.255380757024691, 1.2690509571917332, 1.2828700160787783,
+    1.2968395546510096, 1.3109612115247644, 1.3252366431597413, 1.339667524053303,
+    1.3542555469368927, 1.3690024229745905, 1.383909881963832, 1.3989796725383112,
+    1.4142135623730951, 1.42961333839197, 1.4451808069770467, 1.460917794180647,
+    1.4768261459394993, 1.4929077282912648, 1.5091644275934228, 1.5255981507445384,
+    1.5422108254079407, 1.559004400237837, 1.5759808451078865, 1.593142151342267,
+    1.6104903319492543, 1.6280274218573478, 1.645755478153965, 1.6636765803267364,
+    1.681792830507429, 1.7001063537185235, 1.718619298122478, 1.7373338352737062,
+    1.7562521603732995, 1.7753764925265212, 1.7947090750031072, 1.8142521755003989,
+    1.8340080864093424, 1.8539791250833855, 1.8741676341103, 1.8945759815869656,
+    1.9152065613971474, 1.9360617934922943, 1.9571441241754002, 1.978456026387951};
+
+// Load the table into a block's shared copy (call before the first fexp; all threads).
+__device__ __forceinline__ void loadExpTable(double* tab) {
+    for (int j = threadIdx.x; j < 64; j += blockDim.x) tab[j] = c_exp2tab[j];
+    __syncthreads();
+}
+
+// |x| >= 700, infinity or NaN
+__device__ __forceinline__ bool expBigArg(double x) {
+    return (__double2hiint(x) & 0x7fffffff) >= 0x4085E000;
+}
+// exp(x) = m * 2^e with m in (0.99, 2.01); requires !expBigArg(x)
+__device__ __forceinline__ double expSplit(double x, const double* tab, int& e) {
+    const double shifter = 6755399441055744.0;            // 1.5 * 2^52: rounds to an integer
+    const double t = fma(x, 92.33248261689366, shifter);   // x * 64/ln2
+    const int k = __double2loint(t);
+    const double kd = t - shifter;
+    double r = fma(-kd, 0.010830424726009369, x);          // ln2/64, high part (24 bits)
+    r = fma(-kd, -2.9760223436840126e-11, r);              // ln2/64, low part
+    double q = fma(r, 1.0 / 120.0, 1.0 / 24.0);
+    q = fma(q, r, 1.0 / 6.0);
+    q = fma(q, r, 0.5);
+    q = fma(q, r, 1.0);
+    const double p = q * r;
+    const double T = tab[k & 63];
+    e = k >> 6;
+    return fma(T, p, T);
+}
+// m * 2^e by an exponent-field add; the caller guarantees a normal result
+__device__ __forceinline__ double scale2(double m, int e) {
+    return __longlong_as_double(__double_as_longlong(m) + ((long long)e << 52));
+}
+__device__ __forceinline__ double fexp(double x, const double* tab) {
+    if (expBigArg(x)) return exp(x);
+    int e;
+    const double m = expSplit(x, tab, e);
+    return scale2(m, e);
+}
+// a < 0 and b < 0 (IEEE comparison semantics, -0 is not negative) on the integer pipe
+__device__ __forceinline__ bool bothNeg(double a, double b) {
+    const long long la = __double_as_longlong(a), lb = __double_as_longlong(b);
+    const long long nz = (long long)0x8000000000000000ULL;
+    return (la & lb) < 0 && la != nz && lb != nz;
+}
+
 // Per-state scratch in shared memory (sizes in doubles: K, K, K, K, K, R, R, R, NTB, NTB, NF).
 struct KinScratch {
     double* c;      // concentrations [K]
@@ -45,11 +114,24 @@ struct KinScratch {
     double* Mtb;    // third-body concentrations [NTB]
     double* Qtb;    // d(rop)/d[M] per third-body reaction [NTB]
     double* dlk;    // d ln k / d[M] of falloff reactions [NF]
-    __device__ static int doubles(int K, int R, int NTB, int NF) { return 5 * K + 3 * R + 2 * NTB + NF; }
+    double* em;     // exp(g) = em * 2^ee [K]
+    double* emi;    // exp(-g) = emi * 2^eei [K]
+    int* ee;        // [K]
+    int* eei;       // [K]
+    double* pw;     // (RT/P)^dn for dn = -3..3 [8]
+    const double* tab;   // 2^(j/64) table (block shared)
+    int* flags;     // [2] per-state flags (bit 0: some |g| >= 700)
+    __host__ __device__ static int doubles(int K, int R, int NTB, int NF) {
+        return 5 * K + 3 * R + 2 * NTB + NF + 2 * K + K + 8 + 2;
+    }
     __device__ void carve(double* p, int K, int R, int NTB, int NF) {
         c = p; p += K; cpR = p; p += K; hRT = p; p += K; g = p; p += K; wdot = p; p += K;
         rop = p; p += R; kfe = p; p += R; rkc = p; p += R;
-        Mtb = p; p += NTB; Qtb = p; p += NTB; dlk = p;
+        Mtb = p; p += NTB; Qtb = p; p += NTB; dlk = p; p += NF;
+        em = p; p += K; emi = p; p += K;
+        ee = (int*)p; eei = ee + K; p += K;
+        pw = p; p += 8;
+        flags = (int*)p;
     }
 };
 
@@ -65,11 +147,11 @@ __device__ __forceinline__ double massAction(const DevMech& m, int bucket, int4 
     if (bucket == 1) return c[e.x];
     if (bucket == 2) {
         double a = c[e.x], b = c[e.y];
-        return (a < 0 && b < 0) ? 0.0 : a * b;
+        return bothNeg(a, b) ? 0.0 : a * b;
     }
     if (bucket == 3) {
         double a = c[e.x], b = c[e.y], d = c[e.z];
-        if ((a < 0 && (b < 0 || d < 0)) || (b < 0 && d < 0)) return 0.0;
+        if (bothNeg(a, b) || bothNeg(a, d) || bothNeg(b, d)) return 0.0;
         return a * b * d;
     }
     double r = 1.0;
@@ -120,22 +202,23 @@ __device__ __forceinline__ double massActionDeriv(const DevMech& m, int bucket, 
     return d;
 }
 
-__device__ __forceinline__ double arrhenius(double A, double b, double EaR, double lnT, double recipT) {
-    return A * exp(b * lnT - EaR * recipT);
+__device__ __forceinline__ double arrhenius(double A, double b, double EaR, double lnT, double recipT,
+                                            const double* tab) {
+    return A * fexp(b * lnT - EaR * recipT, tab);
 }
 
 // Falloff rate k(T, M) and, optionally, d ln k / d M (analytic).
 __device__ __forceinline__ double falloff(D4 f1, D4 f2, double A, double b, double EaR,
-                                          const KinState& st, double M, double* dlnk_dM) {
+                                          const KinState& st, double M, double* dlnk_dM, const double* tab) {
     double work = 0.0;
     bool troe = f2.w != 0.0;
     if (troe) {
-        double Fcent = (1.0 - f1.w) * exp(-st.T * f2.x) + f1.w * exp(-st.T * f2.y);
-        if (f2.z != 0.0) Fcent += exp(-f2.z / st.T);
+        double Fcent = (1.0 - f1.w) * fexp(-st.T * f2.x, tab) + f1.w * fexp(-st.T * f2.y, tab);
+        if (f2.z != 0.0) Fcent += fexp(-f2.z * st.recipT, tab);
         work = log10(fmax(Fcent, 1e-300));
     }
-    double klow = arrhenius(f1.x, f1.y, f1.z, st.lnT, st.recipT);
-    double khigh = arrhenius(A, b, EaR, st.lnT, st.recipT);
+    double klow = arrhenius(f1.x, f1.y, f1.z, st.lnT, st.recipT, tab);
+    double khigh = arrhenius(A, b, EaR, st.lnT, st.recipT, tab);
     double dPr = klow / (khigh + 1e-300);
     double pr = M * dPr;
     double F = 1.0, dFdPr_over_F = 0.0;
@@ -148,7 +231,7 @@ __device__ __forceinline__ double falloff(D4 f1, D4 f2, double A, double b, doub
         double f1v = u / den;
         double q = 1.0 + f1v * f1v;
         double lgf = work / q;
-        F = pow(10.0, lgf);
+        F = fexp(lgf * 2.302585092994046, tab);
         if (pr > 1e-300) dFdPr_over_F = (-work * 2.0 * f1v / (q * q) * (nn / (den * den))) / pr;
     }
     double k = pr * (F / (1.0 + pr)) * khigh;
@@ -188,6 +271,8 @@ __device__ __forceinline__ void warpState(const DevMech& m, double T, double P, 
 template <bool forJac>
 __device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, int lane) {
     const double lnPP = log(st.P / m.Pref);
+    if (lane == 0) s.flags[0] = 0;
+    __syncwarp();
     for (int k = lane; k < m.K; k += 32) {
         const double* a = m.nasa + (size_t)k * kNasaStride;
         const double* p = (st.T <= a[0]) ? a + 1 : a + 8;
@@ -199,7 +284,28 @@ __device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, i
         double sR = ct0 * st.lnT + ct1 + 0.5 * ct2 + (1.0 / 3.0) * ct3 + 0.25 * ct4 + p[6];
         s.cpR[k] = cp;
         s.hRT[k] = h;
-        s.g[k] = (h - sR) + lnPP;
+        const double gk = (h - sR) + lnPP;
+        s.g[k] = gk;
+        // exp(+-g) with split exponents: Kc of each reaction is then a product over its
+        // species instead of one exponential per reaction
+        if (!expBigArg(gk)) {
+            int e1, e2;
+            s.em[k] = expSplit(gk, s.tab, e1);
+            s.emi[k] = expSplit(-gk, s.tab, e2);
+            s.ee[k] = e1;
+            s.eei[k] = e2;
+        } else {
+            s.flags[0] = 1;
+        }
+    }
+    if (lane < 7) {
+        // (RT/P)^dn for dn = lane - 3  (= exp(-dn * ln(P/RT)))
+        const double a = st.RT / st.P, b = st.P / st.RT;
+        const int dn = lane - 3;
+        double v = 1.0;
+        if (dn > 0) { v = a; if (dn > 1) v *= a; if (dn > 2) v *= a; }
+        if (dn < 0) { v = b; if (dn < -1) v *= b; if (dn < -2) v *= b; }
+        s.pw[lane] = v;
     }
     __syncwarp();
     for (int t = lane; t < m.NTB; t += 32) {
@@ -209,6 +315,7 @@ __device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, i
     }
     __syncwarp();
     const double logStandConc = log(st.P / st.RT);
+    const bool bigG = s.flags[0] != 0;
     for (int i = lane; i < m.R; i += 32) {
         int4 info = __ldg(&m.rinfo[i]);
         D4 ar = m.rarr[i];
@@ -216,12 +323,12 @@ __device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, i
         double kf;
         double dlnk = 0.0;
         if (kind <= 1) {
-            kf = arrhenius(ar.x, ar.y, ar.z, st.lnT, st.recipT);
+            kf = (info.x & kNoExpBit) ? ar.x : arrhenius(ar.x, ar.y, ar.z, st.lnT, st.recipT, s.tab);
         } else {
             D4 f1 = m.fo1[info.z];
             D4 f2 = m.fo2[info.z];
             double M = s.Mtb[info.y];
-            kf = falloff(f1, f2, ar.x, ar.y, ar.z, st, M, forJac ? &dlnk : nullptr);
+            kf = falloff(f1, f2, ar.x, ar.y, ar.z, st, M, forJac ? &dlnk : nullptr, s.tab);
             // the reference sets this derivative to zero unless k != 0 and [M] > 0
             if (!(M > 0.0) || kf == 0.0) dlnk = 0.0;
             if (forJac) s.dlk[info.z] = dlnk;
@@ -234,6 +341,24 @@ __device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, i
         double fwd = massAction(m, rb, re, 2 * i, s.c);
         double rev = 0.0;
         if (info.x & kRevBit) {
+            bool done = false;
+            if (!bigG && pb != 0 && rb != 0 && (info.x & kDnIntBit)) {
+                // 1/Kc = prod_p exp(g_p) * prod_r exp(-g_r) * (RT/P)^dn, exponents carried
+                // separately so that no partial product overflows
+                double mp = s.em[pe.x];
+                int ex = s.ee[pe.x];
+                if (pe.w > 1) { mp *= s.em[pe.y]; ex += s.ee[pe.y]; }
+                if (pe.w > 2) { mp *= s.em[pe.z]; ex += s.ee[pe.z]; }
+                mp *= s.emi[re.x];
+                ex += s.eei[re.x];
+                if (re.w > 1) { mp *= s.emi[re.y]; ex += s.eei[re.y]; }
+                if (re.w > 2) { mp *= s.emi[re.z]; ex += s.eei[re.z]; }
+                if (ex > -980 && ex < 960) {
+                    rkc = scale2(mp * s.pw[(int)ar.w + 3], ex);
+                    done = true;
+                }
+            }
+            if (!done) {
             // Delta G / RT over the expanded species lists (products minus reactants)
             double dG = 0.0;
             if (pb != 0) {
@@ -253,6 +378,7 @@ __device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, i
             }
             dG -= dr;
             rkc = fmin(exp(dG - ar.w * logStandConc), 1e300);
+            }
             rev = massAction(m, pb, pe, 2 * i + 1, s.c);
         }
         double ropf = kfe * fwd;

@@ -560,6 +560,50 @@ Mechanism loadMechanism(const std::string& path, const std::string& phaseName) {
     return m;
 }
 
+void equivalenceRatioMassFractions(const Mechanism& m, double phi, const double* fuelX,
+                                   const double* oxX, double* Y) {
+    if (phi < 0.0) throw std::runtime_error("equivalence ratio phi must be >= 0");
+    const int K = m.K, E = (int)m.elementNames.size();
+    auto toMass = [&](const double* X, std::vector<double>& y) {
+        double s = 0.0;
+        for (int k = 0; k < K; k++) s += X[k] * m.mw[k];
+        if (!(s > 0.0)) throw std::runtime_error("empty fuel or oxidizer composition");
+        for (int k = 0; k < K; k++) y[k] = X[k] * m.mw[k] / s;
+    };
+    std::vector<double> fuel(K), ox(K);
+    toMass(fuelX, fuel);
+    toMass(oxX, ox);
+    auto eidx = [&](const char* e) {
+        for (int i = 0; i < E; i++)
+            if (m.elementNames[i] == e) return i;
+        return -1;
+    };
+    const int iC = eidx("C"), iS = eidx("S"), iH = eidx("H"), iO = eidx("O");
+    if (iO < 0) throw std::runtime_error("equivalence ratio needs element O");
+    // O2 needed (per unit mass) to oxidise C -> CO2, S -> SO2, H -> H2O, minus O2 present
+    auto o2need = [&](const std::vector<double>& y) {
+        double req = 0.0, pres = 0.0, sum = 0.0;
+        for (int k = 0; k < K; k++) {
+            sum += y[k];
+            double x = y[k] / m.mw[k];
+            const double* a = &m.atoms[(size_t)k * E];
+            if (iC >= 0) req += x * a[iC];
+            if (iS >= 0) req += x * a[iS];
+            if (iH >= 0) req += x * 0.25 * a[iH];
+            pres += x * a[iO];
+        }
+        return req / sum - 0.5 * pres / sum;
+    };
+    double of = o2need(fuel), oo = o2need(ox);
+    if (of < 0.0 || oo > 0.0)
+        throw std::runtime_error("fuel contains too much oxygen or oxidizer contains not enough");
+    double afr = of / (-oo);
+    double sf = 0.0, so = 0.0, tot = 0.0;
+    for (int k = 0; k < K; k++) { sf += fuel[k]; so += ox[k]; }
+    for (int k = 0; k < K; k++) { Y[k] = phi * fuel[k] / sf + afr * ox[k] / so; tot += Y[k]; }
+    for (int k = 0; k < K; k++) Y[k] /= tot;
+}
+
 void jacobianPattern(const Mechanism& m, std::vector<int32_t>& colPtr, std::vector<int32_t>& rowIdx) {
     std::vector<std::set<int>> cols(m.K);
     for (int i = 0; i < m.R; i++) {

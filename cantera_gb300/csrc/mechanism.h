@@ -91,6 +91,12 @@ struct Mechanism {
 // Throws std::runtime_error with a message naming the file and line on failure.
 Mechanism loadMechanism(const std::string& path, const std::string& phase);
 
+// Mass fractions of the mixture with equivalence ratio phi of fuel and oxidizer given
+// as mole fractions [K] (ThermoPhase::setEquivalenceRatio with the molar basis,
+// reference src/thermo/ThermoPhase.cpp:783-910); the result is normalised.
+void equivalenceRatioMassFractions(const Mechanism& m, double phi, const double* fuelX,
+                                   const double* oxX, double* Y);
+
 // Structural nonzeros of d(wdot)/d(c) (the union of every reaction's species
 // couplings and its third-body efficiencies, including default efficiencies),
 // returned as compressed sparse columns: colPtr[K+1], rowIdx[nnz], rows ascending.

@@ -38,6 +38,11 @@ int32_t gb_mech_n_reactions(int32_t mech);                /* Kinetics::nReaction
 int32_t gb_mech_species_name(int32_t mech, int32_t k, int32_t buflen, char* buf);
 int32_t gb_mech_species_index(int32_t mech, const char* name);  /* -1 if absent */
 int32_t gb_mech_molecular_weights(int32_t mech, int32_t buflen, double* mw);
+/* Mass fractions Y[K] of the mixture with equivalence ratio phi of a fuel and an
+ * oxidizer given as mole fractions [K] (ThermoPhase::setEquivalenceRatio, molar basis;
+ * src/thermo/ThermoPhase.cpp:879-910). */
+int32_t gb_mech_equivalence_ratio(int32_t mech, double phi, const double* fuelX, const double* oxX,
+                                  int32_t buflen, double* Y);
 
 /* ---- kinetics ----------------------------------------------------------------------
  * Batched Kinetics::getNetProductionRates (src/kinetics/Kinetics.cpp:447-457; CLib
@@ -88,6 +93,9 @@ int32_t gb_net_set_state(int32_t net, const double* T, const double* P, const do
  * Returns the number of reactors whose integration failed (status != 0), or GB_ERR. */
 int32_t gb_net_advance(int32_t net, double t);
 double gb_net_time(int32_t net);
+/* Device time of the integrator launch of the last gb_net_advance, in ms (CUDA events on
+ * the engine's stream around the launch). */
+double gb_net_last_advance_ms(int32_t net);
 int32_t gb_net_get_state(int32_t net, double* T, double* Y, int32_t flags);
 
 /* Per-reactor status: 0 ok, 1 max steps, 2 repeated error-test failures, 3 repeated
@@ -104,6 +112,20 @@ int32_t gb_net_solver_stats(int32_t net, int64_t* stats);
 /* Time of the largest dT/dt seen at accepted steps since gb_net_set_state, refined by the
  * vertex of the parabola through that step and its accepted neighbours. */
 int32_t gb_net_ignition_times(int32_t net, double* tign);
+
+/* ---- measurement helpers (no counterpart in the reference) ---------------------------
+ * Structure counts of a mechanism for the benchmark's FP64 operation model:
+ * counts[0..11] = K, R, reversible, falloff, Troe, three-body reactions, third-body
+ * efficiency entries, species-gather entries, Jacobian column entries, Jacobian scatter
+ * entries, reactant-side species slots, product-side species slots. */
+int32_t gb_mech_structure(int32_t mech, int32_t ncounts, int64_t* counts);
+/* Sustained FP64 FMA rate of the device in GFLOP/s (2 flops per FMA), measured by a
+ * dependent-chain kernel over every SM; also the per-call cost of exp and log in
+ * FMA-equivalents (results[0] = GFLOP/s, [1] = exp, [2] = log). */
+int32_t gb_measure_fp64(double* results);
+/* Evaluate the engine's own FP64 exponential and the CUDA library exp on n device-resident
+ * arguments x (device pointers): out_engine[i], out_library[i].  For accuracy tests. */
+int32_t gb_check_exp(int32_t n, const double* x, double* out_engine, double* out_library);
 
 /* Copy the most recent error message (thread-local) into buf; returns its length. */
 int32_t gb_get_error(int32_t buflen, char* buf);

@@ -1230,7 +1230,7 @@ int32_t or_ddci(int32_t h, double T, double P, const double* Y, int32_t mode, do
 
 int32_t or_rates_batch(int32_t h, int32_t n, const double* T, const double* P, const double* Y,
                        double* wdot, int32_t mode, const int32_t* colPtr, const int32_t* rowIdx,
-                       double* jacVals, int32_t threads) {
+                       double* jacVals, double* gross, int32_t threads) {
     Kin* k = getKin(h);
     if (!k) return -1;
     const int K = k->m.K, R = k->m.R;
@@ -1244,6 +1244,15 @@ int32_t or_rates_batch(int32_t h, int32_t n, const double* T, const double* P, c
         setState(*k, T[s], P[s], y.data(), w);
         updateROP(*k, w);
         if (wdot) for (int j = 0; j < K; j++) wdot[(size_t)j * n + s] = w.wdot[j];
+        if (gross) {
+            const Mechanism& m = k->m;
+            for (int j = 0; j < K; j++) gross[(size_t)j * n + s] = 0.0;
+            for (int i = 0; i < R; i++) {
+                double a = std::fabs(w.ropf[i]) + std::fabs(w.ropr[i]);
+                for (int q = m.reacPtr[i]; q < m.reacPtr[i + 1]; q++) gross[(size_t)m.reacK[q] * n + s] += std::fabs(m.reacNu[q]) * a;
+                for (int q = m.prodPtr[i]; q < m.prodPtr[i + 1]; q++) gross[(size_t)m.prodK[q] * n + s] += std::fabs(m.prodNu[q]) * a;
+            }
+        }
         if (jacVals && colPtr && rowIdx) {
             jbuf[t].resize((size_t)K * K);
             ddCi(*k, w, mode, jbuf[t].data());

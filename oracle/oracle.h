@@ -70,10 +70,11 @@ int32_t or_rates(int32_t h, double T, double P, const double* Y, double* kf, dou
 int32_t or_ddci(int32_t h, double T, double P, const double* Y, int32_t mode, double* jac);
 
 // Batch over n states in species-major layout Y[K][n] (the GPU API layout), using
-// `threads` host threads.  wdot [K][n]; jac [nnz][n] on the pattern colPtr/rowIdx (may be NULL).
+// `threads` host threads.  wdot [K][n]; jac [nnz][n] on the pattern colPtr/rowIdx (may be NULL);
+// gross [K][n] = sum_i |nu_ki| (|ropf_i| + |ropr_i|), the scale of wdot_k's cancellation (may be NULL).
 int32_t or_rates_batch(int32_t h, int32_t n, const double* T, const double* P, const double* Y,
                        double* wdot, int32_t mode, const int32_t* colPtr, const int32_t* rowIdx,
-                       double* jacVals, int32_t threads);
+                       double* jacVals, double* gross, int32_t threads);
 
 // Reactor right-hand side for y = [m, T, Y1..YK] at pressure P: ydot[K+2].
 int32_t or_reactor_rhs(int32_t h, double P, const double* y, double* ydot);

@@ -66,7 +66,7 @@ def lib():
         L.or_mech_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
         L.or_last_error.restype = ctypes.c_char_p
         L.or_rates_batch.argtypes = [I32, I32, D, D, D, D, I32, ctypes.POINTER(I32),
-                                     ctypes.POINTER(I32), D, I32]
+                                     ctypes.POINTER(I32), D, D, I32]
         L.or_advance_batch.argtypes = [I32, I32, D, D, D, ctypes.c_double,
                                        ctypes.POINTER(BdfOpts), D, D,
                                        ctypes.POINTER(ctypes.c_int64), D, I32]
@@ -156,11 +156,13 @@ class Mech:
         lib().or_ddci(self.h, T, P, _p(_c(Y)), mode, _p(J))
         return J
 
-    def rates_batch(self, T, P, Y_sm, mode=1, pattern=None, threads=None):
-        """Species-major batch: Y_sm [K][n].  Returns wdot [K][n] (and jac [nnz][n])."""
+    def rates_batch(self, T, P, Y_sm, mode=1, pattern=None, threads=None, gross=False):
+        """Species-major batch: Y_sm [K][n].  Returns wdot [K][n], jac [nnz][n] (or None)
+        and, with gross=True, the gross-rate scale [K][n] as a third value."""
         n = len(T)
         threads = threads or os.cpu_count()
         wdot = np.zeros((self.K, n))
+        gr = np.zeros((self.K, n)) if gross else None
         jac = None
         cp = ri = None
         if pattern is not None:
@@ -172,7 +174,9 @@ class Mech:
         lib().or_rates_batch(self.h, n, _p(_c(T)), _p(_c(P)), _p(_c(Y_sm)), _p(wdot), mode,
                              cp.ctypes.data_as(I) if cp is not None else None,
                              ri.ctypes.data_as(I) if ri is not None else None,
-                             _p(jac) if jac is not None else None, threads)
+                             _p(jac) if jac is not None else None, _p(gr), threads)
+        if gross:
+            return wdot, jac, gr
         return wdot, jac
 
     def reactor_rhs(self, P, y):

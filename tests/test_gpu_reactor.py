@@ -1,0 +1,128 @@
+"""GPU batched integrator against the oracle (same algorithm, analytic Jacobian) and
+against the reference's blessed outputs."""
+import numpy as np
+import pytest
+
+from conftest import gpu_solution, oracle_mech
+
+pytestmark = pytest.mark.gpu
+
+
+def check_species(Y, Yo, rtol, floor=1e-6):
+    """Species above `floor` within 10 x rtol relative; smaller ones within 10 x rtol x floor
+    absolute (their error is set by the absolute tolerance, not by rtol)."""
+    d = np.abs(Y - Yo)
+    big = np.abs(Yo) >= floor
+    rel = d[big] / np.abs(Yo[big])
+    assert np.max(rel) < 10 * rtol, ("major species", np.max(rel))
+    assert np.max(d[~big], initial=0.0) < 10 * rtol * floor, ("minor species", np.max(d[~big], initial=0.0))
+
+
+def h2o2_batch(n, seed):
+    m = oracle_mech("h2o2")
+    rng = np.random.default_rng(seed)
+    T0 = rng.uniform(1000, 1600, n)
+    phi = rng.uniform(0.5, 2.0, n)
+    Y0 = np.array([m.equivalence_ratio(p, "H2:1", "O2:1, N2:3.76") for p in phi])
+    return T0, np.full(n, 101325.0), Y0
+
+
+@pytest.mark.parametrize("lu", [64, 32])
+def test_h2o2_batch_matches_oracle(lu):
+    import cantera_gb300 as gb
+    from oracle import pyoracle as po
+    sol, m = gpu_solution("h2o2"), oracle_mech("h2o2")
+    rtol, atol = 1e-8, 1e-15
+    T0, P, Y0 = h2o2_batch(128, 3)
+    net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=rtol, atol=atol, lu_precision=lu)
+    assert net.advance(1e-3) == 0
+    T, Y = net.get_state()
+    To, Yo, sto, tio = m.advance_batch(T0, P, Y0, 1e-3, po.opts(rtol=rtol, atol=atol, analytic=True,
+                                                                lu_fp32=(lu == 32)))
+    assert np.all(sto[:, 8] == 0) and np.all(net.status == 0)
+    # final T and Y within 10 x rtol, ignition within 0.1%
+    assert np.max(np.abs(T - To) / To) < 10 * rtol
+    check_species(Y.T, Yo, rtol)
+    tig = net.ignition_times
+    assert np.max(np.abs(tig - tio) / tio) < 1e-3
+    st = net.solver_stats
+    assert np.all(st["steps"] > 0) and np.all(st["rhs_evals"] >= st["steps"])
+
+
+def test_kin1_blessed_on_gpu(goldens):
+    import cantera_gb300 as gb
+    g = goldens["kin1"]
+    sol, m = gpu_solution("h2o2"), oracle_mech("h2o2")
+    data = np.array(g["rows"])
+    Y0 = m.mole_to_mass(m.composition(g["setup"]["X"]))
+    net = gb.ReactorNet(sol, np.array([1001.0]), np.array([101325.0]), Y0.reshape(-1, 1).copy())
+    rows = [[1001.0] + list(Y0)]
+    for t in data[1:, 0]:
+        assert net.advance(t) == 0
+        T, Y = net.get_state()
+        rows.append([T[0]] + list(Y[:, 0]))
+    rows = np.array(rows)
+    X = rows[:, 1:] / m.mw
+    X /= X.sum(axis=1, keepdims=True)
+    idx = [m.species_index(n) for n in g["header"][4:]]
+    mine = np.column_stack([rows[:, 0], X[:, idx]])
+    ref = np.column_stack([data[:, 1], data[:, 4:]])
+    ok = np.abs(mine - ref) / (np.maximum(np.abs(mine), np.abs(ref)) + g["threshold"]) < g["tolerance"]
+    assert ok.all(), np.argwhere(~ok)[:5]
+
+
+def test_gri30_uneven_stiffness_matches_oracle():
+    import cantera_gb300 as gb
+    from oracle import pyoracle as po
+    sol, m = gpu_solution("gri30"), oracle_mech("gri30")
+    rng = np.random.default_rng(20261203 + 2)
+    n = 48
+    T0 = rng.uniform(700, 1800, n)
+    P = 101325.0 * 10 ** rng.uniform(0, np.log10(40), n)
+    phi = rng.uniform(0.5, 1.5, n)
+    Y0 = np.array([m.equivalence_ratio(p, "CH4:1", "O2:1, N2:3.76") for p in phi])
+    rtol, atol = 1e-8, 1e-15
+    net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=rtol, atol=atol)
+    assert net.advance(1e-2) == 0
+    T, Y = net.get_state()
+    To, Yo, sto, tio = m.advance_batch(T0, P, Y0, 1e-2, po.opts(rtol=rtol, atol=atol, analytic=True))
+    assert np.max(np.abs(T - To) / To) < 10 * rtol
+    check_species(Y.T, Yo, rtol)
+    ign = To > T0 + 400
+    assert ign.any() and (~ign).any()   # the batch mixes igniting and inert reactors
+    assert np.max(np.abs(net.ignition_times[ign] - tio[ign]) / tio[ign]) < 1e-3
+
+
+def test_continuation_graph_and_device_state():
+    import cantera_gb300 as gb
+    sol = gpu_solution("h2o2")
+    T0, P, Y0 = h2o2_batch(32, 4)
+    a = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=1e-9)
+    a.advance(1e-3)
+    b = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=1e-9, use_graph=True)
+    b.advance(4e-4)
+    b.advance(1e-3)
+    assert b.time == 1e-3
+    Ta, Tb = a.T, b.T
+    assert np.max(np.abs(Ta - Tb) / Ta) < 1e-6
+    c = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=1e-9, use_graph=True)
+    c.advance(1e-3)
+    assert np.array_equal(c.T, Ta)   # the captured graph runs the same kernel
+
+
+def test_failure_status_without_gpu_fault():
+    """Integration failures are per-reactor status codes, never a device fault."""
+    import cantera_gb300 as gb
+    sol = gpu_solution("h2o2")
+    T0, P, Y0 = h2o2_batch(8, 5)
+    net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), max_steps=5)
+    assert net.advance(1e-3) == 8
+    assert np.all(net.status == 1)
+    T0b = T0.copy()
+    T0b[3] = np.nan
+    net2 = gb.ReactorNet(sol, T0b, P, Y0.T.copy())
+    assert net2.advance(1e-4) == 1
+    st = net2.status
+    assert st[3] == 4 and np.all(np.delete(st, 3) == 0)
+    with pytest.raises(gb.GBError, match="backwards"):
+        net2.advance(1e-5)
