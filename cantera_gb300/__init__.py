@@ -25,7 +25,7 @@ __all__ = ["Solution", "ReactorNet", "library", "DATA_DIR", "GBError"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DATA_DIR = os.path.join(HERE, "data")
-LIB_PATH = os.path.join(HERE, "_build", "libgbchem.so")
+LIB_PATH = os.environ.get("GBCHEM_LIB", os.path.join(HERE, "_build", "libgbchem.so"))
 GB_ERR = -999
 GB_DEVICE_POINTERS = 1
 STAT_NAMES = ["steps", "rhs_evals", "newton_iters", "lin_setups", "jac_evals",

@@ -219,6 +219,43 @@ void packDevMech(MechEntry& e) {
         for (auto& pr : bySpecies[k]) { spRxn.push_back(pr.first); spNu.push_back(pr.second); }
         spPtr.push_back((int)spRxn.size());
     }
+    // gather tasks: species lists cut into pieces of at most `cap` entries, pieces dealt
+    // to lanes heaviest first onto the least-loaded lane
+    std::vector<int> taskPtr(1, 0), taskSp;
+    {
+        const int E = spPtr.back();
+        const int cap = std::max(8, (E + 31) / 32);
+        for (int k = 0; k < K; k++)
+            for (int a0 = spPtr[k]; a0 < spPtr[k + 1]; a0 += cap) {
+                taskPtr.push_back(std::min(a0 + cap, spPtr[k + 1]));
+                taskSp.push_back(k);
+            }
+    }
+    const int NT = (int)taskSp.size();
+    std::vector<int> laneTaskPtr(1, 0), laneTasks, spTaskPtr(1, 0), spTasks;
+    {
+        std::vector<int> ord(NT);
+        std::iota(ord.begin(), ord.end(), 0);
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+            return taskPtr[a + 1] - taskPtr[a] > taskPtr[b + 1] - taskPtr[b];
+        });
+        std::vector<std::vector<int>> lt(32);
+        std::vector<int> ld(32, 0);
+        for (int t : ord) {
+            int l = (int)(std::min_element(ld.begin(), ld.end()) - ld.begin());
+            lt[l].push_back(t);
+            ld[l] += taskPtr[t + 1] - taskPtr[t] + 2;
+        }
+        for (int l = 0; l < 32; l++) {
+            for (int t : lt[l]) laneTasks.push_back(t);
+            laneTaskPtr.push_back((int)laneTasks.size());
+        }
+        for (int k = 0; k < K; k++) {
+            for (int t = 0; t < NT; t++)
+                if (taskSp[t] == k) spTasks.push_back(t);
+            spTaskPtr.push_back((int)spTasks.size());
+        }
+    }
     // third bodies
     std::vector<int> tbRxn(m.tbRxn.size()), tbMA(m.tbMassAction.begin(), m.tbMassAction.end());
     for (size_t t = 0; t < tbRxn.size(); t++) tbRxn[t] = inv[m.tbRxn[t]];
@@ -297,6 +334,8 @@ void packDevMech(MechEntry& e) {
     size_t o_tbRxn = a.add(tbRxn), o_tbDef = a.add(tbDef), o_tbMA = a.add(tbMA), o_tbPtr = a.add(tbPtr),
            o_tbK = a.add(tbK), o_tbE = a.add(tbE);
     size_t o_spPtr = a.add(spPtr), o_spRxn = a.add(spRxn), o_spNu = a.add(spNu);
+    size_t o_taskPtr = a.add(taskPtr), o_ltp = a.add(laneTaskPtr), o_lt = a.add(laneTasks),
+           o_stp = a.add(spTaskPtr), o_st = a.add(spTasks);
     size_t o_colPtr = a.add(colPtr), o_colRxn = a.add(colRxn), o_colE = a.add(colE);
     size_t o_lcp = a.add(laneColPtr), o_lc = a.add(laneCols);
     size_t o_gsPtr = a.add(gsPtr), o_gsTb = a.add(gsTb), o_gsCoef = a.add(gsCoef);
@@ -317,6 +356,9 @@ void packDevMech(MechEntry& e) {
     d.tbRxn = (const int*)(b + o_tbRxn); d.tbDef = (const double*)(b + o_tbDef); d.tbMA = (const int*)(b + o_tbMA);
     d.tbPtr = (const int*)(b + o_tbPtr); d.tbK = (const int*)(b + o_tbK); d.tbE = (const double*)(b + o_tbE);
     d.spPtr = (const int*)(b + o_spPtr); d.spRxn = (const int*)(b + o_spRxn); d.spNu = (const double*)(b + o_spNu);
+    d.NT = NT;
+    d.taskPtr = (const int*)(b + o_taskPtr); d.laneTaskPtr = (const int*)(b + o_ltp); d.laneTasks = (const int*)(b + o_lt);
+    d.spTaskPtr = (const int*)(b + o_stp); d.spTasks = (const int*)(b + o_st);
     d.colPtr = (const int*)(b + o_colPtr); d.colRxn = (const int*)(b + o_colRxn); d.colE = (const double*)(b + o_colE);
     d.laneColPtr = (const int*)(b + o_lcp); d.laneCols = (const int*)(b + o_lc);
     d.gsPtr = (const int*)(b + o_gsPtr); d.gsTb = (const int*)(b + o_gsTb); d.gsCoef = (const double*)(b + o_gsCoef);

@@ -15,7 +15,8 @@ namespace gbchem {
 // four doubles, 32-byte aligned (loaded as two 16-byte vector loads)
 struct alignas(32) D4 { double x, y, z, w; };
 
-constexpr int kMaxSpecies = 256;   // limits of the GPU path (checked at load time)
+constexpr int kMaxSpecies = 255;   // limits of the GPU path (checked at load time)
+constexpr int kMaxN = kMaxSpecies + 1;   // integrated components: T and the species
 constexpr int kNasaStride = 16;    // Tmid, low[7], high[7], pad
 
 // rinfo.x bit fields
@@ -59,6 +60,16 @@ struct DevMech {
     const int* spPtr;            // [K+1]
     const int* spRxn;
     const double* spNu;
+    // the same entries cut into tasks of bounded length for a balanced warp gather:
+    // task t sums entries [taskPtr[t], taskPtr[t+1]) of one species; lane l runs tasks
+    // laneTasks[laneTaskPtr[l] .. laneTaskPtr[l+1]); species k adds the partial sums of
+    // tasks spTasks[spTaskPtr[k] .. spTaskPtr[k+1]) in order
+    int NT;
+    const int* taskPtr;          // [NT+1] into spRxn / spNu
+    const int* laneTaskPtr;      // [33]
+    const int* laneTasks;
+    const int* spTaskPtr;        // [K+1]
+    const int* spTasks;
     // d(wdot)/dc columns: column j -> (reaction, efficiency - default of j or 0)
     const int* colPtr;           // [K+1]
     const int* colRxn;

@@ -19,15 +19,15 @@ namespace gbchem {
 // =============================================================================
 __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
     extern __shared__ double smem[];
-    __shared__ double s_tab[64];
-    loadExpTable(s_tab);
+    __shared__ uint64_t s_tab[64];
+    gbx_load_table(s_tab);
     const DevMech& m = p.m;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     double* base = smem + (size_t)warp * p.warpDoubles;
     KinScratch s;
-    const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF);
-    s.carve(base, m.K, m.R, m.NTB, m.NF);
+    const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
+    s.carve(base, m.K, m.R, m.NTB, m.NF, m.NT);
     s.tab = s_tab;
     double* Yl = base + kinD;
     double* gk = Yl + m.K;
@@ -118,7 +118,7 @@ struct BdfWarp {
     int maxOrder;
     KinScratch s;
     KinState st;
-    double *zn, *ewt, *acor, *y, *ftemp, *tempv, *v1, *v2;
+    double *zn, *ewt, *acor, *y, *ftemp, *tempv, *v1, *v2, *dinv;
     int* piv;
 
     __device__ double wrms(const double* v) const {
@@ -190,19 +190,23 @@ struct BdfWarp {
         }
         const double hJX = warpSum(phj);
         const double rho = st.rho, mmw = st.mmw;
-        const double D = rho * mm.Rgas * (cpmix / mmw);
+        const double rD = 1.0 / (rho * mm.Rgas * (cpmix / mmw));
         const double G = ftemp[0];
+        // v2[k] <- W_k (Jc X)_k - wdot_k W_k mmw / rho, so that the species block is
+        // J[1+k][1+j] = (W_k Jc_kj - v2[k]) / W_j
+        const double c1 = mmw / rho;
+        for (int k = lane; k < K; k += 32) v2[k] = mm.mw[k] * (v2[k] - s.wdot[k] * c1);
         __syncwarp();
+        const double hscale = rho * st.RT, cpscale = rho * mm.Rgas;
         for (int j = lane; j < K; j += 32) {
-            double Wj = mm.mw[j];
+            const double rWj = mm.rmw[j];
             for (int k = 0; k < K; k++) {
-                double Wk = mm.mw[k];
                 MT* p = M + (size_t)(1 + k) * ld + 1 + j;
-                *p = (MT)((Wk / Wj) * ((double)*p - v2[k]) + s.wdot[k] * Wk * mmw / (rho * Wj));
+                *p = (MT)(fma(mm.mw[k], (double)*p, -v2[k]) * rWj);
             }
-            double dH = (rho / Wj) * st.RT * (tempv[j] - hJX);
-            double dD = (rho * mm.Rgas / Wj) * (s.cpR[j] - cpmix);
-            M[1 + j] = (MT)(-(dH + G * dD) / D);
+            double dH = hscale * rWj * (tempv[j] - hJX);
+            double dD = cpscale * rWj * (s.cpR[j] - cpmix);
+            M[1 + j] = (MT)(-(dH + G * dD) * rD);
         }
         __syncwarp();
         // T column: one-sided difference
@@ -233,11 +237,16 @@ struct BdfWarp {
         return luFactor(M);
     }
 
+    // LU with partial pivoting in place (row-major, leading dimension ld).  Afterwards
+    // piv[] holds the gather permutation (row i of P*b is b[piv[i]]) and dinv[] the
+    // reciprocal diagonal of U, both in shared memory.
     template <typename MT>
     __device__ bool luFactor(MT* a) {
         bool nonsingular = true;
+        if (lane == 0)
+            for (int i = 0; i < N; i++) piv[i] = i;
+        __syncwarp();
         for (int k = 0; k < N; k++) {
-            // pivot: largest |a[i][k]|, lowest row index on ties
             double bv = -1.0;
             int bi = N;
             for (int i = k + lane; i < N; i += 32) {
@@ -250,18 +259,18 @@ struct BdfWarp {
                 int oi = __shfl_xor_sync(0xffffffffu, bi, o);
                 if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
             }
-            if (lane == 0) piv[k] = bi;
-            if (!(bv > 0.0)) { nonsingular = false; bi = k; }
+            if (!(bv > 0.0)) { nonsingular = false; break; }
             if (bi != k) {
                 for (int j = lane; j < N; j += 32) {
                     MT t = a[(size_t)k * ld + j];
                     a[(size_t)k * ld + j] = a[(size_t)bi * ld + j];
                     a[(size_t)bi * ld + j] = t;
                 }
+                if (lane == 0) { int t = piv[k]; piv[k] = piv[bi]; piv[bi] = t; }
             }
             __syncwarp();
-            if (!nonsingular) break;
             const MT inv = (MT)1 / a[(size_t)k * ld + k];
+            if (lane == 0) dinv[k] = (double)inv;
             for (int i = k + 1 + lane; i < N; i += 32) a[(size_t)i * ld + k] *= inv;
             __syncwarp();
             for (int j = k + 1 + lane; j < N; j += 32) {
@@ -273,27 +282,50 @@ struct BdfWarp {
         return nonsingular;
     }
 
-    template <typename MT>
+    // Solve (P^T L U) x = b in place.  The vector lives in registers (element i in lane
+    // i % 32, slot i / 32); every substitution step broadcasts one element by a shuffle.
+    template <typename MT, int S>
     __device__ void luSolve(const MT* a, double* b) {
-        if (lane == 0)
-            for (int k = 0; k < N; k++) {
-                int p = piv[k];
-                if (p != k) { double t = b[k]; b[k] = b[p]; b[p] = t; }
+        MT x[S];
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            const int i = lane + 32 * t;
+            x[t] = (i < N) ? (MT)b[piv[i]] : (MT)0;
+        }
+        // forward: unit lower triangle
+#pragma unroll
+        for (int tk = 0; tk < S; tk++) {
+            const int kend = min(N, 32 * (tk + 1));
+            for (int k = 32 * tk; k < kend; k++) {
+                const MT xk = __shfl_sync(0xffffffffu, x[tk], k & 31);
+#pragma unroll
+                for (int t = tk; t < S; t++) {
+                    const int i = lane + 32 * t;
+                    if (i > k && i < N) x[t] -= a[(size_t)i * ld + k] * xk;
+                }
             }
+        }
+        // backward: upper triangle with the stored reciprocal diagonal
+#pragma unroll
+        for (int tk = S - 1; tk >= 0; tk--) {
+            const int kbeg = min(N, 32 * (tk + 1)) - 1;
+            for (int k = kbeg; k >= 32 * tk; k--) {
+                if (lane == (k & 31)) x[tk] = x[tk] * (MT)dinv[k];
+                const MT xk = __shfl_sync(0xffffffffu, x[tk], k & 31);
+#pragma unroll
+                for (int t = 0; t <= tk; t++) {
+                    const int i = lane + 32 * t;
+                    if (i < k) x[t] -= a[(size_t)i * ld + k] * xk;
+                }
+            }
+        }
         __syncwarp();
-        // keep the working vector in the factor's precision
-        for (int k = 0; k < N; k++) {
-            MT bk = (MT)b[k];
-            for (int i = k + 1 + lane; i < N; i += 32) b[i] = (double)((MT)b[i] - a[(size_t)i * ld + k] * bk);
-            __syncwarp();
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            const int i = lane + 32 * t;
+            if (i < N) b[i] = (double)x[t];
         }
-        for (int k = N - 1; k >= 0; k--) {
-            MT bk = (MT)b[k] / a[(size_t)k * ld + k];
-            __syncwarp();
-            if (lane == 0) b[k] = (double)bk;
-            for (int i = lane; i < k; i += 32) b[i] = (double)((MT)b[i] - a[(size_t)i * ld + k] * bk);
-            __syncwarp();
-        }
+        __syncwarp();
     }
 
     __device__ void predict(BdfScal& S) {
@@ -379,7 +411,7 @@ struct BdfWarp {
         S.tq[4] = NLSCOEF / S.tq[2];
     }
 
-    template <typename MT>
+    template <typename MT, int NS>
     __device__ int newton(MT* M, BdfScal& S, bool callSetup) {
         const double rl1 = 1.0 / S.l[1];
         bool jcur = false;
@@ -406,7 +438,7 @@ struct BdfWarp {
                 S.nni++;
                 for (int i = lane; i < N; i += 32) tempv[i] = S.gamma * ftemp[i] - (rl1 * z1[i] + acor[i]);
                 __syncwarp();
-                luSolve<MT>(M, tempv);
+                luSolve<MT, NS>(M, tempv);
                 if (S.gamrat != 1.0) {
                     double f = 2.0 / (1.0 + S.gamrat);
                     for (int i = lane; i < N; i += 32) tempv[i] *= f;
@@ -604,7 +636,7 @@ struct BdfWarp {
     }
 
     // one internal step; returns a status code
-    template <typename MT>
+    template <typename MT, int NS>
     __device__ int step(MT* M, BdfScal& S) {
         const double saved_t = S.tn;
         int ncf = 0, nef = 0;
@@ -631,7 +663,7 @@ struct BdfWarp {
             S.gamrat = (S.nst > 0) ? S.gamma / S.gammap : 1.0;
             bool callSetup = (S.nst == 0) || prevConvFail || (S.nst >= S.nstlp + MSBP) ||
                              (fabs(S.gamrat - 1.0) > DGMAX) || !S.haveLU;
-            int nls = newton<MT>(M, S, callSetup);
+            int nls = newton<MT, NS>(M, S, callSetup);
             if (nls != NLS_OK) {
                 S.ncfn++;
                 ncf++;
@@ -704,11 +736,11 @@ struct BdfWarp {
     }
 };
 
-template <typename MT>
+template <typename MT, int NS>
 __global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
     extern __shared__ double smem[];
-    __shared__ double s_tab[64];
-    loadExpTable(s_tab);
+    __shared__ uint64_t s_tab[64];
+    gbx_load_table(s_tab);
     const DevMech& m = p.m;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -724,8 +756,8 @@ __global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
     W.hmaxInv = p.hmaxInv;
     W.maxOrder = p.maxOrder;
     const int N = m.N;
-    const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF);
-    W.s.carve(base, m.K, m.R, m.NTB, m.NF);
+    const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
+    W.s.carve(base, m.K, m.R, m.NTB, m.NF, m.NT);
     W.s.tab = s_tab;
     double* q = base + kinD;
     W.zn = q; q += (QMAX + 1) * N;
@@ -736,6 +768,7 @@ __global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
     W.tempv = q; q += N;
     W.v1 = q; q += N;
     W.v2 = q; q += N;
+    W.dinv = q; q += N;
     W.piv = (int*)q; q += (N + 1) / 2;
     MT* M = (MT*)q;
 
@@ -811,7 +844,7 @@ __global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
         long long count = 0;
         while (status == ST_OK && S.tn < p.tout) {
             if (count >= p.maxSteps) { status = ST_MAX_STEPS; break; }
-            status = W.step<MT>(M, S);
+            status = W.step<MT, NS>(M, S);
             count++;
         }
         // output: interpolate to tout (or the last state on failure)
@@ -846,22 +879,28 @@ __global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
     }
 }
 
-template __global__ void k_bdf<double>(BdfParams);
-template __global__ void k_bdf<float>(BdfParams);
+template <typename MT, int NS>
+cudaError_t launchBdfT(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
+    size_t smem = (size_t)p.warpDoubles * 8 * warpsPerBlock;
+    cudaError_t e = cudaFuncSetAttribute(k_bdf<MT, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_bdf<MT, NS><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
+    return cudaGetLastError();
+}
 
 int bdfRecordStride(int N) { return (QMAX + 1) * N + R_NSCAL; }
 
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32) {
     int N = m.N;
-    int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF);
-    int vec = (QMAX + 1) * N + 7 * N + (N + 1) / 2;
+    int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
+    int vec = (QMAX + 1) * N + 8 * N + (N + 1) / 2;
     int mat = fp32 ? (N * ld + 1) / 2 : N * ld;
     int tot = kinD + vec + mat;
     return (tot + 1) & ~1;   // keep each warp's slice 16-byte aligned
 }
 
 int ratesWarpDoubles(const DevMech& m) {
-    int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF);
+    int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
     int tot = kinD + 2 * m.K + m.K * (m.K + 1);
     return (tot + 1) & ~1;
 }
@@ -875,18 +914,14 @@ cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cud
 }
 
 cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream) {
-    size_t smem = (size_t)p.warpDoubles * 8 * warpsPerBlock;
-    cudaError_t e;
-    if (fp32) {
-        e = cudaFuncSetAttribute(k_bdf<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        k_bdf<float><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
-    } else {
-        e = cudaFuncSetAttribute(k_bdf<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        k_bdf<double><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
-    }
-    return cudaGetLastError();
+    // register slots of the Newton vector per lane: 32 components each
+    const int N = p.m.N;
+    if (N <= 64) return fp32 ? launchBdfT<float, 2>(p, blocks, warpsPerBlock, stream)
+                             : launchBdfT<double, 2>(p, blocks, warpsPerBlock, stream);
+    if (N <= 128) return fp32 ? launchBdfT<float, 4>(p, blocks, warpsPerBlock, stream)
+                              : launchBdfT<double, 4>(p, blocks, warpsPerBlock, stream);
+    return fp32 ? launchBdfT<float, 8>(p, blocks, warpsPerBlock, stream)
+                : launchBdfT<double, 8>(p, blocks, warpsPerBlock, stream);
 }
 
 // -----------------------------------------------------------------------------
@@ -914,8 +949,8 @@ __global__ void k_probe_exp(double* out, int iters, int useLog) {
 }
 
 __global__ void k_check_exp(int n, const double* x, double* mine, double* lib) {
-    __shared__ double s_tab[64];
-    loadExpTable(s_tab);
+    __shared__ uint64_t s_tab[64];
+    gbx_load_table(s_tab);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         mine[i] = fexp(x[i], s_tab);
         lib[i] = exp(x[i]);

@@ -18,6 +18,7 @@
 #include <math.h>
 
 #include "devmech.h"
+#include "fastexp.h"
 
 namespace gbchem {
 
@@ -32,68 +33,12 @@ __device__ __forceinline__ double warpMax(double v) {
     return v;
 }
 
-// ---------------------------------------------------------------------------
-// FP64 exponential (table-driven method of P. T. P. Tang, ACM TOMS 15(2), 1989):
-// x = (64 e + j) ln2/64 + r with |r| <= ln2/128, exp(x) = 2^e * 2^(j/64) * exp(r), exp(r)
-// by its Taylor polynomial to r^5 (truncation < 4e-17).  Ten FP64 operations against
-// about twenty for the library exp.  Arguments with |x| >= 700, infinities and NaN take
-// the library exp.  The 64-entry table 2^(j/64) (correctly rounded) sits in shared memory.
-// ---------------------------------------------------------------------------
-__device__ __constant__ double c_exp2tab[64] = {
-    1.0, 1.0108892860517005, 1.0218971486541166, 1.0330248790212284,
-    1.0442737824274138, 1.0556451783605572, 1.0671404006768237, 1.0787607977571199,
-    1.0905077326652577, 1.102382583307841, 1.1143867425958924, 1.1265216186082418,
-    1.1387886347566916, 1.1511892299529827, 1.1637248587775775, 1.1763969916502812,
-    1.189207115002721, 1.202156731452703, 1.215247359980469, 1.22848053610687,
-    1.241857812073484, 1.255380757024691, 1.2690509571917332, 1.2828700160787783,
-    1.2968395546510096, 1.3109612115247644, 1.3252366431597413, 1.339667524053303,
-    1.3542555469368927, 1.3690024229745905, 1.383909881963832, 1.3989796725383112,
-    1.4142135623730951, 1.42961333839197, 1.4451808069770467, 1.460917794180647,
-    1.4768261459394993, 1.4929077282912648, 1.5091644275934228, 1.5255981507445384,
-    1.5422108254079407, 1.559004400237837, 1.5759808451078865, 1.593142151342267,
-    1.6104903319492543, 1.6280274218573478, 1.645755478153965, 1.6636765803267364,
-    1.681792830507429, 1.7001063537185235, 1.718619298122478, 1.7373338352737062,
-    1.7562521603732995, 1.7753764925265212, 1.7947090750031072, 1.8142521755003989,
-    1.8340080864093424, 1.8539791250833855, 1.8741676341103, 1.8945759815869656,
-    1.9152065613971474, 1.9360617934922943, 1.9571441241754002, 1.978456026387951};
-
-// Load the table into a block's shared copy (call before the first fexp; all threads).
-__device__ __forceinline__ void loadExpTable(double* tab) {
-    for (int j = threadIdx.x; j < 64; j += blockDim.x) tab[j] = c_exp2tab[j];
-    __syncthreads();
-}
-
-// |x| >= 700, infinity or NaN
-__device__ __forceinline__ bool expBigArg(double x) {
-    return (__double2hiint(x) & 0x7fffffff) >= 0x4085E000;
-}
-// exp(x) = m * 2^e with m in (0.99, 2.01); requires !expBigArg(x)
-__device__ __forceinline__ double expSplit(double x, const double* tab, int& e) {
-    const double shifter = 6755399441055744.0;            // 1.5 * 2^52: rounds to an integer
-    const double t = fma(x, 92.33248261689366, shifter);   // x * 64/ln2
-    const int k = __double2loint(t);
-    const double kd = t - shifter;
-    double r = fma(-kd, 0.010830424726009369, x);          // ln2/64, high part (24 bits)
-    r = fma(-kd, -2.9760223436840126e-11, r);              // ln2/64, low part
-    double q = fma(r, 1.0 / 120.0, 1.0 / 24.0);
-    q = fma(q, r, 1.0 / 6.0);
-    q = fma(q, r, 0.5);
-    q = fma(q, r, 1.0);
-    const double p = q * r;
-    const double T = tab[k & 63];
-    e = k >> 6;
-    return fma(T, p, T);
-}
 // m * 2^e by an exponent-field add; the caller guarantees a normal result
 __device__ __forceinline__ double scale2(double m, int e) {
     return __longlong_as_double(__double_as_longlong(m) + ((long long)e << 52));
 }
-__device__ __forceinline__ double fexp(double x, const double* tab) {
-    if (expBigArg(x)) return exp(x);
-    int e;
-    const double m = expSplit(x, tab, e);
-    return scale2(m, e);
-}
+__device__ __forceinline__ double fexp(double x, const uint64_t* tab) { return gbx_exp(x, tab); }
+
 // a < 0 and b < 0 (IEEE comparison semantics, -0 is not negative) on the integer pipe
 __device__ __forceinline__ bool bothNeg(double a, double b) {
     const long long la = __double_as_longlong(a), lb = __double_as_longlong(b);
@@ -114,24 +59,27 @@ struct KinScratch {
     double* Mtb;    // third-body concentrations [NTB]
     double* Qtb;    // d(rop)/d[M] per third-body reaction [NTB]
     double* dlk;    // d ln k / d[M] of falloff reactions [NF]
-    double* em;     // exp(g) = em * 2^ee [K]
-    double* emi;    // exp(-g) = emi * 2^eei [K]
-    int* ee;        // [K]
-    int* eei;       // [K]
+    uint64_t* xu;   // exp(g) = xu / 2^63 * 2^xe  [K]
+    uint64_t* xiu;  // exp(-g) = xiu / 2^63 * 2^xie  [K]
+    int* xe;        // [K]
+    int* xie;       // [K]
     double* pw;     // (RT/P)^dn for dn = -3..3 [8]
-    const double* tab;   // 2^(j/64) table (block shared)
+    const uint64_t* tab;   // 2^(j/64) table (block shared)
     int* flags;     // [2] per-state flags (bit 0: some |g| >= 700)
-    __host__ __device__ static int doubles(int K, int R, int NTB, int NF) {
-        return 5 * K + 3 * R + 2 * NTB + NF + 2 * K + K + 8 + 2;
+    double* part;   // partial sums of the gather tasks [NT]
+    // (xu, xiu need 8-byte alignment: they follow doubles)
+    __host__ __device__ static int doubles(int K, int R, int NTB, int NF, int NT) {
+        return 5 * K + 3 * R + 2 * NTB + NF + 2 * K + K + 8 + 2 + NT;
     }
-    __device__ void carve(double* p, int K, int R, int NTB, int NF) {
+    __device__ void carve(double* p, int K, int R, int NTB, int NF, int NT) {
         c = p; p += K; cpR = p; p += K; hRT = p; p += K; g = p; p += K; wdot = p; p += K;
         rop = p; p += R; kfe = p; p += R; rkc = p; p += R;
         Mtb = p; p += NTB; Qtb = p; p += NTB; dlk = p; p += NF;
-        em = p; p += K; emi = p; p += K;
-        ee = (int*)p; eei = ee + K; p += K;
+        xu = (uint64_t*)p; p += K; xiu = (uint64_t*)p; p += K;
+        xe = (int*)p; xie = xe + K; p += K;
         pw = p; p += 8;
-        flags = (int*)p;
+        flags = (int*)p; p += 2;
+        part = p;
     }
 };
 
@@ -203,13 +151,13 @@ __device__ __forceinline__ double massActionDeriv(const DevMech& m, int bucket, 
 }
 
 __device__ __forceinline__ double arrhenius(double A, double b, double EaR, double lnT, double recipT,
-                                            const double* tab) {
+                                            const uint64_t* tab) {
     return A * fexp(b * lnT - EaR * recipT, tab);
 }
 
 // Falloff rate k(T, M) and, optionally, d ln k / d M (analytic).
 __device__ __forceinline__ double falloff(D4 f1, D4 f2, double A, double b, double EaR,
-                                          const KinState& st, double M, double* dlnk_dM, const double* tab) {
+                                          const KinState& st, double M, double* dlnk_dM, const uint64_t* tab) {
     double work = 0.0;
     bool troe = f2.w != 0.0;
     if (troe) {
@@ -288,12 +236,13 @@ __device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, i
         s.g[k] = gk;
         // exp(+-g) with split exponents: Kc of each reaction is then a product over its
         // species instead of one exponential per reaction
-        if (!expBigArg(gk)) {
-            int e1, e2;
-            s.em[k] = expSplit(gk, s.tab, e1);
-            s.emi[k] = expSplit(-gk, s.tab, e2);
-            s.ee[k] = e1;
-            s.eei[k] = e2;
+        if (!gbx_big(gk)) {
+            XVal a, b;
+            gbx_exp_pm(gk, a, b, s.tab);
+            s.xu[k] = a.u;
+            s.xe[k] = a.e;
+            s.xiu[k] = b.u;
+            s.xie[k] = b.e;
         } else {
             s.flags[0] = 1;
         }
@@ -343,18 +292,18 @@ __device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, i
         if (info.x & kRevBit) {
             bool done = false;
             if (!bigG && pb != 0 && rb != 0 && (info.x & kDnIntBit)) {
-                // 1/Kc = prod_p exp(g_p) * prod_r exp(-g_r) * (RT/P)^dn, exponents carried
-                // separately so that no partial product overflows
-                double mp = s.em[pe.x];
-                int ex = s.ee[pe.x];
-                if (pe.w > 1) { mp *= s.em[pe.y]; ex += s.ee[pe.y]; }
-                if (pe.w > 2) { mp *= s.em[pe.z]; ex += s.ee[pe.z]; }
-                mp *= s.emi[re.x];
-                ex += s.eei[re.x];
-                if (re.w > 1) { mp *= s.emi[re.y]; ex += s.eei[re.y]; }
-                if (re.w > 2) { mp *= s.emi[re.z]; ex += s.eei[re.z]; }
-                if (ex > -980 && ex < 960) {
-                    rkc = scale2(mp * s.pw[(int)ar.w + 3], ex);
+                // 1/Kc = prod_p exp(g_p) * prod_r exp(-g_r) * (RT/P)^dn, multiplied in Q63
+                // fixed point on the integer pipe and converted to double once
+                XVal v{s.xu[pe.x], s.xe[pe.x]};
+                if (pe.w > 1) v = gbx_mul(v, XVal{s.xu[pe.y], s.xe[pe.y]});
+                if (pe.w > 2) v = gbx_mul(v, XVal{s.xu[pe.z], s.xe[pe.z]});
+                v = gbx_mul(v, XVal{s.xiu[re.x], s.xie[re.x]});
+                if (re.w > 1) v = gbx_mul(v, XVal{s.xiu[re.y], s.xie[re.y]});
+                if (re.w > 2) v = gbx_mul(v, XVal{s.xiu[re.z], s.xie[re.z]});
+                if (v.e > -980 && v.e < 960) {
+                    int c;
+                    const double mant = gbx_mant(v.u, c);
+                    rkc = scale2(mant * s.pw[(int)ar.w + 3], v.e + c);
                     done = true;
                 }
             }
@@ -392,9 +341,17 @@ __device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, i
         }
     }
     __syncwarp();
+    // wdot_k = sum_i nu_ki rop_i: balanced tasks, then a fixed-order sum per species
+    for (int q = m.laneTaskPtr[lane]; q < m.laneTaskPtr[lane + 1]; q++) {
+        const int t = m.laneTasks[q];
+        double w = 0.0;
+        for (int e = m.taskPtr[t]; e < m.taskPtr[t + 1]; e++) w = fma(m.spNu[e], s.rop[m.spRxn[e]], w);
+        s.part[t] = w;
+    }
+    __syncwarp();
     for (int k = lane; k < m.K; k += 32) {
         double w = 0.0;
-        for (int q = m.spPtr[k]; q < m.spPtr[k + 1]; q++) w += m.spNu[q] * s.rop[m.spRxn[q]];
+        for (int q = m.spTaskPtr[k]; q < m.spTaskPtr[k + 1]; q++) w += s.part[m.spTasks[q]];
         s.wdot[k] = w;
     }
     __syncwarp();
