@@ -13,7 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgbchem.so")
 SOURCES = ["capi.cu", "kernels.cu", "mechanism.cpp", "yaml_lite.cpp"]
-HEADERS = ["devmech.h", "kernels.h", "kinetics.cuh", "mechanism.h", "yaml_lite.h"]
+HEADERS = ["devmech.h", "fastexp.h", "kernels.h", "kinetics.cuh", "mechanism.h", "yaml_lite.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

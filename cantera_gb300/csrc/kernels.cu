@@ -96,10 +96,17 @@ struct BdfScal {
     int q, qprime, qwait, L, nst, nstlp;
     bool haveLU;
     // ignition marker
-    double ls_t, ls_v, pv_t, pv_v, bs_t, bs_v, nx_t, nx_v;
-    int nsamp, flags, status0;
-    long long nrhs, nni, nsetups, nje, netf, ncfn;
+    int status0;
 };
+
+// Per-warp bookkeeping touched only by lane 0 (kept out of registers): the ignition
+// marker and the solver counters.
+struct WarpAux {
+    double ls_t, ls_v, pv_t, pv_v, bs_t, bs_v, nx_t, nx_v;
+    long long nrhs, nni, nsetups, nje, netf, ncfn;
+    int nsamp, flags;
+};
+constexpr int kAuxDoubles = (int)((sizeof(WarpAux) + 7) / 8);
 
 // a[i] for a run-time i with every access at a compile-time index (keeps a[] in registers)
 template <int N>
@@ -111,13 +118,195 @@ __device__ __forceinline__ double sel(const double (&a)[N], int i) {
     return v;
 }
 
+// ---------------------------------------------------------------------------
+// The large per-warp routines are kept out of line (one copy of their code: the
+// integrator reaches them from several places) and take plain arguments, so that the
+// integrator's own state stays in registers.  A warp's shared-memory slice starts with
+// the KinState of its last right-hand side (kStateSlots doubles), then the kinetics
+// scratch.
+// ---------------------------------------------------------------------------
+constexpr int kStateSlots = 8;
+
+__device__ __forceinline__ void carveScratch(const DevMech& m, double* base, const uint64_t* tab, KinScratch& s) {
+    s.carve(base + kStateSlots, m.K, m.R, m.NTB, m.NF, m.NT);
+    s.tab = tab;
+}
+__device__ __forceinline__ void loadState(const double* base, KinState& st) {
+    st.T = base[0]; st.P = base[1]; st.RT = base[2]; st.rho = base[3];
+    st.mmw = base[4]; st.ctot = base[5]; st.lnT = base[6]; st.recipT = base[7];
+}
+
+// reactor right-hand side at z = [T, Y]; returns true when every derivative is finite
+__device__ __noinline__ bool devRhs(const DevMech& m, double* base, const uint64_t* tab, double P,
+                                    const double* z, double* zdot, int lane) {
+    KinScratch s;
+    carveScratch(m, base, tab, s);
+    KinState st;
+    warpState(m, z[0], P, z + 1, s, st, lane);
+    __syncwarp();
+    warpRates<true>(m, s, st, lane);
+    if (lane == 0) {
+        base[0] = st.T; base[1] = st.P; base[2] = st.RT; base[3] = st.rho;
+        base[4] = st.mmw; base[5] = st.ctot; base[6] = st.lnT; base[7] = st.recipT;
+    }
+    double ph = 0.0, pc = 0.0;
+    for (int k = lane; k < m.K; k += 32) {
+        ph += s.wdot[k] * s.hRT[k];
+        pc += s.c[k] * s.cpR[k];
+    }
+    const double hw = warpSum(ph);
+    const double rrho = 1.0 / st.rho;
+    const double cpmass = m.Rgas * (warpSum(pc) * rrho);
+    const double dTdt = -(hw * st.RT) * rrho / cpmass;
+    bool ok = isfinite(dTdt);
+    if (lane == 0) zdot[0] = dTdt;
+    for (int k = lane; k < m.K; k += 32) {
+        const double v = s.wdot[k] * m.mw[k] * rrho;
+        zdot[1 + k] = v;
+        ok = ok && isfinite(v);
+    }
+    __syncwarp();
+    return __all_sync(0xffffffffu, ok);
+}
+
+    // LU with partial pivoting in place (row-major, leading dimension ld).  Afterwards
+// piv[] holds the gather permutation (row i of P*b is b[piv[i]]) and dinv[] the
+// reciprocal diagonal of U, both in shared memory.
+template <typename MT>
+__device__ __noinline__ bool devLuFactor(MT* a, int N, int ld, int* piv, double* dinv, int lane) {
+    bool nonsingular = true;
+    if (lane == 0)
+        for (int i = 0; i < N; i++) piv[i] = i;
+    __syncwarp();
+    for (int k = 0; k < N; k++) {
+        double bv = -1.0;
+        int bi = N;
+        for (int i = k + lane; i < N; i += 32) {
+            double v = fabs((double)a[(size_t)i * ld + k]);
+            if (v > bv) { bv = v; bi = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+        }
+        if (!(bv > 0.0)) { nonsingular = false; break; }
+        if (bi != k) {
+            for (int j = lane; j < N; j += 32) {
+                MT t = a[(size_t)k * ld + j];
+                a[(size_t)k * ld + j] = a[(size_t)bi * ld + j];
+                a[(size_t)bi * ld + j] = t;
+            }
+            if (lane == 0) { int t = piv[k]; piv[k] = piv[bi]; piv[bi] = t; }
+        }
+        __syncwarp();
+        const MT inv = (MT)1 / a[(size_t)k * ld + k];
+        if (lane == 0) dinv[k] = (double)inv;
+        for (int i = k + 1 + lane; i < N; i += 32) a[(size_t)i * ld + k] *= inv;
+        __syncwarp();
+        for (int j = k + 1 + lane; j < N; j += 32) {
+            const MT u = a[(size_t)k * ld + j];
+            for (int i = k + 1; i < N; i++) a[(size_t)i * ld + j] -= a[(size_t)i * ld + k] * u;
+        }
+        __syncwarp();
+    }
+    return nonsingular;
+}
+
+// Newton matrix M = I - gamma*J (J analytic in the species columns, one-sided
+// difference in T), factored in place.  The kinetics scratch must hold the state y
+// (the last right-hand side was evaluated at y, giving ftemp).  Returns false if J is
+// not finite or M singular.
+template <typename MT>
+__device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uint64_t* tab, MT* M, int ld,
+                                      double gamma, double P, const double* y, const double* ftemp,
+                                      double* v1, double* v2, double* tempv, int* piv, double* dinv,
+                                      int lane) {
+    const int K = mm.K, N = mm.N;
+    KinScratch s;
+    carveScratch(mm, base, tab, s);
+    KinState st;
+    loadState(base, st);
+    for (int q = lane; q < N * ld; q += 32) M[q] = (MT)0;
+    __syncwarp();
+    warpJacC<MT>(mm, s, M + ld + 1, ld, lane);
+    // v1 = X (mole fractions); v2[k] = (Jc X)_k
+    const double rct = 1.0 / st.ctot;
+    for (int k = lane; k < K; k += 32) v1[k] = s.c[k] * rct;
+    __syncwarp();
+    for (int k = lane; k < K; k += 32) {
+        const MT* row = M + (size_t)(1 + k) * ld + 1;
+        double a = 0.0;
+        for (int l = 0; l < K; l++) a += (double)row[l] * v1[l];
+        v2[k] = a;
+    }
+    double pcp = 0.0;
+    for (int k = lane; k < K; k += 32) pcp += v1[k] * s.cpR[k];
+    const double cpmix = warpSum(pcp);
+    __syncwarp();
+    // column pass: hJ_j, then the transformed species block and the T row
+    double phj = 0.0;
+    for (int j = lane; j < K; j += 32) {
+        double a = 0.0;
+        for (int k = 0; k < K; k++) a += s.hRT[k] * (double)M[(size_t)(1 + k) * ld + 1 + j];
+        tempv[j] = a;
+        phj += a * v1[j];
+    }
+    const double hJX = warpSum(phj);
+    const double rho = st.rho, mmw = st.mmw;
+    const double rD = 1.0 / (rho * mm.Rgas * (cpmix / mmw));
+    const double G = ftemp[0];
+    // v2[k] <- W_k (Jc X)_k - wdot_k W_k mmw / rho: J[1+k][1+j] = (W_k Jc_kj - v2[k]) / W_j
+    const double c1 = mmw / rho;
+    for (int k = lane; k < K; k += 32) v2[k] = mm.mw[k] * (v2[k] - s.wdot[k] * c1);
+    __syncwarp();
+    const double hscale = rho * st.RT, cpscale = rho * mm.Rgas;
+    for (int j = lane; j < K; j += 32) {
+        const double rWj = mm.rmw[j];
+        for (int k = 0; k < K; k++) {
+            MT* p = M + (size_t)(1 + k) * ld + 1 + j;
+            *p = (MT)(fma(mm.mw[k], (double)*p, -v2[k]) * rWj);
+        }
+        const double dH = hscale * rWj * (tempv[j] - hJX);
+        const double dD = cpscale * rWj * (s.cpR[j] - cpmix);
+        M[1 + j] = (MT)(-(dH + G * dD) * rD);
+    }
+    __syncwarp();
+    // T column: one-sided difference
+    const double T0 = y[0];
+    const double dT = sqrt(UROUND) * fmax(1.0, fabs(T0));
+    for (int i = lane; i < N; i += 32) tempv[i] = y[i];
+    __syncwarp();
+    if (lane == 0) tempv[0] = T0 + dT;
+    __syncwarp();
+    bool ok = devRhs(mm, base, tab, P, tempv, v1, lane);
+    const double rdT = 1.0 / dT;
+    for (int i = lane; i < N; i += 32) M[(size_t)i * ld] = (MT)((v1[i] - ftemp[i]) * rdT);
+    __syncwarp();
+    // M = I - gamma*J
+    bool fin = true;
+    for (int q = lane; q < N * ld; q += 32) {
+        const double v = -gamma * (double)M[q];
+        fin = fin && isfinite(v);
+        M[q] = (MT)v;
+    }
+    __syncwarp();
+    for (int i = lane; i < N; i += 32) M[(size_t)i * ld + i] = (MT)((double)M[(size_t)i * ld + i] + 1.0);
+    __syncwarp();
+    ok = __all_sync(0xffffffffu, ok && fin);
+    if (!ok) return false;
+    return devLuFactor<MT>(M, N, ld, piv, dinv, lane);
+}
+
 struct BdfWarp {
     const DevMech* m;
     int N, Nnorm, lane, ld;
     double P, rtol, atol, hmaxInv;
     int maxOrder;
-    KinScratch s;
-    KinState st;
+    double* base;            // the warp's shared-memory slice
+    const uint64_t* tab;     // exp table (block shared)
+    WarpAux* aux;            // lane 0 only
     double *zn, *ewt, *acor, *y, *ftemp, *tempv, *v1, *v2, *dinv;
     int* piv;
 
@@ -131,155 +320,14 @@ struct BdfWarp {
         for (int i = lane; i < N; i += 32) ewt[i] = 1.0 / (rtol * fabs(yv[i]) + atol);
         __syncwarp();
     }
-    // reactor right-hand side; returns true when every derivative is finite
     __device__ bool rhs(const double* z, double* zdot, BdfScal& S) {
-        const DevMech& mm = *m;
-        S.nrhs++;
-        warpState(mm, z[0], P, z + 1, s, st, lane);
-        __syncwarp();
-        warpRates<true>(mm, s, st, lane);
-        double ph = 0.0, pc = 0.0;
-        for (int k = lane; k < mm.K; k += 32) {
-            ph += s.wdot[k] * s.hRT[k];
-            pc += s.c[k] * s.cpR[k];
-        }
-        double hw = warpSum(ph);
-        double cpmass = mm.Rgas * (warpSum(pc) / st.rho);
-        double dTdt = -(hw * st.RT) / (st.rho * cpmass);
-        bool ok = isfinite(dTdt);
-        if (lane == 0) zdot[0] = dTdt;
-        for (int k = lane; k < mm.K; k += 32) {
-            double v = s.wdot[k] * mm.mw[k] / st.rho;
-            zdot[1 + k] = v;
-            ok = ok && isfinite(v);
-        }
-        __syncwarp();
-        return __all_sync(0xffffffffu, ok);
+        if (lane == 0) aux->nrhs++;
+        return devRhs(*m, base, tab, P, z, zdot, lane);
     }
-
-    // Newton matrix M = I - gamma*J (J analytic in the species columns, one-sided
-    // difference in T), factored in place.  Returns false if J is not finite or M singular.
     template <typename MT>
     __device__ bool setup(MT* M, BdfScal& S) {
-        const DevMech& mm = *m;
-        const int K = mm.K;
-        // the kinetics scratch holds the state of y (the last rhs call was at y)
-        for (int q = lane; q < N * ld; q += 32) M[q] = (MT)0;
-        __syncwarp();
-        warpJacC<MT>(mm, s, M + ld + 1, ld, lane);
-        // v1 = X (mole fractions); v2[k] = (Jc X)_k; later hJ
-        for (int k = lane; k < K; k += 32) v1[k] = s.c[k] / st.ctot;
-        __syncwarp();
-        for (int k = lane; k < K; k += 32) {
-            const MT* row = M + (size_t)(1 + k) * ld + 1;
-            double a = 0.0;
-            for (int l = 0; l < K; l++) a += (double)row[l] * v1[l];
-            v2[k] = a;
-        }
-        double pcp = 0.0;
-        for (int k = lane; k < K; k += 32) pcp += v1[k] * s.cpR[k];
-        const double cpmix = warpSum(pcp);
-        __syncwarp();
-        // column pass: hJ_j, the transformed species block, and the T row
-        double phj = 0.0;
-        for (int j = lane; j < K; j += 32) {
-            double a = 0.0;
-            for (int k = 0; k < K; k++) a += s.hRT[k] * (double)M[(size_t)(1 + k) * ld + 1 + j];
-            tempv[j] = a;   // hJ_j (tempv is free during setup)
-            phj += a * v1[j];
-        }
-        const double hJX = warpSum(phj);
-        const double rho = st.rho, mmw = st.mmw;
-        const double rD = 1.0 / (rho * mm.Rgas * (cpmix / mmw));
-        const double G = ftemp[0];
-        // v2[k] <- W_k (Jc X)_k - wdot_k W_k mmw / rho, so that the species block is
-        // J[1+k][1+j] = (W_k Jc_kj - v2[k]) / W_j
-        const double c1 = mmw / rho;
-        for (int k = lane; k < K; k += 32) v2[k] = mm.mw[k] * (v2[k] - s.wdot[k] * c1);
-        __syncwarp();
-        const double hscale = rho * st.RT, cpscale = rho * mm.Rgas;
-        for (int j = lane; j < K; j += 32) {
-            const double rWj = mm.rmw[j];
-            for (int k = 0; k < K; k++) {
-                MT* p = M + (size_t)(1 + k) * ld + 1 + j;
-                *p = (MT)(fma(mm.mw[k], (double)*p, -v2[k]) * rWj);
-            }
-            double dH = hscale * rWj * (tempv[j] - hJX);
-            double dD = cpscale * rWj * (s.cpR[j] - cpmix);
-            M[1 + j] = (MT)(-(dH + G * dD) * rD);
-        }
-        __syncwarp();
-        // T column: one-sided difference
-        const double T0 = y[0];
-        const double dT = sqrt(UROUND) * fmax(1.0, fabs(T0));
-        for (int i = lane; i < N; i += 32) tempv[i] = y[i];
-        __syncwarp();
-        if (lane == 0) tempv[0] = T0 + dT;
-        __syncwarp();
-        bool ok = rhs(tempv, v1, S);
-        for (int i = lane; i < N; i += 32) M[(size_t)i * ld] = (MT)((v1[i] - ftemp[i]) / dT);
-        __syncwarp();
-        // M = I - gamma*J
-        const double g = S.gamma;
-        bool fin = true;
-        for (int q = lane; q < N * ld; q += 32) {
-            double v = -g * (double)M[q];
-            fin = fin && isfinite(v);
-            M[q] = (MT)v;
-        }
-        __syncwarp();
-        for (int i = lane; i < N; i += 32) M[(size_t)i * ld + i] = (MT)((double)M[(size_t)i * ld + i] + 1.0);
-        __syncwarp();
-        ok = __all_sync(0xffffffffu, ok && fin);
-        S.nje++;
-        S.nsetups++;
-        if (!ok) return false;
-        return luFactor(M);
-    }
-
-    // LU with partial pivoting in place (row-major, leading dimension ld).  Afterwards
-    // piv[] holds the gather permutation (row i of P*b is b[piv[i]]) and dinv[] the
-    // reciprocal diagonal of U, both in shared memory.
-    template <typename MT>
-    __device__ bool luFactor(MT* a) {
-        bool nonsingular = true;
-        if (lane == 0)
-            for (int i = 0; i < N; i++) piv[i] = i;
-        __syncwarp();
-        for (int k = 0; k < N; k++) {
-            double bv = -1.0;
-            int bi = N;
-            for (int i = k + lane; i < N; i += 32) {
-                double v = fabs((double)a[(size_t)i * ld + k]);
-                if (v > bv) { bv = v; bi = i; }
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                double ov = __shfl_xor_sync(0xffffffffu, bv, o);
-                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-            }
-            if (!(bv > 0.0)) { nonsingular = false; break; }
-            if (bi != k) {
-                for (int j = lane; j < N; j += 32) {
-                    MT t = a[(size_t)k * ld + j];
-                    a[(size_t)k * ld + j] = a[(size_t)bi * ld + j];
-                    a[(size_t)bi * ld + j] = t;
-                }
-                if (lane == 0) { int t = piv[k]; piv[k] = piv[bi]; piv[bi] = t; }
-            }
-            __syncwarp();
-            const MT inv = (MT)1 / a[(size_t)k * ld + k];
-            if (lane == 0) dinv[k] = (double)inv;
-            for (int i = k + 1 + lane; i < N; i += 32) a[(size_t)i * ld + k] *= inv;
-            __syncwarp();
-            for (int j = k + 1 + lane; j < N; j += 32) {
-                const MT u = a[(size_t)k * ld + j];
-                for (int i = k + 1; i < N; i++) a[(size_t)i * ld + j] -= a[(size_t)i * ld + k] * u;
-            }
-            __syncwarp();
-        }
-        return nonsingular;
+        if (lane == 0) { aux->nje++; aux->nsetups++; aux->nrhs++; }   // nrhs: the difference in T
+        return devSetup<MT>(*m, base, tab, M, ld, S.gamma, P, y, ftemp, v1, v2, tempv, piv, dinv, lane);
     }
 
     // Solve (P^T L U) x = b in place.  The vector lives in registers (element i in lane
@@ -435,7 +483,7 @@ struct BdfWarp {
             bool retry = false;
             const double* z1 = Z(1);
             for (;;) {
-                S.nni++;
+                if (lane == 0) aux->nni++;
                 for (int i = lane; i < N; i += 32) tempv[i] = S.gamma * ftemp[i] - (rl1 * z1[i] + acor[i]);
                 __syncwarp();
                 luSolve<MT, NS>(M, tempv);
@@ -517,21 +565,25 @@ struct BdfWarp {
         __syncwarp();
     }
 
-    __device__ void recordSample(BdfScal& S, double t, double v) {
-        if (S.flags & F_AWAIT) { S.nx_t = t; S.nx_v = v; S.flags = (S.flags & ~F_AWAIT) | F_HASRIGHT; }
-        if (S.nsamp == 0 || v > S.bs_v) {
-            S.pv_t = S.ls_t; S.pv_v = S.ls_v;
-            S.flags = (S.nsamp > 0) ? (S.flags | F_HASPREV) : (S.flags & ~F_HASPREV);
-            S.bs_t = t; S.bs_v = v;
-            S.flags = (S.flags | F_AWAIT) & ~F_HASRIGHT;
+    // lane 0 only
+    __device__ void recordSample(double t, double v) {
+        if (lane != 0) return;
+        WarpAux& A = *aux;
+        if (A.flags & F_AWAIT) { A.nx_t = t; A.nx_v = v; A.flags = (A.flags & ~F_AWAIT) | F_HASRIGHT; }
+        if (A.nsamp == 0 || v > A.bs_v) {
+            A.pv_t = A.ls_t; A.pv_v = A.ls_v;
+            A.flags = (A.nsamp > 0) ? (A.flags | F_HASPREV) : (A.flags & ~F_HASPREV);
+            A.bs_t = t; A.bs_v = v;
+            A.flags = (A.flags | F_AWAIT) & ~F_HASRIGHT;
         }
-        S.ls_t = t; S.ls_v = v;
-        S.nsamp++;
+        A.ls_t = t; A.ls_v = v;
+        A.nsamp++;
     }
-    __device__ double ignitionTime(const BdfScal& S) const {
-        if (!(S.flags & F_HASPREV) || !(S.flags & F_HASRIGHT)) return S.bs_t;
-        double t0 = S.pv_t, t1 = S.bs_t, t2 = S.nx_t;
-        double s0 = (S.bs_v - S.pv_v) / (t1 - t0), s1 = (S.nx_v - S.bs_v) / (t2 - t1);
+    __device__ double ignitionTime() const {
+        const WarpAux& A = *aux;
+        if (!(A.flags & F_HASPREV) || !(A.flags & F_HASRIGHT)) return A.bs_t;
+        double t0 = A.pv_t, t1 = A.bs_t, t2 = A.nx_t;
+        double s0 = (A.bs_v - A.pv_v) / (t1 - t0), s1 = (A.nx_v - A.bs_v) / (t2 - t1);
         double curv = (s1 - s0) / (t2 - t0);
         if (!(curv < 0)) return t1;
         double tv = 0.5 * (t0 + t1) - s0 / (2.0 * curv);
@@ -665,7 +717,7 @@ struct BdfWarp {
                              (fabs(S.gamrat - 1.0) > DGMAX) || !S.haveLU;
             int nls = newton<MT, NS>(M, S, callSetup);
             if (nls != NLS_OK) {
-                S.ncfn++;
+                if (lane == 0) aux->ncfn++;
                 ncf++;
                 restore(S, saved_t);
                 if (ncf == MXNCF) return ST_CONV_FAIL;
@@ -678,7 +730,7 @@ struct BdfWarp {
             }
             double dsm = S.acnrm * S.tq[2];
             if (dsm > 1.0) {
-                S.netf++;
+                if (lane == 0) aux->netf++;
                 nef++;
                 restore(S, saved_t);
                 if (nef == MXNEF) return ST_ERR_FAIL;
@@ -729,7 +781,7 @@ struct BdfWarp {
                 __syncwarp();
                 S.saved_tq5 = S.tq[5];
             }
-            recordSample(S, S.tn, zn[N] / S.h);
+            recordSample(S.tn, zn[N] / S.h);
             prepareNext(S, dsm);
             return ST_OK;
         }
@@ -737,7 +789,7 @@ struct BdfWarp {
 };
 
 template <typename MT, int NS>
-__global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
+__global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     extern __shared__ double smem[];
     __shared__ uint64_t s_tab[64];
     gbx_load_table(s_tab);
@@ -756,10 +808,11 @@ __global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
     W.hmaxInv = p.hmaxInv;
     W.maxOrder = p.maxOrder;
     const int N = m.N;
-    const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
-    W.s.carve(base, m.K, m.R, m.NTB, m.NF, m.NT);
-    W.s.tab = s_tab;
+    const int kinD = kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
+    W.base = base;
+    W.tab = s_tab;
     double* q = base + kinD;
+    W.aux = (WarpAux*)q; q += kAuxDoubles;
     W.zn = q; q += (QMAX + 1) * N;
     W.ewt = q; q += N;
     W.acor = q; q += N;
@@ -793,11 +846,14 @@ __global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
                 for (int i = lane; i < N; i += 32) W.zn[(size_t)j * N + i] = 0.0;
             __syncwarp();
             S.tn = p.t0;
-            S.nrhs = S.nni = S.nsetups = S.nje = S.netf = S.ncfn = 0;
+            if (lane == 0) {
+                WarpAux& A = *W.aux;
+                A.nrhs = A.nni = A.nsetups = A.nje = A.netf = A.ncfn = 0;
+                A.flags = F_INIT; A.nsamp = 0;
+                A.ls_t = A.ls_v = A.pv_t = A.pv_v = A.bs_t = A.bs_v = A.nx_t = A.nx_v = 0.0;
+            }
             S.nst = 0; S.nstlp = 0;
             S.haveLU = false;
-            S.flags = F_INIT; S.nsamp = 0;
-            S.ls_t = S.ls_v = S.pv_t = S.pv_v = S.bs_t = S.bs_v = S.nx_t = S.nx_v = 0.0;
             for (int i = 0; i < QMAX + 2; i++) S.tau[i] = 0.0;
             for (int i = 0; i < 6; i++) S.tq[i] = 0.0;
             for (int i = 0; i <= QMAX; i++) S.l[i] = 0.0;
@@ -814,7 +870,7 @@ __global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
                 S.eta = 1.0;
                 S.q = S.qprime = 1; S.L = 2; S.qwait = 2; S.etamax = ETA_MAX_FIRST;
                 S.tau[1] = h0;
-                W.recordSample(S, S.tn, z1[0] / h0);
+                W.recordSample(S.tn, z1[0] / h0);
             } else {
                 S.h = S.hscale = S.hprime = 0.0;
                 S.q = S.qprime = 1; S.L = 2; S.qwait = 2; S.etamax = ETA_MAX_FIRST; S.eta = 1.0;
@@ -829,15 +885,19 @@ __global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
             for (int i = 0; i < 6; i++) S.tq[i] = rs[R_TQ + i];
             for (int i = 0; i <= QMAX; i++) S.l[i] = rs[R_L + i];
             S.gammap = rs[R_GAMMAP]; S.crate = rs[R_CRATE]; S.saved_tq5 = rs[R_SAVEDTQ5];
-            S.ls_t = rs[R_IGN + 0]; S.ls_v = rs[R_IGN + 1]; S.pv_t = rs[R_IGN + 2]; S.pv_v = rs[R_IGN + 3];
-            S.bs_t = rs[R_IGN + 4]; S.bs_v = rs[R_IGN + 5]; S.nx_t = rs[R_IGN + 6]; S.nx_v = rs[R_IGN + 7];
+            if (lane == 0) {
+                WarpAux& A = *W.aux;
+                A.ls_t = rs[R_IGN + 0]; A.ls_v = rs[R_IGN + 1]; A.pv_t = rs[R_IGN + 2]; A.pv_v = rs[R_IGN + 3];
+                A.bs_t = rs[R_IGN + 4]; A.bs_v = rs[R_IGN + 5]; A.nx_t = rs[R_IGN + 6]; A.nx_v = rs[R_IGN + 7];
+                A.nsamp = (int)rs[R_NSAMP];
+                A.flags = (int)rs[R_FLAGS];
+                A.nrhs = stt[1]; A.nni = stt[2]; A.nsetups = stt[3]; A.nje = stt[4]; A.netf = stt[5]; A.ncfn = stt[6];
+            }
             S.q = (int)rs[R_Q]; S.qprime = (int)rs[R_QPRIME]; S.qwait = (int)rs[R_QWAIT];
-            S.nst = (int)rs[R_NST]; S.nstlp = (int)rs[R_NSTLP]; S.nsamp = (int)rs[R_NSAMP];
-            S.flags = (int)rs[R_FLAGS];
+            S.nst = (int)rs[R_NST]; S.nstlp = (int)rs[R_NSTLP];
             S.L = S.q + 1;
             S.haveLU = false;   // the factorisation is not kept between advance calls
             S.gamrat = 1.0; S.acnrm = 0.0;
-            S.nrhs = stt[1]; S.nni = stt[2]; S.nsetups = stt[3]; S.nje = stt[4]; S.netf = stt[5]; S.ncfn = stt[6];
             S.status0 = (int)rs[R_STATUS];
         }
         int status = S.status0;
@@ -866,14 +926,15 @@ __global__ void __launch_bounds__(256, 1) k_bdf(BdfParams p) {
             for (int i = 0; i < 6; i++) o[R_TQ + i] = S.tq[i];
             for (int i = 0; i <= QMAX; i++) o[R_L + i] = S.l[i];
             o[R_GAMMAP] = S.gammap; o[R_CRATE] = S.crate; o[R_SAVEDTQ5] = S.saved_tq5;
-            o[R_IGN + 0] = S.ls_t; o[R_IGN + 1] = S.ls_v; o[R_IGN + 2] = S.pv_t; o[R_IGN + 3] = S.pv_v;
-            o[R_IGN + 4] = S.bs_t; o[R_IGN + 5] = S.bs_v; o[R_IGN + 6] = S.nx_t; o[R_IGN + 7] = S.nx_v;
+            const WarpAux& A = *W.aux;
+            o[R_IGN + 0] = A.ls_t; o[R_IGN + 1] = A.ls_v; o[R_IGN + 2] = A.pv_t; o[R_IGN + 3] = A.pv_v;
+            o[R_IGN + 4] = A.bs_t; o[R_IGN + 5] = A.bs_v; o[R_IGN + 6] = A.nx_t; o[R_IGN + 7] = A.nx_v;
             o[R_Q] = S.q; o[R_QPRIME] = S.qprime; o[R_QWAIT] = S.qwait; o[R_NST] = S.nst;
-            o[R_NSTLP] = S.nstlp; o[R_NSAMP] = S.nsamp; o[R_FLAGS] = S.flags; o[R_STATUS] = status;
-            stt[0] = S.nst; stt[1] = S.nrhs; stt[2] = S.nni; stt[3] = S.nsetups; stt[4] = S.nje;
-            stt[5] = S.netf; stt[6] = S.ncfn; stt[7] = S.q;
+            o[R_NSTLP] = S.nstlp; o[R_NSAMP] = A.nsamp; o[R_FLAGS] = A.flags | F_INIT; o[R_STATUS] = status;
+            stt[0] = S.nst; stt[1] = A.nrhs; stt[2] = A.nni; stt[3] = A.nsetups; stt[4] = A.nje;
+            stt[5] = A.netf; stt[6] = A.ncfn; stt[7] = S.q;
             p.status[r] = status;
-            p.tign[r] = W.ignitionTime(S);
+            p.tign[r] = W.ignitionTime();
         }
         __syncwarp();
     }
@@ -892,8 +953,8 @@ int bdfRecordStride(int N) { return (QMAX + 1) * N + R_NSCAL; }
 
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32) {
     int N = m.N;
-    int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
-    int vec = (QMAX + 1) * N + 8 * N + (N + 1) / 2;
+    int kinD = kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
+    int vec = (QMAX + 1) * N + 8 * N + (N + 1) / 2 + kAuxDoubles;
     int mat = fp32 ? (N * ld + 1) / 2 : N * ld;
     int tot = kinD + vec + mat;
     return (tot + 1) & ~1;   // keep each warp's slice 16-byte aligned

@@ -39,6 +39,7 @@ struct BdfParams {
     int warpDoubles;
 };
 
+constexpr int kBdfMaxThreads = 256;   // at most 8 warps per block
 int bdfRecordStride(int N);
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32);
 int ratesWarpDoubles(const DevMech& m);

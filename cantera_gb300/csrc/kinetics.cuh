@@ -217,7 +217,7 @@ __device__ __forceinline__ void warpState(const DevMech& m, double T, double P, 
 // Species thermo + rates of progress + net production rates.  With `forJac`, also the
 // per-reaction data d(wdot)/dc needs (Qtb, dlk).
 template <bool forJac>
-__device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, int lane) {
+__device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, int lane) {
     const double lnPP = log(st.P / m.Pref);
     if (lane == 0) s.flags[0] = 0;
     __syncwarp();
@@ -361,7 +361,7 @@ __device__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, i
 // k, j < K.  The dense part is g_k * (1 for every column); warpDenseG returns g in gout.
 // The caller zeroes Jc.  MT is the matrix element type (double or float).
 template <typename MT>
-__device__ void warpJacC(const DevMech& m, const KinScratch& s, MT* Jc, int ld, int lane) {
+__device__ __noinline__ void warpJacC(const DevMech& m, const KinScratch& s, MT* Jc, int ld, int lane) {
     for (int q = m.laneColPtr[lane]; q < m.laneColPtr[lane + 1]; q++) {
         int j = m.laneCols[q];
         for (int e = m.colPtr[j]; e < m.colPtr[j + 1]; e++) {
