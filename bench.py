@@ -29,7 +29,7 @@ METRIC = "GRI-30 reactors advanced/s on 1 GB300: FP64 BDF vs FP32-LU and NN+fall
 WL = dict(mechanism="gri30.yaml", phase="gri30", n=65536, t_end=1e-2, rtol=1e-8, atol=1e-15,
           T0=(700.0, 1800.0), P_atm=(1.0, 40.0), phi=(0.5, 1.5), fuel="CH4:1",
           oxidizer="O2:1, N2:3.76", seed=20261203 + 2)
-CPU_SAMPLE = 256          # reactors in the bounded CPU sample (a seeded subset of the workload)
+CPU_SAMPLE = 2048         # reactors in the bounded CPU sample (a seeded subset of the workload)
 
 
 def workload_arrays(n, seed, eqr):
@@ -212,6 +212,7 @@ def main():
 
     import torch
     import cantera_gb300 as gb
+    from cantera_gb300.sharding import max_over_ranks, shard_range
     ws, rank, local = dist_info()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -226,7 +227,7 @@ def main():
     T0, P, Y0 = workload_arrays(n_all, WL["seed"],
                                 lambda p: sol.equivalence_ratio_mass_fractions(p, WL["fuel"], WL["oxidizer"]))
     # contiguous shard of this rank
-    lo, hi = (n_all * rank) // ws, (n_all * (rank + 1)) // ws
+    lo, hi = shard_range(n_all, rank, ws)
     n = hi - lo
     Ts, Ps, Ys = T0[lo:hi].copy(), P[lo:hi].copy(), np.ascontiguousarray(Y0[lo:hi].T)
     dT, dP, dY = (torch.tensor(a, device=dev) for a in (Ts, Ps, Ys))
@@ -238,11 +239,7 @@ def main():
             pg.barrier()
 
     def maxover(x):
-        if not pg:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        return float(t.item())
+        return max_over_ranks(x, pg, dev)
 
     fp = gb.measure_fp64()
     fm = flop_model(sol.structure(), fp, K + 1)
