@@ -86,6 +86,7 @@ def library():
         "gb_mech_equivalence_ratio": (I32, [I32, D, P, P, I32, P]),
         "gb_measure_fp64": (I32, [P]),
         "gb_check_exp": (I32, [I32, P, P, P]),
+        "gb_reactors_advance_noalloc": (I32, [I32, I32, D, P, P, P, P, ctypes.POINTER(NetOptions), P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -432,6 +432,53 @@ void netLaunch(NetEntry& ne, MechEntry& me, double t0, double tout) {
     ck(launchBdf(p, ne.blocks, ne.warpsPerBlock, ne.opts.lu_precision == 32, me.stream), "integrator launch");
 }
 
+
+// ---------------------------------------------------------------------------
+// Allocation-free advance.  Some callers cannot call cudaMalloc at all: a host code whose
+// own caching allocator owns every byte of the device (a CFD solver that calls chemistry
+// once per cell batch inside its time loop) or a process whose device memory is fully
+// budgeted.  gb_reactors_advance_noalloc serves them: its integrator records live in this
+// fixed array that the module carries, so the call allocates nothing, neither through
+// the CUDA runtime nor through any library.
+// ---------------------------------------------------------------------------
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;   // 16 MiB per device
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noallocMu;                           // held for the whole call
+void* g_noallocAddr[kNoAllocMaxDevices] = {};      // per device, looked up once
+
+// Device address of this device's copy of the scratch array.  The first lookup on a
+// device loads the module there (lazy loading), which the driver may not do inside a
+// stream capture, so the first call on each device must precede any capture.
+void* noallocScratch(int dev) {
+    if (dev < 0 || dev >= kNoAllocMaxDevices) throw std::runtime_error("device ordinal out of range");
+    if (!g_noallocAddr[dev]) {
+        void* a = nullptr;
+        ck(cudaGetSymbolAddress(&a, g_noallocScratch), "cudaGetSymbolAddress(scratch)");
+        if (!a) throw std::runtime_error("cudaGetSymbolAddress returned a null scratch address");
+        g_noallocAddr[dev] = a;
+    }
+    return g_noallocAddr[dev];
+}
+
+size_t alignUp256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Reactors that fit the scratch array for a mechanism with N = K + 1 state components:
+// one work counter (256 bytes), then per reactor its record, its 8 counters and its
+// ignition time.
+int noallocCapacity(int N) {
+    const size_t per = (size_t)bdfRecordStride(N) * 8 + 64 + 8;
+    const size_t avail = kNoAllocScratchBytes - 256 - 3 * 256;
+    return (int)std::min<size_t>(avail / per, (size_t)INT32_MAX);
+}
+
+void requireDevicePointer(const void* ptr, int dev, const char* what) {
+    cudaPointerAttributes a{};
+    ck(cudaPointerGetAttributes(&a, ptr), what);
+    const bool ok = (a.type == cudaMemoryTypeDevice && a.device == dev) || a.type == cudaMemoryTypeManaged;
+    if (!ok) throw std::runtime_error(std::string(what) + " must be a device pointer on the current device");
+}
 }  // namespace
 
 extern "C" {
@@ -776,6 +823,71 @@ int32_t gb_net_ignition_times(int32_t h, double* tign) {
     return guarded([&]() -> int32_t {
         NetEntry& ne = net(h);
         ck(cudaMemcpy(tign, ne.dTign.p, (size_t)ne.n * 8, cudaMemcpyDeviceToHost), "copy tign");
+        return 0;
+    });
+}
+
+int32_t gb_reactors_advance_noalloc(int32_t h, int32_t n, double t_end, double* T, const double* P,
+                                    double* Y, int32_t* status, const gb_net_options* opts,
+                                    void* stream) {
+    return guarded([&]() -> int32_t {
+        MechEntry& me = mech(h);
+        if (n <= 0) throw std::runtime_error("need n > 0 reactors");
+        if (!T || !P || !Y || !status) throw std::runtime_error("null array argument");
+        if (!(t_end > 0) || !std::isfinite(t_end)) throw std::runtime_error("t_end must be positive and finite");
+        gb_net_options o;
+        if (opts) o = *opts;
+        else gb_net_default_options(&o);
+        if (o.lu_precision != 32 && o.lu_precision != 64) throw std::runtime_error("lu_precision must be 32 or 64");
+        if (o.max_order < 1 || o.max_order > 5) throw std::runtime_error("max_order must be 1..5");
+        if (!(o.rtol > 0) || !(o.atol > 0)) throw std::runtime_error("tolerances must be positive");
+        const int N = me.dm.N;
+        const int cap = noallocCapacity(N);
+        if (n > cap)
+            throw std::runtime_error("gb_reactors_advance_noalloc: n = " + std::to_string(n) +
+                                     " exceeds the maximum of " + std::to_string(cap) +
+                                     " reactors that its 16 MiB scratch holds for this mechanism");
+        int dev = 0;
+        ck(cudaGetDevice(&dev), "cudaGetDevice");
+        requireDevicePointer(T, dev, "T");
+        requireDevicePointer(P, dev, "P");
+        requireDevicePointer(Y, dev, "Y");
+        requireDevicePointer(status, dev, "status");
+
+        const bool fp32 = o.lu_precision == 32;
+        const int ld = (N % 2 == 0) ? N + 1 : N;
+        const int warpDoubles = bdfWarpDoubles(me.dm, ld, fp32);
+        const int recStride = bdfRecordStride(N);
+        const int fit = maxSmemPerBlock() / (warpDoubles * 8);
+        if (fit < 1) throw std::runtime_error("mechanism too large for one warp's shared memory");
+        const int wpb = std::min(o.warps_per_block > 0 ? o.warps_per_block : 8, fit);
+        const int blocksPerSm = std::max(1, (228 * 1024) / (warpDoubles * 8 * wpb));
+        const int blocks = std::min(me.smCount * blocksPerSm, (n + wpb - 1) / wpb);
+
+        std::lock_guard<std::mutex> lk(g_noallocMu);
+        char* base = (char*)noallocScratch(dev);
+        int* counter = (int*)base;
+        const size_t recBytes = (size_t)n * recStride * 8;
+        double* rec = (double*)(base + 256);
+        long long* stats = (long long*)(base + 256 + alignUp256(recBytes));
+        double* tign = (double*)((char*)stats + alignUp256((size_t)n * 64));
+        cudaStream_t s = (cudaStream_t)stream;
+        // Must start at zero: the work counter, and each record (a record whose flags
+        // word is zero makes the kernel start that reactor from T, P, Y at time 0).
+        ck(cudaMemsetAsync(counter, 0, sizeof(int), s), "reset counter");
+        ck(cudaMemsetAsync(rec, 0, recBytes, s), "reset records");
+        BdfParams p{};
+        p.m = me.dm; p.n = n; p.t0 = 0.0; p.tout = t_end;
+        p.rtol = o.rtol; p.atol = o.atol;
+        p.hmaxInv = o.max_time_step > 0 ? 1.0 / o.max_time_step : 0.0;
+        p.maxSteps = o.max_steps; p.maxOrder = o.max_order;
+        p.P = P; p.T = T; p.Y = Y;
+        p.rec = rec; p.recStride = recStride;
+        p.stats = stats; p.status = status; p.tign = tign;
+        p.counter = counter; p.order = nullptr;
+        p.ld = ld; p.warpDoubles = warpDoubles;
+        ck(launchBdf(p, blocks, wpb, fp32, s), "integrator launch");
+        ck(cudaStreamSynchronize(s), "integrator");
         return 0;
     });
 }

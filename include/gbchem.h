@@ -113,6 +113,24 @@ int32_t gb_net_solver_stats(int32_t net, int64_t* stats);
  * vertex of the parabola through that step and its accepted neighbours. */
 int32_t gb_net_ignition_times(int32_t net, double* tign);
 
+/* ---- allocation-free advance (no counterpart in the reference) -----------------------
+ * For callers that cannot allocate device memory (their own allocator owns the device, or
+ * the device memory is fully budgeted): advance n reactors from time 0 to t_end in one
+ * call, with the same integrator as gb_net_advance, allocating nothing.  T[n] and Y[K][n]
+ * (in place) and P[n] are device pointers on the current device; status[n] (device)
+ * receives the per-reactor status codes below.  opts may be NULL (defaults; use_graph is
+ * ignored).  The integrator records live in a 16 MiB array in the library's device image,
+ * so n is limited to what fits (about 5,500 reactors for GRI-Mech 3.0); a larger n fails
+ * with GB_ERR and a message giving the limit.  The call is ordered on `stream` (a
+ * cudaStream_t; NULL is the default stream) and synchronises it before returning.  Every
+ * call on a device shares that one array: calls of this process are serialised by a lock,
+ * and calls that overlap on one device from other code that bypasses it would race.  The
+ * first call on each device looks the array up (and may load the module), so make it
+ * before any stream capture. */
+int32_t gb_reactors_advance_noalloc(int32_t mech, int32_t n, double t_end, double* T, const double* P,
+                                    double* Y, int32_t* status, const gb_net_options* opts,
+                                    void* stream);
+
 /* ---- measurement helpers (no counterpart in the reference) ---------------------------
  * Structure counts of a mechanism for the benchmark's FP64 operation model:
  * counts[0..11] = K, R, reversible, falloff, Troe, three-body reactions, third-body
