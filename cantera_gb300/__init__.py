@@ -42,7 +42,8 @@ class NetOptions(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double),
                 ("max_steps", ctypes.c_int32), ("max_order", ctypes.c_int32),
                 ("max_time_step", ctypes.c_double), ("lu_precision", ctypes.c_int32),
-                ("warps_per_block", ctypes.c_int32), ("use_graph", ctypes.c_int32)]
+                ("warps_per_block", ctypes.c_int32), ("use_graph", ctypes.c_int32),
+                ("matrix_placement", ctypes.c_int32), ("mechanism_in_shared", ctypes.c_int32)]
 
 
 _lib = None
@@ -81,11 +82,13 @@ def library():
         "gb_net_get_status": (I32, [I32, P]),
         "gb_net_solver_stats": (I32, [I32, P]),
         "gb_net_ignition_times": (I32, [I32, P]),
+        "gb_net_launch_info": (I32, [I32, P]),
         "gb_get_error": (I32, [I32, ctypes.c_char_p]),
         "gb_mech_structure": (I32, [I32, I32, P]),
         "gb_mech_equivalence_ratio": (I32, [I32, D, P, P, I32, P]),
         "gb_measure_fp64": (I32, [P]),
         "gb_check_exp": (I32, [I32, P, P, P]),
+        "gb_check_log": (I32, [I32, P, P, P]),
         "gb_reactors_advance_noalloc": (I32, [I32, I32, D, P, P, P, P, ctypes.POINTER(NetOptions), P]),
     }
     for name, (res, args) in sig.items():
@@ -253,7 +256,8 @@ class ReactorNet:
     """n independent constant-pressure ideal-gas reactors advanced together."""
 
     def __init__(self, solution, T, P, Y, rtol=1e-9, atol=1e-15, max_steps=20000, max_order=5,
-                 max_time_step=0.0, lu_precision=64, warps_per_block=0, use_graph=False):
+                 max_time_step=0.0, lu_precision=64, warps_per_block=0, use_graph=False,
+                 matrix_placement=0, mechanism_in_shared=0):
         L = library()
         self.solution = solution
         o = NetOptions()
@@ -261,6 +265,8 @@ class ReactorNet:
         o.rtol, o.atol, o.max_steps, o.max_order = rtol, atol, max_steps, max_order
         o.max_time_step, o.lu_precision = max_time_step, lu_precision
         o.warps_per_block, o.use_graph = warps_per_block, int(use_graph)
+        o.matrix_placement = matrix_placement
+        o.mechanism_in_shared = mechanism_in_shared
         n = T.shape[0] if _is_torch_cuda(T) else np.asarray(T).shape[0]
         self.n = n
         self._h = _check(L.gb_net_new(solution._h, n, ctypes.byref(o)))
@@ -275,6 +281,15 @@ class ReactorNet:
     def advance(self, t):
         """Advance every reactor to time t; returns the number of failed reactors."""
         return _check(library().gb_net_advance(self._h, float(t)))
+
+    @property
+    def launch_info(self):
+        """blocks, reactors per block, shared bytes per warp, mechanism bytes in shared
+        memory, matrix placement (1 shared, 2 global)."""
+        v = np.zeros(5, dtype=np.int32)
+        _check(library().gb_net_launch_info(self._h, _ptr(v)))
+        return dict(zip(["blocks", "warps_per_block", "warp_smem_bytes", "mechanism_smem_bytes",
+                         "matrix_placement"], v.tolist()))
 
     @property
     def time(self):

@@ -83,7 +83,10 @@ struct NetEntry {
     gb_net_options opts;
     double time = 0.0;
     int warpsPerBlock = 0, blocks = 0, ld = 0, warpDoubles = 0, recStride = 0;
-    DBuf dP, dT, dY, dRec, dStats, dStatus, dTign, dCounter, dOrder;
+    DBuf dP, dT, dY, dRec, dStats, dStatus, dTign, dCounter, dOrder, dM;
+    size_t Mstride = 0;   // bytes per Newton-matrix slot in dM (0: matrices in shared memory)
+    bool matGlobal = false;
+    int mechSmem = 0;     // bytes of the mechanism arena each block copies into shared memory
     bool haveOrder = false;
     cudaGraphExec_t graph = nullptr;
     double graphTout = -1.0;
@@ -134,9 +137,12 @@ void packDevMech(MechEntry& e) {
     for (int k = 0; k < K; k++) {
         rmw[k] = 1.0 / m.mw[k];
         nasa[(size_t)k * kNasaStride] = m.nasaTmid[k];
-        for (int j = 0; j < 7; j++) {
-            nasa[(size_t)k * kNasaStride + 1 + j] = m.nasaLow[7 * k + j];
-            nasa[(size_t)k * kNasaStride + 8 + j] = m.nasaHigh[7 * k + j];
+        for (int r = 0; r < 2; r++) {
+            const double* a = r == 0 ? &m.nasaLow[7 * k] : &m.nasaHigh[7 * k];
+            double* d = &nasa[(size_t)k * kNasaStride + 1 + r * kNasaRange];
+            for (int j = 0; j < 7; j++) d[j] = a[j];
+            d[7] = a[1] / 2.0; d[8] = a[2] / 3.0; d[9] = a[3] / 4.0; d[10] = a[4] / 5.0;
+            d[11] = a[2] / 2.0; d[12] = a[3] / 3.0; d[13] = a[4] / 4.0;
         }
     }
     // Device reaction order: falloff (Troe, then Lindemann), three-body, reversible, then
@@ -325,25 +331,34 @@ void packDevMech(MechEntry& e) {
         for (int q = e.jcPtr[c]; q < e.jcPtr[c + 1]; q++) jpCol[q] = c;
     std::vector<int> jcPtr(e.jcPtr.begin(), e.jcPtr.end()), jrIdx(e.jrIdx.begin(), e.jrIdx.end());
 
+    // Arena order by use: what every right-hand side reads, then what a Jacobian reads,
+    // then the general (CN) side lists, then the rest.  Kernels copy a prefix of the arena
+    // into shared memory when it fits, so the hottest data goes first.
     Arena a;
-    size_t o_mw = a.add(m.mw), o_rmw = a.add(rmw), o_nasa = a.add(nasa);
+    size_t o_nasa = a.add(nasa), o_rmw = a.add(rmw), o_mw = a.add(m.mw);
     size_t o_rinfo = a.add(rinfo), o_rarr = a.add(rarr), o_rk = a.add(rk), o_pk = a.add(pk);
-    size_t o_sidePtr = a.add(sidePtr), o_sideK = a.add(sideK), o_sideNu = a.add(sideNu), o_sideOrd = a.add(sideOrd);
-    size_t o_rsPtr = a.add(rsPtr), o_rsK = a.add(rsK), o_rsNu = a.add(rsNu);
     size_t o_fo1 = a.add(fo1), o_fo2 = a.add(fo2);
-    size_t o_tbRxn = a.add(tbRxn), o_tbDef = a.add(tbDef), o_tbMA = a.add(tbMA), o_tbPtr = a.add(tbPtr),
-           o_tbK = a.add(tbK), o_tbE = a.add(tbE);
-    size_t o_spPtr = a.add(spPtr), o_spRxn = a.add(spRxn), o_spNu = a.add(spNu);
+    size_t o_tbPtr = a.add(tbPtr), o_tbK = a.add(tbK), o_tbE = a.add(tbE), o_tbDef = a.add(tbDef);
     size_t o_taskPtr = a.add(taskPtr), o_ltp = a.add(laneTaskPtr), o_lt = a.add(laneTasks),
            o_stp = a.add(spTaskPtr), o_st = a.add(spTasks);
-    size_t o_colPtr = a.add(colPtr), o_colRxn = a.add(colRxn), o_colE = a.add(colE);
+    size_t o_spRxn = a.add(spRxn), o_spNu = a.add(spNu);
+    const size_t hotEnd = a.data.size();
     size_t o_lcp = a.add(laneColPtr), o_lc = a.add(laneCols);
+    size_t o_colPtr = a.add(colPtr), o_colRxn = a.add(colRxn), o_colE = a.add(colE);
+    size_t o_rsPtr = a.add(rsPtr), o_rsK = a.add(rsK), o_rsNu = a.add(rsNu);
     size_t o_gsPtr = a.add(gsPtr), o_gsTb = a.add(gsTb), o_gsCoef = a.add(gsCoef);
+    const size_t jacEnd = a.data.size();
+    size_t o_sidePtr = a.add(sidePtr), o_sideK = a.add(sideK), o_sideNu = a.add(sideNu), o_sideOrd = a.add(sideOrd);
+    const size_t sideEnd = a.data.size();
+    size_t o_spPtr = a.add(spPtr), o_tbRxn = a.add(tbRxn), o_tbMA = a.add(tbMA);
     size_t o_jcPtr = a.add(jcPtr), o_jrIdx = a.add(jrIdx), o_jpCol = a.add(jpCol);
     e.arena.ensure(a.data.size());
     ck(cudaMemcpy(e.arena.p, a.data.data(), a.data.size(), cudaMemcpyHostToDevice), "upload mechanism");
     char* b = e.arena.as<char>();
     DevMech& d = e.dm;
+    auto up16 = [](size_t v) { return (int)((v + 15) & ~size_t(15)); };
+    d.arena = b;
+    d.hotBytes = up16(hotEnd); d.jacBytes = up16(jacEnd); d.sideBytes = up16(sideEnd);
     d.K = K; d.R = R; d.N = K + 1; d.NF = (int)fo1.size(); d.NTB = m.nThirdBody(); d.nnz = (int)jrIdx.size();
     d.Pref = m.Pref; d.Rgas = gasConstant();
     d.mw = (const double*)(b + o_mw); d.rmw = (const double*)(b + o_rmw); d.nasa = (const double*)(b + o_nasa);
@@ -365,11 +380,13 @@ void packDevMech(MechEntry& e) {
     d.jcPtr = (const int*)(b + o_jcPtr); d.jrIdx = (const int*)(b + o_jrIdx); d.jpCol = (const int*)(b + o_jpCol);
 }
 
+// dynamic shared memory a block may use: the opt-in maximum less the kernels' static
+// tables (exp/log tables, kGbxTableWords words) and a margin
 int maxSmemPerBlock() {
     int dev = 0, v = 0;
     ck(cudaGetDevice(&dev), "cudaGetDevice");
     ck(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device attribute");
-    return v;
+    return v - 4096;
 }
 
 // Copy n*count doubles to a device buffer unless they are already on the device.
@@ -406,15 +423,67 @@ int32_t runRates(int32_t h, int32_t n, const double* T, const double* P, const d
     RatesParams p{};
     p.m = e.dm; p.n = n; p.T = dT; p.P = dP; p.Y = dY; p.wdot = dW; p.jac = dJ;
     p.counter = e.dCounter.as<int>();
-    p.warpDoubles = ratesWarpDoubles(e.dm);
-    int wpb = std::max(1, std::min(8, maxSmemPerBlock() / (p.warpDoubles * 8)));
-    int blocksPerSm = std::max(1, (228 * 1024) / (p.warpDoubles * 8 * wpb));
+    p.warpDoubles = ratesWarpDoubles(e.dm, dJ != nullptr);
+    // the mechanism data the call reads goes into shared memory when 8 warps still fit
+    const int budget = maxSmemPerBlock();
+    const int want = dJ ? e.dm.sideBytes : e.dm.hotBytes;
+    p.mechSmem = (budget - want) / (p.warpDoubles * 8) >= 8 ? want : 0;
+    int wpb = std::max(1, std::min(8, (budget - p.mechSmem) / (p.warpDoubles * 8)));
+    int blocksPerSm = std::max(1, (228 * 1024) / (p.mechSmem + p.warpDoubles * 8 * wpb + 1024));
     int blocks = std::min(e.smCount * blocksPerSm, (n + wpb - 1) / wpb);
     ck(launchRates(p, blocks, wpb, s), "rates kernel launch");
     if (wdot && !dev) ck(cudaMemcpyAsync(wdot, dW, (size_t)K * n * 8, cudaMemcpyDeviceToHost, s), "copy wdot");
     if (vals && !dev) ck(cudaMemcpyAsync(vals, dJ, (size_t)e.dm.nnz * n * 8, cudaMemcpyDeviceToHost, s), "copy jac");
     ck(cudaStreamSynchronize(s), "rates kernel");
     return 0;
+}
+
+// Launch shape of the integrator: where the Newton matrices live, how much of the
+// mechanism each block copies into shared memory, reactors (warps) per block.  A block's
+// dynamic shared memory is the mechanism prefix plus one slice per warp.  Automatic choice:
+// a block of 8 warps with the matrices in shared memory and as much of the mechanism as
+// fits; if 8 such warps do not fit, the matrices move to global memory (an L2-resident
+// slot per warp).
+void chooseBdfLaunch(const MechEntry& me, const gb_net_options& o, int n, bool fp32, int ld, NetEntry& ne) {
+    const DevMech& d = me.dm;
+    const int budget = maxSmemPerBlock();
+    const int wdShared = bdfWarpDoubles(d, ld, fp32);
+    const int wdGlobal = bdfWarpDoublesNoMatrix(d);
+    const int maxW = o.warps_per_block > 0 ? std::min(o.warps_per_block, kBdfMaxThreads / 32) : kBdfMaxThreads / 32;
+    auto mechBytes = [&](int level) {
+        return level == 4 ? d.sideBytes : (level == 3 ? d.jacBytes : (level == 2 ? d.hotBytes : 0));
+    };
+    std::vector<int> places;
+    if (o.matrix_placement != 2) places.push_back(1);
+    if (o.matrix_placement != 1) places.push_back(2);
+    // first candidate (in preference order) that holds a full block; else the largest block.
+    // Measured on GB300 (gri30): a mechanism copy that costs resident warps, or that takes
+    // the L1 share the global matrices live in, is slower than none, so the automatic
+    // choice copies the mechanism only next to shared-memory matrices.
+    int bestFit = 0, bestPlace = 0, bestMech = 0;
+    bool full = false;
+    for (int pl : places) {
+        std::vector<int> levels;
+        if (o.mechanism_in_shared != 0) levels = {o.mechanism_in_shared};
+        else if (pl == 1) levels = {4, 3, 2, 1};
+        else levels = {1};
+        for (int lv : levels) {
+            const int mech = mechBytes(lv);
+            const int wd = pl == 2 ? wdGlobal : wdShared;
+            const int fit = std::min((budget - mech) / (wd * 8), maxW);
+            if (fit > bestFit) { bestFit = fit; bestPlace = pl; bestMech = mech; }
+            if (fit >= maxW) { full = true; break; }
+        }
+        if (full) break;
+    }
+    if (bestFit < 1) throw std::runtime_error("mechanism too large for one warp's shared memory");
+    ne.matGlobal = bestPlace == 2;
+    ne.mechSmem = bestMech;
+    ne.warpDoubles = ne.matGlobal ? wdGlobal : wdShared;
+    ne.warpsPerBlock = bestFit;
+    const int perBlock = ne.mechSmem + ne.warpDoubles * 8 * bestFit;
+    const int blocksPerSm = std::max(1, (228 * 1024) / (perBlock + 1024));
+    ne.blocks = std::min(me.smCount * blocksPerSm, (n + bestFit - 1) / bestFit);
 }
 
 void netLaunch(NetEntry& ne, MechEntry& me, double t0, double tout) {
@@ -428,6 +497,8 @@ void netLaunch(NetEntry& ne, MechEntry& me, double t0, double tout) {
     p.stats = ne.dStats.as<long long>(); p.status = ne.dStatus.as<int>(); p.tign = ne.dTign.as<double>();
     p.counter = ne.dCounter.as<int>(); p.order = ne.haveOrder ? ne.dOrder.as<int>() : nullptr;
     p.ld = ne.ld; p.warpDoubles = ne.warpDoubles;
+    p.Mbuf = ne.Mstride ? ne.dM.p : nullptr; p.Mstride = (long long)ne.Mstride;
+    p.mechSmem = ne.mechSmem;
     ck(cudaMemsetAsync(ne.dCounter.p, 0, sizeof(int), me.stream), "memset");
     ck(launchBdf(p, ne.blocks, ne.warpsPerBlock, ne.opts.lu_precision == 32, me.stream), "integrator launch");
 }
@@ -606,6 +677,14 @@ int32_t gb_measure_fp64(double* results) {
     });
 }
 
+int32_t gb_check_log(int32_t n, const double* x, double* mine, double* lib) {
+    return guarded([&]() -> int32_t {
+        if (n < 0 || !x || !mine || !lib) throw std::runtime_error("bad arguments");
+        ck(checkLog(n, x, mine, lib), "log check");
+        return 0;
+    });
+}
+
 int32_t gb_check_exp(int32_t n, const double* x, double* mine, double* lib) {
     return guarded([&]() -> int32_t {
         if (n < 0 || !x || !mine || !lib) throw std::runtime_error("bad arguments");
@@ -649,6 +728,8 @@ void gb_net_default_options(gb_net_options* o) {
     o->lu_precision = 64;
     o->warps_per_block = 0;
     o->use_graph = 0;
+    o->matrix_placement = 0;
+    o->mechanism_in_shared = 0;
 }
 
 int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
@@ -667,16 +748,19 @@ int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
         const int N = me.dm.N;
         const bool fp32 = ne->opts.lu_precision == 32;
         ne->ld = fp32 ? (N % 2 == 0 ? N + 1 : N) : (N % 2 == 0 ? N + 1 : N);
-        ne->warpDoubles = bdfWarpDoubles(me.dm, ne->ld, fp32);
+        if (ne->opts.matrix_placement < 0 || ne->opts.matrix_placement > 2)
+            throw std::runtime_error("matrix_placement must be 0, 1 or 2");
+        if (ne->opts.mechanism_in_shared < 0 || ne->opts.mechanism_in_shared > 4)
+            throw std::runtime_error("mechanism_in_shared must be 0..4");
         ne->recStride = bdfRecordStride(N);
-        const int smemMax = maxSmemPerBlock();
-        int fit = smemMax / (ne->warpDoubles * 8);
-        if (fit < 1) throw std::runtime_error("mechanism too large for one warp's shared memory");
-        int wpb = ne->opts.warps_per_block > 0 ? ne->opts.warps_per_block : std::min(fit, 8);
-        wpb = std::min(wpb, fit);
-        ne->warpsPerBlock = wpb;
-        int blocksPerSm = std::max(1, (228 * 1024) / (ne->warpDoubles * 8 * wpb));
-        ne->blocks = std::min(me.smCount * blocksPerSm, (n + wpb - 1) / wpb);
+        chooseBdfLaunch(me, ne->opts, n, fp32, ne->ld, *ne);
+        const int wpb = ne->warpsPerBlock;
+        const bool matGlobal = ne->matGlobal;
+        if (matGlobal) {
+            const size_t elt = fp32 ? 4 : 8;
+            ne->Mstride = ((size_t)N * ne->ld * elt + 255) & ~size_t(255);
+            ne->dM.ensure(ne->Mstride * (size_t)ne->blocks * wpb);
+        }
         const int K = me.m.K;
         ne->dP.ensure((size_t)n * 8);
         ne->dT.ensure((size_t)n * 8);
@@ -694,6 +778,16 @@ int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
         std::lock_guard<std::mutex> lk(g_mu);
         g_nets.push_back(std::move(ne));
         return (int32_t)g_nets.size() - 1;
+    });
+}
+
+int32_t gb_net_launch_info(int32_t h, int32_t* info) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        if (!info) throw std::runtime_error("null array argument");
+        info[0] = ne.blocks; info[1] = ne.warpsPerBlock; info[2] = ne.warpDoubles * 8;
+        info[3] = ne.mechSmem; info[4] = ne.matGlobal ? 2 : 1;
+        return 0;
     });
 }
 

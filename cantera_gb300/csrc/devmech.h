@@ -17,7 +17,11 @@ struct alignas(32) D4 { double x, y, z, w; };
 
 constexpr int kMaxSpecies = 255;   // limits of the GPU path (checked at load time)
 constexpr int kMaxN = kMaxSpecies + 1;   // integrated components: T and the species
-constexpr int kNasaStride = 16;    // Tmid, low[7], high[7], pad
+// NASA7 block per species: Tmid, then per range (low, high) kNasaRange values
+// a0..a6, a1/2, a2/3, a3/4, a4/5, a2/2, a3/3, a4/4 (the scaled coefficients of the
+// Horner forms of h/RT and s/R), padded to kNasaStride.
+constexpr int kNasaRange = 14;
+constexpr int kNasaStride = 32;
 
 // rinfo.x bit fields
 constexpr int kKindMask = 0x7;      // RateKind
@@ -30,6 +34,11 @@ constexpr int kNoExpBit = 1 << 11;  // b = 0 and Ea = 0: k = A
 struct DevMech {
     int K, R, N, NF, NTB, nnz;
     double Pref, Rgas;
+    // the arena holding every array below, and the ends (16-byte rounded) of its parts:
+    // [0, hotBytes) what a right-hand side reads, [hotBytes, jacBytes) what a Jacobian
+    // adds, [jacBytes, sideBytes) the general side lists
+    const char* arena;
+    int hotBytes, jacBytes, sideBytes;
     // species [K]
     const double* mw;
     const double* rmw;
@@ -85,5 +94,40 @@ struct DevMech {
     const int* jrIdx;
     const int* jpCol;
 };
+
+// every array of a DevMech
+#define GB_DEVMECH_ARRAYS(X) \
+    X(mw) X(rmw) X(nasa) X(rinfo) X(rarr) X(rk) X(pk) X(sidePtr) X(sideK) X(sideNu) X(sideOrd) \
+    X(rsPtr) X(rsK) X(rsNu) X(fo1) X(fo2) X(tbRxn) X(tbDef) X(tbMA) X(tbPtr) X(tbK) X(tbE) \
+    X(spPtr) X(spRxn) X(spNu) X(taskPtr) X(laneTaskPtr) X(laneTasks) X(spTaskPtr) X(spTasks) \
+    X(colPtr) X(colRxn) X(colE) X(laneColPtr) X(laneCols) X(gsPtr) X(gsTb) X(gsCoef) \
+    X(jcPtr) X(jrIdx) X(jpCol)
+
+#ifdef __CUDACC__
+// Point the arrays that lie in the first `bytes` of the arena at a copy of that prefix
+// at `copy` (shared memory).
+__device__ __forceinline__ void rebaseMech(DevMech& d, const char* copy, int bytes) {
+#define GB_REBASE(f)                                                                      \
+    {                                                                                     \
+        const char* q = (const char*)d.f;                                                 \
+        if (q >= d.arena && q < d.arena + bytes) d.f = (decltype(d.f))(copy + (q - d.arena)); \
+    }
+    GB_DEVMECH_ARRAYS(GB_REBASE)
+#undef GB_REBASE
+}
+
+// Block prologue of the kernels: copy `bytes` (a multiple of 16) of the arena into the
+// start of dynamic shared memory and build the block's DevMech in `sm` (shared).  The
+// caller synchronises the block afterwards.
+__device__ __forceinline__ void loadMech(const DevMech& src, DevMech& sm, char* dyn, int bytes) {
+    const int4* from = (const int4*)src.arena;
+    int4* to = (int4*)dyn;
+    for (int q = threadIdx.x; q < bytes / 16; q += blockDim.x) to[q] = from[q];
+    if (threadIdx.x == 0) {
+        sm = src;
+        if (bytes > 0) rebaseMech(sm, dyn, bytes);
+    }
+}
+#endif
 
 }  // namespace gbchem

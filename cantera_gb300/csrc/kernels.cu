@@ -18,13 +18,15 @@ namespace gbchem {
 // Kinetics::netProductionRates_ddCi)
 // =============================================================================
 __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
-    extern __shared__ double smem[];
-    __shared__ uint64_t s_tab[64];
-    gbx_load_table(s_tab);
-    const DevMech& m = p.m;
+    extern __shared__ __align__(128) double smem[];
+    __shared__ uint64_t s_tab[kGbxTableWords];
+    __shared__ DevMech s_mech;
+    loadMech(p.m, s_mech, (char*)smem, p.mechSmem);
+    gbx_load_table(s_tab);   // (its barrier also completes the mechanism copy)
+    const DevMech& m = s_mech;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    double* base = smem + (size_t)warp * p.warpDoubles;
+    double* base = smem + p.mechSmem / 8 + (size_t)warp * p.warpDoubles;
     KinScratch s;
     const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
     s.carve(base, m.K, m.R, m.NTB, m.NF, m.NT);
@@ -44,7 +46,8 @@ __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
         __syncwarp();
         warpState(m, T, P, Yl, s, st, lane);
         __syncwarp();
-        warpRates<true>(m, s, st, lane);
+        if (p.jac) warpRates<true>(m, s, st, lane);
+        else warpRates<false>(m, s, st, lane);
         if (p.wdot)
             for (int k = lane; k < m.K; k += 32) p.wdot[(size_t)k * p.n + idx] = s.wdot[k];
         if (p.jac) {
@@ -125,7 +128,18 @@ __device__ __forceinline__ double sel(const double (&a)[N], int i) {
 // the KinState of its last right-hand side (kStateSlots doubles), then the kinetics
 // scratch.
 // ---------------------------------------------------------------------------
-constexpr int kStateSlots = 8;
+constexpr int kStateSlots = 16;
+static_assert(kKinStateDoubles <= kStateSlots, "state slots");
+
+// finite (not inf, not NaN) on the integer pipe
+__device__ __forceinline__ bool finiteBits(double x) {
+    return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+__device__ __forceinline__ void storeState(double* base, const KinState& st) {
+    base[0] = st.T; base[1] = st.P; base[2] = st.RT; base[3] = st.rho;
+    base[4] = st.mmw; base[5] = st.ctot; base[6] = st.lnT; base[7] = st.recipT;
+    base[8] = st.rrho; base[9] = st.lnPP; base[10] = st.lnC0; base[11] = st.RTP; base[12] = st.PRT;
+}
 
 __device__ __forceinline__ void carveScratch(const DevMech& m, double* base, const uint64_t* tab, KinScratch& s) {
     s.carve(base + kStateSlots, m.K, m.R, m.NTB, m.NF, m.NT);
@@ -134,36 +148,37 @@ __device__ __forceinline__ void carveScratch(const DevMech& m, double* base, con
 __device__ __forceinline__ void loadState(const double* base, KinState& st) {
     st.T = base[0]; st.P = base[1]; st.RT = base[2]; st.rho = base[3];
     st.mmw = base[4]; st.ctot = base[5]; st.lnT = base[6]; st.recipT = base[7];
+    st.rrho = base[8]; st.lnPP = base[9]; st.lnC0 = base[10]; st.RTP = base[11]; st.PRT = base[12];
 }
 
 // reactor right-hand side at z = [T, Y]; returns true when every derivative is finite
+// (with forJac the kinetics scratch also keeps what d(wdot)/dc needs: the right-hand side
+// that precedes a Jacobian evaluation)
 __device__ __noinline__ bool devRhs(const DevMech& m, double* base, const uint64_t* tab, double P,
-                                    const double* z, double* zdot, int lane) {
+                                    const double* z, double* zdot, int lane, bool forJac) {
     KinScratch s;
     carveScratch(m, base, tab, s);
     KinState st;
     warpState(m, z[0], P, z + 1, s, st, lane);
     __syncwarp();
-    warpRates<true>(m, s, st, lane);
-    if (lane == 0) {
-        base[0] = st.T; base[1] = st.P; base[2] = st.RT; base[3] = st.rho;
-        base[4] = st.mmw; base[5] = st.ctot; base[6] = st.lnT; base[7] = st.recipT;
-    }
+    if (forJac) warpRates<true>(m, s, st, lane);
+    else warpRates<false>(m, s, st, lane);
+    if (lane == 0) storeState(base, st);
     double ph = 0.0, pc = 0.0;
     for (int k = lane; k < m.K; k += 32) {
         ph += s.wdot[k] * s.hRT[k];
         pc += s.c[k] * s.cpR[k];
     }
+    // dT/dt = -sum(h_k wdot_k) / (rho cp_mass) = -T sum(h_k/RT wdot_k) / sum(c_k cp_k/R)
     const double hw = warpSum(ph);
-    const double rrho = 1.0 / st.rho;
-    const double cpmass = m.Rgas * (warpSum(pc) * rrho);
-    const double dTdt = -(hw * st.RT) * rrho / cpmass;
-    bool ok = isfinite(dTdt);
+    const double dTdt = -(hw * st.T) / warpSum(pc);
+    bool ok = finiteBits(dTdt);
     if (lane == 0) zdot[0] = dTdt;
+    const double rrho = st.rrho;
     for (int k = lane; k < m.K; k += 32) {
         const double v = s.wdot[k] * m.mw[k] * rrho;
         zdot[1 + k] = v;
-        ok = ok && isfinite(v);
+        ok = ok && finiteBits(v);
     }
     __syncwarp();
     return __all_sync(0xffffffffu, ok);
@@ -172,6 +187,13 @@ __device__ __noinline__ bool devRhs(const DevMech& m, double* base, const uint64
     // LU with partial pivoting in place (row-major, leading dimension ld).  Afterwards
 // piv[] holds the gather permutation (row i of P*b is b[piv[i]]) and dinv[] the
 // reciprocal diagonal of U, both in shared memory.
+__device__ __forceinline__ unsigned long long absKey(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFULL;
+}
+__device__ __forceinline__ unsigned long long absKey(float x) {
+    return (unsigned long long)((unsigned)__float_as_int(x) & 0x7FFFFFFFu);
+}
+
 template <typename MT>
 __device__ __noinline__ bool devLuFactor(MT* a, int N, int ld, int* piv, double* dinv, int lane) {
     bool nonsingular = true;
@@ -179,19 +201,21 @@ __device__ __noinline__ bool devLuFactor(MT* a, int N, int ld, int* piv, double*
         for (int i = 0; i < N; i++) piv[i] = i;
     __syncwarp();
     for (int k = 0; k < N; k++) {
-        double bv = -1.0;
+        // pivot search on the integer pipe: for finite values |x| orders like the bits of
+        // x with the sign cleared (the caller has checked that M is finite)
+        unsigned long long bv = 0ULL;
         int bi = N;
         for (int i = k + lane; i < N; i += 32) {
-            double v = fabs((double)a[(size_t)i * ld + k]);
-            if (v > bv) { bv = v; bi = i; }
+            const unsigned long long v = absKey(a[(size_t)i * ld + k]);
+            if (v > bv || bi == N) { bv = v; bi = i; }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            double ov = __shfl_xor_sync(0xffffffffu, bv, o);
-            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
             if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
         }
-        if (!(bv > 0.0)) { nonsingular = false; break; }
+        if (bv == 0ULL) { nonsingular = false; break; }
         if (bi != k) {
             for (int j = lane; j < N; j += 32) {
                 MT t = a[(size_t)k * ld + j];
@@ -205,9 +229,21 @@ __device__ __noinline__ bool devLuFactor(MT* a, int N, int ld, int* piv, double*
         if (lane == 0) dinv[k] = (double)inv;
         for (int i = k + 1 + lane; i < N; i += 32) a[(size_t)i * ld + k] *= inv;
         __syncwarp();
+        // trailing update, eight rows at a time with all loads issued before the stores
         for (int j = k + 1 + lane; j < N; j += 32) {
             const MT u = a[(size_t)k * ld + j];
-            for (int i = k + 1; i < N; i++) a[(size_t)i * ld + j] -= a[(size_t)i * ld + k] * u;
+            int i = k + 1;
+            for (; i + 8 <= N; i += 8) {
+                MT l[8], v[8];
+#pragma unroll
+                for (int r = 0; r < 8; r++) {
+                    l[r] = a[(size_t)(i + r) * ld + k];
+                    v[r] = a[(size_t)(i + r) * ld + j];
+                }
+#pragma unroll
+                for (int r = 0; r < 8; r++) a[(size_t)(i + r) * ld + j] = v[r] - l[r] * u;
+            }
+            for (; i < N; i++) a[(size_t)i * ld + j] -= a[(size_t)i * ld + k] * u;
         }
         __syncwarp();
     }
@@ -232,7 +268,7 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     __syncwarp();
     warpJacC<MT>(mm, s, M + ld + 1, ld, lane);
     // v1 = X (mole fractions); v2[k] = (Jc X)_k
-    const double rct = 1.0 / st.ctot;
+    const double rct = st.RTP;   // 1/ctot
     for (int k = lane; k < K; k += 32) v1[k] = s.c[k] * rct;
     __syncwarp();
     for (int k = lane; k < K; k += 32) {
@@ -255,22 +291,31 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     }
     const double hJX = warpSum(phj);
     const double rho = st.rho, mmw = st.mmw;
-    const double rD = 1.0 / (rho * mm.Rgas * (cpmix / mmw));
+    // 1/(rho R cp_mix/mmw) = 1/(R ctot cp_mix) = (RT/P) / (R cp_mix)
+    const double rD = st.RTP / (mm.Rgas * cpmix);
     const double G = ftemp[0];
     // v2[k] <- W_k (Jc X)_k - wdot_k W_k mmw / rho: J[1+k][1+j] = (W_k Jc_kj - v2[k]) / W_j
-    const double c1 = mmw / rho;
+    const double c1 = mmw * st.rrho;
     for (int k = lane; k < K; k += 32) v2[k] = mm.mw[k] * (v2[k] - s.wdot[k] * c1);
     __syncwarp();
+    // species block of M = I - gamma J in the same pass: M_kj = delta_kj - gamma/W_j (W_k Jc_kj - v2_k)
     const double hscale = rho * st.RT, cpscale = rho * mm.Rgas;
+    bool fin = true;
     for (int j = lane; j < K; j += 32) {
         const double rWj = mm.rmw[j];
+        const double gj = -gamma * rWj;
         for (int k = 0; k < K; k++) {
             MT* p = M + (size_t)(1 + k) * ld + 1 + j;
-            *p = (MT)(fma(mm.mw[k], (double)*p, -v2[k]) * rWj);
+            double v = fma(mm.mw[k], (double)*p, -v2[k]) * gj;
+            if (k == j) v += 1.0;
+            fin = fin && finiteBits(v);
+            *p = (MT)v;
         }
         const double dH = hscale * rWj * (tempv[j] - hJX);
         const double dD = cpscale * rWj * (s.cpR[j] - cpmix);
-        M[1 + j] = (MT)(-(dH + G * dD) * rD);
+        const double v = (dH + G * dD) * rD * gamma;   // -gamma * J[0][1+j]
+        fin = fin && finiteBits(v);
+        M[1 + j] = (MT)v;
     }
     __syncwarp();
     // T column: one-sided difference
@@ -280,24 +325,95 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     __syncwarp();
     if (lane == 0) tempv[0] = T0 + dT;
     __syncwarp();
-    bool ok = devRhs(mm, base, tab, P, tempv, v1, lane);
-    const double rdT = 1.0 / dT;
-    for (int i = lane; i < N; i += 32) M[(size_t)i * ld] = (MT)((v1[i] - ftemp[i]) * rdT);
-    __syncwarp();
-    // M = I - gamma*J
-    bool fin = true;
-    for (int q = lane; q < N * ld; q += 32) {
-        const double v = -gamma * (double)M[q];
-        fin = fin && isfinite(v);
-        M[q] = (MT)v;
+    bool ok = devRhs(mm, base, tab, P, tempv, v1, lane, false);
+    const double gdT = -gamma / dT;
+    for (int i = lane; i < N; i += 32) {
+        double v = (v1[i] - ftemp[i]) * gdT;
+        if (i == 0) v += 1.0;
+        fin = fin && finiteBits(v);
+        M[(size_t)i * ld] = (MT)v;
     }
-    __syncwarp();
-    for (int i = lane; i < N; i += 32) M[(size_t)i * ld + i] = (MT)((double)M[(size_t)i * ld + i] + 1.0);
     __syncwarp();
     ok = __all_sync(0xffffffffu, ok && fin);
     if (!ok) return false;
     return devLuFactor<MT>(M, N, ld, piv, dinv, lane);
 }
+
+// Solve (P^T L U) x = b in place.  The vector lives in registers (element i in lane
+// i % 32, slot i / 32); every substitution step broadcasts one element by a shuffle.
+template <typename MT, int S>
+__device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, const int* piv, const double* dinv,
+                                    int lane) {
+    MT x[S];
+#pragma unroll
+    for (int t = 0; t < S; t++) {
+        const int i = lane + 32 * t;
+        x[t] = (i < N) ? (MT)b[piv[i]] : (MT)0;
+    }
+    // forward: unit lower triangle (the next column's entries are loaded one step ahead)
+    MT nx[S];
+#pragma unroll
+    for (int t = 0; t < S; t++) {
+        const int i = lane + 32 * t;
+        nx[t] = (i < N) ? a[(size_t)i * ld] : (MT)0;
+    }
+#pragma unroll
+    for (int tk = 0; tk < S; tk++) {
+        const int kend = min(N, 32 * (tk + 1));
+        for (int k = 32 * tk; k < kend; k++) {
+            MT cur[S];
+#pragma unroll
+            for (int t = 0; t < S; t++) {
+                cur[t] = nx[t];
+                const int i = lane + 32 * t;
+                if (i < N && k + 1 < N) nx[t] = a[(size_t)i * ld + k + 1];
+            }
+            const MT xk = __shfl_sync(0xffffffffu, x[tk], k & 31);
+#pragma unroll
+            for (int t = tk; t < S; t++) {
+                const int i = lane + 32 * t;
+                if (i > k && i < N) x[t] -= cur[t] * xk;
+            }
+        }
+    }
+    // backward: upper triangle with the stored reciprocal diagonal (prefetched likewise)
+#pragma unroll
+    for (int t = 0; t < S; t++) {
+        const int i = lane + 32 * t;
+        nx[t] = (i < N) ? a[(size_t)i * ld + N - 1] : (MT)0;
+    }
+    MT nd = (MT)dinv[N - 1];
+#pragma unroll
+    for (int tk = S - 1; tk >= 0; tk--) {
+        const int kbeg = min(N, 32 * (tk + 1)) - 1;
+        for (int k = kbeg; k >= 32 * tk; k--) {
+            MT cur[S];
+            const MT dk = nd;
+#pragma unroll
+            for (int t = 0; t < S; t++) {
+                cur[t] = nx[t];
+                const int i = lane + 32 * t;
+                if (i < N && k > 0) nx[t] = a[(size_t)i * ld + k - 1];
+            }
+            if (k > 0) nd = (MT)dinv[k - 1];
+            if (lane == (k & 31)) x[tk] = x[tk] * dk;
+            const MT xk = __shfl_sync(0xffffffffu, x[tk], k & 31);
+#pragma unroll
+            for (int t = 0; t <= tk; t++) {
+                const int i = lane + 32 * t;
+                if (i < k) x[t] -= cur[t] * xk;
+            }
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < S; t++) {
+        const int i = lane + 32 * t;
+        if (i < N) b[i] = (double)x[t];
+    }
+    __syncwarp();
+}
+
 
 struct BdfWarp {
     const DevMech* m;
@@ -312,17 +428,19 @@ struct BdfWarp {
 
     __device__ double wrms(const double* v) const {
         double a = 0.0;
+#pragma unroll 1
         for (int i = lane; i < N; i += 32) { double x = v[i] * ewt[i]; a += x * x; }
         return sqrt(warpSum(a) / Nnorm);
     }
     __device__ double* Z(int j) const { return zn + (size_t)j * N; }
     __device__ void setEwt(const double* yv) {
+#pragma unroll 1
         for (int i = lane; i < N; i += 32) ewt[i] = 1.0 / (rtol * fabs(yv[i]) + atol);
         __syncwarp();
     }
-    __device__ bool rhs(const double* z, double* zdot, BdfScal& S) {
+    __device__ bool rhs(const double* z, double* zdot, BdfScal& S, bool forJac = false) {
         if (lane == 0) aux->nrhs++;
-        return devRhs(*m, base, tab, P, z, zdot, lane);
+        return devRhs(*m, base, tab, P, z, zdot, lane, forJac);
     }
     template <typename MT>
     __device__ bool setup(MT* M, BdfScal& S) {
@@ -330,76 +448,41 @@ struct BdfWarp {
         return devSetup<MT>(*m, base, tab, M, ld, S.gamma, P, y, ftemp, v1, v2, tempv, piv, dinv, lane);
     }
 
-    // Solve (P^T L U) x = b in place.  The vector lives in registers (element i in lane
-    // i % 32, slot i / 32); every substitution step broadcasts one element by a shuffle.
     template <typename MT, int S>
-    __device__ void luSolve(const MT* a, double* b) {
-        MT x[S];
-#pragma unroll
-        for (int t = 0; t < S; t++) {
-            const int i = lane + 32 * t;
-            x[t] = (i < N) ? (MT)b[piv[i]] : (MT)0;
-        }
-        // forward: unit lower triangle
-#pragma unroll
-        for (int tk = 0; tk < S; tk++) {
-            const int kend = min(N, 32 * (tk + 1));
-            for (int k = 32 * tk; k < kend; k++) {
-                const MT xk = __shfl_sync(0xffffffffu, x[tk], k & 31);
-#pragma unroll
-                for (int t = tk; t < S; t++) {
-                    const int i = lane + 32 * t;
-                    if (i > k && i < N) x[t] -= a[(size_t)i * ld + k] * xk;
-                }
-            }
-        }
-        // backward: upper triangle with the stored reciprocal diagonal
-#pragma unroll
-        for (int tk = S - 1; tk >= 0; tk--) {
-            const int kbeg = min(N, 32 * (tk + 1)) - 1;
-            for (int k = kbeg; k >= 32 * tk; k--) {
-                if (lane == (k & 31)) x[tk] = x[tk] * (MT)dinv[k];
-                const MT xk = __shfl_sync(0xffffffffu, x[tk], k & 31);
-#pragma unroll
-                for (int t = 0; t <= tk; t++) {
-                    const int i = lane + 32 * t;
-                    if (i < k) x[t] -= a[(size_t)i * ld + k] * xk;
-                }
-            }
-        }
-        __syncwarp();
-#pragma unroll
-        for (int t = 0; t < S; t++) {
-            const int i = lane + 32 * t;
-            if (i < N) b[i] = (double)x[t];
-        }
-        __syncwarp();
-    }
+    __device__ void luSolve(const MT* a, double* b) { devLuSolve<MT, S>(a, b, N, ld, piv, dinv, lane); }
 
     __device__ void predict(BdfScal& S) {
         S.tn += S.h;
+#pragma unroll 1
         for (int k = 1; k <= S.q; k++)
+#pragma unroll 1
             for (int j = S.q; j >= k; j--) {
                 double* a = Z(j - 1);
                 const double* b = Z(j);
+#pragma unroll 1
                 for (int i = lane; i < N; i += 32) a[i] += b[i];
             }
         __syncwarp();
     }
     __device__ void restore(BdfScal& S, double saved_t) {
         S.tn = saved_t;
+#pragma unroll 1
         for (int k = 1; k <= S.q; k++)
+#pragma unroll 1
             for (int j = S.q; j >= k; j--) {
                 double* a = Z(j - 1);
                 const double* b = Z(j);
+#pragma unroll 1
                 for (int i = lane; i < N; i += 32) a[i] -= b[i];
             }
         __syncwarp();
     }
     __device__ void rescale(BdfScal& S) {
         double f = S.eta;
+#pragma unroll 1
         for (int j = 1; j <= S.q; j++) {
             double* a = Z(j);
+#pragma unroll 1
             for (int i = lane; i < N; i += 32) a[i] *= f;
             f *= S.eta;
         }
@@ -464,9 +547,10 @@ struct BdfWarp {
         const double rl1 = 1.0 / S.l[1];
         bool jcur = false;
         for (;;) {
+#pragma unroll 1
             for (int i = lane; i < N; i += 32) { y[i] = zn[i]; acor[i] = 0.0; }
             __syncwarp();
-            if (!rhs(y, ftemp, S)) return NLS_RECOVER;
+            if (!rhs(y, ftemp, S, callSetup)) return NLS_RECOVER;
             if (callSetup) {
                 callSetup = false;
                 bool ok = setup<MT>(M, S);
@@ -484,15 +568,18 @@ struct BdfWarp {
             const double* z1 = Z(1);
             for (;;) {
                 if (lane == 0) aux->nni++;
+#pragma unroll 1
                 for (int i = lane; i < N; i += 32) tempv[i] = S.gamma * ftemp[i] - (rl1 * z1[i] + acor[i]);
                 __syncwarp();
                 luSolve<MT, NS>(M, tempv);
                 if (S.gamrat != 1.0) {
                     double f = 2.0 / (1.0 + S.gamrat);
+#pragma unroll 1
                     for (int i = lane; i < N; i += 32) tempv[i] *= f;
                     __syncwarp();
                 }
                 del = wrms(tempv);
+#pragma unroll 1
                 for (int i = lane; i < N; i += 32) { acor[i] += tempv[i]; y[i] = zn[i] + acor[i]; }
                 __syncwarp();
                 if (!isfinite(del)) { retry = !jcur; break; }
@@ -538,11 +625,13 @@ struct BdfWarp {
         for (int j = 2; j < QMAX; j++) {
             if (j < S.q) {
                 double* a = Z(j);
+#pragma unroll 1
                 for (int i = lane; i < N; i += 32) a[i] -= w[j] * zq[i];
             }
         }
         __syncwarp();
         double* a = Z(S.q);
+#pragma unroll 1
         for (int i = lane; i < N; i += 32) a[i] = 0.0;
         __syncwarp();
     }
@@ -551,16 +640,19 @@ struct BdfWarp {
         orderPoly(S, S.q - 1, w);
         const double c = lq_prev / (S.q + 1);
         const double* sv = Z(QMAX);
+#pragma unroll 1
         for (int i = lane; i < N; i += 32) tempv[i] = c * sv[i];
         __syncwarp();
 #pragma unroll
         for (int j = 2; j <= QMAX; j++) {
             if (j <= S.q) {
                 double* a = Z(j);
+#pragma unroll 1
                 for (int i = lane; i < N; i += 32) a[i] += w[j] * tempv[i];
             }
         }
         double* top = Z(S.q + 1);
+#pragma unroll 1
         for (int i = lane; i < N; i += 32) top[i] = tempv[i];
         __syncwarp();
     }
@@ -597,6 +689,7 @@ struct BdfWarp {
         const double* z0 = Z(0);
         const double* z1 = Z(1);
         double hi = 0.0;
+#pragma unroll 1
         for (int i = lane; i < N; i += 32) hi = fmax(hi, fabs(z1[i]) / (0.1 * fabs(z0[i]) + atol));
         double hub_inv = warpMax(hi);
         double hub = 0.1 * tdist;
@@ -605,9 +698,11 @@ struct BdfWarp {
         double hg = sqrt(hlb * hub);
         double hnew = hg;
         for (int count = 1; count <= 4; count++) {
+#pragma unroll 1
             for (int i = lane; i < N; i += 32) y[i] = z0[i] + hg * z1[i];
             __syncwarp();
             if (!rhs(y, tempv, S)) { hg *= 0.2; continue; }
+#pragma unroll 1
             for (int i = lane; i < N; i += 32) tempv[i] = (tempv[i] - z1[i]) / hg;
             __syncwarp();
             double yddnrm = wrms(tempv);
@@ -653,6 +748,7 @@ struct BdfWarp {
                     if (i <= L) hp *= hr;
                 double cquot = (S.tq[5] / S.saved_tq5) * hp;
                 const double* sv = Z(QMAX);
+#pragma unroll 1
                 for (int i = lane; i < N; i += 32) tempv[i] = acor[i] - cquot * sv[i];
                 __syncwarp();
                 double dup = wrms(tempv) * S.tq[3];
@@ -672,6 +768,7 @@ struct BdfWarp {
                 S.eta = etaqp1;
                 S.qprime = S.q + 1;
                 double* sv = Z(QMAX);
+#pragma unroll 1
                 for (int i = lane; i < N; i += 32) sv[i] = acor[i];
                 __syncwarp();
             }
@@ -748,9 +845,11 @@ struct BdfWarp {
                     if (S.q > 1) { S.q = 1; S.L = 2; }
                     if (!rhs(Z(0), tempv, S)) return ST_NONFINITE;
                     double* z1 = Z(1);
+#pragma unroll 1
                     for (int i = lane; i < N; i += 32) z1[i] = S.h * tempv[i];
                     for (int j = 2; j <= QMAX; j++) {
                         double* a = Z(j);
+#pragma unroll 1
                         for (int i = lane; i < N; i += 32) a[i] = 0.0;
                     }
                     __syncwarp();
@@ -770,6 +869,7 @@ struct BdfWarp {
                 if (j <= S.q) {
                     double* a = Z(j);
                     const double lj = S.l[j];
+#pragma unroll 1
                     for (int i = lane; i < N; i += 32) a[i] += lj * acor[i];
                 }
             }
@@ -777,6 +877,7 @@ struct BdfWarp {
             S.qwait--;
             if (S.qwait == 1 && S.q != QMAX) {
                 double* sv = Z(QMAX);
+#pragma unroll 1
                 for (int i = lane; i < N; i += 32) sv[i] = acor[i];
                 __syncwarp();
                 S.saved_tq5 = S.tq[5];
@@ -790,13 +891,15 @@ struct BdfWarp {
 
 template <typename MT, int NS>
 __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
-    extern __shared__ double smem[];
-    __shared__ uint64_t s_tab[64];
-    gbx_load_table(s_tab);
-    const DevMech& m = p.m;
+    extern __shared__ __align__(128) double smem[];
+    __shared__ uint64_t s_tab[kGbxTableWords];
+    __shared__ DevMech s_mech;
+    loadMech(p.m, s_mech, (char*)smem, p.mechSmem);
+    gbx_load_table(s_tab);   // (its barrier also completes the mechanism copy)
+    const DevMech& m = s_mech;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    double* base = smem + (size_t)warp * p.warpDoubles;
+    double* base = smem + p.mechSmem / 8 + (size_t)warp * p.warpDoubles;
     BdfWarp W;
     W.m = &m;
     W.N = m.N;
@@ -823,7 +926,8 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     W.v2 = q; q += N;
     W.dinv = q; q += N;
     W.piv = (int*)q; q += (N + 1) / 2;
-    MT* M = (MT*)q;
+    MT* M = p.Mbuf ? (MT*)((char*)p.Mbuf + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * p.Mstride)
+                   : (MT*)q;
 
     for (;;) {
         int idx = 0;
@@ -841,8 +945,11 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
             // zn[0] = state, zn[1] = h*f(state)
             double* z0 = W.zn;
             if (lane == 0) z0[0] = p.T[r];
+#pragma unroll 1
             for (int k = lane; k < m.K; k += 32) z0[1 + k] = p.Y[(size_t)k * p.n + r];
+#pragma unroll 1
             for (int j = 1; j <= QMAX; j++)
+#pragma unroll 1
                 for (int i = lane; i < N; i += 32) W.zn[(size_t)j * N + i] = 0.0;
             __syncwarp();
             S.tn = p.t0;
@@ -854,8 +961,11 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
             }
             S.nst = 0; S.nstlp = 0;
             S.haveLU = false;
+#pragma unroll 1
             for (int i = 0; i < QMAX + 2; i++) S.tau[i] = 0.0;
+#pragma unroll 1
             for (int i = 0; i < 6; i++) S.tq[i] = 0.0;
+#pragma unroll 1
             for (int i = 0; i <= QMAX; i++) S.l[i] = 0.0;
             S.saved_tq5 = 0.0; S.crate = 1.0; S.gammap = 0.0; S.gamrat = 1.0; S.acnrm = 0.0;
             W.setEwt(z0);
@@ -864,6 +974,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
             if (status == ST_OK) {
                 double h0 = W.initialStep(S, p.tout);
                 double* z1 = W.Z(1);
+#pragma unroll 1
                 for (int i = lane; i < N; i += 32) z1[i] *= h0;
                 __syncwarp();
                 S.h = S.hscale = S.hprime = h0;
@@ -877,12 +988,16 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
             }
             S.status0 = status;
         } else {
+#pragma unroll 1
             for (int i = lane; i < (QMAX + 1) * N; i += 32) W.zn[i] = rec[i];
             __syncwarp();
             S.tn = rs[R_TN]; S.h = rs[R_H]; S.hscale = rs[R_HSCALE]; S.hprime = rs[R_HPRIME];
             S.eta = rs[R_ETA]; S.etamax = rs[R_ETAMAX];
+#pragma unroll 1
             for (int i = 0; i < QMAX + 2; i++) S.tau[i] = rs[R_TAU + i];
+#pragma unroll 1
             for (int i = 0; i < 6; i++) S.tq[i] = rs[R_TQ + i];
+#pragma unroll 1
             for (int i = 0; i <= QMAX; i++) S.l[i] = rs[R_L + i];
             S.gammap = rs[R_GAMMAP]; S.crate = rs[R_CRATE]; S.saved_tq5 = rs[R_SAVEDTQ5];
             if (lane == 0) {
@@ -909,21 +1024,27 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
         }
         // output: interpolate to tout (or the last state on failure)
         const double sfac = (status == ST_OK && S.h != 0.0) ? (p.tout - S.tn) / S.h : 0.0;
+#pragma unroll 1
         for (int i = lane; i < N; i += 32) {
             double v = W.zn[(size_t)S.q * N + i];
+#pragma unroll 1
             for (int j = S.q - 1; j >= 0; j--) v = W.zn[(size_t)j * N + i] + sfac * v;
             if (status != ST_OK) v = W.zn[i];
             if (i == 0) p.T[r] = v;
             else p.Y[(size_t)(i - 1) * p.n + r] = v;
         }
         // save the integrator record
+#pragma unroll 1
         for (int i = lane; i < (QMAX + 1) * N; i += 32) rec[i] = W.zn[i];
         if (lane == 0) {
             double* o = rec + (QMAX + 1) * N;
             o[R_TN] = S.tn; o[R_H] = S.h; o[R_HSCALE] = S.hscale; o[R_HPRIME] = S.hprime;
             o[R_ETA] = S.eta; o[R_ETAMAX] = S.etamax;
+#pragma unroll 1
             for (int i = 0; i < QMAX + 2; i++) o[R_TAU + i] = S.tau[i];
+#pragma unroll 1
             for (int i = 0; i < 6; i++) o[R_TQ + i] = S.tq[i];
+#pragma unroll 1
             for (int i = 0; i <= QMAX; i++) o[R_L + i] = S.l[i];
             o[R_GAMMAP] = S.gammap; o[R_CRATE] = S.crate; o[R_SAVEDTQ5] = S.saved_tq5;
             const WarpAux& A = *W.aux;
@@ -942,7 +1063,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
 
 template <typename MT, int NS>
 cudaError_t launchBdfT(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
-    size_t smem = (size_t)p.warpDoubles * 8 * warpsPerBlock;
+    size_t smem = (size_t)p.mechSmem + (size_t)p.warpDoubles * 8 * warpsPerBlock;
     cudaError_t e = cudaFuncSetAttribute(k_bdf<MT, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_bdf<MT, NS><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
@@ -960,14 +1081,21 @@ int bdfWarpDoubles(const DevMech& m, int ld, bool fp32) {
     return (tot + 1) & ~1;   // keep each warp's slice 16-byte aligned
 }
 
-int ratesWarpDoubles(const DevMech& m) {
+int bdfWarpDoublesNoMatrix(const DevMech& m) {
+    int N = m.N;
+    int kinD = kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
+    int vec = (QMAX + 1) * N + 8 * N + (N + 1) / 2 + kAuxDoubles;
+    return (kinD + vec + 1) & ~1;
+}
+
+int ratesWarpDoubles(const DevMech& m, bool jac) {
     int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
-    int tot = kinD + 2 * m.K + m.K * (m.K + 1);
+    int tot = kinD + 2 * m.K + (jac ? m.K * (m.K + 1) : 0);
     return (tot + 1) & ~1;
 }
 
 cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
-    size_t smem = (size_t)p.warpDoubles * 8 * warpsPerBlock;
+    size_t smem = (size_t)p.mechSmem + (size_t)p.warpDoubles * 8 * warpsPerBlock;
     cudaError_t e = cudaFuncSetAttribute(k_rates, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_rates<<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
@@ -1010,12 +1138,28 @@ __global__ void k_probe_exp(double* out, int iters, int useLog) {
 }
 
 __global__ void k_check_exp(int n, const double* x, double* mine, double* lib) {
-    __shared__ uint64_t s_tab[64];
+    __shared__ uint64_t s_tab[kGbxTableWords];
     gbx_load_table(s_tab);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         mine[i] = fexp(x[i], s_tab);
         lib[i] = exp(x[i]);
     }
+}
+
+__global__ void k_check_log(int n, const double* x, double* mine, double* lib) {
+    __shared__ uint64_t s_tab[kGbxTableWords];
+    gbx_load_table(s_tab);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        mine[i] = gbx_log(x[i], s_tab);
+        lib[i] = log(x[i]);
+    }
+}
+
+cudaError_t checkLog(int n, const double* x, double* mine, double* lib) {
+    k_check_log<<<256, 256>>>(n, x, mine, lib);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return cudaDeviceSynchronize();
 }
 
 cudaError_t checkExp(int n, const double* x, double* mine, double* lib) {
@@ -1035,30 +1179,30 @@ cudaError_t measureFp64(double* results, int smCount) {
     cudaEventCreate(&b);
     float ms = 0.f;
     const int it = 4096;
-    double best = 0.0, bestExp = 1e30, bestLog = 1e30;
-    for (int rep = 0; rep < 3; rep++) {
+    double best = 0.0, bestExpRate = 0.0, bestLogRate = 0.0;
+    for (int rep = 0; rep < 6; rep++) {
         cudaEventRecord(a);
         k_probe_fma<<<blocks, threads>>>(d, it, 1.0000001, 1e-9);
         cudaEventRecord(b);
         cudaEventSynchronize(b);
         cudaEventElapsedTime(&ms, a, b);
-        double fmaPerS = 8.0 * it * threads * blocks / (ms * 1e-3);
+        const double fmaPerS = 8.0 * it * threads * blocks / (ms * 1e-3);
         best = fmax(best, fmaPerS);
         cudaEventRecord(a);
         k_probe_exp<<<blocks, threads>>>(d, it / 8, 0);
         cudaEventRecord(b);
         cudaEventSynchronize(b);
         cudaEventElapsedTime(&ms, a, b);
-        double expPerS = 2.0 * (it / 8) * threads * blocks / (ms * 1e-3);
-        bestExp = fmin(bestExp, best / expPerS);
+        bestExpRate = fmax(bestExpRate, 2.0 * (it / 8) * threads * blocks / (ms * 1e-3));
         cudaEventRecord(a);
         k_probe_exp<<<blocks, threads>>>(d, it / 8, 1);
         cudaEventRecord(b);
         cudaEventSynchronize(b);
         cudaEventElapsedTime(&ms, a, b);
-        double logPerS = 2.0 * (it / 8) * threads * blocks / (ms * 1e-3);
-        bestLog = fmin(bestLog, best / logPerS);
+        bestLogRate = fmax(bestLogRate, 2.0 * (it / 8) * threads * blocks / (ms * 1e-3));
     }
+    // costs relative to the best FMA rate, each at its own best (clocks settle during the reps)
+    const double bestExp = best / bestExpRate, bestLog = best / bestLogRate;
     e = cudaGetLastError();
     cudaEventDestroy(a);
     cudaEventDestroy(b);

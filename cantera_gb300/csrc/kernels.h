@@ -17,6 +17,7 @@ struct RatesParams {
     double* jac;          // [nnz][n] or null
     int* counter;         // work counter (zeroed before launch)
     int warpDoubles;      // shared-memory doubles per warp
+    int mechSmem;         // bytes of the mechanism arena copied into shared memory
 };
 
 struct BdfParams {
@@ -37,16 +38,22 @@ struct BdfParams {
     const int* order;     // [n] queue order (null: identity)
     int ld;               // leading dimension of the Newton matrix
     int warpDoubles;
+    int mechSmem;         // bytes of the mechanism arena copied into shared memory (multiple of 16)
+    void* Mbuf;           // Newton matrices in global memory, one slot of Mstride bytes per
+                          // resident warp (L2 resident); null: in the warp's shared slice
+    long long Mstride;
 };
 
 constexpr int kBdfMaxThreads = 256;   // at most 8 warps per block
 int bdfRecordStride(int N);
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32);
-int ratesWarpDoubles(const DevMech& m);
+int bdfWarpDoublesNoMatrix(const DevMech& m);   // the slice when the matrix is in global memory
+int ratesWarpDoubles(const DevMech& m, bool jac);   // dense Jacobian scratch only with jac
 cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
 cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream);
 // FP64 throughput probe: returns {GFLOP/s of FMA, exp cost, log cost in FMA-equivalents}
 cudaError_t measureFp64(double* results, int smCount);
 cudaError_t checkExp(int n, const double* x, double* mine, double* lib);
+cudaError_t checkLog(int n, const double* x, double* mine, double* lib);
 
 }  // namespace gbchem

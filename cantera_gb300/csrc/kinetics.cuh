@@ -86,7 +86,12 @@ struct KinScratch {
 // Scalars of the current state, identical in every lane.
 struct KinState {
     double T, P, RT, rho, mmw, ctot, lnT, recipT;
+    double rrho;       // 1/rho
+    double lnPP;       // ln(P/Pref)
+    double lnC0;       // ln(P/RT), the log of the standard concentration
+    double RTP, PRT;   // RT/P and P/RT
 };
+constexpr int kKinStateDoubles = 13;
 
 // mass-action product of one side (expanded species list e, count n = e.w) with the
 // StoichManager sign rules; `gen` selects the general power-law list (CN bucket).
@@ -103,12 +108,14 @@ __device__ __forceinline__ double massAction(const DevMech& m, int bucket, int4 
         return a * b * d;
     }
     double r = 1.0;
+#pragma unroll 1
     for (int q = m.sidePtr[side]; q < m.sidePtr[side + 1]; q++) {
         double o = m.sideOrd[q];
         if (o != 0.0) {
             double x = c[m.sideK[q]];
-            if (x > 0.0) r *= pow(x, o);
-            else return 0.0;
+            if (!(x > 0.0)) return 0.0;
+            // pow(x, 1) = x and pow(x, 2) = x*x up to rounding
+            r *= (o == 1.0) ? x : ((o == 2.0) ? x * x : pow(x, o));
         }
     }
     return r;
@@ -133,12 +140,14 @@ __device__ __forceinline__ double massActionDeriv(const DevMech& m, int bucket, 
     }
     double d = 0.0;
     int q0 = m.sidePtr[side], q1 = m.sidePtr[side + 1];
+#pragma unroll 1
     for (int q = q0; q < q1; q++) {
         if (m.sideK[q] != j) continue;
         double oi = m.sideOrd[q];
         double x = c[j];
         if (!(x > 0.0) || oi == 0.0) continue;
         double prod = oi * pow(x, oi - 1.0);
+#pragma unroll 1
         for (int p = q0; p < q1; p++) {
             if (p == q) continue;
             double y = c[m.sideK[p]];
@@ -156,80 +165,108 @@ __device__ __forceinline__ double arrhenius(double A, double b, double EaR, doub
 }
 
 // Falloff rate k(T, M) and, optionally, d ln k / d M (analytic).
+//   k = khigh Pr/(1 + Pr) F,  Pr = [M] klow/(khigh + 1e-300)
+//   Troe: log10 F = log10 Fcent / (1 + f^2), f = u/d, u = log10 Pr + c, d = n - 0.14 u
+// The three quotients of the Troe form share one reciprocal, 1/((1 + Pr)(d^2 + u^2)).
+//   d ln k/d[M] = (1/[M]) (1/(1 + Pr) + d ln F/d ln Pr),  d ln F/d ln Pr = -2 log10(Fcent) u n d/(d^2 + u^2)^2
 __device__ __forceinline__ double falloff(D4 f1, D4 f2, double A, double b, double EaR,
                                           const KinState& st, double M, double* dlnk_dM, const uint64_t* tab) {
-    double work = 0.0;
-    bool troe = f2.w != 0.0;
+    const bool troe = f2.w != 0.0;
+    double logFc = 0.0;
     if (troe) {
         double Fcent = (1.0 - f1.w) * fexp(-st.T * f2.x, tab) + f1.w * fexp(-st.T * f2.y, tab);
         if (f2.z != 0.0) Fcent += fexp(-f2.z * st.recipT, tab);
-        work = log10(fmax(Fcent, 1e-300));
+        logFc = gbx_log10(fmax(Fcent, 1e-300), tab);
     }
-    double klow = arrhenius(f1.x, f1.y, f1.z, st.lnT, st.recipT, tab);
-    double khigh = arrhenius(A, b, EaR, st.lnT, st.recipT, tab);
-    double dPr = klow / (khigh + 1e-300);
-    double pr = M * dPr;
-    double F = 1.0, dFdPr_over_F = 0.0;
+    const double klow = arrhenius(f1.x, f1.y, f1.z, st.lnT, st.recipT, tab);
+    const double khigh = arrhenius(A, b, EaR, st.lnT, st.recipT, tab);
+    const double pr = M * (klow / (khigh + 1e-300));
+    const double onep = 1.0 + pr;
+    double k;
     if (troe) {
-        double lpr = log10(fmax(pr, 1e-300));
-        double cc = -0.4 - 0.67 * work;
-        double nn = 0.75 - 1.27 * work;
-        double u = lpr + cc;
-        double den = nn - 0.14 * u;
-        double f1v = u / den;
-        double q = 1.0 + f1v * f1v;
-        double lgf = work / q;
-        F = fexp(lgf * 2.302585092994046, tab);
-        if (pr > 1e-300) dFdPr_over_F = (-work * 2.0 * f1v / (q * q) * (nn / (den * den))) / pr;
-    }
-    double k = pr * (F / (1.0 + pr)) * khigh;
-    if (dlnk_dM) {
-        // k = khigh * Pr/(1+Pr) * F(Pr): dk/dM = khigh*dPr*(F/(1+Pr)^2 + Pr/(1+Pr)*dF/dPr)
-        double s = 1.0 / (1.0 + pr);
-        double dk = khigh * dPr * (s * s * F + pr * s * F * dFdPr_over_F);
-        *dlnk_dM = (k != 0.0) ? dk / k : 0.0;
+        const double lpr = gbx_log10(fmax(pr, 1e-300), tab);
+        const double nn = 0.75 - 1.27 * logFc;
+        const double u = lpr + (-0.4 - 0.67 * logFc);
+        const double d = nn - 0.14 * u;
+        const double q = fma(d, d, u * u);
+        const double inv = 1.0 / (onep * q);
+        const double rq = inv * onep;          // 1/(d^2 + u^2)
+        const double rop = inv * q;            // 1/(1 + Pr)
+        const double lgF = logFc * (d * d) * rq;
+        const double F = fexp(lgF * 2.302585092994046, tab);
+        k = pr * (F * rop) * khigh;
+        if (dlnk_dM) {
+            double t = rop;
+            if (pr > 1e-300) t -= 2.0 * logFc * u * nn * d * (rq * rq);
+            *dlnk_dM = t / M;
+        }
+    } else {
+        const double rop = 1.0 / onep;
+        k = pr * rop * khigh;
+        if (dlnk_dM) *dlnk_dM = rop / M;
     }
     return k;
 }
 
 // Mixture state from (T, P, Y).  Y may alias any readable [K] array.
+// The per-state reciprocals and logarithms are evaluated once for the whole warp, one
+// argument per lane (1/T, 1/sum(Y/W), 1/RT, 1/P and ln T, ln P, ln RT, ln Pref), then
+// broadcast: a double division costs the FP64 pipe the same whether one lane or all 32
+// need it.  The logarithm runs on the integer pipe (fastexp.h).
 __device__ __forceinline__ void warpState(const DevMech& m, double T, double P, const double* Y,
                                           KinScratch& s, KinState& st, int lane) {
     double part = 0.0;
+#pragma unroll 1
     for (int k = lane; k < m.K; k += 32) {
         double ym = Y[k] * m.rmw[k];
         s.c[k] = ym;
         part += ym;
     }
-    double sum = warpSum(part);
+    const double sum = warpSum(part);
+    const double RT = T * m.Rgas;
+    const int l4 = lane & 3;
+    const double xr = l4 == 0 ? T : (l4 == 1 ? sum : (l4 == 2 ? RT : P));
+    const double xl = l4 == 0 ? T : (l4 == 1 ? P : (l4 == 2 ? RT : m.Pref));
+    const double r = 1.0 / xr;
+    const double lg = gbx_log(xl, s.tab);
     st.T = T;
     st.P = P;
-    st.RT = T * m.Rgas;
-    st.mmw = 1.0 / sum;
-    st.rho = P * st.mmw / st.RT;
-    st.ctot = st.rho / st.mmw;
-    st.lnT = log(T);
-    st.recipT = 1.0 / T;
+    st.RT = RT;
+    st.recipT = __shfl_sync(0xffffffffu, r, 0);
+    st.mmw = __shfl_sync(0xffffffffu, r, 1);
+    const double rRT = __shfl_sync(0xffffffffu, r, 2);
+    const double rP = __shfl_sync(0xffffffffu, r, 3);
+    st.lnT = __shfl_sync(0xffffffffu, lg, 0);
+    const double lnP = __shfl_sync(0xffffffffu, lg, 1);
+    const double lnRT = __shfl_sync(0xffffffffu, lg, 2);
+    const double lnPref = __shfl_sync(0xffffffffu, lg, 3);
+    st.PRT = P * rRT;
+    st.RTP = RT * rP;
+    st.ctot = st.PRT;                 // rho / mmw
+    st.rho = st.PRT * st.mmw;
+    st.rrho = st.RTP * sum;
+    st.lnPP = lnP - lnPref;
+    st.lnC0 = lnP - lnRT;
     __syncwarp();
-    for (int k = lane; k < m.K; k += 32) s.c[k] *= st.rho;
+    for (int k = lane; k < m.K; k += 32) s.c[k] *= st.rho;   // c_k = rho Y_k / W_k
 }
 
 // Species thermo + rates of progress + net production rates.  With `forJac`, also the
 // per-reaction data d(wdot)/dc needs (Qtb, dlk).
 template <bool forJac>
 __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, int lane) {
-    const double lnPP = log(st.P / m.Pref);
+    const double lnPP = st.lnPP;
     if (lane == 0) s.flags[0] = 0;
     __syncwarp();
+#pragma unroll 1
     for (int k = lane; k < m.K; k += 32) {
+        // Horner forms with the coefficients scaled on the host (kNasaStride layout)
         const double* a = m.nasa + (size_t)k * kNasaStride;
-        const double* p = (st.T <= a[0]) ? a + 1 : a + 8;
-        double T = st.T;
-        double t2 = T * T, t3 = t2 * T, t4 = t3 * T;
-        double ct0 = p[0], ct1 = p[1] * T, ct2 = p[2] * t2, ct3 = p[3] * t3, ct4 = p[4] * t4;
-        double cp = ct0 + ct1 + ct2 + ct3 + ct4;
-        double h = ct0 + 0.5 * ct1 + (1.0 / 3.0) * ct2 + 0.25 * ct3 + 0.2 * ct4 + p[5] * st.recipT;
-        double sR = ct0 * st.lnT + ct1 + 0.5 * ct2 + (1.0 / 3.0) * ct3 + 0.25 * ct4 + p[6];
+        const double* p = (st.T <= a[0]) ? a + 1 : a + 1 + kNasaRange;
+        const double T = st.T;
+        const double cp = fma(fma(fma(fma(p[4], T, p[3]), T, p[2]), T, p[1]), T, p[0]);
+        const double h = fma(p[5], st.recipT, fma(fma(fma(fma(p[10], T, p[9]), T, p[8]), T, p[7]), T, p[0]));
+        const double sR = fma(p[0], st.lnT, fma(fma(fma(fma(p[13], T, p[12]), T, p[11]), T, p[1]), T, p[6]));
         s.cpR[k] = cp;
         s.hRT[k] = h;
         const double gk = (h - sR) + lnPP;
@@ -249,7 +286,7 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
     }
     if (lane < 7) {
         // (RT/P)^dn for dn = lane - 3  (= exp(-dn * ln(P/RT)))
-        const double a = st.RT / st.P, b = st.P / st.RT;
+        const double a = st.RTP, b = st.PRT;
         const int dn = lane - 3;
         double v = 1.0;
         if (dn > 0) { v = a; if (dn > 1) v *= a; if (dn > 2) v *= a; }
@@ -263,10 +300,11 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
         s.Mtb[t] = m.tbDef[t] * st.ctot + sum;
     }
     __syncwarp();
-    const double logStandConc = log(st.P / st.RT);
+    const double logStandConc = st.lnC0;
     const bool bigG = s.flags[0] != 0;
+#pragma unroll 1
     for (int i = lane; i < m.R; i += 32) {
-        int4 info = __ldg(&m.rinfo[i]);
+        int4 info = m.rinfo[i];
         D4 ar = m.rarr[i];
         int kind = info.x & kKindMask;
         double kf;
@@ -283,8 +321,8 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
             if (forJac) s.dlk[info.z] = dlnk;
         }
         double kfe = (kind == 1) ? kf * s.Mtb[info.y] : kf;
-        int4 re = __ldg(&m.rk[i]);
-        int4 pe = __ldg(&m.pk[i]);
+        int4 re = m.rk[i];
+        int4 pe = m.pk[i];
         int rb = (info.x >> kRBucketShift) & 7, pb = (info.x >> kPBucketShift) & 7;
         double rkc = 0.0;
         double fwd = massAction(m, rb, re, 2 * i, s.c);
@@ -315,6 +353,7 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
                 if (pe.w > 1) dG += s.g[pe.y];
                 if (pe.w > 2) dG += s.g[pe.z];
             } else {
+#pragma unroll 1
                 for (int q = m.sidePtr[2 * i + 1]; q < m.sidePtr[2 * i + 2]; q++) dG += m.sideNu[q] * s.g[m.sideK[q]];
             }
             double dr = 0.0;
@@ -323,10 +362,11 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
                 if (re.w > 1) dr += s.g[re.y];
                 if (re.w > 2) dr += s.g[re.z];
             } else {
+#pragma unroll 1
                 for (int q = m.sidePtr[2 * i]; q < m.sidePtr[2 * i + 1]; q++) dr += m.sideNu[q] * s.g[m.sideK[q]];
             }
             dG -= dr;
-            rkc = fmin(exp(dG - ar.w * logStandConc), 1e300);
+            rkc = fmin(fexp(dG - ar.w * logStandConc, s.tab), 1e300);
             }
             rev = massAction(m, pb, pe, 2 * i + 1, s.c);
         }
@@ -362,18 +402,21 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
 // The caller zeroes Jc.  MT is the matrix element type (double or float).
 template <typename MT>
 __device__ __noinline__ void warpJacC(const DevMech& m, const KinScratch& s, MT* Jc, int ld, int lane) {
+#pragma unroll 1
     for (int q = m.laneColPtr[lane]; q < m.laneColPtr[lane + 1]; q++) {
         int j = m.laneCols[q];
+#pragma unroll 1
         for (int e = m.colPtr[j]; e < m.colPtr[j + 1]; e++) {
             int i = m.colRxn[e];
-            int4 info = __ldg(&m.rinfo[i]);
+            int4 info = m.rinfo[i];
             int rb = (info.x >> kRBucketShift) & 7, pb = (info.x >> kPBucketShift) & 7;
             double kfe = s.kfe[i];
-            double dF = kfe * massActionDeriv(m, rb, __ldg(&m.rk[i]), 2 * i, s.c, j);
-            if (info.x & kRevBit) dF -= (kfe * s.rkc[i]) * massActionDeriv(m, pb, __ldg(&m.pk[i]), 2 * i + 1, s.c, j);
+            double dF = kfe * massActionDeriv(m, rb, m.rk[i], 2 * i, s.c, j);
+            if (info.x & kRevBit) dF -= (kfe * s.rkc[i]) * massActionDeriv(m, pb, m.pk[i], 2 * i + 1, s.c, j);
             double ep = m.colE[e];
             if (ep != 0.0) dF += ep * s.Qtb[info.y];
             if (dF == 0.0) continue;
+#pragma unroll 1
             for (int r = m.rsPtr[i]; r < m.rsPtr[i + 1]; r++) {
                 MT* p = Jc + (size_t)m.rsK[r] * ld + j;
                 *p = (MT)((double)*p + m.rsNu[r] * dF);

@@ -81,6 +81,12 @@ typedef struct {
                                error norm and step control stay FP64) */
     int32_t warps_per_block;/* reactors per thread block; 0 = autotuned */
     int32_t use_graph;      /* 1: launch the advance through a captured CUDA graph */
+    int32_t matrix_placement; /* Newton matrix: 0 = automatic, 1 = shared memory, 2 = an
+                               L2-resident global slot per warp (frees shared memory for
+                               more resident reactors) */
+    int32_t mechanism_in_shared; /* mechanism data copied into each block's shared memory:
+                               0 = automatic, 1 = none, 2 = what the right-hand side reads,
+                               3 = also the Jacobian's data, 4 = everything but the rest */
 } gb_net_options;
 
 void gb_net_default_options(gb_net_options* opts);
@@ -97,6 +103,11 @@ double gb_net_time(int32_t net);
  * the engine's stream around the launch). */
 double gb_net_last_advance_ms(int32_t net);
 int32_t gb_net_get_state(int32_t net, double* T, double* Y, int32_t flags);
+
+/* Launch shape of the integrator: info[0..4] = blocks, reactors (warps) per block, shared
+ * bytes per warp, mechanism bytes in shared memory per block, Newton matrices in shared (1)
+ * or global (2) memory.  (No counterpart in the reference.) */
+int32_t gb_net_launch_info(int32_t net, int32_t* info);
 
 /* Per-reactor status: 0 ok, 1 max steps, 2 repeated error-test failures, 3 repeated
  * convergence failures, 4 non-finite state, 5 step size too small. */
@@ -119,7 +130,7 @@ int32_t gb_net_ignition_times(int32_t net, double* tign);
  * call, with the same integrator as gb_net_advance, allocating nothing.  T[n] and Y[K][n]
  * (in place) and P[n] are device pointers on the current device; status[n] (device)
  * receives the per-reactor status codes below.  opts may be NULL (defaults; use_graph is
- * ignored).  The integrator records live in a 16 MiB array in the library's device image,
+ * ignored; the Newton matrices stay in shared memory).  The integrator records live in a 16 MiB array in the library's device image,
  * so n is limited to what fits (about 5,500 reactors for GRI-Mech 3.0); a larger n fails
  * with GB_ERR and a message giving the limit.  The call is ordered on `stream` (a
  * cudaStream_t; NULL is the default stream) and synchronises it before returning.  Every
@@ -144,6 +155,8 @@ int32_t gb_measure_fp64(double* results);
 /* Evaluate the engine's own FP64 exponential and the CUDA library exp on n device-resident
  * arguments x (device pointers): out_engine[i], out_library[i].  For accuracy tests. */
 int32_t gb_check_exp(int32_t n, const double* x, double* out_engine, double* out_library);
+/* The same for the engine's logarithm against the CUDA library log. */
+int32_t gb_check_log(int32_t n, const double* x, double* out_engine, double* out_library);
 
 /* Copy the most recent error message (thread-local) into buf; returns its length. */
 int32_t gb_get_error(int32_t buflen, char* buf);

@@ -1,5 +1,5 @@
-// Host check of the integer-pipe exponential (cantera_gb300/csrc/fastexp.h) against the
-// C library exp: prints the largest error in units in the last place over a sweep.
+// Host check of the integer-pipe exponential and logarithm (cantera_gb300/csrc/fastexp.h)
+// against the C library: prints the largest errors over sweeps.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -46,6 +46,24 @@ int main(int argc, char** argv) {
         double rel = std::fabs((double)((got - want) / want));
         if (rel > worstprod) worstprod = rel;
     }
-    std::printf("max_ulp %.3f at %.17g max_ulp_neg %.3f max_rel_product %.3e\n", worst, worstx, worstpm, worstprod);
+    // logarithm: ulp error where |ln x| > 1/256, absolute error near x = 1 (against long double)
+    uint64_t tab[kGbxTableWords];
+    gbx_host_table(tab);
+    std::uniform_real_distribution<double> lexp(-690.0, 709.0), temp(200.0, 4000.0), near1(-0.004, 0.004);
+    double worstlog = 0.0, worstlog1 = 0.0;
+    for (long i = 0; i < n; i++) {
+        const int mode = (int)(i % 3);
+        const double x = mode == 0 ? std::exp(lexp(rng)) : (mode == 1 ? temp(rng) : 1.0 + near1(rng));
+        const double a = gbx_log(x, tab), b = std::log(x);
+        if (std::fabs(b) > 1.0 / 256) {
+            const double e = ulp_err(a, b);
+            if (e > worstlog) worstlog = e;
+        } else {
+            const double ab = std::fabs((double)((long double)a - logl((long double)x)));
+            if (ab > worstlog1) worstlog1 = ab;
+        }
+    }
+    std::printf("max_ulp %.3f at %.17g max_ulp_neg %.3f max_rel_product %.3e max_ulp_log %.3f max_abs_log_near1 %.3e\n",
+                worst, worstx, worstpm, worstprod, worstlog, worstlog1);
     return 0;
 }

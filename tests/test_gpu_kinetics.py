@@ -113,3 +113,28 @@ def test_engine_exp_against_library_exp():
     a, b = a.cpu().numpy(), b.cpu().numpy()
     both_nan = np.isnan(a) & np.isnan(b)
     assert np.all(both_nan | (a == b) | (np.abs(a - b) <= 2 * np.spacing(np.abs(b))))
+
+
+def test_engine_log_against_library_log():
+    """The engine's integer-pipe log: within one unit in the last place of CUDA's log where
+    |ln x| > 1/256, within 2^-60 absolute near x = 1; the library log for x <= 0, subnormal,
+    inf and nan."""
+    torch = pytest.importorskip("torch")
+    import cantera_gb300 as gb
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(22)
+    x = np.concatenate([np.exp(rng.uniform(-690, 709, 200000)), rng.uniform(250, 4000, 100000),
+                        1 + rng.uniform(-0.01, 0.01, 100000),
+                        [1.0, 2.0, 0.5, 1e-300, 1e300, 5e-324, 0.0, -1.0, np.inf, np.nan, 101325.0]])
+    xd = torch.tensor(x, device=dev)
+    a = torch.empty_like(xd)
+    b = torch.empty_like(xd)
+    gb._check(gb.library().gb_check_log(len(x), gb._ptr(xd), gb._ptr(a), gb._ptr(b)))
+    a, b = a.cpu().numpy(), b.cpu().numpy()
+    both_nan = np.isnan(a) & np.isnan(b)
+    fin = np.isfinite(b)
+    big = fin & (np.abs(b) > 1 / 256)
+    assert np.all(both_nan | ~fin | (a == b) | ~big | (np.abs(a - b) <= 1.01 * np.spacing(np.abs(b))))
+    small = fin & ~big
+    assert np.max(np.abs(a - b)[small]) < 2 ** -60 + np.max(np.spacing(np.abs(b[small])))
+    assert np.all((a == b)[~fin] | both_nan[~fin])

@@ -135,3 +135,56 @@ def test_failure_status_without_gpu_fault():
     assert st[3] == 4 and np.all(np.delete(st, 3) == 0)
     with pytest.raises(gb.GBError, match="backwards"):
         net2.advance(1e-5)
+
+
+@pytest.mark.parametrize("placement", [1, 2])
+def test_ndodecane_fp32_lu_against_fp64_and_oracle(placement):
+    """n-dodecane (K = 100, R = 553): the FP32-LU Newton against the FP64 one and the
+    oracle, with the Newton matrix in shared memory (1) or in a global slot per warp (2)."""
+    import cantera_gb300 as gb
+    from oracle import pyoracle as po
+    sol, m = gpu_solution("nDodecane"), oracle_mech("nDodecane")
+    rng = np.random.default_rng(20261203 + 3)
+    n = 12
+    T0 = rng.uniform(700, 1400, n)
+    P = 101325.0 * 10 ** rng.uniform(1, np.log10(60), n)
+    phi = rng.uniform(0.5, 2.0, n)
+    Y0 = np.array([m.equivalence_ratio(p, "c12h26:1", "o2:1, n2:3.76") for p in phi])
+    rtol, atol, t_end = 1e-8, 1e-15, 1e-3
+    out = {}
+    for lu in (64, 32):
+        net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=rtol, atol=atol, lu_precision=lu,
+                            matrix_placement=placement)
+        assert net.advance(t_end) == 0
+        out[lu] = net.get_state() + (net.solver_stats,)
+    To, Yo, sto, tio = m.advance_batch(T0, P, Y0, t_end, po.opts(rtol=rtol, atol=atol, analytic=True))
+    assert np.all(sto[:, 8] == 0)
+    dTdt = np.array([m.reactor_rhs(P[s], np.concatenate([[1.0, To[s]], Yo[s]]))[1] for s in range(n)])
+    steady = np.abs(dTdt) * 1e-4 * t_end < 10 * rtol * To
+    assert steady.sum() >= n // 3
+    for lu in (64, 32):
+        T, Y, st = out[lu]
+        assert np.max(np.abs(T - To)[steady] / To[steady]) < 10 * rtol, lu
+        check_species(Y.T[steady], Yo[steady], rtol)
+    # the FP32 factorisation changes the Newton iterates, not the accepted solution
+    T64, T32 = out[64][0], out[32][0]
+    assert np.max(np.abs(T32 - T64)[steady] / T64[steady]) < 10 * rtol
+
+
+def test_matrix_placement_is_bit_identical():
+    """The Newton matrix's location (shared memory or a global slot) does not change a bit."""
+    import cantera_gb300 as gb
+    sol = gpu_solution("gri30")
+    m = oracle_mech("gri30")
+    rng = np.random.default_rng(17)
+    n = 40
+    T0 = rng.uniform(900, 1500, n)
+    P = 101325.0 * rng.uniform(1, 20, n)
+    Y0 = np.array([m.equivalence_ratio(p, "CH4:1", "O2:1, N2:3.76") for p in rng.uniform(0.6, 1.4, n)])
+    res = []
+    for placement in (1, 2):
+        net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=1e-8, matrix_placement=placement)
+        net.advance(2e-3)
+        res.append(net.get_state())
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    np.testing.assert_array_equal(res[0][1], res[1][1])
