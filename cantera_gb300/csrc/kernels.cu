@@ -95,7 +95,7 @@ enum { F_HASPREV = 1, F_HASRIGHT = 2, F_AWAIT = 4, F_INIT = 8 };
 
 struct BdfScal {
     double tn, h, hscale, hprime, eta, etamax, gamma, gammap, gamrat, crate, acnrm, saved_tq5;
-    double tau[QMAX + 2], tq[6], l[QMAX + 1];   // indexed only with compile-time indices (registers)
+    double tau[QMAX + 2], tq[6], l[QMAX + 1];
     int q, qprime, qwait, L, nst, nstlp;
     bool haveLU;
     // ignition marker
@@ -111,16 +111,6 @@ struct WarpAux {
 };
 constexpr int kAuxDoubles = (int)((sizeof(WarpAux) + 7) / 8);
 
-// a[i] for a run-time i with every access at a compile-time index (keeps a[] in registers)
-template <int N>
-__device__ __forceinline__ double sel(const double (&a)[N], int i) {
-    double v = a[0];
-#pragma unroll
-    for (int k = 1; k < N; k++)
-        if (i == k) v = a[k];
-    return v;
-}
-
 // ---------------------------------------------------------------------------
 // The large per-warp routines are kept out of line (one copy of their code: the
 // integrator reaches them from several places) and take plain arguments, so that the
@@ -128,6 +118,12 @@ __device__ __forceinline__ double sel(const double (&a)[N], int i) {
 // the KinState of its last right-hand side (kStateSlots doubles), then the kinetics
 // scratch.
 // ---------------------------------------------------------------------------
+// division and square root for the integrator's scalar step control, out of line: one copy
+// of their code instead of one per use (the step logic runs once per step, its code size
+// matters more than a call)
+__device__ __noinline__ double ddiv(double a, double b) { return a / b; }
+__device__ __noinline__ double dsqrt(double a) { return sqrt(a); }
+
 constexpr int kStateSlots = 16;
 static_assert(kKinStateDoubles <= kStateSlots, "state slots");
 
@@ -165,6 +161,7 @@ __device__ __noinline__ bool devRhs(const DevMech& m, double* base, const uint64
     else warpRates<false>(m, s, st, lane);
     if (lane == 0) storeState(base, st);
     double ph = 0.0, pc = 0.0;
+#pragma unroll 1
     for (int k = lane; k < m.K; k += 32) {
         ph += s.wdot[k] * s.hRT[k];
         pc += s.c[k] * s.cpR[k];
@@ -175,6 +172,7 @@ __device__ __noinline__ bool devRhs(const DevMech& m, double* base, const uint64
     bool ok = finiteBits(dTdt);
     if (lane == 0) zdot[0] = dTdt;
     const double rrho = st.rrho;
+#pragma unroll 1
     for (int k = lane; k < m.K; k += 32) {
         const double v = s.wdot[k] * m.mw[k] * rrho;
         zdot[1 + k] = v;
@@ -264,27 +262,34 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     carveScratch(mm, base, tab, s);
     KinState st;
     loadState(base, st);
+#pragma unroll 1
     for (int q = lane; q < N * ld; q += 32) M[q] = (MT)0;
     __syncwarp();
     warpJacC<MT>(mm, s, M + ld + 1, ld, lane);
     // v1 = X (mole fractions); v2[k] = (Jc X)_k
     const double rct = st.RTP;   // 1/ctot
+#pragma unroll 1
     for (int k = lane; k < K; k += 32) v1[k] = s.c[k] * rct;
     __syncwarp();
+#pragma unroll 1
     for (int k = lane; k < K; k += 32) {
         const MT* row = M + (size_t)(1 + k) * ld + 1;
         double a = 0.0;
+#pragma unroll 1
         for (int l = 0; l < K; l++) a += (double)row[l] * v1[l];
         v2[k] = a;
     }
     double pcp = 0.0;
+#pragma unroll 1
     for (int k = lane; k < K; k += 32) pcp += v1[k] * s.cpR[k];
     const double cpmix = warpSum(pcp);
     __syncwarp();
     // column pass: hJ_j, then the transformed species block and the T row
     double phj = 0.0;
+#pragma unroll 1
     for (int j = lane; j < K; j += 32) {
         double a = 0.0;
+#pragma unroll 1
         for (int k = 0; k < K; k++) a += s.hRT[k] * (double)M[(size_t)(1 + k) * ld + 1 + j];
         tempv[j] = a;
         phj += a * v1[j];
@@ -296,14 +301,17 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     const double G = ftemp[0];
     // v2[k] <- W_k (Jc X)_k - wdot_k W_k mmw / rho: J[1+k][1+j] = (W_k Jc_kj - v2[k]) / W_j
     const double c1 = mmw * st.rrho;
+#pragma unroll 1
     for (int k = lane; k < K; k += 32) v2[k] = mm.mw[k] * (v2[k] - s.wdot[k] * c1);
     __syncwarp();
     // species block of M = I - gamma J in the same pass: M_kj = delta_kj - gamma/W_j (W_k Jc_kj - v2_k)
     const double hscale = rho * st.RT, cpscale = rho * mm.Rgas;
     bool fin = true;
+#pragma unroll 1
     for (int j = lane; j < K; j += 32) {
         const double rWj = mm.rmw[j];
         const double gj = -gamma * rWj;
+#pragma unroll 1
         for (int k = 0; k < K; k++) {
             MT* p = M + (size_t)(1 + k) * ld + 1 + j;
             double v = fma(mm.mw[k], (double)*p, -v2[k]) * gj;
@@ -321,12 +329,14 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     // T column: one-sided difference
     const double T0 = y[0];
     const double dT = sqrt(UROUND) * fmax(1.0, fabs(T0));
+#pragma unroll 1
     for (int i = lane; i < N; i += 32) tempv[i] = y[i];
     __syncwarp();
     if (lane == 0) tempv[0] = T0 + dT;
     __syncwarp();
     bool ok = devRhs(mm, base, tab, P, tempv, v1, lane, false);
     const double gdT = -gamma / dT;
+#pragma unroll 1
     for (int i = lane; i < N; i += 32) {
         double v = (v1[i] - ftemp[i]) * gdT;
         if (i == 0) v += 1.0;
@@ -430,9 +440,11 @@ struct BdfWarp {
         double a = 0.0;
 #pragma unroll 1
         for (int i = lane; i < N; i += 32) { double x = v[i] * ewt[i]; a += x * x; }
-        return sqrt(warpSum(a) / Nnorm);
+        return dsqrt(ddiv(warpSum(a), Nnorm));
     }
     __device__ double* Z(int j) const { return zn + (size_t)j * N; }
+    // x^p for x >= 0 in the step-size heuristics, through the engine's exp and log
+    __device__ double epow(double x, double p) const { return gbx_exp(p * gbx_log(x, tab), tab); }
     __device__ void setEwt(const double* yv) {
 #pragma unroll 1
         for (int i = lane; i < N; i += 32) ewt[i] = 1.0 / (rtol * fabs(yv[i]) + atol);
@@ -492,59 +504,55 @@ struct BdfWarp {
     }
     __device__ void setCoefficients(BdfScal& S) {
         const int q = S.q;
-#pragma unroll
+#pragma unroll 1
         for (int i = 0; i <= QMAX; i++) S.l[i] = 0.0;
         S.l[0] = S.l[1] = 1.0;
         double xi_inv = 1.0, xistar_inv = 1.0, alpha0 = -1.0, alpha0_hat = -1.0, hsum = S.h;
         if (q > 1) {
-#pragma unroll
-            for (int j = 2; j < QMAX; j++) {
-                if (j < q) {
-                    hsum += S.tau[j - 1];
-                    xi_inv = S.h / hsum;
-                    alpha0 -= 1.0 / j;
-#pragma unroll
-                    for (int i = QMAX; i >= 1; i--)
-                        if (i <= j) S.l[i] += S.l[i - 1] * xi_inv;
-                }
+#pragma unroll 1
+            for (int j = 2; j < q; j++) {
+                hsum += S.tau[j - 1];
+                xi_inv = ddiv(S.h, hsum);
+                alpha0 -= ddiv(1.0, j);
+#pragma unroll 1
+                for (int i = j; i >= 1; i--) S.l[i] += S.l[i - 1] * xi_inv;
             }
-            alpha0 -= 1.0 / q;
+            alpha0 -= ddiv(1.0, q);
             xistar_inv = -S.l[1] - alpha0;
-            hsum += sel(S.tau, q - 1);
-            xi_inv = S.h / hsum;
+            hsum += S.tau[q - 1];
+            xi_inv = ddiv(S.h, hsum);
             alpha0_hat = -S.l[1] - xi_inv;
-#pragma unroll
-            for (int i = QMAX; i >= 1; i--)
-                if (i <= q) S.l[i] += S.l[i - 1] * xistar_inv;
+#pragma unroll 1
+            for (int i = q; i >= 1; i--) S.l[i] += S.l[i - 1] * xistar_inv;
         }
-        const double lq = sel(S.l, q);
+        const double lq = S.l[q];
         double A1 = 1.0 - alpha0_hat + alpha0;
         double A2 = 1.0 + q * A1;
-        S.tq[2] = fabs(A1 / (alpha0 * A2));
-        S.tq[5] = fabs(A2 * xistar_inv / (lq * xi_inv));
+        S.tq[2] = fabs(ddiv(A1, alpha0 * A2));
+        S.tq[5] = fabs(ddiv(A2 * xistar_inv, lq * xi_inv));
         if (S.qwait == 1) {
             if (q > 1) {
-                double C = xistar_inv / lq;
-                double A3 = alpha0 + 1.0 / q;
+                double C = ddiv(xistar_inv, lq);
+                double A3 = alpha0 + ddiv(1.0, q);
                 double A4 = alpha0_hat + xi_inv;
-                double Cpinv = (1.0 - A4 + A3) / A3;
+                double Cpinv = ddiv(1.0 - A4 + A3, A3);
                 S.tq[1] = fabs(C * Cpinv);
             } else {
                 S.tq[1] = 1.0;
             }
-            double hs = hsum + sel(S.tau, q);
-            double xi2 = S.h / hs;
-            double A5 = alpha0 - 1.0 / (q + 1);
+            double hs = hsum + S.tau[q];
+            double xi2 = ddiv(S.h, hs);
+            double A5 = alpha0 - ddiv(1.0, q + 1);
             double A6 = alpha0_hat - xi2;
-            double Cppinv = (1.0 - A6 + A5) / A2;
-            S.tq[3] = fabs(Cppinv / (xi2 * (q + 2) * A5));
+            double Cppinv = ddiv(1.0 - A6 + A5, A2);
+            S.tq[3] = fabs(ddiv(Cppinv, xi2 * (q + 2) * A5));
         }
-        S.tq[4] = NLSCOEF / S.tq[2];
+        S.tq[4] = ddiv(NLSCOEF, S.tq[2]);
     }
 
     template <typename MT, int NS>
     __device__ int newton(MT* M, BdfScal& S, bool callSetup) {
-        const double rl1 = 1.0 / S.l[1];
+        const double rl1 = ddiv(1.0, S.l[1]);
         bool jcur = false;
         for (;;) {
 #pragma unroll 1
@@ -573,7 +581,7 @@ struct BdfWarp {
                 __syncwarp();
                 luSolve<MT, NS>(M, tempv);
                 if (S.gamrat != 1.0) {
-                    double f = 2.0 / (1.0 + S.gamrat);
+                    double f = ddiv(2.0, 1.0 + S.gamrat);
 #pragma unroll 1
                     for (int i = lane; i < N; i += 32) tempv[i] *= f;
                     __syncwarp();
@@ -583,8 +591,8 @@ struct BdfWarp {
                 for (int i = lane; i < N; i += 32) { acor[i] += tempv[i]; y[i] = zn[i] + acor[i]; }
                 __syncwarp();
                 if (!isfinite(del)) { retry = !jcur; break; }
-                if (mm > 0) S.crate = fmax(CRDOWN * S.crate, del / delp);
-                double dcon = del * fmin(1.0, S.crate) / S.tq[4];
+                if (mm > 0) S.crate = fmax(CRDOWN * S.crate, ddiv(del, delp));
+                double dcon = ddiv(del * fmin(1.0, S.crate), S.tq[4]);
                 if (dcon <= 1.0) {
                     S.acnrm = (mm == 0) ? del : wrms(acor);
                     return NLS_OK;
@@ -602,32 +610,27 @@ struct BdfWarp {
     // Nordsieck order change (see the CPU restatement for the polynomial construction)
     // w(x) = x^2 prod_{j=1}^{nf}(x + xi_j): coefficients w[2..nf+2]
     __device__ void orderPoly(const BdfScal& S, int nf, double (&w)[QMAX + 2]) const {
-#pragma unroll
+#pragma unroll 1
         for (int i = 0; i < QMAX + 2; i++) w[i] = 0.0;
         w[2] = 1.0;
         double hsum = 0.0;
-#pragma unroll
-        for (int j = 1; j <= QMAX - 1; j++) {
-            if (j <= nf) {
-                hsum += S.tau[j];
-                const double xi = hsum / S.hscale;
-#pragma unroll
-                for (int i = QMAX + 1; i >= 2; i--)
-                    if (i <= j + 2) w[i] = w[i] * xi + w[i - 1];
-            }
+#pragma unroll 1
+        for (int j = 1; j <= nf; j++) {
+            hsum += S.tau[j];
+            const double xi = ddiv(hsum, S.hscale);
+#pragma unroll 1
+            for (int i = j + 2; i >= 2; i--) w[i] = w[i] * xi + w[i - 1];
         }
     }
     __device__ void decreaseOrder(BdfScal& S) {
         double w[QMAX + 2];
         orderPoly(S, S.q - 2, w);
         const double* zq = Z(S.q);
-#pragma unroll
-        for (int j = 2; j < QMAX; j++) {
-            if (j < S.q) {
-                double* a = Z(j);
 #pragma unroll 1
-                for (int i = lane; i < N; i += 32) a[i] -= w[j] * zq[i];
-            }
+        for (int j = 2; j < S.q; j++) {
+            double* a = Z(j);
+#pragma unroll 1
+            for (int i = lane; i < N; i += 32) a[i] -= w[j] * zq[i];
         }
         __syncwarp();
         double* a = Z(S.q);
@@ -638,18 +641,16 @@ struct BdfWarp {
     __device__ void increaseOrder(BdfScal& S, double lq_prev) {
         double w[QMAX + 2];
         orderPoly(S, S.q - 1, w);
-        const double c = lq_prev / (S.q + 1);
+        const double c = ddiv(lq_prev, S.q + 1);
         const double* sv = Z(QMAX);
 #pragma unroll 1
         for (int i = lane; i < N; i += 32) tempv[i] = c * sv[i];
         __syncwarp();
-#pragma unroll
-        for (int j = 2; j <= QMAX; j++) {
-            if (j <= S.q) {
-                double* a = Z(j);
 #pragma unroll 1
-                for (int i = lane; i < N; i += 32) a[i] += w[j] * tempv[i];
-            }
+        for (int j = 2; j <= S.q; j++) {
+            double* a = Z(j);
+#pragma unroll 1
+            for (int i = lane; i < N; i += 32) a[i] += w[j] * tempv[i];
         }
         double* top = Z(S.q + 1);
 #pragma unroll 1
@@ -675,10 +676,10 @@ struct BdfWarp {
         const WarpAux& A = *aux;
         if (!(A.flags & F_HASPREV) || !(A.flags & F_HASRIGHT)) return A.bs_t;
         double t0 = A.pv_t, t1 = A.bs_t, t2 = A.nx_t;
-        double s0 = (A.bs_v - A.pv_v) / (t1 - t0), s1 = (A.nx_v - A.bs_v) / (t2 - t1);
-        double curv = (s1 - s0) / (t2 - t0);
+        double s0 = ddiv(A.bs_v - A.pv_v, t1 - t0), s1 = ddiv(A.nx_v - A.bs_v, t2 - t1);
+        double curv = ddiv(s1 - s0, t2 - t0);
         if (!(curv < 0)) return t1;
-        double tv = 0.5 * (t0 + t1) - s0 / (2.0 * curv);
+        double tv = 0.5 * (t0 + t1) - ddiv(s0, 2.0 * curv);
         return fmin(fmax(tv, t0), t2);
     }
 
@@ -693,9 +694,9 @@ struct BdfWarp {
         for (int i = lane; i < N; i += 32) hi = fmax(hi, fabs(z1[i]) / (0.1 * fabs(z0[i]) + atol));
         double hub_inv = warpMax(hi);
         double hub = 0.1 * tdist;
-        if (hub * hub_inv > 1.0) hub = 1.0 / hub_inv;
-        if (hub < hlb) return sqrt(hlb * hub);
-        double hg = sqrt(hlb * hub);
+        if (hub * hub_inv > 1.0) hub = ddiv(1.0, hub_inv);
+        if (hub < hlb) return dsqrt(hlb * hub);
+        double hg = dsqrt(hlb * hub);
         double hnew = hg;
         for (int count = 1; count <= 4; count++) {
 #pragma unroll 1
@@ -706,16 +707,16 @@ struct BdfWarp {
             for (int i = lane; i < N; i += 32) tempv[i] = (tempv[i] - z1[i]) / hg;
             __syncwarp();
             double yddnrm = wrms(tempv);
-            hnew = (yddnrm * hub * hub > 2.0) ? sqrt(2.0 / yddnrm) : sqrt(hg * hub);
+            hnew = (yddnrm * hub * hub > 2.0) ? dsqrt(ddiv(2.0, yddnrm)) : dsqrt(hg * hub);
             if (count == 4) break;
-            double hrat = hnew / hg;
+            double hrat = ddiv(hnew, hg);
             if (hrat > 0.5 && hrat < 2.0) break;
             if (count > 1 && hrat > 2.0) { hnew = hg; break; }
             hg = hnew;
         }
         double h0 = 0.5 * hnew;
         h0 = fmin(fmax(h0, hlb), hub);
-        if (hmaxInv > 0) h0 = fmin(h0, 1.0 / hmaxInv);
+        if (hmaxInv > 0) h0 = fmin(h0, ddiv(1.0, hmaxInv));
         return h0;
     }
 
@@ -729,7 +730,7 @@ struct BdfWarp {
             return;
         }
         const int L = S.L;
-        double etaq = 1.0 / (pow(BIAS2 * dsm, 1.0 / L) + ADDON);
+        double etaq = ddiv(1.0, epow(BIAS2 * dsm, ddiv(1.0, L)) + ADDON);
         if (S.qwait != 0) {
             S.eta = etaq;
             S.qprime = S.q;
@@ -738,21 +739,20 @@ struct BdfWarp {
             double etaqm1 = 0.0, etaqp1 = 0.0;
             if (S.q > 1) {
                 double ddn = wrms(Z(S.q)) * S.tq[1];
-                etaqm1 = 1.0 / (pow(BIAS1 * ddn, 1.0 / S.q) + ADDON);
+                etaqm1 = ddiv(1.0, epow(BIAS1 * ddn, ddiv(1.0, S.q)) + ADDON);
             }
             if (S.q != maxOrder && S.saved_tq5 != 0.0) {
-                const double hr = S.h / S.tau[2];
+                const double hr = ddiv(S.h, S.tau[2]);
                 double hp = hr;
-#pragma unroll
-                for (int i = 2; i <= QMAX + 1; i++)
-                    if (i <= L) hp *= hr;
-                double cquot = (S.tq[5] / S.saved_tq5) * hp;
+#pragma unroll 1
+                for (int i = 2; i <= L; i++) hp *= hr;
+                double cquot = ddiv(S.tq[5], S.saved_tq5) * hp;
                 const double* sv = Z(QMAX);
 #pragma unroll 1
                 for (int i = lane; i < N; i += 32) tempv[i] = acor[i] - cquot * sv[i];
                 __syncwarp();
                 double dup = wrms(tempv) * S.tq[3];
-                etaqp1 = 1.0 / (pow(BIAS3 * dup, 1.0 / (L + 1)) + ADDON);
+                etaqp1 = ddiv(1.0, epow(BIAS3 * dup, ddiv(1.0, L + 1)) + ADDON);
             }
             double etam = fmax(etaqm1, fmax(etaq, etaqp1));
             if (etam < ETA_FIX_MAX) {
@@ -792,14 +792,14 @@ struct BdfWarp {
         bool prevConvFail = false;
         if (S.nst > 0) {
             if (S.qprime != S.q) {
-                if (S.qprime == S.q + 1) increaseOrder(S, sel(S.l, S.q));
+                if (S.qprime == S.q + 1) increaseOrder(S, S.l[S.q]);
                 else decreaseOrder(S);
                 S.q = S.qprime;
                 S.L = S.q + 1;
                 S.qwait = S.L;
             }
             if (S.hprime != S.h) {
-                S.eta = S.hprime / S.h;
+                S.eta = ddiv(S.hprime, S.h);
                 rescale(S);
             }
         }
@@ -807,9 +807,9 @@ struct BdfWarp {
         for (;;) {
             predict(S);
             setCoefficients(S);
-            S.gamma = S.h / S.l[1];
+            S.gamma = ddiv(S.h, S.l[1]);
             if (S.nst == 0) S.gammap = S.gamma;
-            S.gamrat = (S.nst > 0) ? S.gamma / S.gammap : 1.0;
+            S.gamrat = (S.nst > 0) ? ddiv(S.gamma, S.gammap) : 1.0;
             bool callSetup = (S.nst == 0) || prevConvFail || (S.nst >= S.nstlp + MSBP) ||
                              (fabs(S.gamrat - 1.0) > DGMAX) || !S.haveLU;
             int nls = newton<MT, NS>(M, S, callSetup);
@@ -833,7 +833,7 @@ struct BdfWarp {
                 if (nef == MXNEF) return ST_ERR_FAIL;
                 S.etamax = 1.0;
                 if (nef <= MXNEF1) {
-                    S.eta = 1.0 / (pow(BIAS2 * dsm, 1.0 / S.L) + ADDON);
+                    S.eta = ddiv(1.0, epow(BIAS2 * dsm, ddiv(1.0, S.L)) + ADDON);
                     S.eta = fmax(ETA_MIN_EF, S.eta);
                     if (nef >= SMALL_NEF) S.eta = fmin(S.eta, ETA_MAX_EF);
                     rescale(S);
@@ -882,7 +882,7 @@ struct BdfWarp {
                 __syncwarp();
                 S.saved_tq5 = S.tq[5];
             }
-            recordSample(S.tn, zn[N] / S.h);
+            recordSample(S.tn, ddiv(zn[N], S.h));
             prepareNext(S, dsm);
             return ST_OK;
         }
@@ -981,7 +981,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
                 S.eta = 1.0;
                 S.q = S.qprime = 1; S.L = 2; S.qwait = 2; S.etamax = ETA_MAX_FIRST;
                 S.tau[1] = h0;
-                W.recordSample(S.tn, z1[0] / h0);
+                W.recordSample(S.tn, ddiv(z1[0], h0));
             } else {
                 S.h = S.hscale = S.hprime = 0.0;
                 S.q = S.qprime = 1; S.L = 2; S.qwait = 2; S.etamax = ETA_MAX_FIRST; S.eta = 1.0;
@@ -1023,7 +1023,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
             count++;
         }
         // output: interpolate to tout (or the last state on failure)
-        const double sfac = (status == ST_OK && S.h != 0.0) ? (p.tout - S.tn) / S.h : 0.0;
+        const double sfac = (status == ST_OK && S.h != 0.0) ? ddiv(p.tout - S.tn, S.h) : 0.0;
 #pragma unroll 1
         for (int i = lane; i < N; i += 32) {
             double v = W.zn[(size_t)S.q * N + i];

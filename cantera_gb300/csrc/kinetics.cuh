@@ -248,6 +248,7 @@ __device__ __forceinline__ void warpState(const DevMech& m, double T, double P, 
     st.lnPP = lnP - lnPref;
     st.lnC0 = lnP - lnRT;
     __syncwarp();
+#pragma unroll 1
     for (int k = lane; k < m.K; k += 32) s.c[k] *= st.rho;   // c_k = rho Y_k / W_k
 }
 
@@ -294,8 +295,10 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
         s.pw[lane] = v;
     }
     __syncwarp();
+#pragma unroll 1
     for (int t = lane; t < m.NTB; t += 32) {
         double sum = 0.0;
+#pragma unroll 1
         for (int q = m.tbPtr[t]; q < m.tbPtr[t + 1]; q++) sum += m.tbE[q] * s.c[m.tbK[q]];
         s.Mtb[t] = m.tbDef[t] * st.ctot + sum;
     }
@@ -382,15 +385,19 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
     }
     __syncwarp();
     // wdot_k = sum_i nu_ki rop_i: balanced tasks, then a fixed-order sum per species
+#pragma unroll 1
     for (int q = m.laneTaskPtr[lane]; q < m.laneTaskPtr[lane + 1]; q++) {
         const int t = m.laneTasks[q];
         double w = 0.0;
+#pragma unroll 1
         for (int e = m.taskPtr[t]; e < m.taskPtr[t + 1]; e++) w = fma(m.spNu[e], s.rop[m.spRxn[e]], w);
         s.part[t] = w;
     }
     __syncwarp();
+#pragma unroll 1
     for (int k = lane; k < m.K; k += 32) {
         double w = 0.0;
+#pragma unroll 1
         for (int q = m.spTaskPtr[k]; q < m.spTaskPtr[k + 1]; q++) w += s.part[m.spTasks[q]];
         s.wdot[k] = w;
     }
@@ -429,8 +436,10 @@ __device__ __noinline__ void warpJacC(const DevMech& m, const KinScratch& s, MT*
 // g_k = sum over third-body reactions i with default efficiency d_i of S_net[k][i]*d_i*Q_i:
 // the part of d(wdot_k)/dc_j that is the same for every column j.
 __device__ __forceinline__ void warpDenseG(const DevMech& m, const KinScratch& s, double* gout, int lane) {
+#pragma unroll 1
     for (int k = lane; k < m.K; k += 32) {
         double g = 0.0;
+#pragma unroll 1
         for (int q = m.gsPtr[k]; q < m.gsPtr[k + 1]; q++) g += m.gsCoef[q] * s.Qtb[m.gsTb[q]];
         gout[k] = g;
     }
