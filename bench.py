@@ -29,7 +29,7 @@ METRIC = "GRI-30 reactors advanced/s on 1 GB300: FP64 BDF vs FP32-LU and NN+fall
 WL = dict(mechanism="gri30.yaml", phase="gri30", n=65536, t_end=1e-2, rtol=1e-8, atol=1e-15,
           T0=(700.0, 1800.0), P_atm=(1.0, 40.0), phi=(0.5, 1.5), fuel="CH4:1",
           oxidizer="O2:1, N2:3.76", seed=20261203 + 2)
-CPU_SAMPLE = 2048         # reactors in the bounded CPU sample (a seeded subset of the workload)
+CPU_SAMPLE = 8192         # reactors in the bounded CPU sample (a seeded subset of the workload)
 
 
 def workload_arrays(n, seed, eqr):
