@@ -83,6 +83,18 @@ def library():
         "gb_net_solver_stats": (I32, [I32, P]),
         "gb_net_ignition_times": (I32, [I32, P]),
         "gb_net_launch_info": (I32, [I32, P]),
+        "gb_reactor_rhs": (I32, [I32, I32, P, P, P, P, P, I32]),
+        "gb_mech_n_elements": (I32, [I32]),
+        "gb_mech_element_mass": (I32, [I32, I32, P]),
+        "gb_nn_gemm": (I32, [I32, I32, I32, P, ctypes.c_int64, ctypes.c_int64, P, ctypes.c_int64, ctypes.c_int64,
+                             P, ctypes.c_int64, ctypes.c_int64, I32, ctypes.c_float, P, I32, P, ctypes.c_int64,
+                             ctypes.c_int64, I32]),
+        "gb_nn_adam": (I32, [I32, P, P, P, P, P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, I32]),
+        "gb_nn_colsum": (I32, [I32, I32, P, I32, ctypes.c_float, P]),
+        "gb_nn_mse": (I32, [I32, I32, I32, P, P, P, P]),
+        "gb_nn_features": (I32, [I32, I32, P, P, P, P, P, P, I32]),
+        "gb_nn_apply": (I32, [I32, I32, P, I32, P, P, P, P, D, P, P, P, P]),
+        "gb_nn_gate": (I32, [I32, I32, D, P, P, P, P, P, P, P, P, P, D, D, D, D, P, P]),
         "gb_get_error": (I32, [I32, ctypes.c_char_p]),
         "gb_mech_structure": (I32, [I32, I32, P]),
         "gb_mech_equivalence_ratio": (I32, [I32, D, P, P, I32, P]),

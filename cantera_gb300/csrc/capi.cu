@@ -21,6 +21,7 @@
 #include "devmech.h"
 #include "kernels.h"
 #include "mechanism.h"
+#include "surrogate.h"
 
 using namespace gbchem;
 
@@ -982,6 +983,156 @@ int32_t gb_reactors_advance_noalloc(int32_t h, int32_t n, double t_end, double* 
         p.ld = ld; p.warpDoubles = warpDoubles;
         ck(launchBdf(p, blocks, wpb, fp32, s), "integrator launch");
         ck(cudaStreamSynchronize(s), "integrator");
+        return 0;
+    });
+}
+
+/* ---- batched reactor right-hand side ---------------------------------------------- */
+int32_t gb_reactor_rhs(int32_t h, int32_t n, const double* T, const double* P, const double* Y, double* dTdt,
+                       double* dYdt, int32_t flags) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        if (n < 0) throw std::runtime_error("negative number of states");
+        if (n == 0) return 0;
+        if (!T || !P || !Y || !dTdt || !dYdt) throw std::runtime_error("null array argument");
+        const bool dev = (flags & GB_DEVICE_POINTERS) != 0;
+        const int K = e.m.K;
+        cudaStream_t s = e.stream;
+        const double* dT = stage(T, n, e.dT, dev, s);
+        const double* dP = stage(P, n, e.dP, dev, s);
+        const double* dY = stage(Y, (size_t)K * n, e.dY, dev, s);
+        double* oT = dTdt;
+        double* oY = dYdt;
+        if (!dev) {
+            e.dW.ensure((size_t)(K + 1) * n * 8);
+            oY = e.dW.as<double>();
+            oT = oY + (size_t)K * n;
+        }
+        RhsParams p{};
+        p.m = e.dm; p.n = n; p.T = dT; p.P = dP; p.Y = dY; p.dTdt = oT; p.dYdt = oY;
+        p.warpDoubles = rhsWarpDoubles(e.dm);
+        const int wpb = std::max(1, std::min(8, maxSmemPerBlock() / (p.warpDoubles * 8)));
+        const int blocksPerSm = std::max(1, (228 * 1024) / (p.warpDoubles * 8 * wpb + 1024));
+        const int blocks = std::max(1, std::min(e.smCount * blocksPerSm, (n + wpb - 1) / wpb));
+        ck(launchReactorRhs(p, blocks, wpb, s), "reactor rhs launch");
+        if (!dev) {
+            ck(cudaMemcpyAsync(dYdt, oY, (size_t)K * n * 8, cudaMemcpyDeviceToHost, s), "copy dYdt");
+            ck(cudaMemcpyAsync(dTdt, oT, (size_t)n * 8, cudaMemcpyDeviceToHost, s), "copy dTdt");
+        }
+        ck(cudaStreamSynchronize(s), "reactor rhs");
+        return 0;
+    });
+}
+
+int32_t gb_mech_n_elements(int32_t h) {
+    return guarded([&]() -> int32_t { return (int32_t)mech(h).m.elementNames.size(); });
+}
+
+int32_t gb_mech_element_mass(int32_t h, int32_t buflen, double* out) {
+    return guarded([&]() -> int32_t {
+        const Mechanism& m = mech(h).m;
+        const int E = (int)m.elementNames.size(), K = m.K;
+        if (!out || buflen < E * K) throw std::runtime_error("element mass buffer too small");
+        for (int e = 0; e < E; e++)
+            for (int k = 0; k < K; k++) out[(size_t)e * K + k] = m.atoms[(size_t)k * E + e] * m.elementWeights[e] / m.mw[k];
+        return 0;
+    });
+}
+
+/* ---- learned surrogate: tensor-core MLP operations (device pointers) ---------------- */
+int32_t gb_nn_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, int64_t sak, const void* B,
+                   int64_t sbn, int64_t sbk, void* C, int64_t scm, int64_t scn, int32_t c_float, float alpha,
+                   const float* bias, int32_t act, void* Z, int64_t szm, int64_t szn, int32_t z_float) {
+    return guarded([&]() -> int32_t {
+        if (M <= 0 || N <= 0 || K <= 0 || M % 128 || N % 128 || K % 32)
+            throw std::runtime_error("gemm: M and N must be positive multiples of 128, K of 32");
+        if (!A || !B || !C) throw std::runtime_error("gemm: null operand");
+        if (!((sak == 1 && sam % 8 == 0) || (sam == 1 && sak % 8 == 0)))
+            throw std::runtime_error("gemm: A needs a unit stride and the other a multiple of 8");
+        if (!((sbk == 1 && sbn % 8 == 0) || (sbn == 1 && sbk % 8 == 0)))
+            throw std::runtime_error("gemm: B needs a unit stride and the other a multiple of 8");
+        if (((uintptr_t)A & 15) || ((uintptr_t)B & 15)) throw std::runtime_error("gemm: A and B must be 16-byte aligned");
+        if (act < 0 || act > 2 || (act != 0 && !Z)) throw std::runtime_error("gemm: bad activation arguments");
+        GemmArgs g{};
+        g.M = M; g.N = N; g.K = K;
+        g.A = (const __nv_bfloat16*)A; g.sam = sam; g.sak = sak;
+        g.B = (const __nv_bfloat16*)B; g.sbn = sbn; g.sbk = sbk;
+        g.C = C; g.scm = scm; g.scn = scn; g.cFloat = c_float;
+        g.alpha = alpha; g.bias = bias; g.act = act; g.Z = Z; g.szm = szm; g.szn = szn; g.zFloat = z_float;
+        ck(launchGemm(g, 0), "gemm launch");
+        ck(cudaStreamSynchronize(0), "gemm");
+        return 0;
+    });
+}
+
+int32_t gb_nn_adam(int32_t n, float* w, float* m, float* v, const float* g, void* wb, float lr, float beta1,
+                   float beta2, float eps, int32_t step) {
+    return guarded([&]() -> int32_t {
+        if (n < 0 || !w || !m || !v || !g || !wb || step < 1) throw std::runtime_error("adam: bad arguments");
+        ck(launchAdam(n, w, m, v, g, (__nv_bfloat16*)wb, lr, beta1, beta2, eps, step, 0), "adam launch");
+        ck(cudaStreamSynchronize(0), "adam");
+        return 0;
+    });
+}
+
+int32_t gb_nn_colsum(int32_t M, int32_t N, const void* X, int32_t ld, float alpha, float* out) {
+    return guarded([&]() -> int32_t {
+        if (M < 0 || N < 0 || ld < N || !X || !out) throw std::runtime_error("colsum: bad arguments");
+        ck(launchColSum(M, N, (const __nv_bfloat16*)X, ld, alpha, out, 0), "colsum launch");
+        ck(cudaStreamSynchronize(0), "colsum");
+        return 0;
+    });
+}
+
+int32_t gb_nn_mse(int32_t M, int32_t nout, int32_t ld, const float* P, const float* Y, void* dY, float* loss) {
+    return guarded([&]() -> int32_t {
+        if (M < 0 || nout < 0 || ld < nout || !P || !Y || !dY || !loss) throw std::runtime_error("mse: bad arguments");
+        ck(launchMseGrad(M, nout, ld, P, Y, (__nv_bfloat16*)dY, loss, 0), "mse launch");
+        ck(cudaStreamSynchronize(0), "mse");
+        return 0;
+    });
+}
+
+int32_t gb_nn_features(int32_t h, int32_t n, const double* T, const double* P, const double* Y, const float* mu,
+                       const float* sd, void* X, int32_t ldx) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        if (n < 0 || ldx < e.m.K + 2 || !T || !P || !Y || !mu || !sd || !X) throw std::runtime_error("features: bad arguments");
+        ck(launchFeatures(n, e.m.K, T, P, Y, mu, sd, (__nv_bfloat16*)X, ldx, 0), "features launch");
+        ck(cudaStreamSynchronize(0), "features");
+        return 0;
+    });
+}
+
+int32_t gb_nn_apply(int32_t h, int32_t n, const float* O, int32_t ldo, const float* mu, const float* sd,
+                    const double* T, const double* Y, double dt, const double* f0T, const double* f0Y, double* Tn,
+                    double* Yn) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        if (n < 0 || ldo < e.m.K + 1 || !O || !mu || !sd || !T || !Y || !Tn || !Yn) throw std::runtime_error("apply: bad arguments");
+        if ((f0T == nullptr) != (f0Y == nullptr)) throw std::runtime_error("apply: give both f0T and f0Y or neither");
+        ck(launchApplyDelta(n, e.m.K, O, ldo, mu, sd, T, Y, dt, f0T, f0Y, Tn, Yn, 0), "apply launch");
+        ck(cudaStreamSynchronize(0), "apply");
+        return 0;
+    });
+}
+
+int32_t gb_nn_gate(int32_t h, int32_t n, double dt, const double* T0, const double* Y0, const double* T1,
+                   const double* Y1, const double* f0T, const double* f0Y, const double* f1T, const double* f1Y,
+                   const double* elem_mass, double tol_elem, double tol_h, double tol_trap_t, double tol_trap_y,
+                   int32_t* accept, double* score) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        if (n < 0 || !T0 || !Y0 || !T1 || !Y1 || !f0T || !f0Y || !f1T || !f1Y || !elem_mass || !accept || !score)
+            throw std::runtime_error("gate: bad arguments");
+        GateArgs a{};
+        a.n = n; a.K = e.m.K; a.E = (int)e.m.elementNames.size(); a.dt = dt;
+        a.T0 = T0; a.Y0 = Y0; a.T1 = T1; a.Y1 = Y1; a.f0T = f0T; a.f0Y = f0Y; a.f1T = f1T; a.f1Y = f1Y;
+        a.elemW = elem_mass; a.nasa = e.dm.nasa; a.Rgas = e.dm.Rgas; a.rmw = e.dm.rmw;
+        a.tolElem = tol_elem; a.tolH = tol_h; a.tolTrapT = tol_trap_t; a.tolTrapY = tol_trap_y;
+        a.accept = accept; a.score = score;
+        ck(launchGate(a, 0), "gate launch");
+        ck(cudaStreamSynchronize(0), "gate");
         return 0;
     });
 }

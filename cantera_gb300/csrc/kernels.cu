@@ -1061,6 +1061,48 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     }
 }
 
+// =============================================================================
+// Batched reactor right-hand side: one warp per state (grid-stride over states)
+// =============================================================================
+__global__ void __launch_bounds__(256, 1) k_reactor_rhs(RhsParams p) {
+    extern __shared__ __align__(128) double smem[];
+    __shared__ uint64_t s_tab[kGbxTableWords];
+    __shared__ DevMech s_mech;
+    loadMech(p.m, s_mech, (char*)smem, 0);
+    gbx_load_table(s_tab);
+    const DevMech& m = s_mech;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    double* base = smem + (size_t)warp * p.warpDoubles;
+    double* z = base + kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
+    double* zd = z + m.N;
+    for (int r = blockIdx.x * wpb + warp; r < p.n; r += gridDim.x * wpb) {
+        if (lane == 0) z[0] = p.T[r];
+#pragma unroll 1
+        for (int k = lane; k < m.K; k += 32) z[1 + k] = p.Y[(size_t)k * p.n + r];
+        __syncwarp();
+        devRhs(m, base, s_tab, p.P[r], z, zd, lane, false);
+        if (lane == 0) p.dTdt[r] = zd[0];
+#pragma unroll 1
+        for (int k = lane; k < m.K; k += 32) p.dYdt[(size_t)k * p.n + r] = zd[1 + k];
+        __syncwarp();
+    }
+}
+
+int rhsWarpDoubles(const DevMech& m) {
+    const int tot = kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT) + 2 * m.N;
+    return (tot + 1) & ~1;
+}
+
+cudaError_t launchReactorRhs(const RhsParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
+    size_t smem = (size_t)p.warpDoubles * 8 * warpsPerBlock;
+    cudaError_t e = cudaFuncSetAttribute(k_reactor_rhs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_reactor_rhs<<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
 template <typename MT, int NS>
 cudaError_t launchBdfT(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
     size_t smem = (size_t)p.mechSmem + (size_t)p.warpDoubles * 8 * warpsPerBlock;

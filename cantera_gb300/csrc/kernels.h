@@ -20,6 +20,20 @@ struct RatesParams {
     int mechSmem;         // bytes of the mechanism arena copied into shared memory
 };
 
+// batched reactor right-hand side (IdealGasConstPressureReactor::eval over [T, Y])
+struct RhsParams {
+    DevMech m;
+    int n;
+    const double* T;
+    const double* P;
+    const double* Y;      // [K][n]
+    double* dTdt;         // [n]
+    double* dYdt;         // [K][n]
+    int warpDoubles;
+};
+int rhsWarpDoubles(const DevMech& m);
+cudaError_t launchReactorRhs(const RhsParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
+
 struct BdfParams {
     DevMech m;
     int n;

@@ -142,6 +142,50 @@ int32_t gb_reactors_advance_noalloc(int32_t mech, int32_t n, double t_end, doubl
                                     double* Y, int32_t* status, const gb_net_options* opts,
                                     void* stream);
 
+/* ---- batched reactor right-hand side -------------------------------------------------
+ * IdealGasConstPressureReactor::eval (src/zeroD/IdealGasConstPressureReactor.cpp:53-110)
+ * over n states: dT/dt [n] and dY/dt [K][n] of the state [T, Y] at pressure P. */
+int32_t gb_reactor_rhs(int32_t mech, int32_t n, const double* T, const double* P, const double* Y,
+                       double* dTdt, double* dYdt, int32_t flags);
+int32_t gb_mech_n_elements(int32_t mech);
+/* out[e*K + k] = atoms of element e in species k * W_e / W_k (element mass per species mass). */
+int32_t gb_mech_element_mass(int32_t mech, int32_t buflen, double* out);
+
+/* ---- learned surrogate (no counterpart in the reference) -------------------------------
+ * Device-pointer operations of the MLP surrogate, each on the default stream and finished
+ * on return.  gb_nn_gemm: C(m,n) = epilogue(alpha * sum_k A(m,k) B(n,k)) with BF16 A, B on
+ * the tensor cores, FP32 accumulation; element (i,j) of X at X[i*s_i + j*s_j]; M, N multiples
+ * of 128, K of 32; epilogue: + bias[n] (float, may be NULL), act 1 = GELU (tanh form) with the
+ * pre-activation written to Z, act 2 = multiply by GELU'(Z); C and Z float (flag 1) or bf16. */
+int32_t gb_nn_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, int64_t sak,
+                   const void* B, int64_t sbn, int64_t sbk, void* C, int64_t scm, int64_t scn,
+                   int32_t c_float, float alpha, const float* bias, int32_t act, void* Z, int64_t szm,
+                   int64_t szn, int32_t z_float);
+/* Adam step on FP32 master weights w with moments m, v and gradient g; writes the bf16 copy. */
+int32_t gb_nn_adam(int32_t n, float* w, float* m, float* v, const float* g, void* wb, float lr,
+                   float beta1, float beta2, float eps, int32_t step);
+/* out[j] = alpha * sum_i X[i*ld + j], j < N, X bf16 (bias gradients). */
+int32_t gb_nn_colsum(int32_t M, int32_t N, const void* X, int32_t ld, float alpha, float* out);
+/* Mean-squared-error gradient (bf16 dY [M][ld], zero beyond nout) and loss (added to *loss). */
+int32_t gb_nn_mse(int32_t M, int32_t nout, int32_t ld, const float* P, const float* Y, void* dY, float* loss);
+/* Network inputs (bf16 [n][ldx]): normalised T, ln P and Box-Cox(Y_k, lambda 0.1). */
+int32_t gb_nn_features(int32_t mech, int32_t n, const double* T, const double* P, const double* Y,
+                       const float* mu, const float* sd, void* X, int32_t ldx);
+/* New state from the normalised network output O [n][ldo] (component k < K for Y_k, K for
+ * T): v = O sd + mu; x1 = x0 + v, or, given the right-hand sides f0T, f0Y at the start,
+ * x1 = x0 + dt f0 + v (dt |f0| + floor) with floor 1e-12 (Y) and 1e-6 K (T). */
+int32_t gb_nn_apply(int32_t mech, int32_t n, const float* O, int32_t ldo, const float* mu, const float* sd,
+                    const double* T, const double* Y, double dt, const double* f0T, const double* f0Y,
+                    double* Tn, double* Yn);
+/* Physics gate of a predicted step x0 -> x1 over dt: element mass fractions conserved to
+ * tol_elem, enthalpy to tol_h (relative to cp T), and the trapezoidal rule with the reactor
+ * right-hand sides f0, f1 satisfied to tol_trap_t (T, relative) and tol_trap_y (Y, absolute).
+ * accept[r] = 1 when every check passes; score[r] = the largest normalised violation. */
+int32_t gb_nn_gate(int32_t mech, int32_t n, double dt, const double* T0, const double* Y0,
+                   const double* T1, const double* Y1, const double* f0T, const double* f0Y,
+                   const double* f1T, const double* f1Y, const double* elem_mass, double tol_elem,
+                   double tol_h, double tol_trap_t, double tol_trap_y, int32_t* accept, double* score);
+
 /* ---- measurement helpers (no counterpart in the reference) ---------------------------
  * Structure counts of a mechanism for the benchmark's FP64 operation model:
  * counts[0..11] = K, R, reversible, falloff, Troe, three-body reactions, third-body
