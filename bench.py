@@ -158,6 +158,75 @@ def read_traffic():
     return None
 
 
+SUR = dict(dt=1e-6, train_reactors=16384, held_reactors=65536, hidden=512, layers=4, epochs=8, batch=4096,
+           times=(0.0, 1e-5, 3e-5, 1e-4, 3e-4, 1e-3, 2e-3, 4e-3, 6e-3, 8e-3, 1e-2),
+           held_times=(0.0, 2e-5, 5e-5, 2e-4, 5e-4, 1e-3, 1.5e-3, 2.5e-3, 3e-3, 3.5e-3, 4.5e-3, 5e-3, 6.5e-3, 7e-3,
+                       9e-3, 1e-2))
+
+
+def surrogate_leg(sol, dev, torch):
+    """The learned arm on the same workload: an MLP trained on integrator pairs (states
+    along trajectories of the workload's reactors, each advanced by dt = 1e-6 s), then one
+    dt step for 1,048,576 held-out states (65,536 other reactors at 16 times) by the FP64 BDF
+    integrator alone and by the surrogate with its gate and BDF fallback."""
+    import cantera_gb300 as gb
+    from cantera_gb300.surrogate import Surrogate, generate_pairs, trajectory_states
+    K = sol.n_species
+    eqr = lambda p: sol.equivalence_ratio_mass_fractions(p, WL["fuel"], WL["oxidizer"])
+
+    def initial(n, seed):
+        T0, P, Y0 = workload_arrays(n, seed, eqr)
+        d = lambda a: torch.tensor(a, device=dev)
+        return d(T0), d(P), d(np.ascontiguousarray(Y0.T))
+
+    t0 = time.perf_counter()
+    Ts, Ps, Ys, T1, Y1 = generate_pairs(sol, *initial(SUR["train_reactors"], WL["seed"] + 4), SUR["times"], SUR["dt"],
+                                        WL["rtol"], WL["atol"])
+    t_pairs = time.perf_counter() - t0
+    sur = Surrogate(sol, dt=SUR["dt"], hidden=SUR["hidden"], layers=SUR["layers"], seed=0, device=str(dev))
+    sur.fit_normalization(Ts, Ps, Ys, T1, Y1)
+    X = sur.features(Ts, Ps, Ys)
+    Yt = sur.targets(Ts, Ps, Ys, T1, Y1)
+    t0 = time.perf_counter()
+    losses = sur.train(X, Yt, Ts.shape[0], epochs=SUR["epochs"], batch=SUR["batch"], lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del X, Yt
+    Hs, Hp, Hy = trajectory_states(sol, *initial(SUR["held_reactors"], WL["seed"] + 5), SUR["held_times"],
+                                   WL["rtol"], WL["atol"])
+    n = Hs.shape[0]
+    # the FP64 BDF step alone (the reference result and the method without the network)
+    net = gb.ReactorNet(sol, Hs, Hp, Hy, rtol=WL["rtol"], atol=WL["atol"], use_graph=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net.advance(SUR["dt"])
+    Tb, Yb = torch.empty_like(Hs), torch.empty_like(Hy)
+    net.get_state(Tb, Yb)
+    torch.cuda.synchronize()
+    t_bdf = time.perf_counter() - t0
+    del net
+    # surrogate + gate + fallback
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Tsur, Ysur, acc = sur.advance(Hs, Hp, Hy, rtol=WL["rtol"], atol=WL["atol"])
+    torch.cuda.synchronize()
+    t_sur = time.perf_counter() - t0
+    rel_T = ((Tsur - Tb).abs() / Tb)
+    major = Yb > 1e-2
+    rel_Y = (Ysur - Yb).abs()[major] / Yb[major]
+    gflop = 2.0 * n * sum(a * b for a, b in zip(sur.dims[:-1], sur.dims[1:])) / 1e9
+    return {"dt": SUR["dt"], "states": n, "unit": "reactor-steps/s",
+            "bdf_only": n / t_bdf, "surrogate_with_fallback": n / t_sur, "speedup": t_bdf / t_sur,
+            "accepted_fraction": float(acc.float().mean().item()),
+            "max_rel_err_T": float(rel_T.max().item()), "max_rel_err_major_species": float(rel_Y.max().item()),
+            "network": "%d -> %d x %d (GELU) -> %d, bf16 weights, fp32 accumulation" % (K + 2, SUR["hidden"], SUR["layers"], K + 1),
+            "training": {"pairs": int(Ts.shape[0]), "epochs": SUR["epochs"], "loss_first": losses[0],
+                         "loss_last": losses[-1], "seconds": t_train, "pair_generation_seconds": t_pairs},
+            "inference_gflop": gflop,
+            "data": "pairs from %d workload reactors at %d trajectory times; held-out %d reactors at %d times"
+                    % (SUR["train_reactors"], len(SUR["times"]), SUR["held_reactors"], len(SUR["held_times"]))}
+
+
 def cpu_baseline(T0, P, Y0, idx, threads, kind="port"):
     """The CPU restatement of the reference path on this host's cores: the reference's
     ReactorNet settings (difference-quotient Jacobian kept between setups) on a bounded,
@@ -212,6 +281,7 @@ def main():
     ap.add_argument("--n", type=int, default=WL["n"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--matrix-placement", type=int, default=0, choices=[0, 1, 2],
                     help="Newton matrix: 0 automatic, 1 shared memory, 2 global slot per warp")
     args = ap.parse_args()
@@ -340,6 +410,11 @@ def main():
                                         "ms_per_step": r32["ms"] / r32["steps"],
                                         "solver_stats_mean": r32["stats"], "failed_reactors": r32["failed"],
                                         "clocks": r32["clocks"]}}
+    if not args.no_surrogate and ws == 1:
+        try:
+            line.setdefault("variants", {})["surrogate"] = surrogate_leg(sol, dev, torch)
+        except Exception as e:   # the learned arm must not cost the FP64 line
+            line.setdefault("variants", {})["surrogate"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if not args.no_cpu_baseline and ws == 1:
         idx = cpu_sample_indices(n_all, CPU_SAMPLE, WL["seed"])
         cb, (To, Yo, sto, tio) = cpu_baseline(T0, P, Y0, idx, os.cpu_count())

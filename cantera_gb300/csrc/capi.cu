@@ -1052,7 +1052,7 @@ int32_t gb_nn_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, 
         if (!((sbk == 1 && sbn % 8 == 0) || (sbn == 1 && sbk % 8 == 0)))
             throw std::runtime_error("gemm: B needs a unit stride and the other a multiple of 8");
         if (((uintptr_t)A & 15) || ((uintptr_t)B & 15)) throw std::runtime_error("gemm: A and B must be 16-byte aligned");
-        if (act < 0 || act > 2 || (act != 0 && !Z)) throw std::runtime_error("gemm: bad activation arguments");
+        if (act < 0 || act > 2 || (act == 2 && !Z)) throw std::runtime_error("gemm: bad activation arguments");
         GemmArgs g{};
         g.M = M; g.N = N; g.K = K;
         g.A = (const __nv_bfloat16*)A; g.sam = sam; g.sak = sak;

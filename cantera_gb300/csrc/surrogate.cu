@@ -120,9 +120,11 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm(GemmArgs g) {
                 float v = g.alpha * acc[mi][ni][c];
                 if (g.bias) v += g.bias[n];
                 if (g.act == 1) {
-                    const long long zi = (long long)m * g.szm + (long long)n * g.szn;
-                    if (g.zFloat) ((float*)g.Z)[zi] = v;
-                    else ((__nv_bfloat16*)g.Z)[zi] = __float2bfloat16(v);
+                    if (g.Z) {   // training keeps the pre-activation for the backward pass
+                        const long long zi = (long long)m * g.szm + (long long)n * g.szn;
+                        if (g.zFloat) ((float*)g.Z)[zi] = v;
+                        else ((__nv_bfloat16*)g.Z)[zi] = __float2bfloat16(v);
+                    }
                     v = gelu(v);
                 } else if (g.act == 2) {
                     const long long zi = (long long)m * g.szm + (long long)n * g.szn;

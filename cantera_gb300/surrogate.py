@@ -128,7 +128,7 @@ class Surrogate:
         for l in range(nl):
             n_out, n_in = self.dims[l + 1], self.dims[l]
             if l < nl - 1:
-                Z = torch.empty(M, n_out, device=self.dev)
+                Z = torch.empty(M, n_out, device=self.dev) if keep else None
                 C = torch.empty(M, n_out, dtype=torch.bfloat16, device=self.dev)
                 self._gemm(M, n_out, n_in, A, n_in, 1, self.Wb[l], n_in, 1, C, n_out, 1, 0, 1.0, self.b[l], 1,
                            Z, n_out, 1, 1)
@@ -262,13 +262,10 @@ class Surrogate:
         return T1, Y1, acc
 
 
-def generate_pairs(solution, T0, P, Y0, times, dt, rtol=1e-8, atol=1e-15):
-    """Training pairs along trajectories: the states of reactors started at (T0, P, Y0) at
-    each time in `times`, and the same states advanced by dt.  Device arrays, species-major
-    Y; returns Ts, Ps, Ys (inputs) and T1, Y1 (after dt), n_reactors * len(times) columns."""
+def trajectory_states(solution, T0, P, Y0, times, rtol=1e-8, atol=1e-15):
+    """States of reactors started at (T0, P, Y0) at each time in `times` (device arrays,
+    species-major Y): Ts, Ps, Ys with n_reactors * len(times) columns."""
     import torch
-    n = T0.shape[0]
-    K = solution.n_species
     net = ReactorNet(solution, T0, P, Y0, rtol=rtol, atol=atol, use_graph=False)
     Ts, Ys = [], []
     for t in times:
@@ -279,9 +276,15 @@ def generate_pairs(solution, T0, P, Y0, times, dt, rtol=1e-8, atol=1e-15):
         net.get_state(T, Y)
         Ts.append(T)
         Ys.append(Y)
-    Ts = torch.cat(Ts)
-    Ps = P.repeat(len(times))
-    Ys = torch.cat(Ys, dim=1).contiguous()
+    return torch.cat(Ts), P.repeat(len(times)), torch.cat(Ys, dim=1).contiguous()
+
+
+def generate_pairs(solution, T0, P, Y0, times, dt, rtol=1e-8, atol=1e-15):
+    """Training pairs along trajectories: the states of reactors started at (T0, P, Y0) at
+    each time in `times`, and the same states advanced by dt.  Device arrays, species-major
+    Y; returns Ts, Ps, Ys (inputs) and T1, Y1 (after dt), n_reactors * len(times) columns."""
+    import torch
+    Ts, Ps, Ys = trajectory_states(solution, T0, P, Y0, times, rtol, atol)
     net2 = ReactorNet(solution, Ts, Ps, Ys, rtol=rtol, atol=atol, use_graph=False)
     net2.advance(dt)
     T1 = torch.empty_like(Ts)

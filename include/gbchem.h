@@ -156,7 +156,8 @@ int32_t gb_mech_element_mass(int32_t mech, int32_t buflen, double* out);
  * on return.  gb_nn_gemm: C(m,n) = epilogue(alpha * sum_k A(m,k) B(n,k)) with BF16 A, B on
  * the tensor cores, FP32 accumulation; element (i,j) of X at X[i*s_i + j*s_j]; M, N multiples
  * of 128, K of 32; epilogue: + bias[n] (float, may be NULL), act 1 = GELU (tanh form) with the
- * pre-activation written to Z, act 2 = multiply by GELU'(Z); C and Z float (flag 1) or bf16. */
+ * pre-activation written to Z (unless Z is NULL), act 2 = multiply by GELU'(Z); C and Z float
+ * (flag 1) or bf16. */
 int32_t gb_nn_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, int64_t sak,
                    const void* B, int64_t sbn, int64_t sbk, void* C, int64_t scm, int64_t scn,
                    int32_t c_float, float alpha, const float* bias, int32_t act, void* Z, int64_t szm,
