@@ -243,6 +243,141 @@ def cpu_baseline(T0, P, Y0, idx, threads, kind="port"):
                       % (len(idx), WL["seed"] + 1000, threads, dt)}, (T, Y, st, tig)
 
 
+def run_workload(args):
+    """The other workloads of the hot path, one JSON line each (not the headline):
+    rates - gri30 net production rates and their Jacobian for 1,048,576 random states;
+    ndodecane - 16,384 n-dodecane reactors to 5e-3 s, FP64 vs FP32-LU Newton;
+    h2o2 - 1,024 hydrogen/air reactors to 1e-3 s against the CPU oracle for every reactor."""
+    import torch
+    import cantera_gb300 as gb
+    from oracle import pyoracle as po
+    dev = torch.device("cuda", 0)
+    threads = os.cpu_count()
+    if args.workload == "rates":
+        sol = gb.Solution("gri30.yaml", "gri30")
+        K = sol.n_species
+        n = args.n if args.n != WL["n"] else 1 << 20
+        rng = np.random.default_rng(20261203 + 1)
+        T = rng.uniform(300.0, 3000.0, n)
+        P = 101325.0 * 10 ** rng.uniform(-1.0, 2.0, n)
+        Y = rng.dirichlet(0.5 * np.ones(K), n).T.copy()
+        Td, Pd, Yd = (torch.tensor(a, device=dev) for a in (T, P, Y))
+        out = {}
+        for mode in ("wdot", "wdot+jacobian"):
+            fn = (lambda: sol.net_production_rates(Td, Pd, Yd)) if mode == "wdot" else \
+                 (lambda: sol.net_production_rates_ddCi(Td, Pd, Yd))
+            for _ in range(args.warmup):
+                r = fn()
+                del r
+            torch.cuda.synchronize()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record()
+            for _ in range(args.steps):
+                r = fn()
+                del r
+            ev[1].record()
+            torch.cuda.synchronize()
+            ms = ev[0].elapsed_time(ev[1]) / args.steps
+            nnz = len(sol.jac_rowidx)
+            bytes_ = n * ((K + 2) * 8 + K * 8 + (nnz * 8 if mode != "wdot" else 0))
+            out[mode] = {"states_per_s": n / (ms / 1e3), "ms": ms, "hbm_gbs": bytes_ / (ms / 1e3) / 1e9}
+        # CPU: the oracle's rates (and analytic Jacobian) on a sample, all host threads
+        m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "gri30.yaml"), "gri30")
+        ns = 65536
+        t0 = time.perf_counter()
+        m.rates_batch(T[:ns], P[:ns], np.ascontiguousarray(Y[:, :ns]), threads=threads)
+        cpu = ns / (time.perf_counter() - t0)
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+        line = {"metric": "GRI-30 net production rates (and Jacobian) per second, 1 GB300", "value": out["wdot"]["states_per_s"],
+                "unit": "states/s", "workload": "rates", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                "dtype": "f64", "data": "synthetic", "higher_is_better": True,
+                "config": {"workload": "gri30, %d states, T U[300,3000] K, P log-U[0.1,100] atm, Y Dirichlet(0.5)" % n},
+                "modes": out, "hbm_peak_gbs": peaks.get("hbm_gbs"),
+                "cpu_baseline": {"value": cpu, "unit": "states/s (wdot)", "cores": threads, "kind": "port",
+                                 "sample": "%d of the states, oracle restatement" % ns}}
+        print(json.dumps(line))
+        return
+    if args.workload == "ndodecane":
+        sol = gb.Solution("nDodecane_Reitz.yaml", "nDodecane_IG")
+        K = sol.n_species
+        n = args.n if args.n != WL["n"] else 16384
+        rng = np.random.default_rng(20261203 + 3)
+        T0 = rng.uniform(700.0, 1400.0, n)
+        P = 101325.0 * 10 ** rng.uniform(1.0, math.log10(60.0), n)
+        phi = rng.uniform(0.5, 2.0, n)
+        Y0 = np.array([sol.equivalence_ratio_mass_fractions(p, "c12h26:1", "o2:1, n2:3.76") for p in phi])
+        Td, Pd, Yd = (torch.tensor(a, device=dev) for a in (T0, P, np.ascontiguousarray(Y0.T)))
+        res = {}
+        for lu in (64, 32):
+            net = gb.ReactorNet(sol, Td, Pd, Yd, rtol=1e-8, atol=1e-15, lu_precision=lu, use_graph=True)
+            net.advance(5e-3)
+            net.set_state(Td, Pd, Yd)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            net.advance(5e-3)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            Tg, Yg = net.get_state()
+            st = net.solver_stats
+            res[lu] = {"reactors_per_s": n / dt, "seconds": dt, "launch": net.launch_info,
+                       "newton_iters_mean": float(st["newton_iters"].mean()), "steps_mean": float(st["steps"].mean()),
+                       "T": Tg, "Y": Yg}
+        ns = 64
+        m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "nDodecane_Reitz.yaml"), "nDodecane_IG")
+        t0 = time.perf_counter()
+        To, Yo, sto, _ = m.advance_batch(T0[:ns], P[:ns], Y0[:ns], 5e-3, po.opts(rtol=1e-8, atol=1e-15), threads=threads)
+        cpu = ns / (time.perf_counter() - t0)
+        err = {}
+        for lu in (64, 32):
+            Tg, Yg = res[lu].pop("T"), res[lu].pop("Y")
+            maj = Yo > 1e-2
+            err[lu] = {"T_max_rel_vs_oracle": float(np.max(np.abs(Tg[:ns] - To) / To)),
+                       "major_species_max_rel_vs_oracle": float(np.max((np.abs(Yg[:, :ns].T - Yo))[maj] / Yo[maj]))}
+        line = {"metric": "n-dodecane reactors advanced/s, FP64 vs FP32-LU Newton, 1 GB300",
+                "value": res[64]["reactors_per_s"], "unit": "reactors/s", "workload": "ndodecane", "n_gpus": 1,
+                "dtype": "f64", "data": "synthetic", "higher_is_better": True,
+                "config": {"workload": "nDodecane_IG (K=100, R=553), %d reactors, T0 U[700,1400] K, P log-U[10,60] atm, "
+                                       "phi U[0.5,2.0], to 5e-3 s, rtol 1e-8" % n},
+                "fp64": res[64], "fp32_lu": res[32], "error": {"fp64": err[64], "fp32_lu": err[32]},
+                "cpu_baseline": {"value": cpu, "unit": "reactors/s", "cores": threads, "kind": "port",
+                                 "sample": "%d reactors, oracle restatement (difference-quotient Jacobian)" % ns}}
+        print(json.dumps(line))
+        return
+    if args.workload == "h2o2":
+        sol = gb.Solution("h2o2.yaml", "ohmech")
+        n = 1024
+        rng = np.random.default_rng(20261203 + 0)
+        T0 = rng.uniform(1000.0, 1600.0, n)
+        P = np.full(n, 101325.0)
+        phi = rng.uniform(0.5, 2.0, n)
+        Y0 = np.array([sol.equivalence_ratio_mass_fractions(p, "H2:1", "O2:1, N2:3.76") for p in phi])
+        net = gb.ReactorNet(sol, T0, P, np.ascontiguousarray(Y0.T), rtol=1e-8, atol=1e-15)
+        net.advance(1e-3)
+        net.set_state(T0, P, np.ascontiguousarray(Y0.T))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        net.advance(1e-3)
+        dt = time.perf_counter() - t0
+        Tg, Yg = net.get_state()
+        tig = net.ignition_times
+        m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "h2o2.yaml"), "ohmech")
+        t0 = time.perf_counter()
+        To, Yo, sto, tio = m.advance_batch(T0, P, Y0, 1e-3, po.opts(rtol=1e-8, atol=1e-15), threads=threads)
+        cpu = n / (time.perf_counter() - t0)
+        maj = Yo > 1e-3
+        line = {"metric": "H2/air reactors advanced/s, 1 GB300", "value": n / dt, "unit": "reactors/s",
+                "workload": "h2o2", "n_gpus": 1, "dtype": "f64", "data": "synthetic", "higher_is_better": True,
+                "config": {"workload": "h2o2, 1024 reactors, T0 U[1000,1600] K, 1 atm, phi U[0.5,2.0], to 1e-3 s, rtol 1e-8"},
+                "error_vs_oracle_all_reactors": {"T_max_rel": float(np.max(np.abs(Tg - To) / To)),
+                                                 "major_species_max_rel": float(np.max(np.abs(Yg.T - Yo)[maj] / Yo[maj])),
+                                                 "ignition_time_max_rel": float(np.max(np.abs(tig - tio) / tio))},
+                "cpu_baseline": {"value": cpu, "unit": "reactors/s", "cores": threads, "kind": "port",
+                                 "sample": "all 1024 reactors, oracle restatement"}}
+        print(json.dumps(line))
+        return
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -282,11 +417,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--workload", default="uneven", choices=["uneven", "rates", "ndodecane", "h2o2"],
+                    help="uneven: the headline workload; the others print their own measurement line")
     ap.add_argument("--matrix-placement", type=int, default=0, choices=[0, 1, 2],
                     help="Newton matrix: 0 automatic, 1 shared memory, 2 global slot per warp")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "uneven":
+        return run_workload(args)
 
     import torch
     import cantera_gb300 as gb
