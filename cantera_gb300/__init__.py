@@ -43,7 +43,8 @@ class NetOptions(ctypes.Structure):
                 ("max_steps", ctypes.c_int32), ("max_order", ctypes.c_int32),
                 ("max_time_step", ctypes.c_double), ("lu_precision", ctypes.c_int32),
                 ("warps_per_block", ctypes.c_int32), ("use_graph", ctypes.c_int32),
-                ("matrix_placement", ctypes.c_int32), ("mechanism_in_shared", ctypes.c_int32)]
+                ("matrix_placement", ctypes.c_int32), ("mechanism_in_shared", ctypes.c_int32),
+                ("jacobian_reuse", ctypes.c_int32)]
 
 
 _lib = None
@@ -269,7 +270,7 @@ class ReactorNet:
 
     def __init__(self, solution, T, P, Y, rtol=1e-9, atol=1e-15, max_steps=20000, max_order=5,
                  max_time_step=0.0, lu_precision=64, warps_per_block=0, use_graph=False,
-                 matrix_placement=0, mechanism_in_shared=0):
+                 matrix_placement=0, mechanism_in_shared=0, jacobian_reuse=False):
         L = library()
         self.solution = solution
         o = NetOptions()
@@ -279,6 +280,7 @@ class ReactorNet:
         o.warps_per_block, o.use_graph = warps_per_block, int(use_graph)
         o.matrix_placement = matrix_placement
         o.mechanism_in_shared = mechanism_in_shared
+        o.jacobian_reuse = int(jacobian_reuse)
         n = T.shape[0] if _is_torch_cuda(T) else np.asarray(T).shape[0]
         self.n = n
         self._h = _check(L.gb_net_new(solution._h, n, ctypes.byref(o)))

@@ -84,7 +84,8 @@ struct NetEntry {
     gb_net_options opts;
     double time = 0.0;
     int warpsPerBlock = 0, blocks = 0, ld = 0, warpDoubles = 0, recStride = 0;
-    DBuf dP, dT, dY, dRec, dStats, dStatus, dTign, dCounter, dOrder, dM;
+    DBuf dP, dT, dY, dRec, dStats, dStatus, dTign, dCounter, dOrder, dM, dJ;
+    size_t Jstride = 0;   // bytes per kept-Jacobian slot in dJ (0: no Jacobian reuse)
     size_t Mstride = 0;   // bytes per Newton-matrix slot in dM (0: matrices in shared memory)
     bool matGlobal = false;
     int mechSmem = 0;     // bytes of the mechanism arena each block copies into shared memory
@@ -499,6 +500,7 @@ void netLaunch(NetEntry& ne, MechEntry& me, double t0, double tout) {
     p.counter = ne.dCounter.as<int>(); p.order = ne.haveOrder ? ne.dOrder.as<int>() : nullptr;
     p.ld = ne.ld; p.warpDoubles = ne.warpDoubles;
     p.Mbuf = ne.Mstride ? ne.dM.p : nullptr; p.Mstride = (long long)ne.Mstride;
+    p.Jbuf = ne.Jstride ? ne.dJ.p : nullptr; p.Jstride = (long long)ne.Jstride;
     p.mechSmem = ne.mechSmem;
     ck(cudaMemsetAsync(ne.dCounter.p, 0, sizeof(int), me.stream), "memset");
     ck(launchBdf(p, ne.blocks, ne.warpsPerBlock, ne.opts.lu_precision == 32, me.stream), "integrator launch");
@@ -731,6 +733,7 @@ void gb_net_default_options(gb_net_options* o) {
     o->use_graph = 0;
     o->matrix_placement = 0;
     o->mechanism_in_shared = 0;
+    o->jacobian_reuse = 0;
 }
 
 int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
@@ -761,6 +764,10 @@ int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
             const size_t elt = fp32 ? 4 : 8;
             ne->Mstride = ((size_t)N * ne->ld * elt + 255) & ~size_t(255);
             ne->dM.ensure(ne->Mstride * (size_t)ne->blocks * wpb);
+        }
+        if (ne->opts.jacobian_reuse) {
+            ne->Jstride = ((size_t)N * ne->ld * 8 + 255) & ~size_t(255);
+            ne->dJ.ensure(ne->Jstride * (size_t)ne->blocks * wpb);
         }
         const int K = me.m.K;
         ne->dP.ensure((size_t)n * 8);

@@ -79,6 +79,8 @@ constexpr int SMALL_NEF = 2, MXNEF1 = 3, MXNEF = 7, MXNCF = 10;
 constexpr int MAXCOR = 3;
 constexpr double NLSCOEF = 0.1, CRDOWN = 0.3, RDIV = 2.0;
 constexpr int MSBP = 20;
+constexpr int MSBJ = 51;
+constexpr double DGMAX_JBAD = 0.2;
 constexpr double DGMAX = 0.3;
 constexpr double UROUND = 2.220446049250313e-16;
 enum { ST_OK = 0, ST_MAX_STEPS = 1, ST_ERR_FAIL = 2, ST_CONV_FAIL = 3, ST_NONFINITE = 4, ST_H_TOO_SMALL = 5 };
@@ -96,8 +98,8 @@ enum { F_HASPREV = 1, F_HASRIGHT = 2, F_AWAIT = 4, F_INIT = 8 };
 struct BdfScal {
     double tn, h, hscale, hprime, eta, etamax, gamma, gammap, gamrat, crate, acnrm, saved_tq5;
     double tau[QMAX + 2], tq[6], l[QMAX + 1];
-    int q, qprime, qwait, L, nst, nstlp;
-    bool haveLU;
+    int q, qprime, qwait, L, nst, nstlp, nstlj;
+    bool haveLU, haveJ;
     // ignition marker
     int status0;
 };
@@ -252,7 +254,7 @@ __device__ __noinline__ bool devLuFactor(MT* a, int N, int ld, int* piv, double*
 // difference in T), factored in place.  The kinetics scratch must hold the state y
 // (the last right-hand side was evaluated at y, giving ftemp).  Returns false if J is
 // not finite or M singular.
-template <typename MT>
+template <typename MT, bool kJacOnly>
 __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uint64_t* tab, MT* M, int ld,
                                       double gamma, double P, const double* y, const double* ftemp,
                                       double* v1, double* v2, double* tempv, int* piv, double* dinv,
@@ -315,7 +317,7 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
         for (int k = 0; k < K; k++) {
             MT* p = M + (size_t)(1 + k) * ld + 1 + j;
             double v = fma(mm.mw[k], (double)*p, -v2[k]) * gj;
-            if (k == j) v += 1.0;
+            if (!kJacOnly && k == j) v += 1.0;
             fin = fin && finiteBits(v);
             *p = (MT)v;
         }
@@ -339,13 +341,34 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
 #pragma unroll 1
     for (int i = lane; i < N; i += 32) {
         double v = (v1[i] - ftemp[i]) * gdT;
-        if (i == 0) v += 1.0;
+        if (!kJacOnly && i == 0) v += 1.0;
         fin = fin && finiteBits(v);
         M[(size_t)i * ld] = (MT)v;
     }
     __syncwarp();
     ok = __all_sync(0xffffffffu, ok && fin);
     if (!ok) return false;
+    if (kJacOnly) return true;
+    return devLuFactor<MT>(M, N, ld, piv, dinv, lane);
+}
+
+// M = I - gamma J from a kept Jacobian J (FP64), then the LU factorisation of M.
+template <typename MT>
+__device__ __noinline__ bool devFormLU(MT* M, const double* J, int N, int ld, double gamma, int* piv, double* dinv,
+                                       int lane) {
+    bool fin = true;
+#pragma unroll 1
+    for (int i = 0; i < N; i++) {
+#pragma unroll 1
+        for (int j = lane; j < N; j += 32) {
+            double v = -gamma * J[(size_t)i * ld + j];
+            if (i == j) v += 1.0;
+            fin = fin && finiteBits(v);
+            M[(size_t)i * ld + j] = (MT)v;
+        }
+    }
+    __syncwarp();
+    if (!__all_sync(0xffffffffu, fin)) return false;
     return devLuFactor<MT>(M, N, ld, piv, dinv, lane);
 }
 
@@ -433,6 +456,7 @@ struct BdfWarp {
     double* base;            // the warp's shared-memory slice
     const uint64_t* tab;     // exp table (block shared)
     WarpAux* aux;            // lane 0 only
+    double* Jsv;             // the kept Jacobian (global slot), or null: a new one at every setup
     double *zn, *ewt, *acor, *y, *ftemp, *tempv, *v1, *v2, *dinv;
     int* piv;
 
@@ -454,10 +478,31 @@ struct BdfWarp {
         if (lane == 0) aux->nrhs++;
         return devRhs(*m, base, tab, P, z, zdot, lane, forJac);
     }
+    // Linear-solver setup.  With a kept Jacobian, CVODE's policy decides when to evaluate a
+    // new one (first step, 51 steps since the last, a convergence failure with a stale one
+    // and a small change of gamma, or a failure of the previous step); otherwise M is formed
+    // from the kept one.  convfail: 0 none, 1 retry after a failure with a stale Jacobian,
+    // 2 the previous attempt at this step failed.  fresh: a new Jacobian was evaluated.
     template <typename MT>
-    __device__ bool setup(MT* M, BdfScal& S) {
-        if (lane == 0) { aux->nje++; aux->nsetups++; aux->nrhs++; }   // nrhs: the difference in T
-        return devSetup<MT>(*m, base, tab, M, ld, S.gamma, P, y, ftemp, v1, v2, tempv, piv, dinv, lane);
+    __device__ bool setup(MT* M, BdfScal& S, int convfail, bool& fresh) {
+        if (!Jsv) {
+            if (lane == 0) { aux->nje++; aux->nsetups++; aux->nrhs++; }   // nrhs: the difference in T
+            fresh = true;
+            return devSetup<MT, false>(*m, base, tab, M, ld, S.gamma, P, y, ftemp, v1, v2, tempv, piv, dinv, lane);
+        }
+        const double dgamma = fabs(ddiv(S.gamma, S.gammap) - 1.0);
+        fresh = !S.haveJ || S.nst == 0 || S.nst >= S.nstlj + MSBJ || (convfail == 1 && dgamma < DGMAX_JBAD) ||
+                convfail == 2;
+        if (lane == 0) aux->nsetups++;
+        if (fresh) {
+            if (lane == 0) { aux->nje++; aux->nrhs++; }
+            const bool ok = devSetup<double, true>(*m, base, tab, Jsv, ld, -1.0, P, y, ftemp, v1, v2, tempv, piv, dinv,
+                                                   lane);
+            S.nstlj = S.nst;
+            S.haveJ = ok;
+            if (!ok) return false;
+        }
+        return devFormLU<MT>(M, Jsv, N, ld, S.gamma, piv, dinv, lane);
     }
 
     template <typename MT, int S>
@@ -551,9 +596,10 @@ struct BdfWarp {
     }
 
     template <typename MT, int NS>
-    __device__ int newton(MT* M, BdfScal& S, bool callSetup) {
+    __device__ int newton(MT* M, BdfScal& S, bool callSetup, bool prevFailed) {
         const double rl1 = ddiv(1.0, S.l[1]);
         bool jcur = false;
+        int convfail = prevFailed ? 2 : 0;
         for (;;) {
 #pragma unroll 1
             for (int i = lane; i < N; i += 32) { y[i] = zn[i]; acor[i] = 0.0; }
@@ -561,13 +607,14 @@ struct BdfWarp {
             if (!rhs(y, ftemp, S, callSetup)) return NLS_RECOVER;
             if (callSetup) {
                 callSetup = false;
-                bool ok = setup<MT>(M, S);
+                bool fresh = true;
+                bool ok = setup<MT>(M, S, convfail, fresh);
                 S.gammap = S.gamma;
                 S.gamrat = 1.0;
                 S.crate = 1.0;
                 S.nstlp = S.nst;
                 S.haveLU = ok;
-                jcur = true;
+                jcur = fresh;
                 if (!ok) return NLS_RECOVER;
             }
             double delp = 0.0, del = 0.0;
@@ -602,7 +649,7 @@ struct BdfWarp {
                 delp = del;
                 if (!rhs(y, ftemp, S)) { retry = !jcur; break; }
             }
-            if (retry && S.haveLU) { callSetup = true; continue; }
+            if (retry && S.haveLU) { callSetup = true; convfail = 1; continue; }
             return NLS_RECOVER;
         }
     }
@@ -812,7 +859,7 @@ struct BdfWarp {
             S.gamrat = (S.nst > 0) ? ddiv(S.gamma, S.gammap) : 1.0;
             bool callSetup = (S.nst == 0) || prevConvFail || (S.nst >= S.nstlp + MSBP) ||
                              (fabs(S.gamrat - 1.0) > DGMAX) || !S.haveLU;
-            int nls = newton<MT, NS>(M, S, callSetup);
+            int nls = newton<MT, NS>(M, S, callSetup, prevConvFail);
             if (nls != NLS_OK) {
                 if (lane == 0) aux->ncfn++;
                 ncf++;
@@ -928,6 +975,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     W.piv = (int*)q; q += (N + 1) / 2;
     MT* M = p.Mbuf ? (MT*)((char*)p.Mbuf + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * p.Mstride)
                    : (MT*)q;
+    W.Jsv = p.Jbuf ? (double*)((char*)p.Jbuf + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * p.Jstride) : nullptr;
 
     for (;;) {
         int idx = 0;
@@ -959,8 +1007,8 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
                 A.flags = F_INIT; A.nsamp = 0;
                 A.ls_t = A.ls_v = A.pv_t = A.pv_v = A.bs_t = A.bs_v = A.nx_t = A.nx_v = 0.0;
             }
-            S.nst = 0; S.nstlp = 0;
-            S.haveLU = false;
+            S.nst = 0; S.nstlp = 0; S.nstlj = 0;
+            S.haveLU = false; S.haveJ = false;
 #pragma unroll 1
             for (int i = 0; i < QMAX + 2; i++) S.tau[i] = 0.0;
 #pragma unroll 1
@@ -1011,7 +1059,9 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
             S.q = (int)rs[R_Q]; S.qprime = (int)rs[R_QPRIME]; S.qwait = (int)rs[R_QWAIT];
             S.nst = (int)rs[R_NST]; S.nstlp = (int)rs[R_NSTLP];
             S.L = S.q + 1;
-            S.haveLU = false;   // the factorisation is not kept between advance calls
+            S.haveLU = false;   // the factorisation and the Jacobian are not kept between advance calls
+            S.haveJ = false;
+            S.nstlj = S.nst;
             S.gamrat = 1.0; S.acnrm = 0.0;
             S.status0 = (int)rs[R_STATUS];
         }

@@ -56,6 +56,9 @@ struct BdfParams {
     void* Mbuf;           // Newton matrices in global memory, one slot of Mstride bytes per
                           // resident warp (L2 resident); null: in the warp's shared slice
     long long Mstride;
+    void* Jbuf;           // kept Jacobians (FP64), one slot of Jstride bytes per resident warp;
+                          // null: a new Jacobian at every linear-solver setup
+    long long Jstride;
 };
 
 constexpr int kBdfMaxThreads = 256;   // at most 8 warps per block

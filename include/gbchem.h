@@ -87,6 +87,12 @@ typedef struct {
     int32_t mechanism_in_shared; /* mechanism data copied into each block's shared memory:
                                0 = automatic, 1 = none, 2 = what the right-hand side reads,
                                3 = also the Jacobian's data, 4 = everything but the rest */
+    int32_t jacobian_reuse; /* 1: keep the Jacobian between linear-solver setups as CVODE
+                               does (a new one on the first step, after 51 steps, after a
+                               convergence failure with a stale one or a failed step); 0
+                               (default): a new Jacobian at every setup - with the analytic
+                               Jacobian this is faster (gri30: reuse raised the steps per
+                               reactor from 867 to 1,128 and cost 19 % throughput) */
 } gb_net_options;
 
 void gb_net_default_options(gb_net_options* opts);
@@ -130,7 +136,7 @@ int32_t gb_net_ignition_times(int32_t net, double* tign);
  * call, with the same integrator as gb_net_advance, allocating nothing.  T[n] and Y[K][n]
  * (in place) and P[n] are device pointers on the current device; status[n] (device)
  * receives the per-reactor status codes below.  opts may be NULL (defaults; use_graph is
- * ignored; the Newton matrices stay in shared memory).  The integrator records live in a 16 MiB array in the library's device image,
+ * ignored; the Newton matrices stay in shared memory; a new Jacobian at every setup).  The integrator records live in a 16 MiB array in the library's device image,
  * so n is limited to what fits (about 5,500 reactors for GRI-Mech 3.0); a larger n fails
  * with GB_ERR and a message giving the limit.  The call is ordered on `stream` (a
  * cudaStream_t; NULL is the default stream) and synchronises it before returning.  Every

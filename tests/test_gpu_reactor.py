@@ -188,3 +188,21 @@ def test_matrix_placement_is_bit_identical():
         res.append(net.get_state())
     np.testing.assert_array_equal(res[0][0], res[1][0])
     np.testing.assert_array_equal(res[0][1], res[1][1])
+
+
+def test_jacobian_reuse_option_matches_oracle_policy():
+    """With jacobian_reuse the GPU keeps the Jacobian between setups by CVODE's policy, as
+    the oracle does with jac_reuse: same tolerance-level agreement, fewer Jacobians."""
+    import cantera_gb300 as gb
+    from oracle import pyoracle as po
+    sol, m = gpu_solution("h2o2"), oracle_mech("h2o2")
+    rtol, atol = 1e-8, 1e-15
+    T0, P, Y0 = h2o2_batch(64, 13)
+    net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=rtol, atol=atol, jacobian_reuse=True)
+    assert net.advance(1e-3) == 0
+    T, Y = net.get_state()
+    To, Yo, sto, tio = m.advance_batch(T0, P, Y0, 1e-3, po.opts(rtol=rtol, atol=atol, analytic=True, jac_reuse=True))
+    assert np.max(np.abs(T - To) / To) < 10 * rtol
+    check_species(Y.T, Yo, rtol)
+    st = net.solver_stats
+    assert np.all(st["jac_evals"] <= st["lin_setups"]) and st["jac_evals"].sum() < st["lin_setups"].sum()

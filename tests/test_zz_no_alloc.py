@@ -30,8 +30,9 @@ def _workload(sol, n, seed):
 
 
 def _reference(gb, sol, T0, P, Y0, t_end, opts):
-    """The allocating path: gb_net_new / set_state / advance / get_state / get_status."""
-    net = gb.ReactorNet(sol, T0, P, Y0, **opts)
+    """The allocating path: gb_net_new / set_state / advance / get_state / get_status, with
+    a new Jacobian at every setup as the allocation-free call does."""
+    net = gb.ReactorNet(sol, T0, P, Y0, jacobian_reuse=False, **opts)
     net.advance(t_end)
     T, Y = net.get_state()
     return T, Y, net.status
