@@ -305,10 +305,18 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
     __syncwarp();
     const double logStandConc = st.lnC0;
     const bool bigG = s.flags[0] != 0;
+    // the next reaction's descriptors are loaded one iteration ahead
+    int4 nInfo = make_int4(0, 0, 0, 0), nRe = nInfo, nPe = nInfo;
+    D4 nAr{};
+    if (lane < m.R) { nInfo = m.rinfo[lane]; nAr = m.rarr[lane]; nRe = m.rk[lane]; nPe = m.pk[lane]; }
 #pragma unroll 1
     for (int i = lane; i < m.R; i += 32) {
-        int4 info = m.rinfo[i];
-        D4 ar = m.rarr[i];
+        const int4 info = nInfo;
+        const D4 ar = nAr;
+        const int4 re = nRe, pe = nPe;
+        if (i + 32 < m.R) {
+            nInfo = m.rinfo[i + 32]; nAr = m.rarr[i + 32]; nRe = m.rk[i + 32]; nPe = m.pk[i + 32];
+        }
         int kind = info.x & kKindMask;
         double kf;
         double dlnk = 0.0;
@@ -324,8 +332,6 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
             if (forJac) s.dlk[info.z] = dlnk;
         }
         double kfe = (kind == 1) ? kf * s.Mtb[info.y] : kf;
-        int4 re = m.rk[i];
-        int4 pe = m.pk[i];
         int rb = (info.x >> kRBucketShift) & 7, pb = (info.x >> kPBucketShift) & 7;
         double rkc = 0.0;
         double fwd = massAction(m, rb, re, 2 * i, s.c);
@@ -411,20 +417,35 @@ template <typename MT>
 __device__ __noinline__ void warpJacC(const DevMech& m, const KinScratch& s, MT* Jc, int ld, int lane) {
 #pragma unroll 1
     for (int q = m.laneColPtr[lane]; q < m.laneColPtr[lane + 1]; q++) {
-        int j = m.laneCols[q];
+        const int j = m.laneCols[q];
+        const int e0 = m.colPtr[j], e1 = m.colPtr[j + 1];
+        // the next entry's reaction data are loaded one iteration ahead
+        int iN = 0, rs0N = 0, rs1N = 0;
+        int4 infoN = make_int4(0, 0, 0, 0), rkN = infoN, pkN = infoN;
+        double epN = 0.0;
+        if (e0 < e1) {
+            iN = m.colRxn[e0];
+            infoN = m.rinfo[iN]; rkN = m.rk[iN]; pkN = m.pk[iN]; epN = m.colE[e0];
+            rs0N = m.rsPtr[iN]; rs1N = m.rsPtr[iN + 1];
+        }
 #pragma unroll 1
-        for (int e = m.colPtr[j]; e < m.colPtr[j + 1]; e++) {
-            int i = m.colRxn[e];
-            int4 info = m.rinfo[i];
-            int rb = (info.x >> kRBucketShift) & 7, pb = (info.x >> kPBucketShift) & 7;
-            double kfe = s.kfe[i];
-            double dF = kfe * massActionDeriv(m, rb, m.rk[i], 2 * i, s.c, j);
-            if (info.x & kRevBit) dF -= (kfe * s.rkc[i]) * massActionDeriv(m, pb, m.pk[i], 2 * i + 1, s.c, j);
-            double ep = m.colE[e];
+        for (int e = e0; e < e1; e++) {
+            const int i = iN, rs0 = rs0N, rs1 = rs1N;
+            const int4 info = infoN, rki = rkN, pki = pkN;
+            const double ep = epN;
+            if (e + 1 < e1) {
+                iN = m.colRxn[e + 1];
+                infoN = m.rinfo[iN]; rkN = m.rk[iN]; pkN = m.pk[iN]; epN = m.colE[e + 1];
+                rs0N = m.rsPtr[iN]; rs1N = m.rsPtr[iN + 1];
+            }
+            const int rb = (info.x >> kRBucketShift) & 7, pb = (info.x >> kPBucketShift) & 7;
+            const double kfe = s.kfe[i];
+            double dF = kfe * massActionDeriv(m, rb, rki, 2 * i, s.c, j);
+            if (info.x & kRevBit) dF -= (kfe * s.rkc[i]) * massActionDeriv(m, pb, pki, 2 * i + 1, s.c, j);
             if (ep != 0.0) dF += ep * s.Qtb[info.y];
             if (dF == 0.0) continue;
 #pragma unroll 1
-            for (int r = m.rsPtr[i]; r < m.rsPtr[i + 1]; r++) {
+            for (int r = rs0; r < rs1; r++) {
                 MT* p = Jc + (size_t)m.rsK[r] * ld + j;
                 *p = (MT)((double)*p + m.rsNu[r] * dF);
             }
