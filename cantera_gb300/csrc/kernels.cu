@@ -383,12 +383,14 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
         const int i = lane + 32 * t;
         x[t] = (i < N) ? (MT)b[piv[i]] : (MT)0;
     }
-    // forward: unit lower triangle (the next column's entries are loaded one step ahead)
-    MT nx[S];
+    // forward: unit lower triangle.  Columns k+1 and k+2 are in flight while column k is
+    // applied (the matrix may live in L2).
+    MT n1[S], n2[S];
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        nx[t] = (i < N) ? a[(size_t)i * ld] : (MT)0;
+        n1[t] = (i < N) ? a[(size_t)i * ld] : (MT)0;
+        n2[t] = (i < N && N > 1) ? a[(size_t)i * ld + 1] : (MT)0;
     }
 #pragma unroll
     for (int tk = 0; tk < S; tk++) {
@@ -397,9 +399,10 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
             MT cur[S];
 #pragma unroll
             for (int t = 0; t < S; t++) {
-                cur[t] = nx[t];
+                cur[t] = n1[t];
+                n1[t] = n2[t];
                 const int i = lane + 32 * t;
-                if (i < N && k + 1 < N) nx[t] = a[(size_t)i * ld + k + 1];
+                if (i < N && k + 2 < N) n2[t] = a[(size_t)i * ld + k + 2];
             }
             const MT xk = __shfl_sync(0xffffffffu, x[tk], k & 31);
 #pragma unroll
@@ -413,22 +416,26 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        nx[t] = (i < N) ? a[(size_t)i * ld + N - 1] : (MT)0;
+        n1[t] = (i < N) ? a[(size_t)i * ld + N - 1] : (MT)0;
+        n2[t] = (i < N && N > 1) ? a[(size_t)i * ld + N - 2] : (MT)0;
     }
-    MT nd = (MT)dinv[N - 1];
+    MT nd1 = (MT)dinv[N - 1];
+    MT nd2 = (N > 1) ? (MT)dinv[N - 2] : (MT)0;
 #pragma unroll
     for (int tk = S - 1; tk >= 0; tk--) {
         const int kbeg = min(N, 32 * (tk + 1)) - 1;
         for (int k = kbeg; k >= 32 * tk; k--) {
             MT cur[S];
-            const MT dk = nd;
+            const MT dk = nd1;
+            nd1 = nd2;
+            if (k > 1) nd2 = (MT)dinv[k - 2];
 #pragma unroll
             for (int t = 0; t < S; t++) {
-                cur[t] = nx[t];
+                cur[t] = n1[t];
+                n1[t] = n2[t];
                 const int i = lane + 32 * t;
-                if (i < N && k > 0) nx[t] = a[(size_t)i * ld + k - 1];
+                if (i < N && k > 1) n2[t] = a[(size_t)i * ld + k - 2];
             }
-            if (k > 0) nd = (MT)dinv[k - 1];
             if (lane == (k & 31)) x[tk] = x[tk] * dk;
             const MT xk = __shfl_sync(0xffffffffu, x[tk], k & 31);
 #pragma unroll
