@@ -417,6 +417,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--lu-staging", type=int, default=0,
+                    help="shared-memory factorisation buffers per block: -1 none, 0 automatic, k at most k")
     ap.add_argument("--workload", default="uneven", choices=["uneven", "rates", "ndodecane", "h2o2"],
                     help="uneven: the headline workload; the others print their own measurement line")
     ap.add_argument("--matrix-placement", type=int, default=0, choices=[0, 1, 2],
@@ -464,7 +466,8 @@ def main():
         if variant == "fp32_lu" and args.no_fp32:
             continue
         net = gb.ReactorNet(sol, dT, dP, dY, rtol=WL["rtol"], atol=WL["atol"], lu_precision=lu, use_graph=True,
-                            matrix_placement=args.matrix_placement)
+                            matrix_placement=args.matrix_placement, lu_staging=args.lu_staging)
+        launch = net.launch_info
         for _ in range(args.warmup if variant == "fp64" else 1):
             net.set_state(dT, dP, dY)
             net.advance(WL["t_end"])
@@ -488,7 +491,7 @@ def main():
         stats = net.solver_stats
         f64, f32 = algorithmic_flops(stats, fm, lu == 32)
         Tg, Yg = net.get_state()
-        results[variant] = {"ms": ms_max, "steps": steps, "kernel_ms": kernel_ms, "failed": int(bad),
+        results[variant] = {"ms": ms_max, "steps": steps, "kernel_ms": kernel_ms, "failed": int(bad), "launch": launch,
                             "f64": f64, "f32": f32, "clocks": clk.summary(), "T": Tg, "Y": Yg,
                             "stats": {k: float(v.mean()) for k, v in stats.items()}}
         del net
@@ -496,7 +499,7 @@ def main():
     # end to end through the public API with host buffers: H2D of the initial state,
     # the advance, D2H of the final state, every step
     net = gb.ReactorNet(sol, Ts, Ps, Ys, rtol=WL["rtol"], atol=WL["atol"], lu_precision=64, use_graph=True,
-                        matrix_placement=args.matrix_placement)
+                        matrix_placement=args.matrix_placement, lu_staging=args.lu_staging)
     Th = np.empty(n)
     Yh = np.empty((K, n))
     barrier()
@@ -532,7 +535,8 @@ def main():
                                    "CH4/air phi U[0.5,1.5], to 1e-2 s" % n_all,
                        "rtol": WL["rtol"], "atol": WL["atol"], "seed": WL["seed"],
                        "l2": "flushed (256 MB write) before every timed step",
-                       "launch": "persistent kernel, device work queue, CUDA graph", "shards": ws},
+                       "launch": "persistent kernel, device work queue, CUDA graph", "shards": ws,
+                       "launch_shape": r64["launch"]},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": read_traffic(),
                          "peak_source": "FP64 FMA rate measured live by this run (MEASURED_PEAKS.json has no FP64 figure)",

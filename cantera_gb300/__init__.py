@@ -44,7 +44,7 @@ class NetOptions(ctypes.Structure):
                 ("max_time_step", ctypes.c_double), ("lu_precision", ctypes.c_int32),
                 ("warps_per_block", ctypes.c_int32), ("use_graph", ctypes.c_int32),
                 ("matrix_placement", ctypes.c_int32), ("mechanism_in_shared", ctypes.c_int32),
-                ("jacobian_reuse", ctypes.c_int32)]
+                ("jacobian_reuse", ctypes.c_int32), ("lu_staging", ctypes.c_int32)]
 
 
 _lib = None
@@ -270,7 +270,7 @@ class ReactorNet:
 
     def __init__(self, solution, T, P, Y, rtol=1e-9, atol=1e-15, max_steps=20000, max_order=5,
                  max_time_step=0.0, lu_precision=64, warps_per_block=0, use_graph=False,
-                 matrix_placement=0, mechanism_in_shared=0, jacobian_reuse=False):
+                 matrix_placement=0, mechanism_in_shared=0, jacobian_reuse=False, lu_staging=0):
         L = library()
         self.solution = solution
         o = NetOptions()
@@ -281,6 +281,7 @@ class ReactorNet:
         o.matrix_placement = matrix_placement
         o.mechanism_in_shared = mechanism_in_shared
         o.jacobian_reuse = int(jacobian_reuse)
+        o.lu_staging = int(lu_staging)
         n = T.shape[0] if _is_torch_cuda(T) else np.asarray(T).shape[0]
         self.n = n
         self._h = _check(L.gb_net_new(solution._h, n, ctypes.byref(o)))
@@ -300,10 +301,10 @@ class ReactorNet:
     def launch_info(self):
         """blocks, reactors per block, shared bytes per warp, mechanism bytes in shared
         memory, matrix placement (1 shared, 2 global)."""
-        v = np.zeros(5, dtype=np.int32)
+        v = np.zeros(6, dtype=np.int32)
         _check(library().gb_net_launch_info(self._h, _ptr(v)))
         return dict(zip(["blocks", "warps_per_block", "warp_smem_bytes", "mechanism_smem_bytes",
-                         "matrix_placement"], v.tolist()))
+                         "matrix_placement", "lu_staging_slots"], v.tolist()))
 
     @property
     def time(self):

@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "kernels.h"
 #include "kinetics.cuh"
 
@@ -127,7 +129,7 @@ __device__ __noinline__ double ddiv(double a, double b) { return a / b; }
 __device__ __noinline__ double dsqrt(double a) { return sqrt(a); }
 
 constexpr int kStateSlots = 16;
-static_assert(kKinStateDoubles <= kStateSlots, "state slots");
+static_assert(kKinStateDoubles <= 15, "state slots");
 
 // finite (not inf, not NaN) on the integer pipe
 __device__ __forceinline__ bool finiteBits(double x) {
@@ -139,8 +141,14 @@ __device__ __forceinline__ void storeState(double* base, const KinState& st) {
     base[8] = st.rrho; base[9] = st.lnPP; base[10] = st.lnC0; base[11] = st.RTP; base[12] = st.PRT;
 }
 
+// slot kExtSlot of the state slots holds the address of the warp's external Jacobian
+// scratch (kfe, rkc) or null
+constexpr int kExtSlot = 15;
+__device__ __forceinline__ double* extScratch(const double* base) {
+    return reinterpret_cast<double* const*>(base + kExtSlot)[0];
+}
 __device__ __forceinline__ void carveScratch(const DevMech& m, double* base, const uint64_t* tab, KinScratch& s) {
-    s.carve(base + kStateSlots, m.K, m.R, m.NTB, m.NF, m.NT);
+    s.carve(base + kStateSlots, m.K, m.R, m.NTB, m.NF, m.NT, extScratch(base));
     s.tab = tab;
 }
 __device__ __forceinline__ void loadState(const double* base, KinState& st) {
@@ -250,6 +258,41 @@ __device__ __noinline__ bool devLuFactor(MT* a, int N, int ld, int* piv, double*
     return nonsingular;
 }
 
+// Shared-memory staging of a factorisation whose matrix lives in global memory: a block
+// owns a few matrix-sized buffers; a warp that finds one free (atomic claim, never a wait)
+// copies its matrix in, factors it there and copies the factors back, otherwise it factors
+// in place.
+struct LuPool {
+    char* buf;        // nslots buffers of slotBytes (shared memory), or null
+    int* flags;       // nslots claim flags (shared memory)
+    int nslots;
+    int slotBytes;
+};
+
+template <typename MT>
+__device__ __noinline__ bool devLuStaged(MT* M, int N, int ld, int* piv, double* dinv, int lane, LuPool pool) {
+    int slot = -1;
+    if (pool.nslots > 0 && lane == 0) {
+        for (int q = 0; q < pool.nslots && slot < 0; q++)
+            if (atomicCAS(&pool.flags[q], 0, 1) == 0) slot = q;
+    }
+    slot = __shfl_sync(0xffffffffu, slot, 0);
+    if (slot < 0) return devLuFactor<MT>(M, N, ld, piv, dinv, lane);
+    MT* S = (MT*)(pool.buf + (size_t)slot * pool.slotBytes);
+    const int n = N * ld;
+#pragma unroll 1
+    for (int q = lane; q < n; q += 32) S[q] = M[q];
+    __syncwarp();
+    const bool ok = devLuFactor<MT>(S, N, ld, piv, dinv, lane);
+#pragma unroll 1
+    for (int q = lane; q < n; q += 32) M[q] = S[q];
+    __syncwarp();
+    __threadfence_block();
+    if (lane == 0) atomicExch(&pool.flags[slot], 0);
+    __syncwarp();
+    return ok;
+}
+
 // Newton matrix M = I - gamma*J (J analytic in the species columns, one-sided
 // difference in T), factored in place.  The kinetics scratch must hold the state y
 // (the last right-hand side was evaluated at y, giving ftemp).  Returns false if J is
@@ -258,7 +301,7 @@ template <typename MT, bool kJacOnly>
 __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uint64_t* tab, MT* M, int ld,
                                       double gamma, double P, const double* y, const double* ftemp,
                                       double* v1, double* v2, double* tempv, int* piv, double* dinv,
-                                      int lane) {
+                                      int lane, LuPool pool) {
     const int K = mm.K, N = mm.N;
     KinScratch s;
     carveScratch(mm, base, tab, s);
@@ -349,13 +392,13 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     ok = __all_sync(0xffffffffu, ok && fin);
     if (!ok) return false;
     if (kJacOnly) return true;
-    return devLuFactor<MT>(M, N, ld, piv, dinv, lane);
+    return devLuStaged<MT>(M, N, ld, piv, dinv, lane, pool);
 }
 
 // M = I - gamma J from a kept Jacobian J (FP64), then the LU factorisation of M.
 template <typename MT>
 __device__ __noinline__ bool devFormLU(MT* M, const double* J, int N, int ld, double gamma, int* piv, double* dinv,
-                                       int lane) {
+                                       int lane, LuPool pool) {
     bool fin = true;
 #pragma unroll 1
     for (int i = 0; i < N; i++) {
@@ -369,7 +412,7 @@ __device__ __noinline__ bool devFormLU(MT* M, const double* J, int N, int ld, do
     }
     __syncwarp();
     if (!__all_sync(0xffffffffu, fin)) return false;
-    return devLuFactor<MT>(M, N, ld, piv, dinv, lane);
+    return devLuStaged<MT>(M, N, ld, piv, dinv, lane, pool);
 }
 
 // Solve (P^T L U) x = b in place.  The vector lives in registers (element i in lane
@@ -464,6 +507,7 @@ struct BdfWarp {
     const uint64_t* tab;     // exp table (block shared)
     WarpAux* aux;            // lane 0 only
     double* Jsv;             // the kept Jacobian (global slot), or null: a new one at every setup
+    LuPool pool;             // shared-memory staging buffers for the factorisation
     double *zn, *ewt, *acor, *y, *ftemp, *tempv, *v1, *v2, *dinv;
     int* piv;
 
@@ -495,7 +539,7 @@ struct BdfWarp {
         if (!Jsv) {
             if (lane == 0) { aux->nje++; aux->nsetups++; aux->nrhs++; }   // nrhs: the difference in T
             fresh = true;
-            return devSetup<MT, false>(*m, base, tab, M, ld, S.gamma, P, y, ftemp, v1, v2, tempv, piv, dinv, lane);
+            return devSetup<MT, false>(*m, base, tab, M, ld, S.gamma, P, y, ftemp, v1, v2, tempv, piv, dinv, lane, pool);
         }
         const double dgamma = fabs(ddiv(S.gamma, S.gammap) - 1.0);
         fresh = !S.haveJ || S.nst == 0 || S.nst >= S.nstlj + MSBJ || (convfail == 1 && dgamma < DGMAX_JBAD) ||
@@ -504,12 +548,12 @@ struct BdfWarp {
         if (fresh) {
             if (lane == 0) { aux->nje++; aux->nrhs++; }
             const bool ok = devSetup<double, true>(*m, base, tab, Jsv, ld, -1.0, P, y, ftemp, v1, v2, tempv, piv, dinv,
-                                                   lane);
+                                                   lane, LuPool{nullptr, nullptr, 0, 0});
             S.nstlj = S.nst;
             S.haveJ = ok;
             if (!ok) return false;
         }
-        return devFormLU<MT>(M, Jsv, N, ld, S.gamma, piv, dinv, lane);
+        return devFormLU<MT>(M, Jsv, N, ld, S.gamma, piv, dinv, lane, pool);
     }
 
     template <typename MT, int S>
@@ -948,6 +992,8 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     extern __shared__ __align__(128) double smem[];
     __shared__ uint64_t s_tab[kGbxTableWords];
     __shared__ DevMech s_mech;
+    __shared__ int s_luflags[kMaxLuSlots];
+    if (threadIdx.x < kMaxLuSlots) s_luflags[threadIdx.x] = 0;
     loadMech(p.m, s_mech, (char*)smem, p.mechSmem);
     gbx_load_table(s_tab);   // (its barrier also completes the mechanism copy)
     const DevMech& m = s_mech;
@@ -965,7 +1011,12 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     W.hmaxInv = p.hmaxInv;
     W.maxOrder = p.maxOrder;
     const int N = m.N;
-    const int kinD = kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
+    const bool ext = p.JSbuf != nullptr;
+    const int kinD = kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT, ext);
+    if (lane == 0)
+        reinterpret_cast<double**>(base + kExtSlot)[0] =
+            ext ? (double*)((char*)p.JSbuf + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * p.JSstride) : nullptr;
+    __syncwarp();
     W.base = base;
     W.tab = s_tab;
     double* q = base + kinD;
@@ -983,6 +1034,11 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     MT* M = p.Mbuf ? (MT*)((char*)p.Mbuf + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * p.Mstride)
                    : (MT*)q;
     W.Jsv = p.Jbuf ? (double*)((char*)p.Jbuf + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * p.Jstride) : nullptr;
+    // staging buffers follow the warps' slices
+    W.pool.buf = (char*)(smem + p.mechSmem / 8 + (size_t)(blockDim.x >> 5) * p.warpDoubles);
+    W.pool.flags = s_luflags;
+    W.pool.nslots = p.Mbuf ? p.luSlots : 0;
+    W.pool.slotBytes = p.luSlotBytes;
 
     for (;;) {
         int idx = 0;
@@ -1134,6 +1190,8 @@ __global__ void __launch_bounds__(256, 1) k_reactor_rhs(RhsParams p) {
     double* base = smem + (size_t)warp * p.warpDoubles;
     double* z = base + kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
     double* zd = z + m.N;
+    if (lane == 0) reinterpret_cast<double**>(base + kExtSlot)[0] = nullptr;
+    __syncwarp();
     for (int r = blockIdx.x * wpb + warp; r < p.n; r += gridDim.x * wpb) {
         if (lane == 0) z[0] = p.T[r];
 #pragma unroll 1
@@ -1162,8 +1220,14 @@ cudaError_t launchReactorRhs(const RhsParams& p, int blocks, int warpsPerBlock, 
 
 template <typename MT, int NS>
 cudaError_t launchBdfT(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
-    size_t smem = (size_t)p.mechSmem + (size_t)p.warpDoubles * 8 * warpsPerBlock;
+    size_t smem = (size_t)p.mechSmem + (size_t)p.warpDoubles * 8 * warpsPerBlock +
+                  (size_t)(p.Mbuf ? p.luSlots : 0) * p.luSlotBytes;
     cudaError_t e = cudaFuncSetAttribute(k_bdf<MT, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    // the rest of the SM's 256 KB of L1/shared storage is L1: ask for the smallest carveout
+    // that holds the block (static tables and the per-block reservation included)
+    const int pct = (int)std::min<size_t>(100, ((smem + 4096 + 1024) * 100 + 233471) / 233472);
+    e = cudaFuncSetAttribute(k_bdf<MT, NS>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
     if (e != cudaSuccess) return e;
     k_bdf<MT, NS><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
     return cudaGetLastError();
@@ -1182,7 +1246,7 @@ int bdfWarpDoubles(const DevMech& m, int ld, bool fp32) {
 
 int bdfWarpDoublesNoMatrix(const DevMech& m) {
     int N = m.N;
-    int kinD = kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
+    int kinD = kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT, true);
     int vec = (QMAX + 1) * N + 8 * N + (N + 1) / 2 + kAuxDoubles;
     return (kinD + vec + 1) & ~1;
 }

@@ -56,15 +56,21 @@ struct BdfParams {
     void* Mbuf;           // Newton matrices in global memory, one slot of Mstride bytes per
                           // resident warp (L2 resident); null: in the warp's shared slice
     long long Mstride;
+    int luSlots;          // shared-memory staging buffers per block for factorisations of
+    int luSlotBytes;      // global-memory matrices (0: none); bytes per buffer (multiple of 16)
+    void* JSbuf;          // with global matrices: the Jacobian scratch (kfe, rkc: 2R doubles)
+    long long JSstride;   // of each resident warp, one slot of JSstride bytes; else null
     void* Jbuf;           // kept Jacobians (FP64), one slot of Jstride bytes per resident warp;
                           // null: a new Jacobian at every linear-solver setup
     long long Jstride;
 };
 
 constexpr int kBdfMaxThreads = 256;   // at most 8 warps per block
+constexpr int kMaxLuSlots = 4;         // shared-memory factorisation buffers per block
 int bdfRecordStride(int N);
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32);
-int bdfWarpDoublesNoMatrix(const DevMech& m);   // the slice when the matrix is in global memory
+int bdfWarpDoublesNoMatrix(const DevMech& m);   // the slice when the matrix (and the Jacobian
+                                                 // scratch kfe, rkc) are in global memory
 int ratesWarpDoubles(const DevMech& m, bool jac);   // dense Jacobian scratch only with jac
 cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
 cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream);

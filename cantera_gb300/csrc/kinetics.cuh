@@ -68,12 +68,15 @@ struct KinScratch {
     int* flags;     // [2] per-state flags (bit 0: some |g| >= 700)
     double* part;   // partial sums of the gather tasks [NT]
     // (xu, xiu need 8-byte alignment: they follow doubles)
-    __host__ __device__ static int doubles(int K, int R, int NTB, int NF, int NT) {
-        return 5 * K + 3 * R + 2 * NTB + NF + 2 * K + K + 8 + 2 + NT;
+    // ext: kfe and rkc live elsewhere (they are only written before a Jacobian evaluation)
+    __host__ __device__ static int doubles(int K, int R, int NTB, int NF, int NT, bool ext = false) {
+        return 5 * K + (ext ? 1 : 3) * R + 2 * NTB + NF + 2 * K + K + 8 + 2 + NT;
     }
-    __device__ void carve(double* p, int K, int R, int NTB, int NF, int NT) {
+    __device__ void carve(double* p, int K, int R, int NTB, int NF, int NT, double* ext = nullptr) {
         c = p; p += K; cpR = p; p += K; hRT = p; p += K; g = p; p += K; wdot = p; p += K;
-        rop = p; p += R; kfe = p; p += R; rkc = p; p += R;
+        rop = p; p += R;
+        if (ext) { kfe = ext; rkc = ext + R; }
+        else { kfe = p; p += R; rkc = p; p += R; }
         Mtb = p; p += NTB; Qtb = p; p += NTB; dlk = p; p += NF;
         xu = (uint64_t*)p; p += K; xiu = (uint64_t*)p; p += K;
         xe = (int*)p; xie = xe + K; p += K;

@@ -93,6 +93,10 @@ typedef struct {
                                (default): a new Jacobian at every setup - with the analytic
                                Jacobian this is faster (gri30: reuse raised the steps per
                                reactor from 867 to 1,128 and cost 19 % throughput) */
+    int32_t lu_staging;     /* with the Newton matrices in global memory, factor them in
+                               shared-memory buffers a block keeps for that (a warp that finds
+                               none free factors in place): 0 = automatic (none: the buffers
+                               take L1 capacity the global matrices need), k > 0 = at most k */
 } gb_net_options;
 
 void gb_net_default_options(gb_net_options* opts);
@@ -110,9 +114,9 @@ double gb_net_time(int32_t net);
 double gb_net_last_advance_ms(int32_t net);
 int32_t gb_net_get_state(int32_t net, double* T, double* Y, int32_t flags);
 
-/* Launch shape of the integrator: info[0..4] = blocks, reactors (warps) per block, shared
+/* Launch shape of the integrator: info[0..5] = blocks, reactors (warps) per block, shared
  * bytes per warp, mechanism bytes in shared memory per block, Newton matrices in shared (1)
- * or global (2) memory.  (No counterpart in the reference.) */
+ * or global (2) memory, factorisation buffers per block.  (No counterpart in the reference.) */
 int32_t gb_net_launch_info(int32_t net, int32_t* info);
 
 /* Per-reactor status: 0 ok, 1 max steps, 2 repeated error-test failures, 3 repeated
