@@ -497,7 +497,7 @@ void chooseBdfLaunch(const MechEntry& me, const gb_net_options& o, int n, bool f
         ne.luSlots = std::max(0, std::min(room, cap));
     }
     const int perBlock = ne.mechSmem + ne.warpDoubles * 8 * bestFit + ne.luSlots * ne.luSlotBytes;
-    const int blocksPerSm = std::max(1, (228 * 1024) / (perBlock + 1024));
+    const int blocksPerSm = bdfBlocksPerSm(d.N, fp32, bestFit, (size_t)perBlock);
     ne.blocks = std::min(me.smCount * blocksPerSm, (n + bestFit - 1) / bestFit);
 }
 
@@ -780,7 +780,7 @@ int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
             const size_t elt = fp32 ? 4 : 8;
             ne->Mstride = ((size_t)N * ne->ld * elt + 255) & ~size_t(255);
             ne->dM.ensure(ne->Mstride * (size_t)ne->blocks * wpb);
-            ne->JSstride = ((size_t)2 * me.m.R * 8 + 255) & ~size_t(255);
+            ne->JSstride = (((size_t)2 * me.m.R + bdfNordsieckDoubles(N)) * 8 + 255) & ~size_t(255);
             ne->dJS.ensure(ne->JSstride * (size_t)ne->blocks * wpb);
         }
         if (ne->opts.jacobian_reuse) {

@@ -1021,7 +1021,10 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     W.tab = s_tab;
     double* q = base + kinD;
     W.aux = (WarpAux*)q; q += kAuxDoubles;
-    W.zn = q; q += (QMAX + 1) * N;
+    // with global matrices the Nordsieck array lives in the warp's global slot too, after the
+    // Jacobian scratch (more shared memory left as L1)
+    if (ext) W.zn = extScratch(base) + 2 * m.R;
+    else { W.zn = q; q += (QMAX + 1) * N; }
     W.ewt = q; q += N;
     W.acor = q; q += N;
     W.y = q; q += N;
@@ -1234,6 +1237,7 @@ cudaError_t launchBdfT(const BdfParams& p, int blocks, int warpsPerBlock, cudaSt
 }
 
 int bdfRecordStride(int N) { return (QMAX + 1) * N + R_NSCAL; }
+int bdfNordsieckDoubles(int N) { return (QMAX + 1) * N; }
 
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32) {
     int N = m.N;
@@ -1247,7 +1251,7 @@ int bdfWarpDoubles(const DevMech& m, int ld, bool fp32) {
 int bdfWarpDoublesNoMatrix(const DevMech& m) {
     int N = m.N;
     int kinD = kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT, true);
-    int vec = (QMAX + 1) * N + 8 * N + (N + 1) / 2 + kAuxDoubles;
+    int vec = 8 * N + (N + 1) / 2 + kAuxDoubles;   // the Nordsieck array is in the global slot
     return (kinD + vec + 1) & ~1;
 }
 
@@ -1263,6 +1267,27 @@ cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cud
     if (e != cudaSuccess) return e;
     k_rates<<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
     return cudaGetLastError();
+}
+
+template <typename MT, int NS>
+int bdfBlocksPerSmT(int warpsPerBlock, size_t smem) {
+    int nb = 0;
+    if (cudaFuncSetAttribute(k_bdf<MT, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bdf<MT, NS>, 32 * warpsPerBlock, smem) != cudaSuccess)
+        return 1;
+    return nb > 0 ? nb : 1;
+}
+
+int bdfBlocksPerSm(int N, bool fp32, int warpsPerBlock, size_t smem) {
+    if (fp32) {
+        if (N <= 64) return bdfBlocksPerSmT<float, 2>(warpsPerBlock, smem);
+        if (N <= 128) return bdfBlocksPerSmT<float, 4>(warpsPerBlock, smem);
+        return bdfBlocksPerSmT<float, 8>(warpsPerBlock, smem);
+    }
+    if (N <= 64) return bdfBlocksPerSmT<double, 2>(warpsPerBlock, smem);
+    if (N <= 128) return bdfBlocksPerSmT<double, 4>(warpsPerBlock, smem);
+    return bdfBlocksPerSmT<double, 8>(warpsPerBlock, smem);
 }
 
 cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream) {

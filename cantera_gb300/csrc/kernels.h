@@ -58,8 +58,9 @@ struct BdfParams {
     long long Mstride;
     int luSlots;          // shared-memory staging buffers per block for factorisations of
     int luSlotBytes;      // global-memory matrices (0: none); bytes per buffer (multiple of 16)
-    void* JSbuf;          // with global matrices: the Jacobian scratch (kfe, rkc: 2R doubles)
-    long long JSstride;   // of each resident warp, one slot of JSstride bytes; else null
+    void* JSbuf;          // with global matrices: the Jacobian scratch (kfe, rkc: 2R doubles) and
+    long long JSstride;   // the Nordsieck array of each resident warp, one slot of JSstride
+                          // bytes; else null
     void* Jbuf;           // kept Jacobians (FP64), one slot of Jstride bytes per resident warp;
                           // null: a new Jacobian at every linear-solver setup
     long long Jstride;
@@ -68,12 +69,15 @@ struct BdfParams {
 constexpr int kBdfMaxThreads = 256;   // at most 8 warps per block
 constexpr int kMaxLuSlots = 4;         // shared-memory factorisation buffers per block
 int bdfRecordStride(int N);
+int bdfNordsieckDoubles(int N);
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32);
 int bdfWarpDoublesNoMatrix(const DevMech& m);   // the slice when the matrix (and the Jacobian
                                                  // scratch kfe, rkc) are in global memory
 int ratesWarpDoubles(const DevMech& m, bool jac);   // dense Jacobian scratch only with jac
 cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
 cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream);
+// resident blocks per SM of the integrator kernel for this launch shape (registers included)
+int bdfBlocksPerSm(int N, bool fp32, int warpsPerBlock, size_t smem);
 // FP64 throughput probe: returns {GFLOP/s of FMA, exp cost, log cost in FMA-equivalents}
 cudaError_t measureFp64(double* results, int smCount);
 cudaError_t checkExp(int n, const double* x, double* mine, double* lib);
