@@ -243,22 +243,38 @@ class Surrogate:
                                     _p(acc), _p(score)))
         return acc, score
 
-    def advance(self, T, P, Y, rtol=1e-8, atol=1e-15, **tols):
+    def advance(self, T, P, Y, rtol=1e-8, atol=1e-15, timings=None, **tols):
         """One step dt for every reactor: the surrogate where the gate accepts it, the FP64
-        BDF integrator elsewhere.  Returns T1, Y1 and the accepted mask."""
+        BDF integrator elsewhere.  Returns T1, Y1 and the accepted mask (and, given a dict
+        `timings`, the seconds of its phases)."""
+        import time
         torch = self.torch
+
+        def mark(name, t0):
+            if timings is not None:
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                timings[name] = timings.get(name, 0.0) + (t1 - t0)
+                return t1
+            return t0
+        t0 = time.perf_counter()
         T1, Y1, f0 = self.predict(T, P, Y)
+        t0 = mark("predict", t0)
         acc, _ = self.gate(T, P, Y, T1, Y1, f0=f0, **tols)
+        t0 = mark("gate", t0)
         rej = torch.nonzero(acc == 0).flatten()
         if rej.numel() > 0:
             Tr, Pr = T[rej].contiguous(), P[rej].contiguous()
             Yr = Y[:, rej].contiguous()
             net = ReactorNet(self.sol, Tr, Pr, Yr, rtol=rtol, atol=atol)
+            t0 = mark("fallback_setup", t0)
             net.advance(self.dt)
+            t0 = mark("fallback_advance", t0)
             Tf, Yf = torch.empty_like(Tr), torch.empty_like(Yr)
             net.get_state(Tf, Yf)
             T1[rej] = Tf
             Y1[:, rej] = Yf
+            t0 = mark("fallback_gather", t0)
         return T1, Y1, acc
 
 
