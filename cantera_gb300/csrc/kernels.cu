@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
         if (p.jac) {
             for (int q = lane; q < m.K * ld; q += 32) Jc[q] = 0.0;
             __syncwarp();
-            warpJacC<double>(m, s, Jc, ld, lane);
+            warpJacC<double, false>(m, s, Jc, ld, lane);
             warpDenseG(m, s, gk, lane);
             for (int q = lane; q < m.nnz; q += 32) {
                 int r = m.jrIdx[q], c = m.jpCol[q];
@@ -294,11 +294,14 @@ __device__ __noinline__ bool devLuStaged(MT* M, int N, int ld, int* piv, double*
 }
 
 // Newton matrix M = I - gamma*J (J analytic in the species columns, one-sided
-// difference in T), factored in place.  The kinetics scratch must hold the state y
-// (the last right-hand side was evaluated at y, giving ftemp).  Returns false if J is
-// not finite or M singular.
+// difference in T), stored TRANSPOSED (element M[r][c] at A[c*ld + r]) and factored in
+// place: the factorisation of A = M^T pivots on M's columns, and the triangular solves
+// then read rows of A, which are contiguous (coalesced when A lives in global memory).
+// The kinetics scratch must hold the state y (the last right-hand side was evaluated at y,
+// giving ftemp).  kJacOnly: store J (transposed, no identity) and skip the factorisation.
+// Returns false if J is not finite or M singular.
 template <typename MT, bool kJacOnly>
-__device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uint64_t* tab, MT* M, int ld,
+__device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uint64_t* tab, MT* A, int ld,
                                       double gamma, double P, const double* y, const double* ftemp,
                                       double* v1, double* v2, double* tempv, int* piv, double* dinv,
                                       int lane, LuPool pool) {
@@ -308,9 +311,10 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     KinState st;
     loadState(base, st);
 #pragma unroll 1
-    for (int q = lane; q < N * ld; q += 32) M[q] = (MT)0;
+    for (int q = lane; q < N * ld; q += 32) A[q] = (MT)0;
     __syncwarp();
-    warpJacC<MT>(mm, s, M + ld + 1, ld, lane);
+    MT* Jt = A + ld + 1;   // Jc^T: Jc[k][j] at Jt[j*ld + k]
+    warpJacC<MT, true>(mm, s, Jt, ld, lane);
     // v1 = X (mole fractions); v2[k] = (Jc X)_k
     const double rct = st.RTP;   // 1/ctot
 #pragma unroll 1
@@ -318,10 +322,9 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     __syncwarp();
 #pragma unroll 1
     for (int k = lane; k < K; k += 32) {
-        const MT* row = M + (size_t)(1 + k) * ld + 1;
         double a = 0.0;
 #pragma unroll 1
-        for (int l = 0; l < K; l++) a += (double)row[l] * v1[l];
+        for (int l = 0; l < K; l++) a += (double)Jt[(size_t)l * ld + k] * v1[l];
         v2[k] = a;
     }
     double pcp = 0.0;
@@ -329,13 +332,14 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     for (int k = lane; k < K; k += 32) pcp += v1[k] * s.cpR[k];
     const double cpmix = warpSum(pcp);
     __syncwarp();
-    // column pass: hJ_j, then the transformed species block and the T row
+    // hJ_j = sum_k h_k Jc[k][j]
     double phj = 0.0;
 #pragma unroll 1
     for (int j = lane; j < K; j += 32) {
+        const MT* row = Jt + (size_t)j * ld;
         double a = 0.0;
 #pragma unroll 1
-        for (int k = 0; k < K; k++) a += s.hRT[k] * (double)M[(size_t)(1 + k) * ld + 1 + j];
+        for (int k = 0; k < K; k++) a += s.hRT[k] * (double)row[k];
         tempv[j] = a;
         phj += a * v1[j];
     }
@@ -349,29 +353,34 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
 #pragma unroll 1
     for (int k = lane; k < K; k += 32) v2[k] = mm.mw[k] * (v2[k] - s.wdot[k] * c1);
     __syncwarp();
-    // species block of M = I - gamma J in the same pass: M_kj = delta_kj - gamma/W_j (W_k Jc_kj - v2_k)
-    const double hscale = rho * st.RT, cpscale = rho * mm.Rgas;
+    // species block of M = I - gamma J: M_kj = delta_kj - gamma/W_j (W_k Jc_kj - v2_k), by
+    // rows of A (lanes along k)
     bool fin = true;
+#pragma unroll 1
+    for (int j = 0; j < K; j++) {
+        const double gj = -gamma * mm.rmw[j];
+        MT* row = Jt + (size_t)j * ld;
+#pragma unroll 1
+        for (int k = lane; k < K; k += 32) {
+            double v = fma(mm.mw[k], (double)row[k], -v2[k]) * gj;
+            if (!kJacOnly && k == j) v += 1.0;
+            fin = fin && finiteBits(v);
+            row[k] = (MT)v;
+        }
+    }
+    // T row of M (column 0 of A)
+    const double hscale = rho * st.RT, cpscale = rho * mm.Rgas;
 #pragma unroll 1
     for (int j = lane; j < K; j += 32) {
         const double rWj = mm.rmw[j];
-        const double gj = -gamma * rWj;
-#pragma unroll 1
-        for (int k = 0; k < K; k++) {
-            MT* p = M + (size_t)(1 + k) * ld + 1 + j;
-            double v = fma(mm.mw[k], (double)*p, -v2[k]) * gj;
-            if (!kJacOnly && k == j) v += 1.0;
-            fin = fin && finiteBits(v);
-            *p = (MT)v;
-        }
         const double dH = hscale * rWj * (tempv[j] - hJX);
         const double dD = cpscale * rWj * (s.cpR[j] - cpmix);
         const double v = (dH + G * dD) * rD * gamma;   // -gamma * J[0][1+j]
         fin = fin && finiteBits(v);
-        M[1 + j] = (MT)v;
+        A[(size_t)(1 + j) * ld] = (MT)v;
     }
     __syncwarp();
-    // T column: one-sided difference
+    // T column of M (row 0 of A): one-sided difference
     const double T0 = y[0];
     const double dT = sqrt(UROUND) * fmax(1.0, fabs(T0));
 #pragma unroll 1
@@ -386,16 +395,17 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
         double v = (v1[i] - ftemp[i]) * gdT;
         if (!kJacOnly && i == 0) v += 1.0;
         fin = fin && finiteBits(v);
-        M[(size_t)i * ld] = (MT)v;
+        A[i] = (MT)v;
     }
     __syncwarp();
     ok = __all_sync(0xffffffffu, ok && fin);
     if (!ok) return false;
     if (kJacOnly) return true;
-    return devLuStaged<MT>(M, N, ld, piv, dinv, lane, pool);
+    return devLuStaged<MT>(A, N, ld, piv, dinv, lane, pool);
 }
 
-// M = I - gamma J from a kept Jacobian J (FP64), then the LU factorisation of M.
+// A = M^T = I - gamma J^T from a kept Jacobian (stored transposed, FP64), then the LU
+// factorisation of A.
 template <typename MT>
 __device__ __noinline__ bool devFormLU(MT* M, const double* J, int N, int ld, double gamma, int* piv, double* dinv,
                                        int lane, LuPool pool) {
@@ -419,72 +429,76 @@ __device__ __noinline__ bool devFormLU(MT* M, const double* J, int N, int ld, do
 // i % 32, slot i / 32); every substitution step broadcasts one element by a shuffle.
 template <typename MT, int S>
 __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, const int* piv, const double* dinv,
-                                    int lane) {
+                                        int lane) {
+    // a holds the factors of A = M^T: P A = L U (row i of P A is row piv[i] of A), so
+    // M = U^T L^T P and M x = b is solved by U^T w = b (forward), L^T z = w (backward),
+    // x[piv[i]] = z[i].  Step k of either sweep reads row k of a (coalesced); rows k+1 and
+    // k+2 are in flight meanwhile.  The vector lives in registers: element i in lane i % 32,
+    // slot i / 32.
     MT x[S];
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        x[t] = (i < N) ? (MT)b[piv[i]] : (MT)0;
+        x[t] = (i < N) ? (MT)b[i] : (MT)0;
     }
-    // forward: unit lower triangle.  Columns k+1 and k+2 are in flight while column k is
-    // applied (the matrix may live in L2).
     MT n1[S], n2[S];
+    // forward: U^T w = b; w_k = b_k / U_kk, then b_i -= U[k][i] w_k for i > k
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        n1[t] = (i < N) ? a[(size_t)i * ld] : (MT)0;
-        n2[t] = (i < N && N > 1) ? a[(size_t)i * ld + 1] : (MT)0;
+        n1[t] = (i < N) ? a[i] : (MT)0;
+        n2[t] = (i < N && N > 1) ? a[(size_t)ld + i] : (MT)0;
     }
+    MT nd1 = (MT)dinv[0];
+    MT nd2 = (N > 1) ? (MT)dinv[1] : (MT)0;
 #pragma unroll
     for (int tk = 0; tk < S; tk++) {
         const int kend = min(N, 32 * (tk + 1));
         for (int k = 32 * tk; k < kend; k++) {
             MT cur[S];
+            const MT dk = nd1;
+            nd1 = nd2;
+            if (k + 2 < N) nd2 = (MT)dinv[k + 2];
 #pragma unroll
             for (int t = 0; t < S; t++) {
                 cur[t] = n1[t];
                 n1[t] = n2[t];
                 const int i = lane + 32 * t;
-                if (i < N && k + 2 < N) n2[t] = a[(size_t)i * ld + k + 2];
+                if (i < N && k + 2 < N) n2[t] = a[(size_t)(k + 2) * ld + i];
             }
-            const MT xk = __shfl_sync(0xffffffffu, x[tk], k & 31);
+            if (lane == (k & 31)) x[tk] = x[tk] * dk;
+            const MT wk = __shfl_sync(0xffffffffu, x[tk], k & 31);
 #pragma unroll
             for (int t = tk; t < S; t++) {
                 const int i = lane + 32 * t;
-                if (i > k && i < N) x[t] -= cur[t] * xk;
+                if (i > k && i < N) x[t] -= cur[t] * wk;
             }
         }
     }
-    // backward: upper triangle with the stored reciprocal diagonal (prefetched likewise)
+    // backward: L^T z = w (unit diagonal); w_i -= L[k][i] z_k for i < k
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        n1[t] = (i < N) ? a[(size_t)i * ld + N - 1] : (MT)0;
-        n2[t] = (i < N && N > 1) ? a[(size_t)i * ld + N - 2] : (MT)0;
+        n1[t] = (i < N) ? a[(size_t)(N - 1) * ld + i] : (MT)0;
+        n2[t] = (i < N && N > 1) ? a[(size_t)(N - 2) * ld + i] : (MT)0;
     }
-    MT nd1 = (MT)dinv[N - 1];
-    MT nd2 = (N > 1) ? (MT)dinv[N - 2] : (MT)0;
 #pragma unroll
     for (int tk = S - 1; tk >= 0; tk--) {
         const int kbeg = min(N, 32 * (tk + 1)) - 1;
         for (int k = kbeg; k >= 32 * tk; k--) {
             MT cur[S];
-            const MT dk = nd1;
-            nd1 = nd2;
-            if (k > 1) nd2 = (MT)dinv[k - 2];
 #pragma unroll
             for (int t = 0; t < S; t++) {
                 cur[t] = n1[t];
                 n1[t] = n2[t];
                 const int i = lane + 32 * t;
-                if (i < N && k > 1) n2[t] = a[(size_t)i * ld + k - 2];
+                if (i < N && k > 1) n2[t] = a[(size_t)(k - 2) * ld + i];
             }
-            if (lane == (k & 31)) x[tk] = x[tk] * dk;
-            const MT xk = __shfl_sync(0xffffffffu, x[tk], k & 31);
+            const MT zk = __shfl_sync(0xffffffffu, x[tk], k & 31);
 #pragma unroll
             for (int t = 0; t <= tk; t++) {
                 const int i = lane + 32 * t;
-                if (i < k) x[t] -= cur[t] * xk;
+                if (i < k) x[t] -= cur[t] * zk;
             }
         }
     }
@@ -492,7 +506,7 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        if (i < N) b[i] = (double)x[t];
+        if (i < N) b[piv[i]] = (double)x[t];
     }
     __syncwarp();
 }

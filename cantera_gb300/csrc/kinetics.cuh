@@ -414,9 +414,10 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
 }
 
 // d(wdot)/dc without the dense default-efficiency part: Jc[k*ld + j] (+)= ... for
-// k, j < K.  The dense part is g_k * (1 for every column); warpDenseG returns g in gout.
-// The caller zeroes Jc.  MT is the matrix element type (double or float).
-template <typename MT>
+// k, j < K (kT: the transpose, at Jc[j*ld + k]).  The dense part is g_k * (1 for every
+// column); warpDenseG returns g in gout.  The caller zeroes Jc.  MT is the matrix element
+// type (double or float).
+template <typename MT, bool kT>
 __device__ __noinline__ void warpJacC(const DevMech& m, const KinScratch& s, MT* Jc, int ld, int lane) {
 #pragma unroll 1
     for (int q = m.laneColPtr[lane]; q < m.laneColPtr[lane + 1]; q++) {
@@ -449,7 +450,7 @@ __device__ __noinline__ void warpJacC(const DevMech& m, const KinScratch& s, MT*
             if (dF == 0.0) continue;
 #pragma unroll 1
             for (int r = rs0; r < rs1; r++) {
-                MT* p = Jc + (size_t)m.rsK[r] * ld + j;
+                MT* p = kT ? Jc + (size_t)j * ld + m.rsK[r] : Jc + (size_t)m.rsK[r] * ld + j;
                 *p = (MT)((double)*p + m.rsNu[r] * dF);
             }
         }
