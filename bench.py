@@ -423,6 +423,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="skip the launch-shape autotuner (use the engine's rule)")
     ap.add_argument("--lu-staging", type=int, default=0,
                     help="shared-memory factorisation buffers per block: -1 none, 0 automatic, k at most k")
     ap.add_argument("--workload", default="uneven", choices=["uneven", "rates", "ndodecane", "h2o2"],
@@ -467,12 +469,21 @@ def main():
         return max_over_ranks(x, pg, dev)
 
     fm = flop_model(sol.structure(), K + 1)
+    # the launch shape: measured on a strided sample of this rank's reactors (before the
+    # timed region)
+    tuned = {}
+    tune_log = None
+    if args.autotune:
+        from cantera_gb300.tuning import autotune
+        tuned, tune_log = autotune(sol, dT, dP, dY, WL["t_end"] / 10, sample=min(2048, n))
     results = {}
     for variant, lu in (("fp64", 64), ("fp32_lu", 32)):
         if variant == "fp32_lu" and args.no_fp32:
             continue
+        shape = dict(tuned) if lu == 64 else {}
+        shape.setdefault("matrix_placement", args.matrix_placement)
         net = gb.ReactorNet(sol, dT, dP, dY, rtol=WL["rtol"], atol=WL["atol"], lu_precision=lu, use_graph=True,
-                            matrix_placement=args.matrix_placement, lu_staging=args.lu_staging)
+                            lu_staging=args.lu_staging, **shape)
         launch = net.launch_info
         for _ in range(args.warmup if variant == "fp64" else 1):
             net.set_state(dT, dP, dY)
@@ -504,8 +515,10 @@ def main():
 
     # end to end through the public API with host buffers: H2D of the initial state,
     # the advance, D2H of the final state, every step
+    shape = dict(tuned)
+    shape.setdefault("matrix_placement", args.matrix_placement)
     net = gb.ReactorNet(sol, Ts, Ps, Ys, rtol=WL["rtol"], atol=WL["atol"], lu_precision=64, use_graph=True,
-                        matrix_placement=args.matrix_placement, lu_staging=args.lu_staging)
+                        lu_staging=args.lu_staging, **shape)
     Th = np.empty(n)
     Yh = np.empty((K, n))
     barrier()
@@ -542,7 +555,8 @@ def main():
                        "rtol": WL["rtol"], "atol": WL["atol"], "seed": WL["seed"],
                        "l2": "flushed (256 MB write) before every timed step",
                        "launch": "persistent kernel, device work queue, CUDA graph", "shards": ws,
-                       "launch_shape": r64["launch"]},
+                       "launch_shape": r64["launch"],
+                       "autotune": tune_log and [{"seconds": round(t["seconds"], 4), **t["options"]} for t in tune_log]},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": read_traffic(),
                          "peak_source": "FP64 FMA rate measured live by this run (MEASURED_PEAKS.json has no FP64 figure)",

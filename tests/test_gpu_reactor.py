@@ -207,3 +207,13 @@ def test_jacobian_reuse_option_matches_oracle_policy():
     check_species(Y.T, Yo, 3 * rtol)
     st = net.solver_stats
     assert np.all(st["jac_evals"] <= st["lin_setups"]) and st["jac_evals"].sum() < st["lin_setups"].sum()
+
+
+def test_autotune_picks_a_measured_candidate():
+    from cantera_gb300.tuning import autotune, candidates
+    sol = gpu_solution("h2o2")
+    T0, P, Y0 = h2o2_batch(256, 17)
+    best, log = autotune(sol, T0, P, Y0.T.copy(), 1e-4, sample=64, use_cache=False)
+    assert best in list(candidates())
+    assert log and log[0]["options"] == best
+    assert all(a["seconds"] <= b["seconds"] for a, b in zip(log, log[1:]))
