@@ -62,6 +62,7 @@ def library():
     I32, D, P = ctypes.c_int32, ctypes.c_double, ctypes.c_void_p
     sig = {
         "gb_mech_load": (I32, [ctypes.c_char_p, ctypes.c_char_p]),
+        "gb_add_data_directory": (I32, [ctypes.c_char_p]),
         "gb_mech_del": (I32, [I32]),
         "gb_mech_n_species": (I32, [I32]),
         "gb_mech_n_reactions": (I32, [I32]),
@@ -108,6 +109,8 @@ def library():
         f = getattr(L, name)
         f.restype = res
         f.argtypes = args
+    # mechanisms may draw species from the packaged files ("gri30.yaml/species")
+    L.gb_add_data_directory(DATA_DIR.encode())
     _lib = L
     return L
 

@@ -149,16 +149,20 @@ void packDevMech(MechEntry& e) {
             d[11] = a[2] / 2.0; d[12] = a[3] / 3.0; d[13] = a[4] / 4.0;
         }
     }
-    // Device reaction order: falloff (Troe, then Lindemann), three-body, reversible, then
-    // irreversible reactions, and within each group those whose rate constant needs an
-    // exponential first.  A warp evaluates 32 consecutive reactions at a time, so grouping
-    // keeps its lanes on the same code path.  Results are per species and do not depend on
-    // this order (beyond summation order).
+    // Device reaction order: falloff (Troe, then Lindemann), the other falloff forms (SRI,
+    // Tsang, chemically activated), three-body, pressure-dependent Arrhenius, Chebyshev,
+    // reversible, then irreversible reactions, and within each group those whose rate
+    // constant needs an exponential first.  A warp evaluates 32 consecutive reactions at a
+    // time, so grouping keeps its lanes on the same code path.  Results are per species and
+    // do not depend on this order (beyond summation order).
     auto group = [&](int i) {
-        if (m.kind[i] == kTroe) return 0;
-        if (m.kind[i] == kLindemann) return 1;
-        if (m.kind[i] == kThreeBody) return 2;
-        return m.reversible[i] ? 3 : 4;
+        if (m.kind[i] == kTroe && !m.chemAct[i]) return 0;
+        if (m.kind[i] == kLindemann && !m.chemAct[i]) return 1;
+        if (isFalloffKind(m.kind[i])) return 2;
+        if (m.kind[i] == kThreeBody) return 3;
+        if (m.kind[i] == kPlog) return 4;
+        if (m.kind[i] == kChebyshev) return 5;
+        return m.reversible[i] ? 6 : 7;
     };
     auto noExp = [&](int i) { return m.kind[i] <= kThreeBody && m.b[i] == 0.0 && m.EaR[i] == 0.0; };
     std::vector<int> perm(R), inv(R);
@@ -175,6 +179,7 @@ void packDevMech(MechEntry& e) {
     std::vector<int> sidePtr(1, 0), sideK;
     std::vector<double> sideNu, sideOrd;
     std::vector<D4> fo1, fo2;
+    std::vector<double> pdep;
     std::vector<int> rsPtr(1, 0), rsK;
     std::vector<double> rsNu;
     std::vector<std::map<int, double>> net(R);
@@ -184,15 +189,51 @@ void packDevMech(MechEntry& e) {
         if (m.reversible[i]) flags |= kRevBit;
         flags |= (m.reacBucket[i] & 7) << kRBucketShift;
         flags |= (m.prodBucket[i] & 7) << kPBucketShift;
+        if (m.chemAct[i]) flags |= kChemActBit;
         int fo = -1;
-        if (m.kind[i] == kLindemann || m.kind[i] == kTroe) {
+        if (isFalloffKind(m.kind[i])) {
             fo = (int)fo1.size();
-            fo1.push_back(D4{m.A0[i], m.b0[i], m.Ea0R[i], m.troe[4 * i]});
-            fo2.push_back(D4{m.troe[4 * i + 1], m.troe[4 * i + 2], m.troe[4 * i + 3], m.kind[i] == kTroe ? 1.0 : 0.0});
+            const double* x = &m.falloffX[5 * i];
+            if (m.kind[i] == kSri) {
+                fo1.push_back(D4{m.A0[i], m.b0[i], m.Ea0R[i], x[0]});
+                fo2.push_back(D4{x[1], x[2], x[3], x[4]});
+            } else if (m.kind[i] == kTsang) {
+                fo1.push_back(D4{m.A0[i], m.b0[i], m.Ea0R[i], x[0]});
+                fo2.push_back(D4{x[1], 0.0, 0.0, 0.0});
+            } else {
+                fo1.push_back(D4{m.A0[i], m.b0[i], m.Ea0R[i], m.troe[4 * i]});
+                fo2.push_back(D4{m.troe[4 * i + 1], m.troe[4 * i + 2], m.troe[4 * i + 3], m.kind[i] == kTroe ? 1.0 : 0.0});
+            }
+        }
+        int pd = -1;
+        if (m.kind[i] == kPlog) {
+            pd = (int)pdep.size();
+            const int l0 = m.plogPtr[i], l1 = m.plogPtr[i + 1], L = l1 - l0;
+            const int q0 = m.plogFirst[l0];          // first rate of the reaction
+            int nrates = 0;
+            for (int l = l0; l < l1; l++) nrates = std::max(nrates, m.plogLast[l] - q0);
+            pdep.push_back((double)L);
+            const int rbase = 1 + 3 * L;             // offset of the first rate triple
+            for (int l = l0; l < l1; l++) {
+                pdep.push_back(m.plogLogP[l]);
+                pdep.push_back((double)(rbase + 3 * (m.plogFirst[l] - q0)));
+                pdep.push_back((double)(rbase + 3 * (m.plogLast[l] - q0)));
+            }
+            for (int q = q0; q < q0 + nrates; q++) {
+                pdep.push_back(m.plogA[q]);
+                pdep.push_back(m.plogB[q]);
+                pdep.push_back(m.plogEaR[q]);
+            }
+        } else if (m.kind[i] == kChebyshev) {
+            pd = (int)pdep.size();
+            pdep.push_back((double)m.chebNT[i]);
+            pdep.push_back((double)m.chebNP[i]);
+            for (int j = 0; j < 4; j++) pdep.push_back(m.chebLim[4 * i + j]);
+            for (int q = m.chebPtr[i]; q < m.chebPtr[i + 1]; q++) pdep.push_back(m.chebCoef[q]);
         }
         if (m.dn[i] == std::floor(m.dn[i]) && std::fabs(m.dn[i]) <= 3.0) flags |= kDnIntBit;
         if (noExp(i)) flags |= kNoExpBit;
-        rinfo[ni] = int4{flags, m.tbOfRxn[i], fo, 0};
+        rinfo[ni] = int4{flags, m.tbOfRxn[i], fo, pd};
         rarr[ni] = D4{m.A[i], m.b[i], m.EaR[i], m.dn[i]};
         auto expand = [&](const int32_t* ks, const double* nus, int n) {
             int4 e4{-1, -1, -1, 0};
@@ -356,6 +397,7 @@ void packDevMech(MechEntry& e) {
     const size_t sideEnd = a.data.size();
     size_t o_spPtr = a.add(spPtr), o_tbRxn = a.add(tbRxn), o_tbMA = a.add(tbMA);
     size_t o_jcPtr = a.add(jcPtr), o_jrIdx = a.add(jrIdx), o_jpCol = a.add(jpCol);
+    size_t o_pdep = a.add(pdep);
     e.arena.ensure(a.data.size());
     ck(cudaMemcpy(e.arena.p, a.data.data(), a.data.size(), cudaMemcpyHostToDevice), "upload mechanism");
     char* b = e.arena.as<char>();
@@ -364,6 +406,8 @@ void packDevMech(MechEntry& e) {
     d.arena = b;
     d.hotBytes = up16(hotEnd); d.jacBytes = up16(jacEnd); d.sideBytes = up16(sideEnd);
     d.K = K; d.R = R; d.N = K + 1; d.NF = (int)fo1.size(); d.NTB = m.nThirdBody(); d.nnz = (int)jrIdx.size();
+    d.NX = 0;
+    for (int i = 0; i < R; i++) d.NX += (m.kind[i] > kTroe || m.chemAct[i]) ? 1 : 0;
     d.Pref = m.Pref; d.Rgas = gasConstant();
     d.mw = (const double*)(b + o_mw); d.rmw = (const double*)(b + o_rmw); d.nasa = (const double*)(b + o_nasa);
     d.rinfo = (const int4*)(b + o_rinfo); d.rarr = (const D4*)(b + o_rarr);
@@ -382,6 +426,7 @@ void packDevMech(MechEntry& e) {
     d.laneColPtr = (const int*)(b + o_lcp); d.laneCols = (const int*)(b + o_lc);
     d.gsPtr = (const int*)(b + o_gsPtr); d.gsTb = (const int*)(b + o_gsTb); d.gsCoef = (const double*)(b + o_gsCoef);
     d.jcPtr = (const int*)(b + o_jcPtr); d.jrIdx = (const int*)(b + o_jrIdx); d.jpCol = (const int*)(b + o_jpCol);
+    d.pdep = (const double*)(b + o_pdep);
 }
 
 // dynamic shared memory a block may use: the opt-in maximum less the kernels' static
@@ -497,7 +542,7 @@ void chooseBdfLaunch(const MechEntry& me, const gb_net_options& o, int n, bool f
         ne.luSlots = std::max(0, std::min(room, cap));
     }
     const int perBlock = ne.mechSmem + ne.warpDoubles * 8 * bestFit + ne.luSlots * ne.luSlotBytes;
-    const int blocksPerSm = bdfBlocksPerSm(d.N, fp32, bestFit, (size_t)perBlock);
+    const int blocksPerSm = bdfBlocksPerSm(d.N, fp32, bestFit, (size_t)perBlock, d.NX > 0);
     ne.blocks = std::min(me.smCount * blocksPerSm, (n + bestFit - 1) / bestFit);
 }
 
@@ -578,6 +623,14 @@ int32_t gb_get_error(int32_t buflen, char* buf) {
         buf[buflen - 1] = '\0';
     }
     return (int32_t)g_error.size();
+}
+
+int32_t gb_add_data_directory(const char* dir) {
+    return guarded([&]() -> int32_t {
+        if (!dir) throw std::runtime_error("null directory");
+        addDataDirectory(dir);
+        return 0;
+    });
 }
 
 int32_t gb_mech_load(const char* path, const char* phase) {
@@ -663,7 +716,7 @@ int32_t gb_mech_structure(int32_t h, int32_t ncounts, int64_t* counts) {
         int64_t rev = 0, fo = 0, troe = 0, rslots = 0, pslots = 0;
         for (int i = 0; i < m.R; i++) {
             rev += m.reversible[i];
-            fo += (m.kind[i] == kLindemann || m.kind[i] == kTroe);
+            fo += isFalloffKind(m.kind[i]);
             troe += (m.kind[i] == kTroe);
             for (int j = m.reacPtr[i]; j < m.reacPtr[i + 1]; j++) rslots += (int64_t)m.reacNu[j];
             for (int j = m.prodPtr[i]; j < m.prodPtr[i + 1]; j++) pslots += (int64_t)m.prodNu[j];

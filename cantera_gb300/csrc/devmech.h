@@ -30,6 +30,9 @@ constexpr int kRBucketShift = 4;    // reactant StoichBucket (3 bits)
 constexpr int kPBucketShift = 7;    // product StoichBucket (3 bits)
 constexpr int kDnIntBit = 1 << 10;  // dn is an integer in [-3, 3]
 constexpr int kNoExpBit = 1 << 11;  // b = 0 and Ea = 0: k = A
+constexpr int kChemActBit = 1 << 12;  // chemically-activated falloff: k = klow F / (1 + Pr)
+// rate kinds (the RateKind values of mechanism.h)
+constexpr int kKindLindemann = 2, kKindTroe = 3, kKindPlog = 4, kKindCheb = 5, kKindSri = 6, kKindTsang = 7;
 
 struct DevMech {
     int K, R, N, NF, NTB, nnz;
@@ -44,7 +47,8 @@ struct DevMech {
     const double* rmw;
     const double* nasa;          // [K][kNasaStride]
     // reactions [R]
-    const int4* rinfo;           // x flags, y third-body index (-1), z falloff index (-1), w unused
+    const int4* rinfo;           // x flags, y third-body index (-1), z falloff index (-1),
+                                 // w offset of the reaction's table in pdep (-1)
     const D4* rarr;         // A, b, Ea/R, dn
     const int4* rk;              // reactant species repeated by coefficient (x,y,z; -1 unused), w = count
     const int4* pk;              // product species, same form
@@ -56,8 +60,8 @@ struct DevMech {
     const int* rsK;
     const double* rsNu;
     // falloff [NF]
-    const D4* fo1;          // A0, b0, Ea0/R, Troe a
-    const D4* fo2;          // 1/T3, 1/T1, T2, isTroe
+    const D4* fo1;          // A0, b0, Ea0/R, then Troe a | SRI a | Tsang a
+    const D4* fo2;          // Troe 1/T3, 1/T1, T2, 1 | SRI b, c, d, e | Tsang b, 0, 0, 0 | Lindemann 0
     // third bodies [NTB]
     const int* tbRxn;
     const double* tbDef;
@@ -93,6 +97,15 @@ struct DevMech {
     const int* jcPtr;
     const int* jrIdx;
     const int* jpCol;
+    // the less common rate forms (last, so that the fields above keep their offsets)
+    int NX;                      // reactions of those forms (PLOG, Chebyshev, SRI, Tsang,
+                                 // chemically activated), evaluated out of line
+    // pressure-dependent reactions, one table per reaction at rinfo.w (doubles):
+    //   PLOG:      L, then L levels (ln P, first, end) with first/end offsets (from the table
+    //              start) of the level's (A, b, Ea/R) triples, which follow; the first and
+    //              last levels are the sentinels at ln P = -1000 and +1000
+    //   Chebyshev: nT, nP, TrNum, TrDen, PrNum, PrDen, then nT x nP coefficients (row-major)
+    const double* pdep;
 };
 
 // every array of a DevMech
@@ -101,7 +114,7 @@ struct DevMech {
     X(rsPtr) X(rsK) X(rsNu) X(fo1) X(fo2) X(tbRxn) X(tbDef) X(tbMA) X(tbPtr) X(tbK) X(tbE) \
     X(spPtr) X(spRxn) X(spNu) X(taskPtr) X(laneTaskPtr) X(laneTasks) X(spTaskPtr) X(spTasks) \
     X(colPtr) X(colRxn) X(colE) X(laneColPtr) X(laneCols) X(gsPtr) X(gsTb) X(gsCoef) \
-    X(jcPtr) X(jrIdx) X(jpCol)
+    X(jcPtr) X(jrIdx) X(jpCol) X(pdep)
 
 #ifdef __CUDACC__
 // Point the arrays that lie in the first `bytes` of the arena at a copy of that prefix

@@ -28,6 +28,14 @@
 #include <stdint.h>
 #include <string.h>
 
+// Non-inline functions of these headers have internal linkage in the second kernel module
+// (kernels_x.cu), which compiles the same code again: their host-side stubs must not collide
+// at link time.
+#ifdef GB_KERNELS_EXTRA
+#define GB_TU_LOCAL static
+#else
+#define GB_TU_LOCAL
+#endif
 #ifdef __CUDACC__
 #define GBX_HD __host__ __device__ __forceinline__
 #else
@@ -214,8 +222,8 @@ GBX_HD bool gbx_big(double x) {
 
 // the library functions for the rare arguments, out of line (one copy of their code)
 #ifdef __CUDACC__
-__device__ __noinline__ double gbx_exp_slow(double x) { return exp(x); }
-__device__ __noinline__ double gbx_log_slow(double x) { return log(x); }
+GB_TU_LOCAL __device__ __noinline__ double gbx_exp_slow(double x) { return exp(x); }
+GB_TU_LOCAL __device__ __noinline__ double gbx_log_slow(double x) { return log(x); }
 #endif
 #ifdef __CUDA_ARCH__
 #define GBX_EXP_SLOW(x) gbx_exp_slow(x)
@@ -307,7 +315,7 @@ GBX_HD double gbx_todouble(XVal v) {
 }
 
 // exp(x) in double
-GBX_HD_NOINLINE double gbx_exp(double x, const uint64_t* tab) {
+GB_TU_LOCAL GBX_HD_NOINLINE double gbx_exp(double x, const uint64_t* tab) {
     if (gbx_big(x)) return GBX_EXP_SLOW(x);
     int k;
     const double r = gbx_reduce(x, k);
@@ -342,7 +350,7 @@ GBX_HD double gbx_q64_to_double(__int128 v) {
 }
 
 // ln(x); positive normal x on the integer pipe, anything else through the library log
-GBX_HD_NOINLINE double gbx_log(double x, const uint64_t* tab) {
+GB_TU_LOCAL GBX_HD_NOINLINE double gbx_log(double x, const uint64_t* tab) {
     const int64_t b = gbx_bits(x);
     if ((uint64_t)(b - 0x0010000000000000LL) >= 0x7FE0000000000000ULL) return GBX_LOG_SLOW(x);
     const int e = (int)(b >> 52) - 1023;

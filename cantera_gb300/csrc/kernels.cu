@@ -19,6 +19,7 @@ namespace gbchem {
 // Rates and d(wdot)/dc over a batch of states (Kinetics::getNetProductionRates,
 // Kinetics::netProductionRates_ddCi)
 // =============================================================================
+template <bool kX>
 __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
     extern __shared__ __align__(128) double smem[];
     __shared__ uint64_t s_tab[kGbxTableWords];
@@ -48,8 +49,8 @@ __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
         __syncwarp();
         warpState(m, T, P, Yl, s, st, lane);
         __syncwarp();
-        if (p.jac) warpRates<true>(m, s, st, lane);
-        else warpRates<false>(m, s, st, lane);
+        if (p.jac) warpRates<true, kX>(m, s, st, lane);
+        else warpRates<false, kX>(m, s, st, lane);
         if (p.wdot)
             for (int k = lane; k < m.K; k += 32) p.wdot[(size_t)k * p.n + idx] = s.wdot[k];
         if (p.jac) {
@@ -125,8 +126,8 @@ constexpr int kAuxDoubles = (int)((sizeof(WarpAux) + 7) / 8);
 // division and square root for the integrator's scalar step control, out of line: one copy
 // of their code instead of one per use (the step logic runs once per step, its code size
 // matters more than a call)
-__device__ __noinline__ double ddiv(double a, double b) { return a / b; }
-__device__ __noinline__ double dsqrt(double a) { return sqrt(a); }
+GB_TU_LOCAL __device__ __noinline__ double ddiv(double a, double b) { return a / b; }
+GB_TU_LOCAL __device__ __noinline__ double dsqrt(double a) { return sqrt(a); }
 
 constexpr int kStateSlots = 16;
 static_assert(kKinStateDoubles <= 15, "state slots");
@@ -160,6 +161,7 @@ __device__ __forceinline__ void loadState(const double* base, KinState& st) {
 // reactor right-hand side at z = [T, Y]; returns true when every derivative is finite
 // (with forJac the kinetics scratch also keeps what d(wdot)/dc needs: the right-hand side
 // that precedes a Jacobian evaluation)
+template <bool kX>
 __device__ __noinline__ bool devRhs(const DevMech& m, double* base, const uint64_t* tab, double P,
                                     const double* z, double* zdot, int lane, bool forJac) {
     KinScratch s;
@@ -167,8 +169,8 @@ __device__ __noinline__ bool devRhs(const DevMech& m, double* base, const uint64
     KinState st;
     warpState(m, z[0], P, z + 1, s, st, lane);
     __syncwarp();
-    if (forJac) warpRates<true>(m, s, st, lane);
-    else warpRates<false>(m, s, st, lane);
+    if (forJac) warpRates<true, kX>(m, s, st, lane);
+    else warpRates<false, kX>(m, s, st, lane);
     if (lane == 0) storeState(base, st);
     double ph = 0.0, pc = 0.0;
 #pragma unroll 1
@@ -300,7 +302,7 @@ __device__ __noinline__ bool devLuStaged(MT* M, int N, int ld, int* piv, double*
 // The kinetics scratch must hold the state y (the last right-hand side was evaluated at y,
 // giving ftemp).  kJacOnly: store J (transposed, no identity) and skip the factorisation.
 // Returns false if J is not finite or M singular.
-template <typename MT, bool kJacOnly>
+template <typename MT, bool kJacOnly, bool kX>
 __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uint64_t* tab, MT* A, int ld,
                                       double gamma, double P, const double* y, const double* ftemp,
                                       double* v1, double* v2, double* tempv, int* piv, double* dinv,
@@ -388,7 +390,7 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     __syncwarp();
     if (lane == 0) tempv[0] = T0 + dT;
     __syncwarp();
-    bool ok = devRhs(mm, base, tab, P, tempv, v1, lane, false);
+    bool ok = devRhs<kX>(mm, base, tab, P, tempv, v1, lane, false);
     const double gdT = -gamma / dT;
 #pragma unroll 1
     for (int i = lane; i < N; i += 32) {
@@ -512,6 +514,7 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
 }
 
 
+template <bool kX>
 struct BdfWarp {
     const DevMech* m;
     int N, Nnorm, lane, ld;
@@ -541,7 +544,7 @@ struct BdfWarp {
     }
     __device__ bool rhs(const double* z, double* zdot, BdfScal& S, bool forJac = false) {
         if (lane == 0) aux->nrhs++;
-        return devRhs(*m, base, tab, P, z, zdot, lane, forJac);
+        return devRhs<kX>(*m, base, tab, P, z, zdot, lane, forJac);
     }
     // Linear-solver setup.  With a kept Jacobian, CVODE's policy decides when to evaluate a
     // new one (first step, 51 steps since the last, a convergence failure with a stale one
@@ -553,7 +556,7 @@ struct BdfWarp {
         if (!Jsv) {
             if (lane == 0) { aux->nje++; aux->nsetups++; aux->nrhs++; }   // nrhs: the difference in T
             fresh = true;
-            return devSetup<MT, false>(*m, base, tab, M, ld, S.gamma, P, y, ftemp, v1, v2, tempv, piv, dinv, lane, pool);
+            return devSetup<MT, false, kX>(*m, base, tab, M, ld, S.gamma, P, y, ftemp, v1, v2, tempv, piv, dinv, lane, pool);
         }
         const double dgamma = fabs(ddiv(S.gamma, S.gammap) - 1.0);
         fresh = !S.haveJ || S.nst == 0 || S.nst >= S.nstlj + MSBJ || (convfail == 1 && dgamma < DGMAX_JBAD) ||
@@ -561,7 +564,7 @@ struct BdfWarp {
         if (lane == 0) aux->nsetups++;
         if (fresh) {
             if (lane == 0) { aux->nje++; aux->nrhs++; }
-            const bool ok = devSetup<double, true>(*m, base, tab, Jsv, ld, -1.0, P, y, ftemp, v1, v2, tempv, piv, dinv,
+            const bool ok = devSetup<double, true, kX>(*m, base, tab, Jsv, ld, -1.0, P, y, ftemp, v1, v2, tempv, piv, dinv,
                                                    lane, LuPool{nullptr, nullptr, 0, 0});
             S.nstlj = S.nst;
             S.haveJ = ok;
@@ -1001,7 +1004,7 @@ struct BdfWarp {
     }
 };
 
-template <typename MT, int NS>
+template <typename MT, int NS, bool kX>
 __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     extern __shared__ __align__(128) double smem[];
     __shared__ uint64_t s_tab[kGbxTableWords];
@@ -1014,7 +1017,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     double* base = smem + p.mechSmem / 8 + (size_t)warp * p.warpDoubles;
-    BdfWarp W;
+    BdfWarp<kX> W;
     W.m = &m;
     W.N = m.N;
     W.Nnorm = m.N + 1;
@@ -1149,7 +1152,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
         long long count = 0;
         while (status == ST_OK && S.tn < p.tout) {
             if (count >= p.maxSteps) { status = ST_MAX_STEPS; break; }
-            status = W.step<MT, NS>(M, S);
+            status = W.template step<MT, NS>(M, S);
             count++;
         }
         // output: interpolate to tout (or the last state on failure)
@@ -1194,6 +1197,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
 // =============================================================================
 // Batched reactor right-hand side: one warp per state (grid-stride over states)
 // =============================================================================
+template <bool kX>
 __global__ void __launch_bounds__(256, 1) k_reactor_rhs(RhsParams p) {
     extern __shared__ __align__(128) double smem[];
     __shared__ uint64_t s_tab[kGbxTableWords];
@@ -1214,7 +1218,7 @@ __global__ void __launch_bounds__(256, 1) k_reactor_rhs(RhsParams p) {
 #pragma unroll 1
         for (int k = lane; k < m.K; k += 32) z[1 + k] = p.Y[(size_t)k * p.n + r];
         __syncwarp();
-        devRhs(m, base, s_tab, p.P[r], z, zd, lane, false);
+        devRhs<kX>(m, base, s_tab, p.P[r], z, zd, lane, false);
         if (lane == 0) p.dTdt[r] = zd[0];
 #pragma unroll 1
         for (int k = lane; k < m.K; k += 32) p.dYdt[(size_t)k * p.n + r] = zd[1 + k];
@@ -1222,32 +1226,77 @@ __global__ void __launch_bounds__(256, 1) k_reactor_rhs(RhsParams p) {
     }
 }
 
+template <bool kX>
+cudaError_t launchReactorRhsT(const RhsParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
+    size_t smem = (size_t)p.warpDoubles * 8 * warpsPerBlock;
+    cudaError_t e = cudaFuncSetAttribute(k_reactor_rhs<kX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_reactor_rhs<kX><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+template <typename MT, int NS, bool kX>
+cudaError_t launchBdfT(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
+    size_t smem = (size_t)p.mechSmem + (size_t)p.warpDoubles * 8 * warpsPerBlock +
+                  (size_t)(p.Mbuf ? p.luSlots : 0) * p.luSlotBytes;
+    cudaError_t e = cudaFuncSetAttribute(k_bdf<MT, NS, kX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    // the rest of the SM's 256 KB of L1/shared storage is L1: ask for the smallest carveout
+    // that holds the block (static tables and the per-block reservation included)
+    const int pct = (int)std::min<size_t>(100, ((smem + 4096 + 1024) * 100 + 233471) / 233472);
+    e = cudaFuncSetAttribute(k_bdf<MT, NS, kX>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+    if (e != cudaSuccess) return e;
+    k_bdf<MT, NS, kX><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+template <bool kX>
+cudaError_t launchRatesT(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
+    size_t smem = (size_t)p.mechSmem + (size_t)p.warpDoubles * 8 * warpsPerBlock;
+    cudaError_t e = cudaFuncSetAttribute(k_rates<kX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_rates<kX><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+template <typename MT, int NS, bool kX>
+int bdfBlocksPerSmT(int warpsPerBlock, size_t smem) {
+    int nb = 0;
+    if (cudaFuncSetAttribute(k_bdf<MT, NS, kX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bdf<MT, NS, kX>, 32 * warpsPerBlock, smem) != cudaSuccess)
+        return 1;
+    return nb > 0 ? nb : 1;
+}
+
+#ifdef GB_KERNELS_EXTRA
+// Mechanisms with the less common rate forms (DevMech::NX > 0): their own instantiations
+// (kX), compiled in a module of their own (kernels_x.cu) so that the common instantiations
+// keep their register allocation; the integrator uses the widest register slots (NS = 8,
+// any N).
+cudaError_t launchReactorRhsX(const RhsParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
+    return launchReactorRhsT<true>(p, blocks, warpsPerBlock, stream);
+}
+cudaError_t launchRatesX(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
+    return launchRatesT<true>(p, blocks, warpsPerBlock, stream);
+}
+cudaError_t launchBdfX(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream) {
+    return fp32 ? launchBdfT<float, 8, true>(p, blocks, warpsPerBlock, stream)
+                : launchBdfT<double, 8, true>(p, blocks, warpsPerBlock, stream);
+}
+int bdfBlocksPerSmX(bool fp32, int warpsPerBlock, size_t smem) {
+    return fp32 ? bdfBlocksPerSmT<float, 8, true>(warpsPerBlock, smem)
+                : bdfBlocksPerSmT<double, 8, true>(warpsPerBlock, smem);
+}
+#else
 int rhsWarpDoubles(const DevMech& m) {
     const int tot = kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT) + 2 * m.N;
     return (tot + 1) & ~1;
 }
 
 cudaError_t launchReactorRhs(const RhsParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
-    size_t smem = (size_t)p.warpDoubles * 8 * warpsPerBlock;
-    cudaError_t e = cudaFuncSetAttribute(k_reactor_rhs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k_reactor_rhs<<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
-    return cudaGetLastError();
-}
-
-template <typename MT, int NS>
-cudaError_t launchBdfT(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
-    size_t smem = (size_t)p.mechSmem + (size_t)p.warpDoubles * 8 * warpsPerBlock +
-                  (size_t)(p.Mbuf ? p.luSlots : 0) * p.luSlotBytes;
-    cudaError_t e = cudaFuncSetAttribute(k_bdf<MT, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    // the rest of the SM's 256 KB of L1/shared storage is L1: ask for the smallest carveout
-    // that holds the block (static tables and the per-block reservation included)
-    const int pct = (int)std::min<size_t>(100, ((smem + 4096 + 1024) * 100 + 233471) / 233472);
-    e = cudaFuncSetAttribute(k_bdf<MT, NS>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
-    if (e != cudaSuccess) return e;
-    k_bdf<MT, NS><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
-    return cudaGetLastError();
+    return p.m.NX ? launchReactorRhsX(p, blocks, warpsPerBlock, stream)
+                  : launchReactorRhsT<false>(p, blocks, warpsPerBlock, stream);
 }
 
 int bdfRecordStride(int N) { return (QMAX + 1) * N + R_NSCAL; }
@@ -1276,43 +1325,32 @@ int ratesWarpDoubles(const DevMech& m, bool jac) {
 }
 
 cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
-    size_t smem = (size_t)p.mechSmem + (size_t)p.warpDoubles * 8 * warpsPerBlock;
-    cudaError_t e = cudaFuncSetAttribute(k_rates, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k_rates<<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
-    return cudaGetLastError();
+    return p.m.NX ? launchRatesX(p, blocks, warpsPerBlock, stream)
+                  : launchRatesT<false>(p, blocks, warpsPerBlock, stream);
 }
 
-template <typename MT, int NS>
-int bdfBlocksPerSmT(int warpsPerBlock, size_t smem) {
-    int nb = 0;
-    if (cudaFuncSetAttribute(k_bdf<MT, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bdf<MT, NS>, 32 * warpsPerBlock, smem) != cudaSuccess)
-        return 1;
-    return nb > 0 ? nb : 1;
-}
-
-int bdfBlocksPerSm(int N, bool fp32, int warpsPerBlock, size_t smem) {
+int bdfBlocksPerSm(int N, bool fp32, int warpsPerBlock, size_t smem, bool extra) {
+    if (extra) return bdfBlocksPerSmX(fp32, warpsPerBlock, smem);
     if (fp32) {
-        if (N <= 64) return bdfBlocksPerSmT<float, 2>(warpsPerBlock, smem);
-        if (N <= 128) return bdfBlocksPerSmT<float, 4>(warpsPerBlock, smem);
-        return bdfBlocksPerSmT<float, 8>(warpsPerBlock, smem);
+        if (N <= 64) return bdfBlocksPerSmT<float, 2, false>(warpsPerBlock, smem);
+        if (N <= 128) return bdfBlocksPerSmT<float, 4, false>(warpsPerBlock, smem);
+        return bdfBlocksPerSmT<float, 8, false>(warpsPerBlock, smem);
     }
-    if (N <= 64) return bdfBlocksPerSmT<double, 2>(warpsPerBlock, smem);
-    if (N <= 128) return bdfBlocksPerSmT<double, 4>(warpsPerBlock, smem);
-    return bdfBlocksPerSmT<double, 8>(warpsPerBlock, smem);
+    if (N <= 64) return bdfBlocksPerSmT<double, 2, false>(warpsPerBlock, smem);
+    if (N <= 128) return bdfBlocksPerSmT<double, 4, false>(warpsPerBlock, smem);
+    return bdfBlocksPerSmT<double, 8, false>(warpsPerBlock, smem);
 }
 
 cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream) {
+    if (p.m.NX) return launchBdfX(p, blocks, warpsPerBlock, fp32, stream);
     // register slots of the Newton vector per lane: 32 components each
     const int N = p.m.N;
-    if (N <= 64) return fp32 ? launchBdfT<float, 2>(p, blocks, warpsPerBlock, stream)
-                             : launchBdfT<double, 2>(p, blocks, warpsPerBlock, stream);
-    if (N <= 128) return fp32 ? launchBdfT<float, 4>(p, blocks, warpsPerBlock, stream)
-                              : launchBdfT<double, 4>(p, blocks, warpsPerBlock, stream);
-    return fp32 ? launchBdfT<float, 8>(p, blocks, warpsPerBlock, stream)
-                : launchBdfT<double, 8>(p, blocks, warpsPerBlock, stream);
+    if (N <= 64) return fp32 ? launchBdfT<float, 2, false>(p, blocks, warpsPerBlock, stream)
+                             : launchBdfT<double, 2, false>(p, blocks, warpsPerBlock, stream);
+    if (N <= 128) return fp32 ? launchBdfT<float, 4, false>(p, blocks, warpsPerBlock, stream)
+                              : launchBdfT<double, 4, false>(p, blocks, warpsPerBlock, stream);
+    return fp32 ? launchBdfT<float, 8, false>(p, blocks, warpsPerBlock, stream)
+                : launchBdfT<double, 8, false>(p, blocks, warpsPerBlock, stream);
 }
 
 // -----------------------------------------------------------------------------
@@ -1414,5 +1452,7 @@ cudaError_t measureFp64(double* results, int smCount) {
     results[2] = bestLog;
     return e;
 }
+
+#endif  // GB_KERNELS_EXTRA
 
 }  // namespace gbchem

@@ -77,7 +77,12 @@ int ratesWarpDoubles(const DevMech& m, bool jac);   // dense Jacobian scratch on
 cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
 cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream);
 // resident blocks per SM of the integrator kernel for this launch shape (registers included)
-int bdfBlocksPerSm(int N, bool fp32, int warpsPerBlock, size_t smem);
+int bdfBlocksPerSm(int N, bool fp32, int warpsPerBlock, size_t smem, bool extra);
+// the instantiations for mechanisms with the less common rate forms (kernels_x.cu)
+cudaError_t launchReactorRhsX(const RhsParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
+cudaError_t launchRatesX(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
+cudaError_t launchBdfX(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream);
+int bdfBlocksPerSmX(bool fp32, int warpsPerBlock, size_t smem);
 // FP64 throughput probe: returns {GFLOP/s of FMA, exp cost, log cost in FMA-equivalents}
 cudaError_t measureFp64(double* results, int smCount);
 cudaError_t checkExp(int n, const double* x, double* mine, double* lib);

@@ -10,7 +10,9 @@
 //   Kc and reverse rates      src/kinetics/BulkKinetics.cpp:465-484,562-569
 //   third bodies              include/cantera/kinetics/ThirdBodyCalc.h:75-92
 //   Arrhenius                 include/cantera/kinetics/Arrhenius.h:196-198
-//   falloff                   include/cantera/kinetics/Falloff.h:154-176; src/kinetics/Falloff.cpp:283-300
+//   falloff                   include/cantera/kinetics/Falloff.h:154-176; src/kinetics/Falloff.cpp:283-494
+//   pressure-dependent Arrh.  include/cantera/kinetics/PlogRate.h:110-164
+//   Chebyshev                 include/cantera/kinetics/ChebyshevRate.h:133-171
 //   mass action + sign rules  include/cantera/kinetics/StoichManager.h:131-480
 //   d(wdot)/dc                src/kinetics/BulkKinetics.cpp:712-811; StoichManager.h:164-168,227-236,300-312,406-430
 #pragma once
@@ -211,6 +213,120 @@ __device__ __forceinline__ double falloff(D4 f1, D4 f2, double A, double b, doub
     return k;
 }
 
+// Rate constants of the less common forms, out of line so that the common reactions'
+// instruction stream stays small: pressure-dependent Arrhenius (PLOG), Chebyshev, and the
+// falloff forms SRI, Tsang and chemically activated reactions (with any falloff function).
+// These use the integer-pipe exp / log of fastexp.h (powers as exp(y ln x)).  For falloff
+// forms, *dlnk_dM
+// receives d ln k / d[M] (analytic):
+//   falloff               k = khigh Pr/(1 + Pr) F,  d ln k/d ln Pr = 1/(1 + Pr) + d ln F/d ln Pr
+//   chemically activated  k = klow F/(1 + Pr),      d ln k/d ln Pr = -Pr/(1 + Pr) + d ln F/d ln Pr
+//   Troe / Tsang          d ln F/d ln Pr = -2 log10(Fcent) f/(1 + f^2)^2 n/d^2,  f = u/d
+//   SRI                   d ln F/d ln Pr = -2 ln(X) log10(Pr) x^2 / ln 10,  x = 1/(1 + log10(Pr)^2)
+// (0 where Pr <= 1e-300, where log10 Pr is clamped).
+GB_TU_LOCAL __device__ __noinline__ double rateExtra(const DevMech& m, int4 info, D4 ar, const KinState& st,
+                                         double M, double* dlnk_dM, const uint64_t* tab) {
+    constexpr double kLn10 = 2.302585092994046;
+    const int kind = info.x & kKindMask;
+    if (kind == kKindPlog) {
+        const double* t = m.pdep + info.w;
+        const int nl = (int)t[0];
+        const double lnP = gbx_log(st.P, tab);
+        // upper_bound over the levels: the first one above ln P
+        int hi = 0;
+#pragma unroll 1
+        while (hi < nl && !(t[1 + 3 * hi] > lnP)) hi++;
+        if (hi == 0 || hi == nl) return __longlong_as_double(0x7ff8000000000000LL);
+        const int lo = hi - 1;
+        double lk[2];
+#pragma unroll 1
+        for (int side = 0; side < 2; side++) {
+            const int l = side ? hi : lo;
+            double k = 1e-300;
+            const int q1 = (int)t[3 + 3 * l];
+#pragma unroll 1
+            for (int q = (int)t[2 + 3 * l]; q < q1; q += 3) k += t[q] * fexp(t[q + 1] * st.lnT - t[q + 2] * st.recipT, tab);
+            lk[side] = gbx_log(k, tab);
+        }
+        const double lp1 = t[1 + 3 * lo];
+        const double rDeltaP = 1.0 / (t[1 + 3 * hi] - lp1);
+        return fexp(lk[0] + (lk[1] - lk[0]) * (lnP - lp1) * rDeltaP, tab);
+    }
+    if (kind == kKindCheb) {
+        const double* t = m.pdep + info.w;
+        const int nT = (int)t[0], nP = (int)t[1];
+        const double* c = t + 6;
+        const double Pr = (2 * gbx_log10(st.P, tab) + t[4]) * t[5];
+        const double Tr = (2 * st.recipT + t[2]) * t[3];
+        // per temperature row the pressure series, then the temperature series over rows
+        double logk = 0.0, CTm1 = Tr, CT = 1.0;
+#pragma unroll 1
+        for (int r = 0; r < nT; r++) {
+            double dot = c[r * nP], Cm1 = Pr, C = 1.0;
+#pragma unroll 1
+            for (int j = 1; j < nP; j++) {
+                const double Cp1 = 2 * Pr * C - Cm1;
+                dot += Cp1 * c[r * nP + j];
+                Cm1 = C;
+                C = Cp1;
+            }
+            if (r == 0) {
+                logk = dot;
+            } else {
+                const double CTp1 = 2 * Tr * CT - CTm1;
+                logk += CTp1 * dot;
+                CTm1 = CT;
+                CT = CTp1;
+            }
+        }
+        return fexp(logk * kLn10, tab);
+    }
+    // falloff forms
+    const D4 f1 = m.fo1[info.z], f2 = m.fo2[info.z];
+    const double T = st.T;
+    const double klow = f1.x * fexp(f1.y * st.lnT - f1.z * st.recipT, tab);
+    const double khigh = ar.x * fexp(ar.y * st.lnT - ar.z * st.recipT, tab);
+    const double pr = M * (klow / (khigh + 1e-300));
+    const bool live = pr > 1e-300;
+    const double lpr = gbx_log10(fmax(pr, 1e-300), tab);
+    double F = 1.0, dlnF = 0.0;
+    if (kind == kKindTroe || kind == kKindTsang) {
+        double Fcent;
+        if (kind == kKindTroe) {
+            Fcent = (1.0 - f1.w) * fexp(-T * f2.x, tab) + f1.w * fexp(-T * f2.y, tab);
+            if (f2.z != 0.0) Fcent += fexp(-f2.z / T, tab);
+        } else {
+            Fcent = f1.w + (f2.x * T);
+        }
+        const double lfc = gbx_log10(fmax(Fcent, 1e-300), tab);
+        const double cc = -0.4 - 0.67 * lfc, nn = 0.75 - 1.27 * lfc;
+        const double u = lpr + cc, d = nn - 0.14 * u;
+        const double f = u / d, q = 1.0 + f * f;
+        F = fexp(lfc / q * kLn10, tab);
+        if (live) dlnF = -lfc * 2.0 * f / (q * q) * (nn / (d * d));
+    } else if (kind == kKindSri) {
+        double X = f1.w * fexp(-f2.x / T, tab);
+        if (f2.y != 0.0) X += fexp(-T / f2.y, tab);
+        const double xx = 1.0 / (1.0 + lpr * lpr);
+        // X^xx (X > 0; 0 for X = 0) times d T^e
+        const double lnX = X > 0.0 ? gbx_log(X, tab) : -INFINITY;
+        F = (X > 0.0 ? fexp(xx * lnX, tab) : (X == 0.0 ? 0.0 : __longlong_as_double(0x7ff8000000000000LL))) *
+            (f2.z * fexp(f2.w * st.lnT, tab));
+        if (live) dlnF = lnX * (-2.0 * lpr * xx * xx) / kLn10;
+    }
+    const double s1 = 1.0 / (1.0 + pr);
+    double k, dl;
+    if (info.x & kChemActBit) {
+        k = (F * s1) * klow;
+        dl = -pr * s1 + dlnF;
+    } else {
+        k = (pr * (F * s1)) * khigh;
+        dl = s1 + dlnF;
+    }
+    if (dlnk_dM) *dlnk_dM = dl / M;
+    return k;
+}
+
 // Mixture state from (T, P, Y).  Y may alias any readable [K] array.
 // The per-state reciprocals and logarithms are evaluated once for the whole warp, one
 // argument per lane (1/T, 1/sum(Y/W), 1/RT, 1/P and ln T, ln P, ln RT, ln Pref), then
@@ -256,8 +372,9 @@ __device__ __forceinline__ void warpState(const DevMech& m, double T, double P, 
 }
 
 // Species thermo + rates of progress + net production rates.  With `forJac`, also the
-// per-reaction data d(wdot)/dc needs (Qtb, dlk).
-template <bool forJac>
+// per-reaction data d(wdot)/dc needs (Qtb, dlk).  kX: the mechanism has reactions of the
+// less common forms (rateExtra); without it, such reactions must not occur.
+template <bool forJac, bool kX = false>
 __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, int lane) {
     const double lnPP = st.lnPP;
     if (lane == 0) s.flags[0] = 0;
@@ -325,7 +442,8 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
         double dlnk = 0.0;
         if (kind <= 1) {
             kf = (info.x & kNoExpBit) ? ar.x : arrhenius(ar.x, ar.y, ar.z, st.lnT, st.recipT, s.tab);
-        } else {
+        } else if (!kX) {
+            // Lindemann / Troe falloff (the only other forms without kX)
             D4 f1 = m.fo1[info.z];
             D4 f2 = m.fo2[info.z];
             double M = s.Mtb[info.y];
@@ -333,6 +451,19 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
             // the reference sets this derivative to zero unless k != 0 and [M] > 0
             if (!(M > 0.0) || kf == 0.0) dlnk = 0.0;
             if (forJac) s.dlk[info.z] = dlnk;
+        } else {
+            const double M = info.y >= 0 ? s.Mtb[info.y] : 0.0;
+            if (kind <= kKindTroe && !(info.x & kChemActBit)) {
+                D4 f1 = m.fo1[info.z];
+                D4 f2 = m.fo2[info.z];
+                kf = falloff(f1, f2, ar.x, ar.y, ar.z, st, M, forJac ? &dlnk : nullptr, s.tab);
+            } else {
+                kf = rateExtra(m, info, ar, st, M, forJac ? &dlnk : nullptr, s.tab);
+            }
+            if (info.z >= 0) {
+                if (!(M > 0.0) || kf == 0.0) dlnk = 0.0;
+                if (forJac) s.dlk[info.z] = dlnk;
+            }
         }
         double kfe = (kind == 1) ? kf * s.Mtb[info.y] : kf;
         int rb = (info.x >> kRBucketShift) & 7, pb = (info.x >> kPBucketShift) & 7;
@@ -389,7 +520,7 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
             s.kfe[i] = kfe;
             s.rkc[i] = rkc;
             if (kind == 1) s.Qtb[info.y] = kf * (fwd - rkc * rev);
-            else if (kind >= 2) s.Qtb[info.y] = kf * dlnk * (fwd - rkc * rev);
+            else if (kX ? info.z >= 0 : kind >= 2) s.Qtb[info.y] = kf * dlnk * (fwd - rkc * rev);
         }
     }
     __syncwarp();

@@ -26,7 +26,12 @@ enum RateKind : int32_t {
     kThreeBody = 1,        // Arrhenius, rate of progress multiplied by [M]
     kLindemann = 2,        // falloff, F = 1
     kTroe = 3,             // falloff, Troe F(Pr, T)
+    kPlog = 4,             // pressure-dependent Arrhenius: ln k interpolated linearly in ln P
+    kChebyshev = 5,        // log10 k = Chebyshev series in reduced 1/T and log10 P
+    kSri = 6,              // falloff, SRI F(Pr, T)
+    kTsang = 7,            // falloff, Tsang F(Pr, T) (the Troe form with Fcent = a + b T)
 };
+inline bool isFalloffKind(int k) { return k == kLindemann || k == kTroe || k == kSri || k == kTsang; }
 
 // Stoichiometry bucket of one side of a reaction (reference StoichManager.h:676-722):
 // C1/C2/C3 when every coefficient equals its order, is integral and at most three
@@ -60,6 +65,26 @@ struct Mechanism {
     std::vector<double> A, b, EaR;           // [R] high-pressure (or only) Arrhenius
     std::vector<double> A0, b0, Ea0R;        // [R] low-pressure Arrhenius (falloff only)
     std::vector<double> troe;                // [R][4] a, 1/T3, 1/T1, T2 (Troe only)
+    std::vector<double> falloffX;            // [R][5] SRI a, b, c, d, e; Tsang a, b
+    std::vector<int32_t> chemAct;            // [R] 1: chemically-activated falloff, k = klow F / (1 + Pr)
+
+    // Pressure-dependent Arrhenius (PlogRate::setRates, reference src/kinetics/PlogRate.cpp:
+    // 91-120): reaction i has pressure levels plogPtr[i] .. plogPtr[i+1], ascending in ln P
+    // and bracketed by the reference's sentinels at ln P = -1000 and +1000 (copies of the
+    // first and last level); level l holds the Arrhenius expressions plogFirst[l] ..
+    // plogLast[l] of the rate tables, summed at evaluation.
+    std::vector<int32_t> plogPtr;            // [R+1]
+    std::vector<double> plogLogP;            // [levels]
+    std::vector<int32_t> plogFirst, plogLast;   // [levels]
+    std::vector<double> plogA, plogB, plogEaR;  // [rates]
+
+    // Chebyshev (ChebyshevRate::setLimits / setData, reference src/kinetics/ChebyshevRate.cpp:
+    // 64-118): nT x nP coefficients, row-major (temperature index first), with the unit
+    // offset log10(conversion factor) already added to the (0, 0) coefficient.
+    std::vector<int32_t> chebPtr;            // [R+1] into chebCoef
+    std::vector<int32_t> chebNT, chebNP;     // [R]
+    std::vector<double> chebLim;             // [R][4] TrNum, TrDen, PrNum, PrDen
+    std::vector<double> chebCoef;
 
     // Third bodies, in installation order (reference ThirdBodyCalc.h:23-45).
     std::vector<int32_t> tbOfRxn;            // [R] index into the tables below or -1
@@ -89,7 +114,13 @@ struct Mechanism {
 
 // Load phase `phase` (empty: the first phase) of a Cantera YAML mechanism.
 // Throws std::runtime_error with a message naming the file and line on failure.
+// Sections named "file.yaml/section" are looked up next to the including file, then in
+// the working directory, then in the data directories (addDataDirectory).
 Mechanism loadMechanism(const std::string& path, const std::string& phase);
+
+// Add a directory to the search path for mechanism files referenced by other files
+// (Application::addDataDirectory, reference src/base/application.cpp:286).
+void addDataDirectory(const std::string& dir);
 
 // Mass fractions of the mixture with equivalence ratio phi of fuel and oxidizer given
 // as mole fractions [K] (ThermoPhase::setEquivalenceRatio with the molar basis,

@@ -369,6 +369,31 @@ std::vector<LLine> logicalLines(const std::string& src) {
             bal = bracketBalance(body);
         }
         if (bal != 0) throw YamlError("YAML line " + std::to_string(i + 1) + ": unbalanced brackets");
+        // a plain scalar value continues on following lines indented deeper than its key
+        // (or than its "-"), folded with single spaces
+        {
+            std::string b2 = body;
+            int keyCol = ind;
+            if (b2.size() >= 2 && b2[0] == '-' && b2[1] == ' ') {
+                size_t off = b2.find_first_not_of(' ', 1);
+                if (off != std::string::npos) {
+                    keyCol = ind + (int)off;
+                    b2 = b2.substr(off);
+                }
+            }
+            size_t ks = findKeySep(b2);
+            std::string v = trim(ks != std::string::npos ? b2.substr(ks + 1) : b2);
+            const int limit = ks != std::string::npos ? keyCol : ind;
+            bool plain = !v.empty() && std::string("[{\"'&*!|>").find(v[0]) == std::string::npos;
+            if (plain && j == i) {
+                while (j + 1 < raw.size()) {
+                    std::string c = rtrim(stripComment(raw[j + 1]));
+                    if (trim(c).empty() || indentOf(c) <= limit) break;
+                    body += " " + trim(c);
+                    j++;
+                }
+            }
+        }
         LLine L{ind, body, (int)i + 1};
         out.push_back(L);
         // block scalar indicator at the end of "key: |" or "- |"

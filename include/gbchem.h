@@ -29,9 +29,15 @@ extern "C" {
 
 /* ---- mechanisms -------------------------------------------------------------------
  * gb_mech_load replaces newSolution(yaml, phase, "none") (src/base/Solution.cpp:242-330)
- * for ideal-gas phases with NASA7 thermo and elementary / three-body / Lindemann / Troe
- * reactions.  Returns a handle >= 0 or GB_ERR. */
+ * for ideal-gas phases with NASA7 thermo and elementary, three-body, falloff (Lindemann,
+ * Troe, SRI, Tsang; falloff or chemically activated), pressure-dependent Arrhenius (PLOG)
+ * and Chebyshev reactions.  Returns a handle >= 0 or GB_ERR. */
 int32_t gb_mech_load(const char* yaml_path, const char* phase_name);
+/* Adds a directory to the search path of files that a mechanism references
+ * ("gri30.yaml/species"): CLib ct_addDataDirectory (interfaces/sourcegen/src/sourcegen/
+ * headers/ct.yaml:12, Application::addDataDirectory, src/base/application.cpp:286).
+ * Returns 0. */
+int32_t gb_add_data_directory(const char* dir);
 int32_t gb_mech_del(int32_t mech);
 int32_t gb_mech_n_species(int32_t mech);                  /* Kinetics::nTotalSpecies */
 int32_t gb_mech_n_reactions(int32_t mech);                /* Kinetics::nReactions */

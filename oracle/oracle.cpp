@@ -206,62 +206,137 @@ double arrhenius(double A, double b, double EaR, double logT, double recipT) {
     return A * std::exp(b * logT - EaR * recipT);
 }
 
-// FalloffRate::evalFromStruct with an explicit third-body concentration
-double falloffRate(const Mechanism& m, int i, double T, double logT, double recipT, double M) {
-    double work = 0.0;
-    const double* tr = &m.troe[4 * i];
+// Temperature-dependent part of a falloff function (the updateTemp methods):
+// Troe (reference src/kinetics/Falloff.cpp:283-290), SRI (:392-399), Tsang (:479-483).
+void falloffWork(const Mechanism& m, int i, double T, double* work) {
+    work[0] = 0.0;
+    work[1] = 1.0;
     if (m.kind[i] == kTroe) {
+        const double* tr = &m.troe[4 * i];
         double Fcent = (1.0 - tr[0]) * std::exp(-T * tr[1]) + tr[0] * std::exp(-T * tr[2]);
         if (tr[3] != 0.0) Fcent += std::exp(-tr[3] / T);
-        work = std::log10(std::max(Fcent, kSmallNumber));
+        work[0] = std::log10(std::max(Fcent, kSmallNumber));
+    } else if (m.kind[i] == kSri) {
+        const double* x = &m.falloffX[5 * i];
+        work[0] = x[0] * std::exp(-x[1] / T);
+        if (x[2] != 0.0) work[0] += std::exp(-T / x[2]);
+        work[1] = x[3] * std::pow(T, x[4]);
+    } else if (m.kind[i] == kTsang) {
+        const double* x = &m.falloffX[5 * i];
+        double Fcent = x[0] + (x[1] * T);
+        work[0] = std::log10(std::max(Fcent, kSmallNumber));
     }
+}
+
+// Falloff function F(Pr) (the F methods: Troe Falloff.cpp:292-300, SRI :401-406, Tsang
+// :485-494) and, if dlnF is given, d ln F / d ln Pr (analytic; 0 where Pr <= 1e-300, where
+// the reference clamps log10 Pr).
+double falloffF(const Mechanism& m, int i, double pr, const double* work, double* dlnF) {
+    if (dlnF) *dlnF = 0.0;
+    const int kind = m.kind[i];
+    if (kind == kTroe || kind == kTsang) {
+        double lpr = std::log10(std::max(pr, kSmallNumber));
+        double cc = -0.4 - 0.67 * work[0];
+        double nn = 0.75 - 1.27 * work[0];
+        double f1 = (lpr + cc) / (nn - 0.14 * (lpr + cc));
+        double lgf = work[0] / (1.0 + f1 * f1);
+        if (dlnF && pr > kSmallNumber) {
+            double u = lpr + cc, den = nn - 0.14 * u, q = 1.0 + f1 * f1;
+            *dlnF = -work[0] * 2.0 * f1 / (q * q) * (nn / (den * den));   // ln 10 factors cancel
+        }
+        return std::pow(10.0, lgf);
+    }
+    if (kind == kSri) {
+        double lpr = std::log10(std::max(pr, kSmallNumber));
+        double xx = 1.0 / (1.0 + lpr * lpr);
+        if (dlnF && pr > kSmallNumber) *dlnF = std::log(work[0]) * (-2.0 * lpr * xx * xx) / std::log(10.0);
+        return std::pow(work[0], xx) * work[1];
+    }
+    return 1.0;
+}
+
+// FalloffRate::evalFromStruct with an explicit third-body concentration (reference
+// include/cantera/kinetics/Falloff.h:154-176): falloff k = khigh Pr/(1+Pr) F, chemically
+// activated k = klow F/(1+Pr).
+double falloffRate(const Mechanism& m, int i, double T, double logT, double recipT, double M) {
+    double work[2];
+    falloffWork(m, i, T, work);
     double klow = arrhenius(m.A0[i], m.b0[i], m.Ea0R[i], logT, recipT);
     double khigh = arrhenius(m.A[i], m.b[i], m.EaR[i], logT, recipT);
     double pr = M * klow / (khigh + kSmallNumber);
-    double F = 1.0;
-    if (m.kind[i] == kTroe) {
-        double lpr = std::log10(std::max(pr, kSmallNumber));
-        double cc = -0.4 - 0.67 * work;
-        double nn = 0.75 - 1.27 * work;
-        double f1 = (lpr + cc) / (nn - 0.14 * (lpr + cc));
-        double lgf = work / (1.0 + f1 * f1);
-        F = std::pow(10.0, lgf);
+    if (m.chemAct[i]) {
+        pr = falloffF(m, i, pr, work, nullptr) / (1.0 + pr);
+        return pr * klow;
     }
-    pr *= F / (1.0 + pr);
+    pr *= falloffF(m, i, pr, work, nullptr) / (1.0 + pr);
     return pr * khigh;
 }
 
 // Analytic d k / d[M] of a falloff rate (k as above).
 double falloffRate_dM(const Mechanism& m, int i, double T, double logT, double recipT, double M) {
-    double work = 0.0;
-    const double* tr = &m.troe[4 * i];
-    if (m.kind[i] == kTroe) {
-        double Fcent = (1.0 - tr[0]) * std::exp(-T * tr[1]) + tr[0] * std::exp(-T * tr[2]);
-        if (tr[3] != 0.0) Fcent += std::exp(-tr[3] / T);
-        work = std::log10(std::max(Fcent, kSmallNumber));
-    }
+    double work[2];
+    falloffWork(m, i, T, work);
     double klow = arrhenius(m.A0[i], m.b0[i], m.Ea0R[i], logT, recipT);
     double khigh = arrhenius(m.A[i], m.b[i], m.EaR[i], logT, recipT);
     double dPr_dM = klow / (khigh + kSmallNumber);
     double pr = M * dPr_dM;
-    double F = 1.0, dF_dPr = 0.0;
-    if (m.kind[i] == kTroe) {
-        double lpr = std::log10(std::max(pr, kSmallNumber));
-        double cc = -0.4 - 0.67 * work;
-        double nn = 0.75 - 1.27 * work;
-        double u = lpr + cc;
-        double den = nn - 0.14 * u;
-        double f1 = u / den;
-        double q = 1.0 + f1 * f1;
-        double lgf = work / q;
-        F = std::pow(10.0, lgf);
-        if (pr > kSmallNumber) {
-            double dlgf_dlpr = -work * 2.0 * f1 / (q * q) * (nn / (den * den));
-            dF_dPr = F * dlgf_dlpr / pr;   // ln10 factors cancel
-        }
-    }
+    double dlnF = 0.0;
+    double F = falloffF(m, i, pr, work, &dlnF);
+    double dF_dPr = pr > kSmallNumber ? F * dlnF / pr : 0.0;
     double s = 1.0 / (1.0 + pr);
+    if (m.chemAct[i]) return klow * (dF_dPr * s - F * s * s) * dPr_dM;
     return khigh * (s * s * F + pr * s * dF_dPr) * dPr_dM;
+}
+
+// PlogRate::updateFromStruct / evalFromStruct (reference include/cantera/kinetics/
+// PlogRate.h:110-164): the pressure interval by upper_bound over the levels (with the
+// +-1000 sentinels), ln k of each bracketing level from its summed Arrhenius expressions
+// (plus 1e-300), interpolated linearly in ln P.
+double plogRate(const Mechanism& m, int i, double logP, double logT, double recipT) {
+    const int l0 = m.plogPtr[i], l1 = m.plogPtr[i + 1];
+    int hi = l0;
+    while (hi < l1 && !(m.plogLogP[hi] > logP)) hi++;
+    if (hi == l0 || hi == l1) return NAN;   // outside (-1000, 1000): the reference throws
+    const int lo = hi - 1;
+    auto logk = [&](int l) {
+        double k = 1e-300;
+        for (int q = m.plogFirst[l]; q < m.plogLast[l]; q++)
+            k += m.plogA[q] * std::exp(m.plogB[q] * logT - m.plogEaR[q] * recipT);
+        return std::log(k);
+    };
+    const double lk1 = logk(lo), lk2 = logk(hi);
+    const double rDeltaP = 1.0 / (m.plogLogP[hi] - m.plogLogP[lo]);
+    return std::exp(lk1 + (lk2 - lk1) * (logP - m.plogLogP[lo]) * rDeltaP);
+}
+
+// ChebyshevRate::updateFromStruct / evalFromStruct (reference include/cantera/kinetics/
+// ChebyshevRate.h:133-171): the pressure series first (one dot product per temperature
+// row), then the temperature series; k = 10^(log10 k).
+double chebRate(const Mechanism& m, int i, double log10P, double recipT) {
+    const int nT = m.chebNT[i], nP = m.chebNP[i];
+    const double* c = &m.chebCoef[m.chebPtr[i]];
+    const double* lim = &m.chebLim[4 * i];
+    std::vector<double> dot(nT);
+    const double Pr = (2 * log10P + lim[2]) * lim[3];
+    double Cnm1 = Pr, Cn = 1, Cnp1;
+    for (int t = 0; t < nT; t++) dot[t] = c[t * nP];
+    for (int j = 1; j < nP; j++) {
+        Cnp1 = 2 * Pr * Cn - Cnm1;
+        for (int t = 0; t < nT; t++) dot[t] += Cnp1 * c[t * nP + j];
+        Cnm1 = Cn;
+        Cn = Cnp1;
+    }
+    const double Tr = (2 * recipT + lim[0]) * lim[1];
+    Cnm1 = Tr;
+    Cn = 1;
+    double logk = dot[0];
+    for (int t = 1; t < nT; t++) {
+        Cnp1 = 2 * Tr * Cn - Cnm1;
+        logk += Cnp1 * dot[t];
+        Cnm1 = Cn;
+        Cn = Cnp1;
+    }
+    return std::pow(10, logk);
 }
 
 // BulkKinetics::updateROP + Kinetics::getNetProductionRates
@@ -292,6 +367,10 @@ void updateROP(const Kin& kn, Work& w) {
     for (int i = 0; i < R; i++) {
         if (m.kind[i] == kArrhenius || m.kind[i] == kThreeBody)
             w.kf0[i] = arrhenius(m.A[i], m.b[i], m.EaR[i], w.logT, w.recipT);
+        else if (m.kind[i] == kPlog)
+            w.kf0[i] = plogRate(m, i, std::log(w.P), w.logT, w.recipT);
+        else if (m.kind[i] == kChebyshev)
+            w.kf0[i] = chebRate(m, i, std::log10(w.P), w.recipT);
         else
             w.kf0[i] = falloffRate(m, i, w.T, w.logT, w.recipT, w.concm[i]);
     }
@@ -341,7 +420,7 @@ void accumulateCompDeriv(const Kin& kn, Work& w, const StoichMgr& sm, const std:
     sm.multiply(w.c.data(), outV.data());
     const double deltaM = 1e-8;
     for (int i = 0; i < R; i++) {
-        if (m.kind[i] != kLindemann && m.kind[i] != kTroe) continue;
+        if (!isFalloffKind(m.kind[i])) continue;
         double M = w.concm[i];
         if (mode == 0) {
             double Mp = M * (1. + deltaM);
@@ -1152,6 +1231,10 @@ int runReactor(const Kin* kn, double T0, double P, const double* Y0, double t_en
 extern "C" {
 
 const char* or_last_error(void) { return g_err.c_str(); }
+
+void or_add_data_directory(const char* dir) {
+    if (dir) addDataDirectory(dir);
+}
 
 int32_t or_mech_load(const char* path, const char* phase) {
     try {

@@ -9,7 +9,10 @@
 //   * rates of progress + wdot       src/kinetics/BulkKinetics.cpp:457-545; src/kinetics/Kinetics.cpp:408-418,447-457
 //   * stoichiometry managers         include/cantera/kinetics/StoichManager.h:131-480,725-797
 //   * third bodies                   include/cantera/kinetics/ThirdBodyCalc.h:47-100
-//   * falloff (Lindemann / Troe)     include/cantera/kinetics/Falloff.h:154-176; src/kinetics/Falloff.cpp:283-300
+//   * falloff (Lindemann / Troe / SRI / Tsang, falloff and chemically activated)
+//                                    include/cantera/kinetics/Falloff.h:154-176; src/kinetics/Falloff.cpp:283-494
+//   * pressure-dependent Arrhenius   include/cantera/kinetics/PlogRate.h:110-164
+//   * Chebyshev                       include/cantera/kinetics/ChebyshevRate.h:133-171
 //   * d(wdot)/d(c)                   src/kinetics/BulkKinetics.cpp:712-811; include/cantera/kinetics/MultiRate.h:135-165
 //   * const-pressure reactor RHS     src/zeroD/IdealGasConstPressureReactor.cpp:34-110; src/zeroD/ReactorNet.cpp:617-635
 //   * integrator                      SUNDIALS CVODES 7.5 (not vendored in the reference: ext/sundials is an
@@ -24,7 +27,9 @@
 // The reference itself cannot be built in this environment (SUNDIALS, Eigen, yaml-cpp and
 // fmt submodules are empty), so parity is pinned by the reference's blessed outputs
 // (test_problems/cxx_samples/kin1_blessed.csv, opmenmp_ignition_blessed.txt) and the
-// known-answer tests in test/thermo/nasapoly.cpp.
+// known-answer tests in test/thermo/nasapoly.cpp, test/kinetics/pdep.cpp (PLOG and Chebyshev
+// rate constants and rates of progress) and test/python/test_kinetics.py (chemically
+// activated rates of progress).
 #pragma once
 #include <stdint.h>
 
@@ -52,6 +57,7 @@ enum { OR_ST_STEPS = 0, OR_ST_RHS, OR_ST_NEWTON, OR_ST_SETUPS, OR_ST_JACS, OR_ST
        OR_ST_CONVFAIL, OR_ST_ORDER, OR_ST_STATUS, OR_NSTAT };
 
 int32_t or_mech_load(const char* path, const char* phase);      // handle >= 0, or -1
+void or_add_data_directory(const char* dir);                     // search path of referenced files
 int32_t or_mech_sizes(int32_t h, int32_t* K, int32_t* R);
 const char* or_last_error(void);
 int32_t or_species_index(int32_t h, const char* name);

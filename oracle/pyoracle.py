@@ -84,6 +84,9 @@ def lib():
         L.or_mole_to_mass.argtypes = [I32, D, D]
         L.or_molecular_weights.argtypes = [I32, D]
         L.or_species_index.argtypes = [I32, ctypes.c_char_p]
+        L.or_add_data_directory.argtypes = [ctypes.c_char_p]
+        # files that other mechanism files reference (e.g. "gri30.yaml/species")
+        L.or_add_data_directory(os.path.join(ROOT, "cantera_gb300", "data").encode())
         _lib = L
     return _lib
 

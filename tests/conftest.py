@@ -9,8 +9,14 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 DATA = os.path.join(ROOT, "cantera_gb300", "data")
+GOLDEN = os.path.join(ROOT, "tests", "golden")
 MECHS = {"h2o2": ("h2o2.yaml", "ohmech"), "gri30": ("gri30.yaml", "gri30"),
-         "nDodecane": ("nDodecane_Reitz.yaml", "nDodecane_IG")}
+         "nDodecane": ("nDodecane_Reitz.yaml", "nDodecane_IG"),
+         # the reference's test mechanisms for the less common rate forms (tests/golden)
+         "pdep": (os.path.join(GOLDEN, "pdep-test.yaml"), "gas"),
+         "chemact": (os.path.join(GOLDEN, "chemically-activated-reaction.yaml"), "gas"),
+         "sri": (os.path.join(GOLDEN, "sri-falloff.yaml"), "gas"),
+         "tsang": (os.path.join(GOLDEN, "tsang-falloff.yaml"), "gas")}
 
 
 def pytest_configure(config):

@@ -8,12 +8,101 @@ Sources (paths inside the reference project):
   * test_problems/cxx_samples/opmenmp_ignition_blessed.txt - gri30 ignition delays
     (samples/cxx/openmp_ignition/openmp_ignition.cpp)
   * test/thermo/nasapoly.cpp - NASA7 CO2 coefficients and CHEMKIN-II known answers
+  * test/kinetics/pdep.cpp - PLOG and Chebyshev rate constants and rates of progress
+    (mechanism test/data/pdep-test.yaml, copied next to this script)
+  * test/python/test_kinetics.py (TestChemicallyActivated) - chemically activated rates of
+    progress (mechanism test/data/chemically-activated-reaction.yaml, copied)
+  * test/data/sri-falloff.yaml, test/data/tsang-falloff.yaml - SRI and Tsang falloff
+    mechanisms (copied; no numeric answers in the reference's tests)
 """
+import ast
 import csv
 import json
+import math
 import os
 import re
+import shutil
 import sys
+
+AVOGADRO = 6.02214076e26                              # 1/kmol (ct_defs.h)
+GAS_CONST_CAL = AVOGADRO * 1.380649e-23 / 4184.0      # cal/mol/K (GasConst_cal_mol_K)
+HERE = os.path.dirname(os.path.abspath(__file__))
+MECH_FILES = ["pdep-test.yaml", "chemically-activated-reaction.yaml", "sri-falloff.yaml",
+              "tsang-falloff.yaml"]
+
+
+def _num(expr, env=None):
+    """Evaluate a numeric C++/Python expression of the tests (numbers, + - * /, names in env)."""
+    env = dict(env or {})
+    tree = ast.parse(expr.strip(), mode="eval")
+
+    def ev(n):
+        if isinstance(n, ast.Expression):
+            return ev(n.body)
+        if isinstance(n, ast.Constant):
+            return float(n.value)
+        if isinstance(n, ast.UnaryOp) and isinstance(n.op, ast.USub):
+            return -ev(n.operand)
+        if isinstance(n, ast.BinOp):
+            a, b = ev(n.left), ev(n.right)
+            return {ast.Add: a + b, ast.Sub: a - b, ast.Mult: a * b, ast.Div: a / b if b else math.inf}[type(n.op)]
+        if isinstance(n, ast.Name):
+            return env[n.id]
+        if isinstance(n, ast.Call) and isinstance(n.func, ast.Name):
+            return env[n.func.id](*[ev(a) for a in n.args])
+        raise ValueError("unsupported expression: " + expr)
+    return ev(tree)
+
+
+def pdep_cases(src):
+    """One case per EXPECT_NEAR of test/kinetics/pdep.cpp: the state (T, P) set before it,
+    the compared quantity (kf or ropf, reaction index) and the expected value with its
+    absolute tolerance; the molec-vs-mol checks become ratio cases."""
+    cases = []
+    for name, body in re.findall(r"TEST_F\(PdepTest, (\w+)\)\s*\{(.*?)\n\}", src, re.S):
+        T = P = None
+        local = {}
+        for stmt in re.split(r";", body):
+            stmt = " ".join(stmt.split())
+            m = re.search(r"set_TP\((.*),(.*)\)", stmt)
+            if m:
+                T, P = _num(m.group(1)), _num(m.group(2))
+                continue
+            env = {"Avogadro": AVOGADRO,
+                   "k": lambda A, n, Ea, T=T: A * T ** n * math.exp(-Ea / (GAS_CONST_CAL * T))}
+            m = re.search(r"double (kf\d) = (.*)", stmt)
+            if m:
+                local[m.group(1)] = _num(m.group(2), env)
+                continue
+            m = re.search(r"EXPECT_NEAR\((.*?), (.*?), (.*)\)$", stmt)
+            if not m:
+                continue
+            a, b, tol = m.groups()
+            env.update(local)
+            q = re.match(r"(kf|ropf)\[(\d)\]$", b)
+            if q:
+                cases.append({"test": name, "T": T, "P": P, "quantity": q.group(1), "index": int(q.group(2)),
+                              "expected": _num(a, env), "tol": _num(tol, env)})
+                continue
+            r = re.match(r"kf\[(\d)\]/\(Avogadro\*1e-3\)$", b)
+            qa = re.match(r"kf\[(\d)\]$", a)
+            if r and qa:
+                cases.append({"test": name, "T": T, "P": P, "quantity": "kf_ratio", "index": int(qa.group(1)),
+                              "other": int(r.group(1)), "factor": AVOGADRO * 1e-3, "tol": _num(tol, env)})
+                continue
+            raise ValueError("unparsed check in %s: %s" % (name, stmt))
+    m = re.search(r'string Xref = "([^"]*)"', src)
+    return {"X": m.group(1), "cases": cases}
+
+
+def chemact_cases(src):
+    block = src[src.index("class TestChemicallyActivated"):]
+    block = block[:block.index("\nclass ", 10)]
+    P = ast.literal_eval(re.search(r"P = (\[[^\]]*\])", block).group(1))
+    Rf = ast.literal_eval(re.search(r"Rf = (\[[^\]]*\])", block).group(1))
+    m = re.search(r"gas.TPX = ([\d.]+), P\[i\], (\[[^\]]*\])", block)
+    rel = float(re.search(r"rel=([\d.e-]+)", block).group(1))
+    return {"T": float(m.group(1)), "X": ast.literal_eval(m.group(2)), "P": P, "ropf": Rf, "rel": rel}
 
 
 def main(ref):
@@ -39,7 +128,11 @@ def main(ref):
         for val, name, tol in re.findall(r"EXPECT_NEAR\(([-\d.e+]+), (\w+), ([\d.e-]+)\)", block[1]):
             checks.append([T, name, float(val), float(tol)])
     out["nasa7"] = {"coeffs_low": coeffs, "Tmin": 200.0, "Tmax": 1000.0, "checks": checks}
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "goldens.json")
+    out["pdep"] = pdep_cases(open(os.path.join(ref, "test/kinetics/pdep.cpp")).read())
+    out["chemact"] = chemact_cases(open(os.path.join(ref, "test/python/test_kinetics.py")).read())
+    for f in MECH_FILES:
+        shutil.copyfile(os.path.join(ref, "test/data", f), os.path.join(HERE, f))
+    path = os.path.join(HERE, "goldens.json")
     json.dump(out, open(path, "w"), indent=1)
     print("wrote", path)
 
