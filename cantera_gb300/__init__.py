@@ -203,10 +203,12 @@ class Solution:
 
     def equivalence_ratio_mass_fractions(self, phi, fuel, oxidizer):
         """Mass fractions of the fuel/oxidizer mixture with equivalence ratio phi
-        (``ThermoPhase.set_equivalence_ratio(phi, fuel, oxidizer)``, molar basis)."""
+        (``ThermoPhase.set_equivalence_ratio(phi, fuel, oxidizer)``, molar basis); fuel and
+        oxidizer as 'A:1, B:2' strings or mole-fraction arrays over the species."""
         Y = np.zeros(self.n_species)
-        f = np.ascontiguousarray(self.composition(fuel))
-        o = np.ascontiguousarray(self.composition(oxidizer))
+        comp = lambda c: self.composition(c) if isinstance(c, str) else np.asarray(c, dtype=np.float64)
+        f = np.ascontiguousarray(comp(fuel))
+        o = np.ascontiguousarray(comp(oxidizer))
         _check(library().gb_mech_equivalence_ratio(self._h, float(phi), _ptr(f), _ptr(o),
                                                    self.n_species, _ptr(Y)))
         return Y

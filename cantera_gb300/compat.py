@@ -1,0 +1,380 @@
+"""A ``cantera``-shaped facade over the engine, for scripts written against the reference.
+
+    import cantera_gb300.compat as ct
+
+    gas = ct.Solution("gri30.yaml")
+    gas.TPX = 1200.0, ct.one_atm, "CH4:1, O2:2, N2:7.52"
+    wdot = gas.net_production_rates                 # this state, kmol/m^3/s
+    reactors = []
+    for T in (1000.0, 1100.0, 1200.0):
+        gas.TP = T, ct.one_atm
+        reactors.append(ct.IdealGasConstPressureReactor(gas))
+    net = ct.ReactorNet(reactors)
+    net.rtol, net.atol = 1e-8, 1e-15
+    net.advance(1e-3)
+    print([r.T for r in reactors], reactors[0].thermo.Y)
+
+The names and semantics follow the reference's Python interface:
+``Solution`` / ``ThermoPhase`` state setters and getters (interfaces/cython/cantera/
+thermo.py: ``TP``, ``TPX``, ``TPY``, ``X``, ``Y``, ``set_equivalence_ratio``,
+``density``, ``mean_molecular_weight``, ``concentrations``), ``Kinetics``
+(interfaces/cython/cantera/kinetics.py:456-461,928-940: ``net_production_rates``,
+``net_production_rates_ddCi`` as a scipy CSC matrix), ``IdealGasConstPressureReactor``
+and ``ReactorNet`` (interfaces/cython/cantera/reactor.py:1781-2100: ``advance``, ``time``,
+``initial_time``, ``reinitialize``, ``rtol``, ``atol``, ``max_steps``, ``max_time_step``,
+``solver_stats``).  One ``ReactorNet`` over many reactors is one batched GPU network: every
+reactor is independent (no walls or inlets), shares the network's mechanism and tolerances,
+and reaches each ``advance`` time together.  What the batched engine does not do raises:
+``ReactorNet.step`` (one internal step of a batch has no single meaning), reactors of
+different mechanisms in one network, thermodynamic properties beyond the state.
+"""
+import numpy as np
+
+from . import GBError, ReactorNet as _Net, Solution as _Mech
+
+one_atm = 101325.0
+avogadro = 6.02214076e26
+gas_constant = avogadro * 1.380649e-23   # J/kmol/K
+
+__all__ = ["Solution", "IdealGasConstPressureReactor", "ReactorNet", "one_atm", "avogadro",
+           "gas_constant", "CanteraError"]
+CanteraError = GBError
+
+
+class Solution:
+    """An ideal-gas phase with kinetics: one thermodynamic state over a loaded mechanism."""
+
+    def __init__(self, infile, name="", *, _mech=None):
+        self._m = _mech if _mech is not None else _Mech(infile, name)
+        self._T = 300.0
+        self._P = one_atm
+        self._Y = np.zeros(self._m.n_species)
+        self._Y[0] = 1.0
+
+    # ---- mechanism ----
+    @property
+    def species_names(self):
+        return list(self._m.species_names)
+
+    @property
+    def n_species(self):
+        return self._m.n_species
+
+    @property
+    def n_reactions(self):
+        return self._m.n_reactions
+
+    @property
+    def molecular_weights(self):
+        return self._m.molecular_weights.copy()
+
+    def species_index(self, name):
+        return self._m.species_index(name)
+
+    def _composition(self, comp):
+        """A composition as a string 'A:1, B:2', a dict or an array over the species."""
+        if isinstance(comp, str):
+            v = np.zeros(self.n_species)
+            for item in comp.split(","):
+                if item.strip():
+                    name, x = item.split(":")
+                    v[self.species_index(name.strip())] += float(x)
+        elif isinstance(comp, dict):
+            v = np.zeros(self.n_species)
+            for name, x in comp.items():
+                v[self.species_index(name)] += float(x)
+        else:
+            v = np.array(comp, dtype=np.float64).reshape(self.n_species)
+        s = v.sum()
+        if not s > 0:
+            raise ValueError("composition must have a positive sum")
+        return v / s
+
+    # ---- state ----
+    @property
+    def T(self):
+        return self._T
+
+    @property
+    def P(self):
+        return self._P
+
+    @property
+    def Y(self):
+        return self._Y.copy()
+
+    @Y.setter
+    def Y(self, comp):
+        self._Y = self._composition(comp)
+
+    @property
+    def X(self):
+        x = self._Y / self._m.molecular_weights
+        return x / x.sum()
+
+    @X.setter
+    def X(self, comp):
+        self._Y = self._m.mole_to_mass(self._composition(comp))
+
+    @property
+    def TP(self):
+        return self._T, self._P
+
+    @TP.setter
+    def TP(self, v):
+        T, P = v
+        self._set_TP(T, P)
+
+    @property
+    def TPX(self):
+        return self._T, self._P, self.X
+
+    @TPX.setter
+    def TPX(self, v):
+        T, P, X = v
+        self._set_TP(T, P)
+        if X is not None:
+            self.X = X
+
+    @property
+    def TPY(self):
+        return self._T, self._P, self.Y
+
+    @TPY.setter
+    def TPY(self, v):
+        T, P, Y = v
+        self._set_TP(T, P)
+        if Y is not None:
+            self.Y = Y
+
+    @property
+    def TDY(self):
+        return self._T, self.density, self.Y
+
+    @TDY.setter
+    def TDY(self, v):
+        T, D, Y = v
+        if Y is not None:
+            self.Y = Y
+        T = self._T if T is None else float(T)
+        D = self.density if D is None else float(D)
+        self._set_TP(T, D * gas_constant * T / self.mean_molecular_weight)
+
+    def _set_TP(self, T, P):
+        if T is not None:
+            if not T > 0:
+                raise ValueError("temperature must be positive")
+            self._T = float(T)
+        if P is not None:
+            if not P > 0:
+                raise ValueError("pressure must be positive")
+            self._P = float(P)
+
+    def set_equivalence_ratio(self, phi, fuel, oxidizer, basis="mole"):
+        """The mixture of fuel and oxidizer with equivalence ratio phi; T and P are kept
+        (``ThermoPhase.set_equivalence_ratio``, src/thermo/ThermoPhase.cpp:879-910)."""
+        if basis not in ("mole", "molar"):
+            raise NotImplementedError("only the molar basis is supported")
+        self._Y = self._m.equivalence_ratio_mass_fractions(phi, self._composition(fuel), self._composition(oxidizer))
+
+    @property
+    def mean_molecular_weight(self):
+        """kg/kmol, from the mass fractions as given (no normalisation)."""
+        return 1.0 / np.sum(self._Y / self._m.molecular_weights)
+
+    @property
+    def density(self):
+        return self._P * self.mean_molecular_weight / (gas_constant * self._T)
+
+    @property
+    def density_mole(self):
+        return self._P / (gas_constant * self._T)
+
+    @property
+    def concentrations(self):
+        return self.density * self._Y / self._m.molecular_weights
+
+    # ---- kinetics (one state through the batched GPU kernels) ----
+    def _one(self):
+        return np.array([self._T]), np.array([self._P]), self._Y[:, None].copy()
+
+    @property
+    def net_production_rates(self):
+        return self._m.net_production_rates(*self._one())[:, 0]
+
+    @property
+    def net_production_rates_ddCi(self):
+        """d(wdot)/d(c) at constant T and other concentrations, as a scipy CSC matrix on the
+        reference's sparsity pattern."""
+        import scipy.sparse as sp
+        vals = self._m.net_production_rates_ddCi(*self._one())[:, 0]
+        K = self.n_species
+        return sp.csc_matrix((vals, self._m.jac_rowidx.copy(), self._m.jac_colptr.copy()), shape=(K, K))
+
+    def _copy(self):
+        s = Solution(None, _mech=self._m)
+        s._T, s._P, s._Y = self._T, self._P, self._Y.copy()
+        return s
+
+
+class IdealGasConstPressureReactor:
+    """A constant-pressure ideal-gas reactor holding its own copy of the gas state."""
+
+    def __init__(self, contents, *, name="", volume=1.0, energy="on"):
+        if energy != "on":
+            raise NotImplementedError("only the energy equation 'on' is supported")
+        self.name = name
+        self.volume = float(volume)
+        self._thermo = contents._copy()
+        self._net = None
+
+    @property
+    def thermo(self):
+        """The reactor's gas (its state is the reactor's after each advance)."""
+        return self._thermo
+
+    @property
+    def T(self):
+        return self._thermo.T
+
+    @property
+    def density(self):
+        return self._thermo.density
+
+    @property
+    def mass(self):
+        return self._thermo.density * self.volume
+
+    def insert(self, gas):
+        """Replace the contents (and state) of the reactor."""
+        self._thermo = gas._copy()
+
+
+class ReactorNet:
+    """Independent reactors advanced together as one batched GPU network."""
+
+    def __init__(self, reactors=(), **engine_options):
+        self._reactors = []
+        self._opts = dict(engine_options)
+        self._rtol, self._atol = 1e-9, 1e-15
+        self._max_steps, self._max_time_step = 20000, 0.0
+        self._t0 = 0.0
+        self._t = 0.0
+        self._engine = None
+        for r in reactors:
+            self.add_reactor(r)
+
+    def add_reactor(self, r):
+        if self._reactors and r.thermo._m is not self._reactors[0].thermo._m:
+            raise NotImplementedError("all reactors of a network must share one Solution's mechanism")
+        if r._net is not None and r._net is not self:
+            raise ValueError("reactor already belongs to another network")
+        r._net = self
+        self._reactors.append(r)
+        self._engine = None
+
+    @property
+    def reactors(self):
+        return list(self._reactors)
+
+    def _build(self):
+        if not self._reactors:
+            raise ValueError("the network has no reactors")
+        g = [r.thermo for r in self._reactors]
+        T = np.array([s.T for s in g])
+        P = np.array([s.P for s in g])
+        Y = np.array([s._Y for s in g]).T.copy()
+        self._engine = _Net(g[0]._m, T, P, Y, rtol=self._rtol, atol=self._atol, max_steps=self._max_steps,
+                            max_time_step=self._max_time_step, **self._opts)
+        self._t0 = self._t
+
+    def reinitialize(self):
+        """Restart the integration from the reactors' current states at the current time."""
+        self._build()
+
+    def advance(self, t, apply_limit=True):
+        """Advance every reactor to time t; returns t.  Raises if any reactor fails (its
+        status is in ``status``; the states of the others are updated)."""
+        if self._engine is None:
+            self._build()
+        if t < self._t:
+            raise ValueError("cannot integrate backwards in time")
+        failed = self._engine.advance(float(t) - self._t0)
+        self._t = float(t)
+        T, Y = self._engine.get_state()
+        for i, r in enumerate(self._reactors):
+            r._thermo._T = float(T[i])
+            r._thermo._Y = Y[:, i].copy()
+        if failed:
+            bad = np.nonzero(self._engine.status)[0]
+            raise CanteraError("%d reactor(s) failed to reach t = %g (first: %s)" % (failed, t, bad[:8].tolist()))
+        return self._t
+
+    def step(self):
+        raise NotImplementedError("ReactorNet.step: a batched network advances to given times only")
+
+    @property
+    def time(self):
+        return self._t
+
+    @property
+    def initial_time(self):
+        return self._t0
+
+    @initial_time.setter
+    def initial_time(self, t):
+        self._t = float(t)
+        self._build()
+
+    def _set(self, name, v):
+        setattr(self, name, v)
+        self._engine = None if self._engine is None else self._rebuild_keep_time()
+
+    def _rebuild_keep_time(self):
+        self._build()
+        return self._engine
+
+    @property
+    def rtol(self):
+        return self._rtol
+
+    @rtol.setter
+    def rtol(self, v):
+        self._set("_rtol", float(v))
+
+    @property
+    def atol(self):
+        return self._atol
+
+    @atol.setter
+    def atol(self, v):
+        self._set("_atol", float(v))
+
+    @property
+    def max_steps(self):
+        return self._max_steps
+
+    @max_steps.setter
+    def max_steps(self, v):
+        self._set("_max_steps", int(v))
+
+    @property
+    def max_time_step(self):
+        return self._max_time_step
+
+    @max_time_step.setter
+    def max_time_step(self, v):
+        self._set("_max_time_step", float(v))
+
+    @property
+    def status(self):
+        """Per-reactor status codes (0 = reached the last advance time)."""
+        return self._engine.status if self._engine is not None else np.zeros(len(self._reactors), dtype=np.int32)
+
+    @property
+    def solver_stats(self):
+        """Integrator counters (CVodesIntegrator::solverStats names) as arrays over the
+        reactors, summed since the last (re)initialisation."""
+        if self._engine is None:
+            return {}
+        return self._engine.solver_stats

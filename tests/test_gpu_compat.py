@@ -1,0 +1,134 @@
+"""The cantera-shaped facade (cantera_gb300.compat): state setters and getters, single-state
+kinetics and reactor networks built from reactor objects, against the oracle."""
+import numpy as np
+import pytest
+
+from conftest import oracle_mech
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ct():
+    import cantera_gb300.compat as ct
+    return ct
+
+
+def test_state_setters(ct):
+    gas = ct.Solution("gri30.yaml", "gri30")
+    gas.TPX = 1200.0, 2 * ct.one_atm, "CH4:1, O2:2, N2:7.52"
+    assert gas.T == 1200.0 and gas.P == 2 * ct.one_atm
+    X = gas.X
+    assert X[gas.species_index("CH4")] == pytest.approx(1 / 10.52, rel=1e-14)
+    assert np.sum(gas.Y) == pytest.approx(1.0, rel=1e-14)
+    # Y and X are consistent through the molecular weights
+    y = X * gas.molecular_weights
+    assert np.allclose(gas.Y, y / y.sum(), rtol=1e-14, atol=0)
+    # ideal gas
+    assert gas.density == pytest.approx(gas.P * gas.mean_molecular_weight / (ct.gas_constant * gas.T), rel=1e-14)
+    assert np.sum(gas.concentrations) == pytest.approx(gas.density_mole, rel=1e-13)
+    # TP keeps the composition; TDY sets the pressure from the density
+    Y0 = gas.Y
+    gas.TP = 900.0, None
+    assert gas.T == 900.0 and gas.P == 2 * ct.one_atm and np.array_equal(gas.Y, Y0)
+    d = gas.density
+    gas.TDY = 1800.0, d, None
+    assert gas.P == pytest.approx(2 * ct.one_atm * 2.0, rel=1e-13)
+    # dict and array compositions
+    gas.TPY = 1000.0, ct.one_atm, {"H2": 1.0, "O2": 8.0}
+    assert gas.Y[gas.species_index("O2")] == pytest.approx(8 / 9, rel=1e-14)
+    gas.Y = np.ones(gas.n_species)
+    assert np.allclose(gas.Y, 1.0 / gas.n_species)
+    with pytest.raises(ValueError):
+        gas.TP = -5.0, ct.one_atm
+
+
+def test_equivalence_ratio_matches_oracle(ct):
+    gas = ct.Solution("gri30.yaml", "gri30")
+    m = oracle_mech("gri30")
+    for phi in (0.5, 1.0, 1.7):
+        gas.set_equivalence_ratio(phi, "CH4:1", "O2:1, N2:3.76")
+        assert np.allclose(gas.Y, m.equivalence_ratio(phi, "CH4:1", "O2:1, N2:3.76"), rtol=1e-13, atol=1e-300)
+
+
+def test_single_state_kinetics_match_oracle(ct):
+    gas = ct.Solution("gri30.yaml", "gri30")
+    m = oracle_mech("gri30")
+    rng = np.random.default_rng(3)
+    for _ in range(5):
+        gas.TPY = rng.uniform(600, 2500), ct.one_atm * 10 ** rng.uniform(-1, 1.5), rng.dirichlet(0.5 * np.ones(gas.n_species))
+        w = gas.net_production_rates
+        wo, _, g = m.rates_batch(np.array([gas.T]), np.array([gas.P]), gas.Y[:, None].copy(), gross=True)
+        assert np.all(np.abs(w - wo[:, 0]) <= 1e-12 * g[:, 0] + 1e-300)
+        J = gas.net_production_rates_ddCi
+        assert J.shape == (gas.n_species, gas.n_species) and J.format == "csc"
+        Jo = m.ddci(gas.T, gas.P, gas.Y, mode=1)
+        assert np.max(np.abs(J.toarray() - Jo)) <= 1e-12 * np.max(np.abs(Jo))
+
+
+def test_reactor_network_matches_oracle(ct):
+    from oracle import pyoracle as po
+    gas = ct.Solution("h2o2.yaml", "ohmech")
+    m = oracle_mech("h2o2")
+    reactors = []
+    rng = np.random.default_rng(8)
+    T0 = rng.uniform(1000, 1500, 12)
+    for i, T in enumerate(T0):
+        gas.TP = T, ct.one_atm * (1 + i % 3)
+        gas.set_equivalence_ratio(0.6 + 0.1 * i, "H2:1", "O2:1, N2:3.76")
+        reactors.append(ct.IdealGasConstPressureReactor(gas, name="r%d" % i))
+    net = ct.ReactorNet(reactors)
+    rtol = 1e-8
+    net.rtol, net.atol = rtol, 1e-15
+    assert net.advance(1e-3) == 1e-3 and net.time == 1e-3
+    T = np.array([r.T for r in reactors])
+    Y = np.array([r.thermo.Y for r in reactors])
+    P = np.array([r.thermo.P for r in reactors])
+    Y0 = np.array([m.equivalence_ratio(0.6 + 0.1 * i, "H2:1", "O2:1, N2:3.76") for i in range(12)])
+    To, Yo, st, _ = m.advance_batch(T0, P, Y0, 1e-3, po.opts(rtol=rtol, atol=1e-15, analytic=True))
+    assert np.all(st[:, 8] == 0) and np.all(net.status == 0)
+    # the bars of the integrator's own parity tests: T and major species within 10 x rtol
+    assert np.max(np.abs(T - To) / To) < 10 * rtol
+    major = Yo >= 1e-3
+    assert np.max(np.abs(Y - Yo)[major] / Yo[major]) < 10 * rtol
+    assert np.all(net.solver_stats["steps"] > 0)
+    # continuing: the reactors' states follow the network
+    net.advance(2e-3)
+    assert net.time == 2e-3 and np.all(net.status == 0)
+    assert all(r.T != t for r, t in zip(reactors, T))
+    assert reactors[0].mass == pytest.approx(reactors[0].density * reactors[0].volume)
+
+
+def test_reinitialize_and_tolerances(ct):
+    gas = ct.Solution("h2o2.yaml", "ohmech")
+    gas.TPX = 1100.0, ct.one_atm, "H2:2, O2:1, N2:4"
+    a, b = ct.IdealGasConstPressureReactor(gas), ct.IdealGasConstPressureReactor(gas)
+    na, nb = ct.ReactorNet([a]), ct.ReactorNet([b])
+    for n in (na, nb):
+        n.rtol, n.atol = 1e-9, 1e-15
+    na.advance(1e-3)
+    nb.advance(4e-4)
+    nb.reinitialize()            # restart from the state at 4e-4 s, time kept
+    assert nb.time == 4e-4
+    nb.advance(1e-3)
+    assert nb.time == 1e-3
+    assert b.T == pytest.approx(a.T, rel=1e-6)
+    assert np.allclose(b.thermo.Y, a.thermo.Y, rtol=1e-4, atol=1e-9)
+
+
+def test_failures_raise(ct):
+    gas = ct.Solution("h2o2.yaml", "ohmech")
+    gas.TPX = 1200.0, ct.one_atm, "H2:2, O2:1, N2:4"
+    r = ct.IdealGasConstPressureReactor(gas)
+    net = ct.ReactorNet([r])
+    net.max_steps = 5
+    with pytest.raises(ct.CanteraError, match="failed"):
+        net.advance(1e-3)
+    assert net.status[0] != 0
+    with pytest.raises(NotImplementedError):
+        net.step()
+    with pytest.raises(ValueError, match="another network"):
+        ct.ReactorNet([r])
+    other = ct.Solution("h2o2.yaml", "ohmech")
+    with pytest.raises(NotImplementedError):
+        ct.ReactorNet([ct.IdealGasConstPressureReactor(gas), ct.IdealGasConstPressureReactor(other)])
