@@ -49,8 +49,7 @@ __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
         __syncwarp();
         warpState(m, T, P, Yl, s, st, lane);
         __syncwarp();
-        if (p.jac) warpRates<true, kX>(m, s, st, lane);
-        else warpRates<false, kX>(m, s, st, lane);
+        warpRates<kX>(m, s, st, lane, p.jac != nullptr);
         if (p.wdot)
             for (int k = lane; k < m.K; k += 32) p.wdot[(size_t)k * p.n + idx] = s.wdot[k];
         if (p.jac) {
@@ -169,8 +168,7 @@ __device__ __noinline__ bool devRhs(const DevMech& m, double* base, const uint64
     KinState st;
     warpState(m, z[0], P, z + 1, s, st, lane);
     __syncwarp();
-    if (forJac) warpRates<true, kX>(m, s, st, lane);
-    else warpRates<false, kX>(m, s, st, lane);
+    warpRates<kX>(m, s, st, lane, forJac);
     if (lane == 0) storeState(base, st);
     double ph = 0.0, pc = 0.0;
 #pragma unroll 1

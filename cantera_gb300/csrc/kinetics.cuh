@@ -373,9 +373,11 @@ __device__ __forceinline__ void warpState(const DevMech& m, double T, double P, 
 
 // Species thermo + rates of progress + net production rates.  With `forJac`, also the
 // per-reaction data d(wdot)/dc needs (Qtb, dlk).  kX: the mechanism has reactions of the
-// less common forms (rateExtra); without it, such reactions must not occur.
-template <bool forJac, bool kX = false>
-__device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, int lane) {
+// less common forms (rateExtra); without it, such reactions must not occur.  forJac is a
+// run-time flag: one copy of this large routine serves both the Newton iterations and the
+// Jacobian evaluations, which keeps the integrator's instruction footprint small.
+template <bool kX = false>
+__device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const KinState& st, int lane, bool forJac) {
     const double lnPP = st.lnPP;
     if (lane == 0) s.flags[0] = 0;
     __syncwarp();
