@@ -475,7 +475,7 @@ def main():
     tune_log = None
     if args.autotune:
         from cantera_gb300.tuning import autotune
-        tuned, tune_log = autotune(sol, dT, dP, dY, WL["t_end"] / 10, sample=min(2048, n))
+        tuned, tune_log = autotune(sol, dT, dP, dY, WL["t_end"] / 10)
     results = {}
     for variant, lu in (("fp64", 64), ("fp32_lu", 32)):
         if variant == "fp32_lu" and args.no_fp32:

@@ -4,7 +4,12 @@ The engine's automatic launch shape is a rule (Newton matrices in shared memory 
 of 8 reactors fits, otherwise in an L2-resident global slot per warp).  ``autotune`` measures
 instead: it advances a strided sample of the caller's reactors with each candidate shape
 (matrix placement x reactors per block) and returns the options of the fastest, so that the
-choice follows the mechanism size and the GPU.  Results are cached per (mechanism, options).
+choice follows the mechanism size and the GPU.  Each candidate's sample is a whole number of
+waves of its own resident capacity (blocks x reactors per block), and candidates are compared
+by time per reactor: a sample of a fixed size would favour the shape whose capacity happens
+to divide it well (the tail of a partial wave dominates a short run).  Within ``margin`` of
+the fastest, the shape with more resident reactors wins (more latency hiding on the long
+runs the tuner stands in for).  Results are cached per (mechanism, options).
 """
 import time
 
@@ -19,30 +24,40 @@ def candidates(max_warps=8):
             yield {"matrix_placement": placement, "warps_per_block": wpb}
 
 
-def autotune(solution, T, P, Y, t_probe, sample=2048, rtol=1e-8, atol=1e-15, lu_precision=64, repeat=1,
-             use_cache=True):
+def _subset(T, P, Y, idx_stride, count):
+    Ts, Ps, Ys = T[::idx_stride][:count], P[::idx_stride][:count], Y[:, ::idx_stride][:, :count]
+    if hasattr(Ys, "contiguous"):
+        return Ts.contiguous(), Ps.contiguous(), Ys.contiguous()
+    import numpy as np
+    return np.ascontiguousarray(Ts), np.ascontiguousarray(Ps), np.ascontiguousarray(Ys)
+
+
+def autotune(solution, T, P, Y, t_probe, waves=3, pool=8192, rtol=1e-8, atol=1e-15, lu_precision=64,
+             repeat=1, margin=0.03, use_cache=True):
     """Options dict (matrix_placement, warps_per_block) of the fastest launch shape for
-    advancing these reactors (host or device arrays; Y species-major [K, n]) to t_probe,
-    timed on every (n // sample)-th reactor.  Also returns the timings of every candidate."""
-    key = (solution._h, lu_precision, sample, float(t_probe))
+    advancing these reactors (host or device arrays; Y species-major [K, n]) to t_probe.
+    Each candidate advances `waves` full waves of its resident capacity, drawn with a stride
+    from the caller's reactors (at most `pool` of them).  Also returns every candidate's
+    timing (seconds per reactor)."""
+    key = (solution._h, lu_precision, waves, pool, float(t_probe))
     if use_cache and key in _cache:
         return _cache[key]
     n = T.shape[0]
-    stride = max(1, n // sample)
-    Ts, Ps, Ys = T[::stride][:sample], P[::stride][:sample], Y[:, ::stride][:, :sample]
-    if hasattr(Ys, "contiguous"):
-        Ts, Ps, Ys = Ts.contiguous(), Ps.contiguous(), Ys.contiguous()
-    else:
-        import numpy as np
-        Ts, Ps, Ys = np.ascontiguousarray(Ts), np.ascontiguousarray(Ps), np.ascontiguousarray(Ys)
+    npool = min(n, pool)
+    Tp, Pp, Yp = _subset(T, P, Y, max(1, n // npool), npool)
     timings = []
     seen = set()
     for c in candidates():
-        net = ReactorNet(solution, Ts, Ps, Ys, rtol=rtol, atol=atol, lu_precision=lu_precision, **c)
-        shape = tuple(sorted(net.launch_info.items()))
+        probe = ReactorNet(solution, Tp, Pp, Yp, rtol=rtol, atol=atol, lu_precision=lu_precision, **c)
+        info = probe.launch_info
+        del probe
+        shape = tuple(sorted(info.items()))
         if shape in seen:          # the engine capped this request to a shape already timed
             continue
         seen.add(shape)
+        m = min(npool, waves * info["blocks"] * info["warps_per_block"])
+        Ts, Ps, Ys = _subset(Tp, Pp, Yp, max(1, npool // m), m)
+        net = ReactorNet(solution, Ts, Ps, Ys, rtol=rtol, atol=atol, lu_precision=lu_precision, **c)
         net.advance(t_probe)       # warm-up (module load, first launch)
         best = float("inf")
         for _ in range(repeat):
@@ -50,9 +65,12 @@ def autotune(solution, T, P, Y, t_probe, sample=2048, rtol=1e-8, atol=1e-15, lu_
             t0 = time.perf_counter()
             net.advance(t_probe)
             best = min(best, time.perf_counter() - t0)
-        timings.append((best, c, dict(shape)))
+        timings.append((best / m, c, dict(shape)))
         del net
     timings.sort(key=lambda x: x[0])
-    result = (dict(timings[0][1]), [{"seconds": t, "options": c, "shape": s} for t, c, s in timings])
+    fastest = timings[0][0]
+    near = [t for t in timings if t[0] <= fastest * (1 + margin)]
+    pick = max(near, key=lambda t: t[2]["blocks"] * t[2]["warps_per_block"])
+    result = (dict(pick[1]), [{"seconds": t, "options": c, "shape": s} for t, c, s in timings])
     _cache[key] = result
     return result

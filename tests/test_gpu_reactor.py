@@ -213,7 +213,12 @@ def test_autotune_picks_a_measured_candidate():
     from cantera_gb300.tuning import autotune, candidates
     sol = gpu_solution("h2o2")
     T0, P, Y0 = h2o2_batch(256, 17)
-    best, log = autotune(sol, T0, P, Y0.T.copy(), 1e-4, sample=64, use_cache=False)
+    best, log = autotune(sol, T0, P, Y0.T.copy(), 1e-4, waves=1, pool=256, use_cache=False)
     assert best in list(candidates())
-    assert log and log[0]["options"] == best
     assert all(a["seconds"] <= b["seconds"] for a, b in zip(log, log[1:]))
+    # the pick is within the margin of the fastest time per reactor, and among those the one
+    # with the most resident reactors
+    pick = next(e for e in log if e["options"] == best)
+    assert pick["seconds"] <= log[0]["seconds"] * 1.03
+    cap = lambda e: e["shape"]["blocks"] * e["shape"]["warps_per_block"]
+    assert all(cap(e) <= cap(pick) for e in log if e["seconds"] <= log[0]["seconds"] * 1.03)
