@@ -556,7 +556,7 @@ def main():
                        "l2": "flushed (256 MB write) before every timed step",
                        "launch": "persistent kernel, device work queue, CUDA graph", "shards": ws,
                        "launch_shape": r64["launch"],
-                       "autotune": tune_log and [{"seconds": round(t["seconds"], 4), **t["options"]} for t in tune_log]},
+                       "autotune": tune_log and [{"us_per_reactor": round(t["seconds"] * 1e6, 2), **t["options"]} for t in tune_log]},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": read_traffic(),
                          "peak_source": "FP64 FMA rate measured live by this run (MEASURED_PEAKS.json has no FP64 figure)",
