@@ -327,12 +327,11 @@ class ReactorNet:
         self._build()
 
     def _set(self, name, v):
+        """Change an integrator setting; a running network restarts from the reactors'
+        current states at the current time (ReactorNet reinitialises after such a change)."""
         setattr(self, name, v)
-        self._engine = None if self._engine is None else self._rebuild_keep_time()
-
-    def _rebuild_keep_time(self):
-        self._build()
-        return self._engine
+        if self._engine is not None:
+            self._build()
 
     @property
     def rtol(self):

@@ -1,0 +1,72 @@
+"""The cantera-shaped facade's state logic (cantera_gb300.compat) without a GPU: the
+Solution state setters and getters over a stand-in mechanism object (the kinetics getters
+and reactor networks need the engine and are covered by tests/test_gpu_compat.py)."""
+import numpy as np
+import pytest
+
+
+class StandInMech:
+    """The part of cantera_gb300.Solution the facade's state logic uses."""
+
+    def __init__(self):
+        self.species_names = ["H2", "O2", "H2O", "N2"]
+        self.n_species = 4
+        self.n_reactions = 0
+        self.molecular_weights = np.array([2.016, 31.998, 18.015, 28.014])
+
+    def species_index(self, name):
+        return self.species_names.index(name)
+
+    def mole_to_mass(self, X):
+        y = np.asarray(X) * self.molecular_weights
+        return y / y.sum()
+
+
+@pytest.fixture
+def gas():
+    from cantera_gb300.compat import Solution
+    return Solution(None, _mech=StandInMech())
+
+
+def test_composition_forms(gas):
+    gas.TPX = 1000.0, 2e5, "H2:2, O2:1"
+    assert gas.X == pytest.approx([2 / 3, 1 / 3, 0, 0], rel=1e-14)
+    gas.X = {"H2": 1.0, "N2": 3.0}
+    assert gas.X == pytest.approx([0.25, 0, 0, 0.75], rel=1e-14)
+    gas.Y = [1, 1, 0, 2]
+    assert gas.Y == pytest.approx([0.25, 0.25, 0, 0.5], rel=1e-14)
+    with pytest.raises(ValueError):
+        gas.Y = [0, 0, 0, 0]
+    with pytest.raises(ValueError):
+        gas.X = "H2:1, XX:1"
+
+
+def test_state_relations(gas):
+    from cantera_gb300.compat import gas_constant
+    gas.TPY = 1500.0, 3e5, [0.1, 0.2, 0.3, 0.4]
+    W = 1 / np.sum(gas.Y / gas.molecular_weights)
+    assert gas.mean_molecular_weight == pytest.approx(W, rel=1e-14)
+    assert gas.density == pytest.approx(3e5 * W / (gas_constant * 1500.0), rel=1e-14)
+    assert gas.density_mole == pytest.approx(3e5 / (gas_constant * 1500.0), rel=1e-14)
+    assert gas.concentrations == pytest.approx(gas.density * gas.Y / gas.molecular_weights, rel=1e-14)
+    # TP keeps the composition, None leaves a value unchanged
+    y = gas.Y
+    gas.TP = None, 1e5
+    assert gas.T == 1500.0 and gas.P == 1e5 and np.array_equal(gas.Y, y)
+    # TDY: density held while T doubles means P doubles
+    d = gas.density
+    gas.TDY = 3000.0, d, None
+    assert gas.P == pytest.approx(2e5, rel=1e-13)
+    with pytest.raises(ValueError):
+        gas.TP = 300.0, 0.0
+
+
+def test_copies_are_independent(gas):
+    from cantera_gb300.compat import IdealGasConstPressureReactor
+    gas.TPX = 1200.0, 1e5, "H2:2, O2:1, N2:4"
+    r = IdealGasConstPressureReactor(gas, volume=2.0)
+    gas.TPX = 300.0, 1e5, "N2:1"
+    assert r.T == 1200.0 and r.thermo.X[0] == pytest.approx(2 / 7)
+    assert r.mass == pytest.approx(r.thermo.density * 2.0)
+    with pytest.raises(NotImplementedError):
+        IdealGasConstPressureReactor(gas, energy="off")
