@@ -477,6 +477,8 @@ struct System {
     virtual int normSize() const = 0;                   // WRMS-norm divisor
     virtual int rhs(const double* z, double* zdot) = 0; // 0 ok, 1 recoverable failure
     virtual int jac(const double* z, const double* fz, double* J) = 0;
+    // Approximate Jacobian for a preconditioner (dense storage); -1: not available
+    virtual int precJac(const double* z, double atol, double* J) { (void)z; (void)atol; (void)J; return -1; }
     int nrhs = 0;
 };
 
@@ -513,6 +515,90 @@ struct Reactor : System {
         for (int n = 0; n < K; n++) zdot[1 + n] /= mass;
         for (int i = 0; i <= K; i++)
             if (!std::isfinite(zdot[i])) return 1;
+        return 0;
+    }
+};
+
+// Constant-pressure ideal-gas reactor with moles as the state, z = [T, n_1..n_K] (kmol):
+// IdealGasConstPressureMoleReactor::updateState / eval (reference src/zeroD/
+// IdealGasConstPressureMoleReactor.cpp:34-104).  The mass follows from the moles, the volume
+// from the mass and the density; dn_k/dt = wdot_k V, m cp dT/dt = -sum_k h_k wdot_k V.
+struct MoleReactor : System {
+    MoleReactor(const Kin* k, double p) : kn(k), P(p) { w.init(k->m.K, k->m.R); }
+    const Kin* kn;
+    double P;
+    Work w;
+    double mass = 0.0, vol = 0.0, mcp = 0.0;
+    int size() const override { return kn->m.K + 1; }
+    int normSize() const override { return kn->m.K + 1; }
+    int jac(const double*, const double*, double*) override { return -1; }
+    // thermo state from z (setMassFromMoles, setMolesNoTruncate, setState_TP)
+    void update(const double* z) {
+        const Mechanism& m = kn->m;
+        const int K = m.K;
+        mass = 0.0;
+        for (int k = 0; k < K; k++) mass += z[1 + k] * m.mw[k];
+        std::vector<double> Y(K);
+        for (int k = 0; k < K; k++) Y[k] = z[1 + k] * m.mw[k] / mass;
+        setState(*kn, z[0], P, Y.data(), w);
+        vol = mass / w.density;
+        updateROP(*kn, w);
+        double s = 0.0;
+        for (int k = 0; k < K; k++) s += w.ym[k] * w.cp_R[k];
+        mcp = mass * kn->R_gas * s;        // m * cp_mass = m * R * sum(Y_k/W_k cp_k/R)
+    }
+    int rhs(const double* z, double* zdot) override {
+        const int K = kn->m.K;
+        nrhs++;
+        update(z);
+        double mcpdTdt = 0.0;
+        for (int n = 0; n < K; n++) {
+            mcpdTdt -= w.wdot[n] * (w.h_RT[n] * w.RT) * vol;
+            zdot[1 + n] = w.wdot[n] * vol;
+        }
+        zdot[0] = mcpdTdt / mcp;
+        for (int i = 0; i <= K; i++)
+            if (!std::isfinite(zdot[i])) return 1;
+        return 0;
+    }
+    // IdealGasConstPressureMoleReactor::getJacobianElements (reference
+    // IdealGasConstPressureMoleReactor.cpp:106-221) at the state adjusted by
+    // AdaptivePreconditioner::stateAdjustment (components clipped below at atol,
+    // src/numerics/AdaptivePreconditioner.cpp:17-22): d(dn_k/dt)/dn_j = d(wdot_k)/dc_j (the
+    // reference's ddCi; the -n_i/(V N) dc_i/dn_j terms are left out, as there), the T column by
+    // a one-sided difference with dT = T sqrt(eps), and the T row
+    // d(dT/dt)/dn_j = (cp_j qdot - m cp sum_k h_k d(dn_k/dt)/dn_j) / (m cp)^2, qdot = sum_k h_k wdot_k V.
+    int precJac(const double* z0, double atol, double* J) override {
+        const int K = kn->m.K, N = K + 1;
+        std::vector<double> z(z0, z0 + N), fc(N), fp(N);
+        for (int i = 0; i < N; i++) z[i] = std::max(z[i], atol);
+        std::fill(J, J + (size_t)N * N, 0.0);
+        // temperature column (perturbed first, then the current state, as the reference)
+        const double dT = z[0] * std::sqrt(std::numeric_limits<double>::epsilon());
+        std::vector<double> zp(z);
+        zp[0] += dT;
+        if (rhs(zp.data(), fp.data())) return 1;
+        if (rhs(z.data(), fc.data())) return 1;
+        for (int j = 0; j < N; j++) J[(size_t)j * N] = (fp[j] - fc[j]) / dT;
+        // species block: ddCi at the current state (the work arrays hold it after rhs(z))
+        std::vector<double> D((size_t)K * K);
+        ddCi(*kn, w, 0, D.data());
+        for (int k = 0; k < K; k++)
+            for (int j = 0; j < K; j++) J[(size_t)(1 + k) * N + 1 + j] = D[(size_t)k * K + j];
+        // temperature row
+        double qdot = 0.0;
+        std::vector<double> hk(K);
+        for (int k = 0; k < K; k++) {
+            hk[k] = w.h_RT[k] * w.RT;
+            qdot += hk[k] * (w.wdot[k] * vol);
+        }
+        const double denom = 1.0 / (mcp * mcp);
+        for (int j = 0; j < K; j++) {
+            double hs = 0.0;
+            for (int k = 0; k < K; k++) hs += D[(size_t)k * K + j] * hk[k];
+            const double cpj = w.cp_R[j] * kn->R_gas;    // partial molar cp, J/kmol/K
+            J[1 + j] = (cpj * qdot - mcp * hs) * denom;
+        }
         return 0;
     }
 };
@@ -604,6 +690,9 @@ struct Bdf {
     long nst = 0, nstlp = 0, nstlj = 0, nsetups = 0, nje = 0, nni = 0, netf = 0, ncfn = 0;
     std::vector<double> Jsaved;
     bool haveJ = false;
+    // GMRES with the adaptive preconditioner (linear_solver = 1)
+    std::vector<double> Jp, Pf;        // preconditioner Jacobian (kept between setups), factors of I - gamma Jp
+    long nli = 0, nps = 0, njtv = 0;    // linear iterations, preconditioner solves, J v products
     bool jcur = false, haveLU = false;
     // ignition tracking (see recordSample)
     long nsamp = 0;
@@ -627,6 +716,7 @@ struct Bdf {
         zn.assign(QMAX + 1, std::vector<double>(N, 0.0));
         ewt.assign(N, 0); acor.assign(N, 0); y.assign(N, 0); ftemp.assign(N, 0); tempv.assign(N, 0);
         Jm.assign((size_t)N * N, 0); Mlu.assign((size_t)N * N, 0); Mlu32.assign((size_t)N * N, 0); piv.assign(N, 0);
+        if (o.linear_solver == 1) { Jp.assign((size_t)N * N, 0); Pf.assign((size_t)N * N, 0); }
         for (int i = 0; i < N; i++) zn[0][i] = z0[i];
         tn = 0.0;
         setEwt(z0);
@@ -745,6 +835,7 @@ struct Bdf {
     // M = I - gamma*J, LU with partial pivoting (row-major, in place).
     // convfail: 0 none, 1 retry after a failed solve with a stale J, 2 previous attempt failed
     int setupLinear(int convfail) {
+        if (o.linear_solver == 1) return setupPreconditioner(convfail);
         int st = 0;
         double dgamma = std::fabs(gamma / gammap - 1.0);
         bool jbad = !o.jac_reuse || !haveJ || (nst == 0) || (nst >= nstlj + MSBJ) ||
@@ -776,6 +867,213 @@ struct Bdf {
         haveLU = true;
         return fail ? 1 : 0;
     }
+    // Preconditioner setup, as CVODE's linear-solver interface drives it for a matrix-free
+    // solver (cvLsSetup: the preconditioner's Jacobian is re-evaluated on the first step, every
+    // MSBJ = 51 steps, after a convergence failure with a stale one and a small change of
+    // gamma, or after a failed step; otherwise only gamma changes) and as the reference's
+    // callback answers it (CVodesIntegrator.cpp:67-80: a new Jacobian through
+    // ReactorNet::preconditionerSetup, or EigenSparseJacobian::updatePreconditioner with the
+    // kept elements): P = I - gamma Jp, factored incompletely.
+    int setupPreconditioner(int convfail) {
+        const double dgamma = std::fabs(gamma / gammap - 1.0);
+        const bool jbad = !haveJ || (nst == 0) || (nst >= nstlj + MSBJ) ||
+                          (convfail == 1 && dgamma < DGMAX_JBAD) || (convfail == 2);
+        if (jbad) {
+            int st = r->precJac(y.data(), o.atol, Jp.data());
+            if (st) return st;
+            nje++;
+            nstlj = nst;
+            haveJ = true;
+            jcur = true;
+        } else {
+            jcur = false;
+        }
+        nsetups++;
+        for (size_t i = 0; i < (size_t)N * N; i++) Pf[i] = -gamma * Jp[i];
+        for (int i = 0; i < N; i++) Pf[(size_t)i * N + i] += 1.0;
+        ilut(Pf.data());
+        gammap = gamma;
+        gamrat = 1.0;
+        crate = 1.0;
+        nstlp = nst;
+        haveLU = true;
+        return 0;
+    }
+
+    // ILUT(p, tau), the dual-threshold incomplete LU of Saad (1994), row by row, with the
+    // parameters the reference's AdaptivePreconditioner leaves Eigen's IncompleteLUT
+    // (AdaptivePreconditioner.cpp:24-38: drop tolerance 1e-12; its fill factor is set only when
+    // no drop tolerance was, so Eigen's default of 10 holds): a multiplier at or below tau is
+    // dropped, then the entries of the row below tau times its 2-norm, then all but the p
+    // largest of its L and of its U part, p = 10 nnz(P) / N + 1.  A zero pivot becomes a small
+    // multiple of the row norm.  Eigen's fill-reducing ordering ahead of the factorisation is
+    // left out (it changes what is dropped, not what the preconditioner approximates).
+    void ilut(double* a) const {
+        const double tau = 1e-12;
+        long nnz = 0;
+        for (size_t i = 0; i < (size_t)N * N; i++) nnz += a[i] != 0.0;
+        const int fill = (int)(nnz * 10 / N) + 1;
+        std::vector<double> w(N);
+        std::vector<std::pair<double, int>> e;
+        for (int i = 0; i < N; i++) {
+            double rn = 0.0;
+            for (int j = 0; j < N; j++) { w[j] = a[(size_t)i * N + j]; rn += w[j] * w[j]; }
+            rn = std::sqrt(rn);
+            for (int k = 0; k < i; k++) {
+                if (w[k] == 0.0) continue;
+                const double f = w[k] / a[(size_t)k * N + k];
+                if (std::fabs(f) <= tau) { w[k] = 0.0; continue; }
+                w[k] = f;
+                for (int j = k + 1; j < N; j++) {
+                    const double u = a[(size_t)k * N + j];
+                    if (u != 0.0) w[j] -= f * u;
+                }
+            }
+            auto keep = [&](int j0, int j1) {
+                e.clear();
+                for (int j = j0; j < j1; j++) {
+                    if (std::fabs(w[j]) > tau * rn) e.push_back({std::fabs(w[j]), j});
+                    else w[j] = 0.0;
+                }
+                if ((int)e.size() > fill) {
+                    std::nth_element(e.begin(), e.begin() + fill, e.end(),
+                                     [](const std::pair<double, int>& x, const std::pair<double, int>& y) { return x.first > y.first; });
+                    for (size_t q = fill; q < e.size(); q++) w[e[q].second] = 0.0;
+                }
+            };
+            keep(0, i);
+            keep(i + 1, N);
+            if (w[i] == 0.0) w[i] = std::sqrt(tau) * rn;
+            for (int j = 0; j < N; j++) a[(size_t)i * N + j] = w[j];
+        }
+    }
+    void precSolve(double* x) {
+        nps++;
+        const double* a = Pf.data();
+        for (int i = 0; i < N; i++) {
+            double s = x[i];
+            for (int k = 0; k < i; k++) s -= a[(size_t)i * N + k] * x[k];
+            x[i] = s;
+        }
+        for (int i = N - 1; i >= 0; i--) {
+            double s = x[i];
+            for (int j = i + 1; j < N; j++) s -= a[(size_t)i * N + j] * x[j];
+            x[i] = s / a[(size_t)i * N + i];
+        }
+    }
+    // J v by the difference quotient (f(y + sig v) - f(y)) / sig, sig = 1 / ||v||_wrms, sig
+    // shrunk by 1/4 (at most three tries) when f fails recoverably (CVODE's default
+    // Jacobian-times-vector product); y and f(y) are the current Newton iterate.
+    int jtimes(const double* v, double* Jv) {
+        double sig = 1.0 / wrms(v);
+        std::vector<double> work(N);
+        int st = 1;
+        for (int it = 0; it < 3; it++) {
+            for (int i = 0; i < N; i++) work[i] = y[i] + sig * v[i];
+            st = r->rhs(work.data(), Jv);
+            njtv++;
+            if (st == 0) break;
+            sig *= 0.25;
+        }
+        if (st) return st;
+        const double siginv = 1.0 / sig;
+        for (int i = 0; i < N; i++) Jv[i] = (Jv[i] - ftemp[i]) * siginv;
+        return 0;
+    }
+    // (I - gamma J) x = b by right-preconditioned GMRES, as CVODE's iterative linear-solver
+    // interface runs SUNDIALS' SPGMR (cvLsSolve): tolerance eplifac = 0.05 times the Newton
+    // test constant tq[4] in the weighted RMS norm (sqrt(N) times it in the scaled 2-norm),
+    // both scaling vectors the error weights, zero initial guess, at most MAXL = 5 Krylov
+    // vectors, no restarts, modified Gram-Schmidt with one reorthogonalisation when the new
+    // vector's norm collapses by the factor 1000, Givens rotations for the least-squares
+    // problem.  A right-hand side already below the tolerance is returned as the solution on
+    // the first Newton iteration and as zero afterwards.  Returns 0, or 1 (recoverable: not
+    // converged and, after the first Newton iteration, only reduced).
+    int gmresSolve(double* b, int mnewt) {
+        constexpr int MAXL = 5;
+        constexpr double EPLIFAC = 0.05;
+        const double deltar = EPLIFAC * tq[4];
+        if (wrms(b) <= deltar) {
+            if (mnewt > 0) std::fill(b, b + N, 0.0);
+            return 0;
+        }
+        const double delta = deltar * std::sqrt((double)N);
+        auto dot = [&](const std::vector<double>& x, const std::vector<double>& z) {
+            double s = 0.0;
+            for (int i = 0; i < N; i++) s += x[i] * z[i];
+            return s;
+        };
+        std::vector<std::vector<double>> V(MAXL + 1, std::vector<double>(N, 0.0));
+        double H[MAXL + 1][MAXL] = {{0}};
+        double cs[MAXL] = {0}, sn[MAXL] = {0}, g[MAXL + 1] = {0};
+        for (int i = 0; i < N; i++) V[0][i] = ewt[i] * b[i];
+        const double beta = std::sqrt(dot(V[0], V[0]));
+        for (int i = 0; i < N; i++) V[0][i] /= beta;
+        g[0] = beta;
+        double rho = beta;
+        bool converged = false;
+        int m = 0;
+        std::vector<double> z(N), Az(N);
+        while (m < MAXL) {
+            const int l = m;
+            for (int i = 0; i < N; i++) z[i] = V[l][i] / ewt[i];
+            precSolve(z.data());
+            if (jtimes(z.data(), Az.data())) return 1;
+            std::vector<double>& vn = V[l + 1];
+            for (int i = 0; i < N; i++) vn[i] = ewt[i] * (z[i] - gamma * Az[i]);
+            const double vk = std::sqrt(dot(vn, vn));
+            for (int i = 0; i <= l; i++) {
+                H[i][l] = dot(V[i], vn);
+                for (int q = 0; q < N; q++) vn[q] -= H[i][l] * V[i][q];
+            }
+            double vnorm = std::sqrt(dot(vn, vn));
+            const double fac = 1000.0 * vk;
+            if (fac + vnorm == fac) {
+                for (int i = 0; i <= l; i++) {
+                    const double p = dot(V[i], vn);
+                    for (int q = 0; q < N; q++) vn[q] -= p * V[i][q];
+                    H[i][l] += p;
+                }
+                vnorm = std::sqrt(dot(vn, vn));
+            }
+            H[l + 1][l] = vnorm;
+            for (int i = 0; i < l; i++) {
+                const double t1 = H[i][l], t2 = H[i + 1][l];
+                H[i][l] = cs[i] * t1 + sn[i] * t2;
+                H[i + 1][l] = -sn[i] * t1 + cs[i] * t2;
+            }
+            const double d = std::hypot(H[l][l], H[l + 1][l]);
+            cs[l] = H[l][l] / d;
+            sn[l] = H[l + 1][l] / d;
+            H[l][l] = d;
+            H[l + 1][l] = 0.0;
+            g[l + 1] = -sn[l] * g[l];
+            g[l] = cs[l] * g[l];
+            rho = std::fabs(g[l + 1]);
+            m++;
+            if (rho <= delta) { converged = true; break; }
+            if (vnorm == 0.0) break;
+            for (int q = 0; q < N; q++) vn[q] /= vnorm;
+        }
+        nli += m;
+        double yv[MAXL] = {0};
+        for (int i = m - 1; i >= 0; i--) {
+            double s = g[i];
+            for (int j = i + 1; j < m; j++) s -= H[i][j] * yv[j];
+            yv[i] = s / H[i][i];
+        }
+        for (int q = 0; q < N; q++) {
+            double s = 0.0;
+            for (int j = 0; j < m; j++) s += yv[j] * V[j][q];
+            z[q] = s / ewt[q];
+        }
+        precSolve(z.data());
+        for (int q = 0; q < N; q++) b[q] = z[q];
+        if (converged) return 0;
+        if (rho < beta && mnewt == 0) return 0;
+        return 1;
+    }
+
     int dqJacobian() {
         // difference-quotient Jacobian as in the dense CVODE linear solver
         double fnorm = wrms(ftemp.data());
@@ -891,10 +1189,15 @@ struct Bdf {
             for (;;) {
                 nni++;
                 for (int i = 0; i < N; i++) tempv[i] = gamma * ftemp[i] - (rl1 * zn[1][i] + acor[i]);
-                luSolve(tempv.data());
-                if (gamrat != 1.0) {
-                    double f = 2.0 / (1.0 + gamrat);
-                    for (int i = 0; i < N; i++) tempv[i] *= f;
+                if (o.linear_solver == 1) {
+                    // an iterative solve uses the current gamma: no correction for its change
+                    if (gmresSolve(tempv.data(), m)) { retryWithJ = !jcur; break; }
+                } else {
+                    luSolve(tempv.data());
+                    if (gamrat != 1.0) {
+                        double f = 2.0 / (1.0 + gamrat);
+                        for (int i = 0; i < N; i++) tempv[i] *= f;
+                    }
                 }
                 del = wrms(tempv.data());
                 for (int i = 0; i < N; i++) { acor[i] += tempv[i]; y[i] = zn[0][i] + acor[i]; }
@@ -1154,6 +1457,9 @@ void fillStats(const Bdf& b, int status, int64_t* st) {
     st[OR_ST_CONVFAIL] = b.ncfn;
     st[OR_ST_ORDER] = b.q;
     st[OR_ST_STATUS] = status;
+    st[OR_ST_LIN_ITERS] = b.nli;
+    st[OR_ST_PREC_SOLVES] = b.nps;
+    st[OR_ST_JTIMES] = b.njtv;
 }
 
 Kin* buildKin(const std::string& path, const std::string& phase) {
@@ -1210,15 +1516,34 @@ void parallelFor(int n, int threads, F&& f) {
 int runReactor(const Kin* kn, double T0, double P, const double* Y0, double t_end, const or_bdf_opts& o,
                double* Tout, double* Yout, int64_t* stats, double* tign) {
     const int K = kn->m.K;
+    if (o.linear_solver == 1 && !o.mole_reactor) {
+        if (stats) stats[OR_ST_STATUS] = ST_NONFINITE;
+        return ST_NONFINITE;   // GMRES with the preconditioner needs the mole reactor (as the reference)
+    }
     Reactor r(kn, P);
+    MoleReactor mr(kn, P);
     std::vector<double> z0(K + 1), zout(K + 1);
     z0[0] = T0;
-    for (int k = 0; k < K; k++) z0[1 + k] = Y0[k];
+    if (o.mole_reactor) {
+        // moles in an initial volume of 1 m^3: n_k = rho Y_k / W_k
+        Work w0;
+        w0.init(K, kn->m.R);
+        setState(*kn, T0, P, Y0, w0);
+        for (int k = 0; k < K; k++) z0[1 + k] = w0.density * Y0[k] / kn->m.mw[k];
+    } else {
+        for (int k = 0; k < K; k++) z0[1 + k] = Y0[k];
+    }
     Bdf b;
-    b.init(&r, z0.data(), o, t_end);
+    b.init(o.mole_reactor ? (System*)&mr : (System*)&r, z0.data(), o, t_end);
     long steps = 0;
     int st = b.advance(t_end, zout.data(), steps);
     if (st != ST_OK) for (int i = 0; i <= K; i++) zout[i] = b.zn[0][i];
+    if (o.mole_reactor) {
+        // mass fractions from the moles
+        double m = 0.0;
+        for (int k = 0; k < K; k++) m += zout[1 + k] * kn->m.mw[k];
+        for (int k = 0; k < K; k++) zout[1 + k] = zout[1 + k] * kn->m.mw[k] / m;
+    }
     if (Tout) *Tout = zout[0];
     if (Yout) for (int k = 0; k < K; k++) Yout[k] = zout[1 + k];
     fillStats(b, st, stats);
@@ -1359,6 +1684,20 @@ int32_t or_reactor_rhs(int32_t h, double P, const double* y, double* ydot) {
     return st;
 }
 
+int32_t or_mole_reactor_rhs(int32_t h, double P, const double* z, double* zdot) {
+    Kin* k = getKin(h);
+    if (!k) return -1;
+    MoleReactor r(k, P);
+    return r.rhs(z, zdot);
+}
+
+int32_t or_mole_precond_jacobian(int32_t h, double P, const double* z, double atol, double* J) {
+    Kin* k = getKin(h);
+    if (!k) return -1;
+    MoleReactor r(k, P);
+    return r.precJac(z, atol, J);
+}
+
 int32_t or_advance_batch(int32_t h, int32_t n, const double* T0, const double* P, const double* Y0,
                          double t_end, const or_bdf_opts* opts, double* T, double* Y,
                          int64_t* stats, double* tign, int32_t threads) {
@@ -1378,17 +1717,31 @@ int32_t or_advance_trajectory(int32_t h, double T0, double P, const double* Y0, 
     Kin* k = getKin(h);
     if (!k) return -1;
     const int K = k->m.K;
+    if (opts->linear_solver == 1 && !opts->mole_reactor) return -1;
     Reactor r(k, P);
+    MoleReactor mr(k, P);
     std::vector<double> z0(K + 1), zo(K + 1);
     z0[0] = T0;
-    for (int i = 0; i < K; i++) z0[1 + i] = Y0[i];
+    if (opts->mole_reactor) {
+        Work w0;
+        w0.init(K, k->m.R);
+        setState(*k, T0, P, Y0, w0);
+        for (int i = 0; i < K; i++) z0[1 + i] = w0.density * Y0[i] / k->m.mw[i];
+    } else {
+        for (int i = 0; i < K; i++) z0[1 + i] = Y0[i];
+    }
     Bdf b;
-    b.init(&r, z0.data(), *opts, times[nt - 1]);
+    b.init(opts->mole_reactor ? (System*)&mr : (System*)&r, z0.data(), *opts, times[nt - 1]);
     long steps = 0;
     int st = ST_OK;
     for (int i = 0; i < nt; i++) {
         st = b.advance(times[i], zo.data(), steps);
         if (st != ST_OK) break;
+        if (opts->mole_reactor) {
+            double m = 0.0;
+            for (int j = 0; j < K; j++) m += zo[1 + j] * k->m.mw[j];
+            for (int j = 0; j < K; j++) zo[1 + j] = zo[1 + j] * k->m.mw[j] / m;
+        }
         for (int j = 0; j <= K; j++) out[(size_t)i * (K + 1) + j] = zo[j];
     }
     fillStats(b, st, stats);

@@ -19,7 +19,14 @@
 //                                    empty submodule) as configured by src/numerics/CVodesIntegrator.cpp:281-529
 //                                    and src/zeroD/ReactorNet.cpp:164-169: variable-order (1-5) BDF in Nordsieck
 //                                    form, fixed-leading-coefficient variable-step coefficients, modified Newton
-//                                    with a dense LU and a difference-quotient Jacobian.  Restated from the
+//                                    with a dense LU and a difference-quotient Jacobian, or (mole
+//                                    reactor) with right-preconditioned GMRES: CVODE's SPGMR
+//                                    iterative linear solver with the reference's adaptive
+//                                    preconditioner (src/zeroD/IdealGasConstPressureMoleReactor.cpp:
+//                                    16-229, src/zeroD/ReactorNet.cpp:881-903,
+//                                    src/numerics/AdaptivePreconditioner.cpp:24-81,
+//                                    src/numerics/EigenSparseJacobian.cpp:41-49,
+//                                    src/numerics/CVodesIntegrator.cpp:67-88,424-434).  Restated from the
 //                                    published algorithm (Cohen & Hindmarsh 1996; Hindmarsh et al., ACM TOMS
 //                                    31(3) 2005; Brown, Byrne & Hindmarsh, SIAM J. Sci. Stat. Comput. 10(5) 1989;
 //                                    Jackson & Sacks-Davis 1980) and the documented CVODE default parameters.
@@ -50,11 +57,16 @@ typedef struct {
                                 //    re-evaluate it only on the first step, every 51 steps and after
                                 //    convergence failures (CVODE's documented msbj policy);
                                 // 0: evaluate it at every setup (the GPU engine's policy)
+    int32_t mole_reactor;       // 1: IdealGasConstPressureMoleReactor, state [T, n_1..n_K] (kmol, initial
+                                //    volume 1 m^3); 0: IdealGasConstPressureReactor, state [T, Y]
+    int32_t linear_solver;      // 0: dense direct LU; 1: GMRES with the adaptive preconditioner
+                                //    (needs mole_reactor = 1)
 } or_bdf_opts;
 
 // Per-reactor counters, mirroring CVodesIntegrator::solverStats.
 enum { OR_ST_STEPS = 0, OR_ST_RHS, OR_ST_NEWTON, OR_ST_SETUPS, OR_ST_JACS, OR_ST_ERRFAIL,
-       OR_ST_CONVFAIL, OR_ST_ORDER, OR_ST_STATUS, OR_NSTAT };
+       OR_ST_CONVFAIL, OR_ST_ORDER, OR_ST_STATUS, OR_ST_LIN_ITERS, OR_ST_PREC_SOLVES, OR_ST_JTIMES,
+       OR_NSTAT };
 
 int32_t or_mech_load(const char* path, const char* phase);      // handle >= 0, or -1
 void or_add_data_directory(const char* dir);                     // search path of referenced files
@@ -84,6 +96,11 @@ int32_t or_rates_batch(int32_t h, int32_t n, const double* T, const double* P, c
 
 // Reactor right-hand side for y = [m, T, Y1..YK] at pressure P: ydot[K+2].
 int32_t or_reactor_rhs(int32_t h, double P, const double* y, double* ydot);
+
+// Mole reactor (z = [T, n_1..n_K], kmol) at pressure P: right-hand side zdot[K+1], and the
+// preconditioner's Jacobian elements J[(K+1)^2] (row-major) at z clipped below at atol.
+int32_t or_mole_reactor_rhs(int32_t h, double P, const double* z, double* zdot);
+int32_t or_mole_precond_jacobian(int32_t h, double P, const double* z, double atol, double* J);
 
 // Advance n independent constant-pressure reactors from t=0 to t_end.
 //  T0[n], P[n], Y0[n][K] (reactor-major); outputs T[n], Y[n][K], stats[n][OR_NSTAT],

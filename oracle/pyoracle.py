@@ -18,9 +18,10 @@ SOURCES = [
     os.path.join(ROOT, "cantera_gb300", "csrc", "mechanism.cpp"),
     os.path.join(ROOT, "cantera_gb300", "csrc", "yaml_lite.cpp"),
 ]
-NSTAT = 9
+NSTAT = 12
 STAT_NAMES = ["steps", "rhs_evals", "newton_iters", "lin_setups", "jac_evals",
-              "err_test_fails", "conv_fails", "last_order", "status"]
+              "err_test_fails", "conv_fails", "last_order", "status", "lin_iters", "prec_solves",
+              "jtimes_evals"]
 
 
 def build(force=False):
@@ -39,17 +40,22 @@ class BdfOpts(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double),
                 ("max_steps", ctypes.c_int32), ("max_order", ctypes.c_int32),
                 ("analytic_jacobian", ctypes.c_int32), ("lu_fp32", ctypes.c_int32),
-                ("max_time_step", ctypes.c_double), ("jac_reuse", ctypes.c_int32)]
+                ("max_time_step", ctypes.c_double), ("jac_reuse", ctypes.c_int32),
+                ("mole_reactor", ctypes.c_int32), ("linear_solver", ctypes.c_int32)]
 
 
 def opts(rtol=1e-9, atol=1e-15, max_steps=20000, max_order=5, analytic=False,
-         lu_fp32=False, max_time_step=0.0, jac_reuse=None):
+         lu_fp32=False, max_time_step=0.0, jac_reuse=None, mole_reactor=False, gmres=False):
     """Integrator options.  Defaults follow the reference ReactorNet (rtol 1e-9, atol 1e-15,
-    20000 steps per advance, order 5, difference-quotient Jacobian kept between setups)."""
+    20000 steps per advance, order 5, difference-quotient Jacobian kept between setups).
+    mole_reactor: the reactor with moles as its state (IdealGasConstPressureMoleReactor);
+    gmres: GMRES with the adaptive preconditioner instead of the dense LU (mole reactor only)."""
     if jac_reuse is None:
         jac_reuse = not analytic
+    if (mole_reactor or gmres) and analytic:
+        raise ValueError("the mole reactor has no analytic Jacobian: use the difference-quotient one")
     return BdfOpts(rtol, atol, max_steps, max_order, int(analytic), int(lu_fp32), max_time_step,
-                   int(jac_reuse))
+                   int(jac_reuse), int(mole_reactor or gmres), int(gmres))
 
 
 _lib = None
@@ -80,6 +86,8 @@ def lib():
         L.or_rates.argtypes = [I32, ctypes.c_double, ctypes.c_double, D, D, D, D, D, D, D]
         L.or_ddci.argtypes = [I32, ctypes.c_double, ctypes.c_double, D, I32, D]
         L.or_reactor_rhs.argtypes = [I32, ctypes.c_double, D, D]
+        L.or_mole_reactor_rhs.argtypes = [I32, ctypes.c_double, D, D]
+        L.or_mole_precond_jacobian.argtypes = [I32, ctypes.c_double, D, ctypes.c_double, D]
         L.or_equivalence_ratio.argtypes = [I32, ctypes.c_double, D, D, D]
         L.or_mole_to_mass.argtypes = [I32, D, D]
         L.or_molecular_weights.argtypes = [I32, D]
@@ -186,6 +194,18 @@ class Mech:
         ydot = np.zeros(self.K + 2)
         lib().or_reactor_rhs(self.h, P, _p(_c(y)), _p(ydot))
         return ydot
+
+    def mole_reactor_rhs(self, P, z):
+        """Mole-reactor right-hand side for z = [T, n_1..n_K] (kmol) at pressure P."""
+        zdot = np.zeros(self.K + 1)
+        st = lib().or_mole_reactor_rhs(self.h, P, _p(_c(z)), _p(zdot))
+        return zdot, st
+
+    def mole_precond_jacobian(self, P, z, atol=1e-15):
+        """The adaptive preconditioner's Jacobian elements [K+1, K+1] at z."""
+        J = np.zeros((self.K + 1, self.K + 1))
+        st = lib().or_mole_precond_jacobian(self.h, P, _p(_c(z)), atol, _p(J))
+        return J, st
 
     def advance_batch(self, T0, P, Y0, t_end, o=None, threads=None):
         """Reactor-major Y0 [n][K].  Returns T [n], Y [n][K], stats [n][9], tign [n]."""

@@ -1,0 +1,131 @@
+"""The oracle's mole-reactor formulation with the preconditioned Krylov linear solver (no GPU):
+IdealGasConstPressureMoleReactor (state T and species moles) against the mass-fraction reactor,
+the adaptive preconditioner's Jacobian elements, and GMRES-with-preconditioner integrations
+against the direct solver with the bars of the reference's own test
+(test/python/test_reactor.py:1696-1727: Y within 5e-4 relative / 1e-6 absolute, T within 1e-5)
+and against the reference's blessed kin1 trajectory."""
+import numpy as np
+import pytest
+
+from conftest import oracle_mech
+
+R = 6.02214076e26 * 1.380649e-23
+
+
+def mole_state(m, T, P, Y, V=1.0):
+    rho = P / (R * T) / np.sum(Y / m.mw)
+    return np.concatenate([[T], rho * V * Y / m.mw])
+
+
+@pytest.mark.parametrize("name", ["h2o2", "gri30"])
+def test_mole_rhs_matches_mass_fraction_rhs(name):
+    """d/dt of the moles, turned into d/dt of the mass fractions (the mass is constant), and
+    dT/dt agree with the mass-fraction reactor's right-hand side."""
+    m = oracle_mech(name)
+    rng = np.random.default_rng(2)
+    for _ in range(5):
+        T = rng.uniform(900, 2500)
+        P = 101325.0 * 10 ** rng.uniform(-0.5, 1.5)
+        Y = rng.dirichlet(0.5 * np.ones(m.K))
+        z = mole_state(m, T, P, Y)
+        zdot, st = m.mole_reactor_rhs(P, z)
+        assert st == 0
+        ydot = m.reactor_rhs(P, np.concatenate([[1.0, T], Y]))
+        mass = np.sum(z[1:] * m.mw)
+        dY = zdot[1:] * m.mw / mass
+        assert zdot[0] == pytest.approx(ydot[1], rel=1e-12)
+        assert np.max(np.abs(dY - ydot[2:])) <= 1e-12 * np.max(np.abs(ydot[2:]))
+        # mass conservation of the mole form
+        assert abs(np.sum(zdot[1:] * m.mw)) <= 1e-12 * np.sum(np.abs(zdot[1:] * m.mw))
+
+
+def test_preconditioner_jacobian_elements():
+    """Species block = the reference's ddCi, temperature column = a one-sided difference of
+    the right-hand side, temperature row from the enthalpy-weighted species block."""
+    m = oracle_mech("gri30")
+    T, P = 1500.0, 3 * 101325.0
+    Y = np.random.default_rng(4).dirichlet(0.5 * np.ones(m.K))
+    z = mole_state(m, T, P, Y)
+    J, st = m.mole_precond_jacobian(P, z)
+    assert st == 0
+    D = m.ddci(T, P, Y, mode=0)
+    assert np.allclose(J[1:, 1:], D, rtol=1e-12, atol=1e-12 * np.max(np.abs(D)))
+    dT = T * np.sqrt(np.finfo(float).eps)
+    zp = z.copy()
+    zp[0] += dT
+    fp, _ = m.mole_reactor_rhs(P, zp)
+    f0, _ = m.mole_reactor_rhs(P, z)
+    assert np.allclose(J[:, 0], (fp - f0) / dT, rtol=1e-12, atol=0)
+    # the T row is the derivative of -sum_k h_k dn_k/dt / (m cp) with d(dn_k/dt)/dn_j from
+    # the species block and d(m cp)/dn_j = cp_j: check it against that formula's pieces
+    cp, h, _ = m.thermo(T)
+    hk, cpj = h * R * T, cp * R
+    mcp = np.sum(z[1:] * cpj)
+    qdot = np.sum(hk * f0[1:])
+    row = (cpj * qdot - mcp * (hk @ D)) / mcp ** 2
+    assert np.allclose(J[0, 1:], row, rtol=1e-10, atol=1e-10 * np.max(np.abs(row)))
+
+
+def test_gmres_matches_direct_solver():
+    """gri30 ignition at several initial temperatures: the mole reactor with GMRES and the
+    adaptive preconditioner, the mole reactor with the dense solver and the mass-fraction
+    reactor agree within the reference test's bars."""
+    from oracle import pyoracle as po
+    m = oracle_mech("gri30")
+    Y0 = m.equivalence_ratio(1.0, "CH4:1", "O2:1, N2:3.76")
+    T0 = np.array([1200.0, 1150.0, 1300.0, 1450.0])
+    P = np.array([101325.0, 3 * 101325.0, 101325.0, 10 * 101325.0])
+    Y = np.tile(Y0, (4, 1))
+    runs = {}
+    for name, o in [("mass", po.opts(rtol=1e-8, atol=1e-16)),
+                    ("mole", po.opts(rtol=1e-8, atol=1e-16, mole_reactor=True)),
+                    ("gmres", po.opts(rtol=1e-8, atol=1e-16, gmres=True))]:
+        T, Yo, st, tig = m.advance_batch(T0, P, Y, 0.1, o, threads=4)
+        assert np.all(st[:, 8] == 0), (name, st[:, 8])
+        runs[name] = (T, Yo, st, tig)
+    Tg, Yg, stg, tg = runs["gmres"]
+    for ref in ("mass", "mole"):
+        Tr, Yr, _, tr = runs[ref]
+        assert np.all(np.abs(Tg - Tr) <= 1e-5 * Tr)
+        assert np.all(np.abs(Yg - Yr) <= 5e-4 * np.abs(Yr) + 1e-6)
+        assert np.all(tr < 0.09) and np.all(np.abs(tg - tr) <= 1e-3 * tr)   # ignition inside the run
+    # the Krylov path did its work through J v products and preconditioner solves
+    lin, ps, jtv = stg[:, 9], stg[:, 10], stg[:, 11]
+    assert np.all(lin > 0) and np.all(jtv == lin) and np.all(ps > lin)
+    assert np.all(runs["mass"][2][:, 9] == 0)
+
+
+def test_gmres_kin1_blessed_trajectory(goldens):
+    """The reference's blessed h2o2 trajectory (kinetics1 sample) through the mole reactor
+    with GMRES and the adaptive preconditioner, with the DQ-Jacobian tolerance of the
+    direct-solver oracle test.  The absolute tolerance applies to moles here: 1e-17 kmol in the
+    reactor's 1 m^3 (about 0.012 kmol of gas) is the 1e-15 the blessed run put on mass fractions."""
+    from oracle import pyoracle as po
+    from test_oracle_goldens import _csv_close
+    g = goldens["kin1"]
+    m = oracle_mech("h2o2")
+    data = np.array(g["rows"])
+    Y0 = m.mole_to_mass(m.composition(g["setup"]["X"]))
+    out, st, rc = m.trajectory(1001.0, 101325.0, Y0, data[1:, 0], po.opts(gmres=True, atol=1e-17))
+    assert rc == 0 and st[9] > 0
+    T = np.concatenate([[1001.0], out[:, 0]])
+    Yt = np.vstack([Y0, out[:, 1:]])
+    X = Yt / m.mw
+    X /= X.sum(axis=1, keepdims=True)
+    idx = [m.species_index(n) for n in g["header"][4:]]
+    rho = 101325.0 / (R * T) / np.sum(Yt / m.mw, axis=1)
+    mine = np.column_stack([data[:, 0], T, rho, np.full_like(T, 101325.0), X[:, idx]])
+    ok = _csv_close(mine, data, 5e-4, g["threshold"])
+    assert ok.all(), np.argwhere(~ok)[:5]
+
+
+def test_gmres_needs_the_mole_reactor():
+    from oracle import pyoracle as po
+    m = oracle_mech("h2o2")
+    o = po.opts(gmres=True)
+    o.mole_reactor = 0
+    Y0 = m.equivalence_ratio(1.0, "H2:1", "O2:1, N2:3.76")
+    _, _, st, _ = m.advance_batch(np.array([1200.0]), np.array([101325.0]), Y0[None, :], 1e-4, o, threads=1)
+    assert st[0, 8] != 0
+    with pytest.raises(ValueError):
+        po.opts(gmres=True, analytic=True)
