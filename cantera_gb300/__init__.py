@@ -77,6 +77,9 @@ def library():
         "gb_net_new": (I32, [I32, I32, ctypes.POINTER(NetOptions)]),
         "gb_net_del": (I32, [I32]),
         "gb_net_set_state": (I32, [I32, P, P, P, I32]),
+        "gb_net_set_tolerances": (I32, [I32, D, D]),
+        "gb_net_set_max_steps": (I32, [I32, I32]),
+        "gb_net_set_max_time_step": (I32, [I32, D]),
         "gb_net_advance": (I32, [I32, D]),
         "gb_net_time": (D, [I32]),
         "gb_net_last_advance_ms": (D, [I32]),
@@ -289,8 +292,47 @@ class ReactorNet:
         o.lu_staging = int(lu_staging)
         n = T.shape[0] if _is_torch_cuda(T) else np.asarray(T).shape[0]
         self.n = n
+        self._rtol, self._atol, self._max_steps, self._max_time_step = rtol, atol, max_steps, max_time_step
         self._h = _check(L.gb_net_new(solution._h, n, ctypes.byref(o)))
         self.set_state(T, P, Y)
+
+    # integrator settings, applied from the next step on without restarting the integration
+    # (ReactorNet.rtol / atol / max_steps / max_time_step)
+    @property
+    def rtol(self):
+        return self._rtol
+
+    @rtol.setter
+    def rtol(self, v):
+        _check(library().gb_net_set_tolerances(self._h, float(v), -1.0))
+        self._rtol = float(v)
+
+    @property
+    def atol(self):
+        return self._atol
+
+    @atol.setter
+    def atol(self, v):
+        _check(library().gb_net_set_tolerances(self._h, -1.0, float(v)))
+        self._atol = float(v)
+
+    @property
+    def max_steps(self):
+        return self._max_steps
+
+    @max_steps.setter
+    def max_steps(self, v):
+        _check(library().gb_net_set_max_steps(self._h, int(v)))
+        self._max_steps = int(v)
+
+    @property
+    def max_time_step(self):
+        return self._max_time_step
+
+    @max_time_step.setter
+    def max_time_step(self, v):
+        _check(library().gb_net_set_max_time_step(self._h, float(v)))
+        self._max_time_step = float(v)
 
     def set_state(self, T, P, Y):
         n, T, P, Y, flags = self.solution._args(T, P, Y)

@@ -327,11 +327,11 @@ class ReactorNet:
         self._build()
 
     def _set(self, name, v):
-        """Change an integrator setting; a running network restarts from the reactors'
-        current states at the current time (ReactorNet reinitialises after such a change)."""
+        """Change an integrator setting; a running network takes it from its next step on
+        without restarting (as ReactorNet passes it to a live CVODES integrator)."""
         setattr(self, name, v)
         if self._engine is not None:
-            self._build()
+            setattr(self._engine, name[1:], v)
 
     @property
     def rtol(self):

@@ -910,6 +910,47 @@ int32_t gb_net_set_state(int32_t h, const double* T, const double* P, const doub
     });
 }
 
+// a captured advance holds the old settings: drop it so that the next advance re-captures
+static void dropGraph(NetEntry& ne) {
+    if (ne.graph) {
+        cudaGraphExecDestroy(ne.graph);
+        ne.graph = nullptr;
+    }
+    ne.graphTout = -1.0;
+}
+
+int32_t gb_net_set_tolerances(int32_t h, double rtol, double atol) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        if (!std::isfinite(rtol) || !std::isfinite(atol)) throw std::runtime_error("tolerances must be finite");
+        if (rtol > 0.0) ne.opts.rtol = rtol;
+        if (atol > 0.0) ne.opts.atol = atol;
+        dropGraph(ne);
+        return 0;
+    });
+}
+
+int32_t gb_net_set_max_steps(int32_t h, int32_t max_steps) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        if (max_steps <= 0) throw std::runtime_error("max_steps must be positive");
+        ne.opts.max_steps = max_steps;
+        dropGraph(ne);
+        return 0;
+    });
+}
+
+int32_t gb_net_set_max_time_step(int32_t h, double max_time_step) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        if (!(max_time_step >= 0.0) || !std::isfinite(max_time_step))
+            throw std::runtime_error("max_time_step must be finite and >= 0");
+        ne.opts.max_time_step = max_time_step;
+        dropGraph(ne);
+        return 0;
+    });
+}
+
 int32_t gb_net_advance(int32_t h, double t) {
     return guarded([&]() -> int32_t {
         NetEntry& ne = net(h);

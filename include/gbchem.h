@@ -111,6 +111,14 @@ int32_t gb_net_del(int32_t net);
 /* Set the initial state of every reactor and restart the integrators at time 0
  * (IdealGasConstPressureReactor::getState; ReactorNet::reinitialize). */
 int32_t gb_net_set_state(int32_t net, const double* T, const double* P, const double* Y, int32_t flags);
+/* Integrator settings of a running network, applied from the next step on without restarting
+ * the integration (ReactorNet::setTolerances / setMaxSteps / setMaxTimeStep,
+ * src/zeroD/ReactorNet.cpp:179-183,218-231,341-344, which pass them to CVODES unchanged:
+ * src/numerics/CVodesIntegrator.cpp:171-180,209-230).  A tolerance <= 0 keeps the current
+ * value; max_steps must be positive; max_time_step 0 means unlimited.  Returns 0 or GB_ERR. */
+int32_t gb_net_set_tolerances(int32_t net, double rtol, double atol);
+int32_t gb_net_set_max_steps(int32_t net, int32_t max_steps);
+int32_t gb_net_set_max_time_step(int32_t net, double max_time_step);
 /* Advance every reactor to time t (ReactorNet::advance: step past t, interpolate back).
  * Returns the number of reactors whose integration failed (status != 0), or GB_ERR. */
 int32_t gb_net_advance(int32_t net, double t);

@@ -222,3 +222,26 @@ def test_autotune_picks_a_measured_candidate():
     assert pick["seconds"] <= log[0]["seconds"] * 1.03
     cap = lambda e: e["shape"]["blocks"] * e["shape"]["warps_per_block"]
     assert all(cap(e) <= cap(pick) for e in log if e["seconds"] <= log[0]["seconds"] * 1.03)
+
+
+def test_settings_of_a_network():
+    """rtol / atol / max_steps / max_time_step set on a network (ReactorNet's setters) act
+    like the same values given at construction; invalid values are errors."""
+    import cantera_gb300 as gb
+    sol = gpu_solution("h2o2")
+    T0, P, Y0 = h2o2_batch(32, 23)
+    a = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=1e-7, atol=1e-14, max_time_step=1e-5)
+    b = gb.ReactorNet(sol, T0, P, Y0.T.copy())
+    b.rtol, b.atol, b.max_time_step = 1e-7, 1e-14, 1e-5
+    assert (b.rtol, b.atol, b.max_time_step) == (1e-7, 1e-14, 1e-5)
+    assert a.advance(2e-4) == 0 and b.advance(2e-4) == 0
+    Ta, Ya = a.get_state()
+    Tb, Yb = b.get_state()
+    assert np.array_equal(Ta, Tb) and np.array_equal(Ya, Yb)
+    c = gb.ReactorNet(sol, T0, P, Y0.T.copy())
+    c.max_steps = 3
+    assert c.advance(1e-3) > 0 and np.all(c.status == 1)
+    with pytest.raises(gb.GBError):
+        c.max_steps = 0
+    with pytest.raises(gb.GBError):
+        c.max_time_step = -1.0
