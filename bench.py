@@ -17,6 +17,7 @@ import json
 import math
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -63,7 +64,8 @@ class Clocks:
     def __init__(self, gpu):
         self.gpu = gpu
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        # the raw samples (the JSON line carries their summary)
+        self.path = os.environ.get("GBCHEM_CLOCKS_CSV") or os.path.join(tempfile.gettempdir(), "clocks_bench.csv")
 
     def __enter__(self):
         try:

@@ -583,7 +583,7 @@ std::mutex g_noallocMu;                           // held for the whole call
 void* g_noallocAddr[kNoAllocMaxDevices] = {};      // per device, looked up once
 
 // Device address of this device's copy of the scratch array.  The first lookup on a
-// device loads the module there (lazy loading), which the driver may not do inside a
+// device loads the module there (lazy loading), which the CUDA driver may not do inside a
 // stream capture, so the first call on each device must precede any capture.
 void* noallocScratch(int dev) {
     if (dev < 0 || dev >= kNoAllocMaxDevices) throw std::runtime_error("device ordinal out of range");
