@@ -34,3 +34,16 @@ def test_error_convention(tmp_path):
     L.gb_get_error(512, buf)
     assert "handle" in buf.value.decode()
     assert L.gb_mech_n_species(-1) == gb.GB_ERR
+
+
+def test_error_paths_of_the_network_settings_and_data_directories():
+    import cantera_gb300 as gb
+    L = gb.library()
+    buf = ctypes.create_string_buffer(512)
+    for rc in (L.gb_net_set_tolerances(12345, 1e-8, 1e-15), L.gb_net_set_max_steps(12345, 100),
+               L.gb_net_set_max_time_step(12345, 1e-3)):
+        assert rc == gb.GB_ERR
+        L.gb_get_error(512, buf)
+        assert "handle" in buf.value.decode()
+    assert L.gb_add_data_directory(None) == gb.GB_ERR
+    assert L.gb_add_data_directory(gb.DATA_DIR.encode()) == 0
