@@ -8,7 +8,18 @@ atol 1e-15 in one persistent launch with a device work queue.  Some reactors ign
 cold ones stay nearly inert.  A "step" re-initialises every reactor and advances all of
 them to 1e-2 s.  Inputs are synthetic (no dataset is involved).
 
+The JSON line: `value` (FP64 Newton matrix, state resident in HBM), `e2e` (the same through
+the public API with host arrays, copies in the timed region), `roofline` (FP64 operations
+of the algorithm per advance over the mean integrator launch, against the FP64 FMA rate
+measured live), `variants` (FP32 Newton matrix; the learned surrogate with its fallback),
+`workloads` (the other configurations of the hot path: h2o2 1,024 reactors, gri30 rates and
+Jacobian for 2^20 states, n-dodecane 16,384 reactors FP64 / FP32), `cpu_baseline` (the
+oracle built with the reference's release flags on the host cores), `error_vs_cpu_oracle`
+and `error_protocol` (against the oracle configured as the reference's ReactorNet, and
+against its tight run at rtol 1e-12, atol 1e-20, with ignition delays).
+
 Usage:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+        python bench.py --workload rates|ndodecane|h2o2      (one workload's line alone)
 Under torchrun each rank takes a contiguous shard of the reactors (no collective on the
 data path); the time is the maximum over ranks.
 """
@@ -128,7 +139,11 @@ def flop_model(st, N):
     lu = (2.0 / 3.0) * N ** 3 + N * Dv
     newton = 2 * N * N + 9 * N
     step = 40 * N + 4 * E
-    return {"rhs": rhs, "jac": jac, "lu": lu, "newton": newton, "step": step}
+    # the kinetics calls alone: wdot without the reactor's energy and species equations, and
+    # d(wdot)/dc (column entries, species scatter, the dense default-efficiency part)
+    rates = rhs - (4 * K + 10 + Dv)
+    ddci = 6 * st["jac_col_entries"] + 2 * st["jac_scatter_entries"] + 2 * K * K
+    return {"rhs": rhs, "jac": jac, "lu": lu, "newton": newton, "step": step, "rates": rates, "ddci": ddci}
 
 
 def algorithmic_flops(stats, fm, fp32_lu):
@@ -235,155 +250,274 @@ def surrogate_leg(sol, dev, torch):
                     % (SUR["train_reactors"], len(SUR["times"]), SUR["held_reactors"], len(SUR["held_times"]))}
 
 
+TIGHT = dict(rtol=1e-12, atol=1e-20)     # the tight reference run of the error protocol
+TIGHT_SAMPLE = 512                        # reactors of the headline workload in that protocol
+
+
+def oracle_opts(po, rtol, atol, tight=False):
+    """The reference's ReactorNet configuration (CVODES with its difference-quotient
+    Jacobian kept between setups); tight=True: the same method at rtol 1e-12, atol 1e-20."""
+    if tight:
+        return po.opts(rtol=TIGHT["rtol"], atol=TIGHT["atol"], analytic=False, jac_reuse=True)
+    return po.opts(rtol=rtol, atol=atol, analytic=False, jac_reuse=True)
+
+
 def cpu_baseline(T0, P, Y0, idx, threads, kind="port"):
-    """The CPU restatement of the reference path on this host's cores: the reference's
-    ReactorNet settings (difference-quotient Jacobian kept between setups) on a bounded,
-    seeded sample of the same workload."""
+    """The CPU restatement of the reference path on this host's cores, built with the
+    reference's release flags: the reference's ReactorNet settings (difference-quotient
+    Jacobian kept between setups) on a bounded, seeded sample of the same workload."""
     from oracle import pyoracle as po
-    m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", WL["mechanism"]), WL["phase"])
-    o = po.opts(rtol=WL["rtol"], atol=WL["atol"], analytic=False, jac_reuse=True)
+    m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", WL["mechanism"]), WL["phase"], fast=True)
+    o = oracle_opts(po, WL["rtol"], WL["atol"])
     t0 = time.perf_counter()
     T, Y, st, tig = m.advance_batch(T0[idx], P[idx], Y0[idx], WL["t_end"], o, threads=threads)
     dt = time.perf_counter() - t0
     return {"value": len(idx) / dt, "unit": "reactors/s", "cores": threads, "kind": kind,
             "sample": "%d seeded reactors of the workload (subset seed %d), oracle restatement of the "
-                      "reference path (not the reference binary), %d host threads, %.1f s"
-                      % (len(idx), WL["seed"] + 1000, threads, dt)}, (T, Y, st, tig)
+                      "reference path (not the reference binary) built with %s, %d host threads, %.1f s"
+                      % (len(idx), WL["seed"] + 1000, po.FLAGS[True], threads, dt)}, (T, Y, st, tig)
+
+
+def state_errors(T, Y, Tr, Yr, major_min=1e-3):
+    """T relative, major-species (Y_ref >= 1e-3) relative and Y absolute errors; Y, Yr
+    reactor-major."""
+    major = Yr >= major_min
+    return {"T_max_rel": float(np.max(np.abs(T - Tr) / Tr)),
+            "major_species_max_rel": float(np.max(np.abs(Y - Yr)[major] / Yr[major])) if major.any() else 0.0,
+            "Y_max_abs": float(np.max(np.abs(Y - Yr)))}
+
+
+def settled_mask(m, P, Tt, Yt, t_end, rtol):
+    """Reactors that are not in mid-ignition at t_end: a relative time shift of 1e-4 moves
+    their T by less than 10 x rtol (the tight run's own dT/dt)."""
+    dTdt = np.array([m.reactor_rhs(P[s], np.concatenate([[1.0, Tt[s]], Yt[s]]))[1] for s in range(len(P))])
+    return np.abs(dTdt) * 1e-4 * t_end < 10 * rtol * Tt
+
+
+def error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, gpu, threads):
+    """Error protocol of the integrator workloads on one sample: (i) against the CPU oracle
+    configured as the reference's ReactorNet at the same tolerances, (ii) against a tight
+    run of it (rtol 1e-12, atol 1e-20), with the oracle's own error against (ii) beside the
+    GPU's, and the ignition-delay (time of the largest dT/dt) error of every igniting
+    reactor.  gpu: {variant: (T [n], Y [n][K], tign [n])} on the same sample."""
+    t0 = time.perf_counter()
+    To, Yo, sto, tio = m.advance_batch(T0, P, Y0, t_end, oracle_opts(po, rtol, atol), threads=threads)
+    Tt, Yt, stt, tit = m.advance_batch(T0, P, Y0, t_end, oracle_opts(po, rtol, atol, tight=True), threads=threads)
+    secs = time.perf_counter() - t0
+    settled = settled_mask(m, P, Tt, Yt, t_end, rtol)
+    ign = (Tt > T0 + 400.0) & (tit > 0) & (tit < t_end)
+    bar = 10 * rtol
+    out = {"reactors": int(len(T0)), "igniting": int(ign.sum()), "settled": int(settled.sum()),
+           "bar_10rtol": bar, "tight": dict(TIGHT), "oracle_seconds": secs,
+           "oracle_vs_tight": {"all": state_errors(To, Yo, Tt, Yt),
+                               "settled": state_errors(To[settled], Yo[settled], Tt[settled], Yt[settled])},
+           "oracle_failed": int(np.sum(sto[:, 8] != 0) + np.sum(stt[:, 8] != 0))}
+    if ign.any():
+        out["oracle_vs_tight"]["ignition_delay_max_rel"] = float(np.max(np.abs(tio[ign] - tit[ign]) / tit[ign]))
+    for name, (Tg, Yg, tg) in gpu.items():
+        e = {"vs_tight": {"all": state_errors(Tg, Yg, Tt, Yt),
+                          "settled": state_errors(Tg[settled], Yg[settled], Tt[settled], Yt[settled])},
+             "vs_oracle": state_errors(Tg, Yg, To, Yo)}
+        if ign.any():
+            e["ignition_delay_max_rel_vs_oracle"] = float(np.max(np.abs(tg[ign] - tio[ign]) / tio[ign]))
+            e["ignition_delay_max_rel_vs_tight"] = float(np.max(np.abs(tg[ign] - tit[ign]) / tit[ign]))
+        a, o_ = e["vs_tight"]["all"], out["oracle_vs_tight"]["all"]
+        e["T_within_bar"] = a["T_max_rel"] <= bar
+        e["T_within_oracle_error"] = a["T_max_rel"] <= max(bar, o_["T_max_rel"])
+        e["major_species_within_oracle_error"] = a["major_species_max_rel"] <= max(bar, o_["major_species_max_rel"])
+        e["settled_T_within_bar"] = e["vs_tight"]["settled"]["T_max_rel"] <= bar
+        if ign.any():
+            e["ignition_within_1e-3"] = e["ignition_delay_max_rel_vs_oracle"] <= 1e-3
+        out[name] = e
+    return out
+
+
+def time_advance(net, T, P, Y, t_end, flush, torch):
+    """One timed advance from the given state (L2 flushed before it): CUDA events on the
+    engine's stream around the integrator launch (kernel ms) and on the host (wall ms)."""
+    flush.zero_()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net.set_state(T, P, Y)
+    bad = net.advance(t_end)
+    torch.cuda.synchronize()
+    return bad, net.last_kernel_ms, 1e3 * (time.perf_counter() - t0)
+
+
+def variant_h2o2(dev, torch, flush, threads):
+    """Plain method, small: h2o2, 1,024 reactors, T0 U[1000,1600] K, 1 atm, H2/air phi
+    U[0.5,2.0] (seed 20261203), to 1e-3 s at rtol 1e-8, atol 1e-15, every reactor compared
+    with the oracle (reference configuration and tight run)."""
+    import cantera_gb300 as gb
+    from oracle import pyoracle as po
+    sol = gb.Solution("h2o2.yaml", "ohmech")
+    n, t_end, rtol, atol = 1024, 1e-3, 1e-8, 1e-15
+    rng = np.random.default_rng(20261203 + 0)
+    T0 = rng.uniform(1000.0, 1600.0, n)
+    P = np.full(n, 101325.0)
+    phi = rng.uniform(0.5, 2.0, n)
+    Y0 = np.array([sol.equivalence_ratio_mass_fractions(p, "H2:1", "O2:1, N2:3.76") for p in phi])
+    d = lambda a: torch.tensor(a, device=dev)
+    Td, Pd, Yd = d(T0), d(P), d(np.ascontiguousarray(Y0.T))
+    res, gpu = {}, {}
+    for name, lu in (("fp64", 64), ("fp32_lu", 32)):
+        net = gb.ReactorNet(sol, Td, Pd, Yd, rtol=rtol, atol=atol, lu_precision=lu, use_graph=True)
+        for _ in range(3):
+            time_advance(net, Td, Pd, Yd, t_end, flush, torch)
+        runs = [time_advance(net, Td, Pd, Yd, t_end, flush, torch) for _ in range(5)]
+        ms = float(np.median([r[1] for r in runs]))
+        Tg, Yg = net.get_state()
+        res[name] = {"value": n / (ms / 1e3), "unit": "reactors/s", "kernel_ms": ms,
+                     "failed_reactors": int(runs[-1][0]),
+                     "solver_stats_mean": {k: float(v.mean()) for k, v in net.solver_stats.items()}}
+        gpu[name] = (Tg, Yg.T, net.ignition_times)
+        del net
+    m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "h2o2.yaml"), "ohmech")
+    errs = error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, gpu, threads)
+    mf = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "h2o2.yaml"), "ohmech", fast=True)
+    t0 = time.perf_counter()
+    mf.advance_batch(T0, P, Y0, t_end, oracle_opts(po, rtol, atol), threads=threads)
+    cpu = n / (time.perf_counter() - t0)
+    return dict(res["fp64"], variants={"fp32_lu": res["fp32_lu"]},
+                config={"workload": "h2o2, 1024 reactors, T0 U[1000,1600] K, 1 atm, H2/air phi U[0.5,2.0], "
+                                    "to 1e-3 s", "rtol": rtol, "atol": atol, "seed": 20261203},
+                errors=errs,
+                cpu_baseline={"value": cpu, "unit": "reactors/s", "cores": threads, "kind": "port",
+                              "sample": "all 1024 reactors, oracle restatement built with %s" % po.FLAGS[True]})
+
+
+def variant_rates(dev, torch, flush, threads, n=1 << 20, peaks=None):
+    """Rate evaluation only: gri30, 1,048,576 states, T U[300,3000] K, P log-U[0.1,100] atm,
+    Y ~ Dirichlet(0.5) (seed 20261204); wdot and wdot + d(wdot)/dc on the reference's
+    pattern, kernel time by CUDA events on the engine's stream, parity of the first 65,536
+    states against the oracle (gross-rate-scaled 1e-12 for wdot; 1e-12 of the state's
+    largest entry for the Jacobian)."""
+    import cantera_gb300 as gb
+    from oracle import pyoracle as po
+    sol = gb.Solution("gri30.yaml", "gri30")
+    K = sol.n_species
+    rng = np.random.default_rng(20261203 + 1)
+    T = rng.uniform(300.0, 3000.0, n)
+    P = 101325.0 * 10 ** rng.uniform(-1.0, 2.0, n)
+    Y = rng.dirichlet(0.5 * np.ones(K), n).T.copy()
+    Td, Pd, Yd = (torch.tensor(a, device=dev) for a in (T, P, Y))
+    fm = flop_model(sol.structure(), K + 1)
+    nnz = len(sol.jac_rowidx)
+    wdot = torch.empty((K, n), dtype=torch.float64, device=dev)
+    jac = torch.empty((nnz, n), dtype=torch.float64, device=dev)
+    out = {}
+    for mode in ("wdot", "wdot+jacobian"):
+        fn = (lambda: sol.net_production_rates(Td, Pd, Yd, out=wdot)) if mode == "wdot" else \
+             (lambda: sol.net_production_rates_ddCi(Td, Pd, Yd, vals=jac, wdot=wdot))
+        for _ in range(3):
+            fn()
+        ks = []
+        for _ in range(5):
+            flush.zero_()
+            torch.cuda.synchronize()
+            fn()
+            ks.append(sol.last_kernel_ms)
+        ms = float(np.median(ks))
+        bytes_ = n * ((K + 2) * 8 + K * 8 + (nnz * 8 if mode != "wdot" else 0))
+        flops = n * (fm["rates"] + (fm["ddci"] if mode != "wdot" else 0.0))
+        out[mode] = {"states_per_s": n / (ms / 1e3), "kernel_ms": ms,
+                     "algorithmic_bytes_per_state": bytes_ / n, "hbm_gbs": bytes_ / (ms / 1e3) / 1e9,
+                     "flops_per_state_model": flops / n, "fp64_tflops_model": flops / (ms / 1e3) / 1e12}
+    # parity of the first 65,536 states against the oracle (checker build)
+    ns = 65536
+    m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "gri30.yaml"), "gri30")
+    wo, jo, gross = m.rates_batch(T[:ns], P[:ns], np.ascontiguousarray(Y[:, :ns]), mode=1,
+                                  pattern=(sol.jac_colptr, sol.jac_rowidx), threads=threads, gross=True)
+    wg = wdot[:, :ns].cpu().numpy()
+    jg = jac[:, :ns].cpu().numpy()
+    w_err = float(np.max(np.abs(wg - wo) / (gross + 1e-300)))
+    j_err = float(np.max(np.max(np.abs(jg - jo), axis=0) / np.maximum(np.max(np.abs(jo), axis=0), 1e-300)))
+    parity = {"states": ns, "wdot_max_err_over_gross": w_err, "wdot_within_1e-12": w_err <= 1e-12,
+              "jac_max_err_over_state_max": j_err, "jac_within_1e-12": j_err <= 1e-12}
+    # CPU: the timing build on the same 65,536 states, all host threads
+    mf = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "gri30.yaml"), "gri30", fast=True)
+    t0 = time.perf_counter()
+    mf.rates_batch(T[:ns], P[:ns], np.ascontiguousarray(Y[:, :ns]), mode=0, threads=threads)
+    cpu_w = ns / (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    mf.rates_batch(T[:ns], P[:ns], np.ascontiguousarray(Y[:, :ns]), mode=1,
+                   pattern=(sol.jac_colptr, sol.jac_rowidx), threads=threads)
+    cpu_j = ns / (time.perf_counter() - t0)
+    hbm = (peaks or {}).get("hbm_gbs")
+    return {"value": out["wdot"]["states_per_s"], "unit": "states/s", "modes": out,
+            "config": {"workload": "gri30, %d states, T U[300,3000] K, P log-U[0.1,100] atm, Y Dirichlet(0.5)" % n,
+                       "seed": 20261204, "l2": "flushed (256 MB write) before every timed call"},
+            "hbm_roofline": {"peak_gbs": hbm, "frac_wdot": out["wdot"]["hbm_gbs"] / hbm if hbm else None,
+                             "frac_jacobian": out["wdot+jacobian"]["hbm_gbs"] / hbm if hbm else None,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else None},
+            "parity_vs_oracle": parity,
+            "cpu_baseline": {"value": cpu_w, "unit": "states/s (wdot)", "value_jacobian": cpu_j, "cores": threads,
+                             "kind": "port", "sample": "%d of the states, oracle restatement built with %s"
+                                                       % (ns, po.FLAGS[True])}}
+
+
+def variant_ndodecane(dev, torch, flush, threads, n=16384, sample=64):
+    """Mixed-precision Newton: nDodecane_IG (K=100, R=553), 16,384 reactors, T0 U[700,1400] K,
+    P log-U[10,60] atm, n-dodecane/air phi U[0.5,2.0] (seed 20261206), to 5e-3 s at rtol 1e-8:
+    FP64 Newton matrix vs FP32, with Newton counts and the error protocol on a sample."""
+    import cantera_gb300 as gb
+    from oracle import pyoracle as po
+    sol = gb.Solution("nDodecane_Reitz.yaml", "nDodecane_IG")
+    t_end, rtol, atol = 5e-3, 1e-8, 1e-15
+    rng = np.random.default_rng(20261203 + 3)
+    T0 = rng.uniform(700.0, 1400.0, n)
+    P = 101325.0 * 10 ** rng.uniform(1.0, math.log10(60.0), n)
+    phi = rng.uniform(0.5, 2.0, n)
+    Y0 = np.array([sol.equivalence_ratio_mass_fractions(p, "c12h26:1", "o2:1, n2:3.76") for p in phi])
+    Td, Pd, Yd = (torch.tensor(a, device=dev) for a in (T0, P, np.ascontiguousarray(Y0.T)))
+    idx = cpu_sample_indices(n, sample, 20261203 + 3)
+    res, gpu = {}, {}
+    for name, lu in (("fp64", 64), ("fp32_lu", 32)):
+        net = gb.ReactorNet(sol, Td, Pd, Yd, rtol=rtol, atol=atol, lu_precision=lu)
+        net.advance(1e-7)          # untimed first launch (module load, attributes)
+        bad, ms, wall = time_advance(net, Td, Pd, Yd, t_end, flush, torch)
+        Tg, Yg = net.get_state()
+        st = net.solver_stats
+        res[name] = {"value": n / (ms / 1e3), "unit": "reactors/s", "kernel_ms": ms, "wall_ms": wall,
+                     "failed_reactors": int(bad), "launch": net.launch_info,
+                     "newton_iters_mean": float(st["newton_iters"].mean()), "steps_mean": float(st["steps"].mean()),
+                     "solver_stats_mean": {k: float(v.mean()) for k, v in st.items()}}
+        gpu[name] = (Tg[idx], Yg[:, idx].T, net.ignition_times[idx])
+        del net
+    m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "nDodecane_Reitz.yaml"), "nDodecane_IG")
+    errs = error_protocol(m, po, T0[idx], P[idx], Y0[idx], t_end, rtol, atol, gpu, threads)
+    mf = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "nDodecane_Reitz.yaml"), "nDodecane_IG", fast=True)
+    t0 = time.perf_counter()
+    mf.advance_batch(T0[idx], P[idx], Y0[idx], t_end, oracle_opts(po, rtol, atol), threads=threads)
+    cpu = len(idx) / (time.perf_counter() - t0)
+    return dict(res["fp64"], variants={"fp32_lu": res["fp32_lu"]},
+                config={"workload": "nDodecane_IG (K=100, R=553), %d reactors, T0 U[700,1400] K, P log-U[10,60] atm, "
+                                    "phi U[0.5,2.0], to 5e-3 s" % n, "rtol": rtol, "atol": atol,
+                        "seed": 20261206, "l2": "flushed (256 MB write) before the timed advance"},
+                errors=errs,
+                cpu_baseline={"value": cpu, "unit": "reactors/s", "cores": threads, "kind": "port",
+                              "sample": "%d seeded reactors, oracle restatement built with %s" % (len(idx), po.FLAGS[True])})
 
 
 def run_workload(args):
-    """The other workloads of the hot path, one JSON line each (not the headline):
-    rates - gri30 net production rates and their Jacobian for 1,048,576 random states;
-    ndodecane - 16,384 n-dodecane reactors to 5e-3 s, FP64 vs FP32-LU Newton;
-    h2o2 - 1,024 hydrogen/air reactors to 1e-3 s against the CPU oracle for every reactor."""
+    """One secondary workload on its own, one JSON line (the default run carries all of
+    them in the headline line's "workloads")."""
     import torch
-    import cantera_gb300 as gb
-    from oracle import pyoracle as po
     dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     threads = os.cpu_count()
-    if args.workload == "rates":
-        sol = gb.Solution("gri30.yaml", "gri30")
-        K = sol.n_species
-        n = args.n if args.n != WL["n"] else 1 << 20
-        rng = np.random.default_rng(20261203 + 1)
-        T = rng.uniform(300.0, 3000.0, n)
-        P = 101325.0 * 10 ** rng.uniform(-1.0, 2.0, n)
-        Y = rng.dirichlet(0.5 * np.ones(K), n).T.copy()
-        Td, Pd, Yd = (torch.tensor(a, device=dev) for a in (T, P, Y))
-        out = {}
-        for mode in ("wdot", "wdot+jacobian"):
-            fn = (lambda: sol.net_production_rates(Td, Pd, Yd)) if mode == "wdot" else \
-                 (lambda: sol.net_production_rates_ddCi(Td, Pd, Yd))
-            for _ in range(args.warmup):
-                r = fn()
-                del r
-            torch.cuda.synchronize()
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-            ev[0].record()
-            for _ in range(args.steps):
-                r = fn()
-                del r
-            ev[1].record()
-            torch.cuda.synchronize()
-            ms = ev[0].elapsed_time(ev[1]) / args.steps
-            nnz = len(sol.jac_rowidx)
-            bytes_ = n * ((K + 2) * 8 + K * 8 + (nnz * 8 if mode != "wdot" else 0))
-            out[mode] = {"states_per_s": n / (ms / 1e3), "ms": ms, "hbm_gbs": bytes_ / (ms / 1e3) / 1e9}
-        # CPU: the oracle's rates (and analytic Jacobian) on a sample, all host threads
-        m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "gri30.yaml"), "gri30")
-        ns = 65536
-        t0 = time.perf_counter()
-        m.rates_batch(T[:ns], P[:ns], np.ascontiguousarray(Y[:, :ns]), threads=threads)
-        cpu = ns / (time.perf_counter() - t0)
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
-        line = {"metric": "GRI-30 net production rates (and Jacobian) per second, 1 GB300", "value": out["wdot"]["states_per_s"],
-                "unit": "states/s", "workload": "rates", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-                "dtype": "f64", "data": "synthetic", "higher_is_better": True,
-                "config": {"workload": "gri30, %d states, T U[300,3000] K, P log-U[0.1,100] atm, Y Dirichlet(0.5)" % n},
-                "modes": out, "hbm_peak_gbs": peaks.get("hbm_gbs"),
-                "cpu_baseline": {"value": cpu, "unit": "states/s (wdot)", "cores": threads, "kind": "port",
-                                 "sample": "%d of the states, oracle restatement" % ns}}
-        print(json.dumps(line))
-        return
-    if args.workload == "ndodecane":
-        sol = gb.Solution("nDodecane_Reitz.yaml", "nDodecane_IG")
-        K = sol.n_species
-        n = args.n if args.n != WL["n"] else 16384
-        rng = np.random.default_rng(20261203 + 3)
-        T0 = rng.uniform(700.0, 1400.0, n)
-        P = 101325.0 * 10 ** rng.uniform(1.0, math.log10(60.0), n)
-        phi = rng.uniform(0.5, 2.0, n)
-        Y0 = np.array([sol.equivalence_ratio_mass_fractions(p, "c12h26:1", "o2:1, n2:3.76") for p in phi])
-        Td, Pd, Yd = (torch.tensor(a, device=dev) for a in (T0, P, np.ascontiguousarray(Y0.T)))
-        res = {}
-        for lu in (64, 32):
-            net = gb.ReactorNet(sol, Td, Pd, Yd, rtol=1e-8, atol=1e-15, lu_precision=lu, use_graph=True)
-            net.advance(5e-3)
-            net.set_state(Td, Pd, Yd)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            net.advance(5e-3)
-            torch.cuda.synchronize()
-            dt = time.perf_counter() - t0
-            Tg, Yg = net.get_state()
-            st = net.solver_stats
-            res[lu] = {"reactors_per_s": n / dt, "seconds": dt, "launch": net.launch_info,
-                       "newton_iters_mean": float(st["newton_iters"].mean()), "steps_mean": float(st["steps"].mean()),
-                       "T": Tg, "Y": Yg}
-        ns = 64
-        m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "nDodecane_Reitz.yaml"), "nDodecane_IG")
-        t0 = time.perf_counter()
-        To, Yo, sto, _ = m.advance_batch(T0[:ns], P[:ns], Y0[:ns], 5e-3, po.opts(rtol=1e-8, atol=1e-15), threads=threads)
-        cpu = ns / (time.perf_counter() - t0)
-        err = {}
-        for lu in (64, 32):
-            Tg, Yg = res[lu].pop("T"), res[lu].pop("Y")
-            maj = Yo > 1e-2
-            err[lu] = {"T_max_rel_vs_oracle": float(np.max(np.abs(Tg[:ns] - To) / To)),
-                       "major_species_max_rel_vs_oracle": float(np.max((np.abs(Yg[:, :ns].T - Yo))[maj] / Yo[maj]))}
-        line = {"metric": "n-dodecane reactors advanced/s, FP64 vs FP32-LU Newton, 1 GB300",
-                "value": res[64]["reactors_per_s"], "unit": "reactors/s", "workload": "ndodecane", "n_gpus": 1,
-                "dtype": "f64", "data": "synthetic", "higher_is_better": True,
-                "config": {"workload": "nDodecane_IG (K=100, R=553), %d reactors, T0 U[700,1400] K, P log-U[10,60] atm, "
-                                       "phi U[0.5,2.0], to 5e-3 s, rtol 1e-8" % n},
-                "fp64": res[64], "fp32_lu": res[32], "error": {"fp64": err[64], "fp32_lu": err[32]},
-                "cpu_baseline": {"value": cpu, "unit": "reactors/s", "cores": threads, "kind": "port",
-                                 "sample": "%d reactors, oracle restatement (difference-quotient Jacobian)" % ns}}
-        print(json.dumps(line))
-        return
-    if args.workload == "h2o2":
-        sol = gb.Solution("h2o2.yaml", "ohmech")
-        n = 1024
-        rng = np.random.default_rng(20261203 + 0)
-        T0 = rng.uniform(1000.0, 1600.0, n)
-        P = np.full(n, 101325.0)
-        phi = rng.uniform(0.5, 2.0, n)
-        Y0 = np.array([sol.equivalence_ratio_mass_fractions(p, "H2:1", "O2:1, N2:3.76") for p in phi])
-        net = gb.ReactorNet(sol, T0, P, np.ascontiguousarray(Y0.T), rtol=1e-8, atol=1e-15)
-        net.advance(1e-3)
-        net.set_state(T0, P, np.ascontiguousarray(Y0.T))
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        net.advance(1e-3)
-        dt = time.perf_counter() - t0
-        Tg, Yg = net.get_state()
-        tig = net.ignition_times
-        m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "h2o2.yaml"), "ohmech")
-        t0 = time.perf_counter()
-        To, Yo, sto, tio = m.advance_batch(T0, P, Y0, 1e-3, po.opts(rtol=1e-8, atol=1e-15), threads=threads)
-        cpu = n / (time.perf_counter() - t0)
-        maj = Yo > 1e-3
-        line = {"metric": "H2/air reactors advanced/s, 1 GB300", "value": n / dt, "unit": "reactors/s",
-                "workload": "h2o2", "n_gpus": 1, "dtype": "f64", "data": "synthetic", "higher_is_better": True,
-                "config": {"workload": "h2o2, 1024 reactors, T0 U[1000,1600] K, 1 atm, phi U[0.5,2.0], to 1e-3 s, rtol 1e-8"},
-                "error_vs_oracle_all_reactors": {"T_max_rel": float(np.max(np.abs(Tg - To) / To)),
-                                                 "major_species_max_rel": float(np.max(np.abs(Yg.T - Yo)[maj] / Yo[maj])),
-                                                 "ignition_time_max_rel": float(np.max(np.abs(tig - tio) / tio))},
-                "cpu_baseline": {"value": cpu, "unit": "reactors/s", "cores": threads, "kind": "port",
-                                 "sample": "all 1024 reactors, oracle restatement"}}
-        print(json.dumps(line))
-        return
+    fn = {"rates": lambda: variant_rates(dev, torch, flush, threads, peaks=measured_peaks()),
+          "ndodecane": lambda: variant_ndodecane(dev, torch, flush, threads),
+          "h2o2": lambda: variant_h2o2(dev, torch, flush, threads)}[args.workload]
+    line = dict(workload=args.workload, n_gpus=1, dtype="f64", data="synthetic", higher_is_better=True)
+    line.update(fn())
+    print(json.dumps(line))
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    return json.load(open(path)) if os.path.exists(path) else {}
 
 
 def run_reference(args):
@@ -391,7 +525,7 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle import pyoracle as po
-    m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", WL["mechanism"]), WL["phase"])
+    m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", WL["mechanism"]), WL["phase"], fast=True)
     T0, P, Y0 = workload_arrays(WL["n"], WL["seed"],
                                 lambda p: m.equivalence_ratio(p, WL["fuel"], WL["oxidizer"]))
     threads = os.cpu_count()
@@ -425,6 +559,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the other workloads (h2o2, rates, n-dodecane) of the default run")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the launch-shape autotuner (use the engine's rule)")
     ap.add_argument("--lu-staging", type=int, default=0,
@@ -507,25 +643,30 @@ def main():
         barrier()
         ms = sum(a.elapsed_time(b) for a, b in ev)
         ms_max = maxover(ms)
+        # the counters are reset by set_state: they hold the last advance (one step's work)
         stats = net.solver_stats
         f64, f32 = algorithmic_flops(stats, fm, lu == 32)
         Tg, Yg = net.get_state()
         results[variant] = {"ms": ms_max, "steps": steps, "kernel_ms": kernel_ms, "failed": int(bad), "launch": launch,
                             "f64": f64, "f32": f32, "clocks": clk.summary(), "T": Tg, "Y": Yg,
+                            "tign": net.ignition_times,
                             "stats": {k: float(v.mean()) for k, v in stats.items()}}
         del net
 
-    # end to end through the public API with host buffers: H2D of the initial state,
-    # the advance, D2H of the final state, every step
+    # end to end through the public API with host buffers: every step the H2D copy of the
+    # initial state, the advance and the D2H copy of the final state; one untimed step
+    # first (the advance's graph capture), then the mean over the timed steps
     shape = dict(tuned)
     shape.setdefault("matrix_placement", args.matrix_placement)
     net = gb.ReactorNet(sol, Ts, Ps, Ys, rtol=WL["rtol"], atol=WL["atol"], lu_precision=64, use_graph=True,
                         lu_staging=args.lu_staging, **shape)
     Th = np.empty(n)
     Yh = np.empty((K, n))
+    net.advance(WL["t_end"])
+    net.get_state(Th, Yh)
     barrier()
     e2e_ms = 0.0
-    e2e_steps = 1
+    e2e_steps = max(1, min(args.steps, 3))
     for i in range(e2e_steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -546,9 +687,10 @@ def main():
         return
     r64 = results["fp64"]
     value = n_all * r64["steps"] / (r64["ms"] / 1e3)
-    kernel_s = r64["kernel_ms"] / 1e3 / r64["steps"]
-    achieved = r64["f64"] / r64["steps"] / kernel_s / 1e12   # this rank's launches
+    kernel_s = r64["kernel_ms"] / 1e3 / r64["steps"]       # mean integrator launch
+    achieved = r64["f64"] / kernel_s / 1e12                  # FLOPs of one advance / its launch
     peak = fp["gflops"] / 1e3
+    fpr = r64["f64"] / n
     line = {"metric": METRIC, "value": value, "unit": "reactors/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r64["ms"] / r64["steps"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -562,7 +704,8 @@ def main():
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": read_traffic(),
                          "peak_source": "FP64 FMA rate measured live by this run (MEASURED_PEAKS.json has no FP64 figure)",
-                         "flops_per_reactor": r64["f64"] / r64["steps"] / n_all,
+                         "flops_per_reactor": fpr, "kernel_ms_mean": kernel_s * 1e3,
+                         "ceiling_reactors_per_s": peak * 1e12 / fpr,
                          "exp_fma_declared": EXP_FMA, "log_fma_declared": LOG_FMA,
                          "exp_fma_measured": fp["exp_fma"], "log_fma_measured": fp["log_fma"]},
             "clocks": r64["clocks"], "gpu_launches": args.steps,
@@ -575,22 +718,42 @@ def main():
                                         "ms_per_step": r32["ms"] / r32["steps"],
                                         "solver_stats_mean": r32["stats"], "failed_reactors": r32["failed"],
                                         "clocks": r32["clocks"]}}
+    threads = os.cpu_count()
     if not args.no_surrogate and ws == 1:
         try:
             line.setdefault("variants", {})["surrogate"] = surrogate_leg(sol, dev, torch)
         except Exception as e:   # the learned arm must not cost the FP64 line
             line.setdefault("variants", {})["surrogate"] = {"error": "%s: %s" % (type(e).__name__, e)}
+    # the other workloads of the hot path (their own configurations), each with its errors
+    # and its CPU baseline
+    if not args.no_workloads and ws == 1:
+        wl = {}
+        for name, fn in (("h2o2_1024", lambda: variant_h2o2(dev, torch, flush, threads)),
+                         ("rates_gri30_2p20", lambda: variant_rates(dev, torch, flush, threads, peaks=measured_peaks())),
+                         ("ndodecane_16384", lambda: variant_ndodecane(dev, torch, flush, threads))):
+            try:
+                t0 = time.perf_counter()
+                wl[name] = fn()
+                wl[name]["seconds"] = time.perf_counter() - t0
+            except Exception as e:
+                wl[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+        line["workloads"] = wl
     if not args.no_cpu_baseline and ws == 1:
         idx = cpu_sample_indices(n_all, CPU_SAMPLE, WL["seed"])
-        cb, (To, Yo, sto, tio) = cpu_baseline(T0, P, Y0, idx, os.cpu_count())
+        cb, (To, Yo, sto, tio) = cpu_baseline(T0, P, Y0, idx, threads)
         line["cpu_baseline"] = cb
         err = {}
         for vname, r in results.items():
             Tg, Yg = r["T"][idx], r["Y"][:, idx].T
-            err[vname] = {"T_max_rel": float(np.max(np.abs(Tg - To) / To)),
-                          "Y_max_abs": float(np.max(np.abs(Yg - Yo))),
-                          "major_species_max_rel": float(np.max(np.abs(Yg - Yo)[Yo > 1e-3] / Yo[Yo > 1e-3]))}
+            err[vname] = state_errors(Tg, Yg, To, Yo)
         line["error_vs_cpu_oracle"] = err
+        # the error protocol: reference-configured oracle and tight run on a seeded sample
+        from oracle import pyoracle as po
+        m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", WL["mechanism"]), WL["phase"])
+        tidx = cpu_sample_indices(n_all, TIGHT_SAMPLE, WL["seed"] + 7)
+        gpu = {v: (r["T"][tidx], r["Y"][:, tidx].T, r["tign"][tidx]) for v, r in results.items()}
+        line["error_protocol"] = error_protocol(m, po, T0[tidx], P[tidx], Y0[tidx], WL["t_end"], WL["rtol"],
+                                                WL["atol"], gpu, threads)
     print(json.dumps(line))
     if pg:
         pg.destroy_process_group()

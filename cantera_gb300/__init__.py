@@ -81,7 +81,9 @@ def library():
         "gb_net_set_max_steps": (I32, [I32, I32]),
         "gb_net_set_max_time_step": (I32, [I32, D]),
         "gb_net_advance": (I32, [I32, D]),
+        "gb_net_step": (I32, [I32, P, I32]),
         "gb_net_time": (D, [I32]),
+        "gb_kin_last_kernel_ms": (D, [I32]),
         "gb_net_last_advance_ms": (D, [I32]),
         "gb_net_get_state": (I32, [I32, P, P, I32]),
         "gb_net_get_status": (I32, [I32, P]),
@@ -230,6 +232,12 @@ class Solution:
         Y = _host(Y, (self.n_species, n))
         return n, T, P, Y, 0
 
+    @property
+    def last_kernel_ms(self):
+        """Device time (ms) of the kernel of the last rates or ddCi call (CUDA events on the
+        engine's stream)."""
+        return library().gb_kin_last_kernel_ms(self._h)
+
     def net_production_rates(self, T, P, Y, out=None):
         """wdot[K, n] (kmol/m^3/s) for n states; Y is species-major [K, n]."""
         n, T, P, Y, flags = self._args(T, P, Y)
@@ -343,6 +351,16 @@ class ReactorNet:
     def advance(self, t):
         """Advance every reactor to time t; returns the number of failed reactors."""
         return _check(library().gb_net_advance(self._h, float(t)))
+
+    def step(self, times=None):
+        """One internal integrator step of every reactor (ReactorNet.step).  Returns each
+        reactor's new time ([n]; written into `times` when given, a CUDA tensor or a numpy
+        array).  The network's time becomes the latest of them."""
+        flags = GB_DEVICE_POINTERS if _is_torch_cuda(times) else 0
+        if times is None:
+            times = np.empty(self.n)
+        self.last_step_failures = _check(library().gb_net_step(self._h, _ptr(times), flags))
+        return times
 
     @property
     def launch_info(self):

@@ -311,7 +311,26 @@ class ReactorNet:
         return self._t
 
     def step(self):
-        raise NotImplementedError("ReactorNet.step: a batched network advances to given times only")
+        """Take one internal integrator step (ReactorNet.step: one CVODES step towards
+        time + 1, the state at the step's end, no interpolation) and return the new time.
+        With one reactor this is the reference's step.  The reactors of a batched network
+        are independent, so each takes a step of its own size; the network's time becomes
+        the latest of their times (each reactor's state is at its own time, in
+        ``reactor_times``), and a later advance(t) needs t >= that time."""
+        if self._engine is None:
+            self._build()
+        times = self._engine.step()
+        failed = self._engine.last_step_failures
+        self.reactor_times = times + self._t0
+        self._t = float(np.max(times)) + self._t0
+        T, Y = self._engine.get_state()
+        for i, r in enumerate(self._reactors):
+            r._thermo._T = float(T[i])
+            r._thermo._Y = Y[:, i].copy()
+        if failed:
+            bad = np.nonzero(self._engine.status)[0]
+            raise CanteraError("%d reactor(s) failed in their step (first: %s)" % (failed, bad[:8].tolist()))
+        return self._t
 
     @property
     def time(self):

@@ -73,9 +73,16 @@ struct MechEntry {
     std::vector<int32_t> jcPtr, jrIdx;
     cudaStream_t stream = nullptr;
     int smCount = 0;
+    int device = -1;      // the CUDA device the mechanism's arena and stream live on
     // kinetics workspace
     DBuf dT, dP, dY, dW, dJ, dCounter;
-    ~MechEntry() { if (stream) cudaStreamDestroy(stream); }
+    cudaEvent_t evA = nullptr, evB = nullptr;   // around the last kinetics kernel launch
+    double lastMs = 0.0;
+    ~MechEntry() {
+        if (evA) cudaEventDestroy(evA);
+        if (evB) cudaEventDestroy(evB);
+        if (stream) cudaStreamDestroy(stream);
+    }
 };
 
 struct NetEntry {
@@ -84,7 +91,7 @@ struct NetEntry {
     gb_net_options opts;
     double time = 0.0;
     int warpsPerBlock = 0, blocks = 0, ld = 0, warpDoubles = 0, recStride = 0;
-    DBuf dP, dT, dY, dRec, dStats, dStatus, dTign, dCounter, dOrder, dM, dJ, dJS;
+    DBuf dP, dT, dY, dRec, dStats, dStatus, dTign, dCounter, dOrder, dM, dJ, dJS, dTnow;
     size_t JSstride = 0;  // bytes per Jacobian-scratch slot in dJS (with global matrices)
     size_t Jstride = 0;   // bytes per kept-Jacobian slot in dJ (0: no Jacobian reuse)
     size_t Mstride = 0;   // bytes per Newton-matrix slot in dM (0: matrices in shared memory)
@@ -112,6 +119,18 @@ MechEntry& mech(int32_t h) {
     if (h < 0 || h >= (int32_t)g_mechs.size() || !g_mechs[h]) throw std::runtime_error("invalid mechanism handle " + std::to_string(h));
     return *g_mechs[h];
 }
+// The mechanism's device arrays and stream belong to the device that was current at
+// gb_mech_load; a kernel launched with another device current would read another GPU's
+// memory, so every call that launches work checks the current device first.
+void requireMechDevice(const MechEntry& e) {
+    int dev = -1;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev != e.device)
+        throw std::runtime_error("the current CUDA device (" + std::to_string(dev) +
+                                 ") is not the device the mechanism was loaded on (" +
+                                 std::to_string(e.device) + ")");
+}
+
 NetEntry& net(int32_t h) {
     std::lock_guard<std::mutex> lk(g_mu);
     if (h < 0 || h >= (int32_t)g_nets.size() || !g_nets[h]) throw std::runtime_error("invalid reactor network handle " + std::to_string(h));
@@ -449,6 +468,7 @@ const double* stage(const double* src, size_t count, DBuf& buf, bool device, cud
 int32_t runRates(int32_t h, int32_t n, const double* T, const double* P, const double* Y, double* wdot,
                  double* vals, int32_t flags) {
     MechEntry& e = mech(h);
+    requireMechDevice(e);
     if (n < 0) throw std::runtime_error("negative number of states");
     if (n == 0) return 0;
     const bool dev = (flags & GB_DEVICE_POINTERS) != 0;
@@ -480,10 +500,19 @@ int32_t runRates(int32_t h, int32_t n, const double* T, const double* P, const d
     int wpb = std::max(1, std::min(8, (budget - p.mechSmem) / (p.warpDoubles * 8)));
     int blocksPerSm = std::max(1, (228 * 1024) / (p.mechSmem + p.warpDoubles * 8 * wpb + 1024));
     int blocks = std::min(e.smCount * blocksPerSm, (n + wpb - 1) / wpb);
+    if (!e.evA) {
+        ck(cudaEventCreate(&e.evA), "event");
+        ck(cudaEventCreate(&e.evB), "event");
+    }
+    ck(cudaEventRecord(e.evA, s), "event record");
     ck(launchRates(p, blocks, wpb, s), "rates kernel launch");
+    ck(cudaEventRecord(e.evB, s), "event record");
     if (wdot && !dev) ck(cudaMemcpyAsync(wdot, dW, (size_t)K * n * 8, cudaMemcpyDeviceToHost, s), "copy wdot");
     if (vals && !dev) ck(cudaMemcpyAsync(vals, dJ, (size_t)e.dm.nnz * n * 8, cudaMemcpyDeviceToHost, s), "copy jac");
     ck(cudaStreamSynchronize(s), "rates kernel");
+    float ms = 0.f;
+    ck(cudaEventElapsedTime(&ms, e.evA, e.evB), "event time");
+    e.lastMs = ms;
     return 0;
 }
 
@@ -546,8 +575,10 @@ void chooseBdfLaunch(const MechEntry& me, const gb_net_options& o, int n, bool f
     ne.blocks = std::min(me.smCount * blocksPerSm, (n + bestFit - 1) / bestFit);
 }
 
-void netLaunch(NetEntry& ne, MechEntry& me, double t0, double tout) {
+void netLaunch(NetEntry& ne, MechEntry& me, double t0, double tout, bool oneStep = false) {
     BdfParams p{};
+    p.oneStep = oneStep ? 1 : 0;
+    p.tnow = ne.dTnow.p ? ne.dTnow.as<double>() : nullptr;
     p.m = me.dm; p.n = ne.n; p.t0 = t0; p.tout = tout;
     p.rtol = ne.opts.rtol; p.atol = ne.opts.atol;
     p.hmaxInv = ne.opts.max_time_step > 0 ? 1.0 / ne.opts.max_time_step : 0.0;
@@ -641,6 +672,7 @@ int32_t gb_mech_load(const char* path, const char* phase) {
         int dev = 0;
         ck(cudaGetDevice(&dev), "cudaGetDevice");
         ck(cudaDeviceGetAttribute(&e->smCount, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+        e->device = dev;
         ck(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
         packDevMech(*e);
         std::lock_guard<std::mutex> lk(g_mu);
@@ -808,6 +840,7 @@ void gb_net_default_options(gb_net_options* o) {
 int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
     return guarded([&]() -> int32_t {
         MechEntry& me = mech(h);
+        requireMechDevice(me);
         if (n <= 0) throw std::runtime_error("a reactor network needs n > 0 reactors");
         auto ne = std::make_unique<NetEntry>();
         ne->mech = h;
@@ -883,6 +916,7 @@ int32_t gb_net_set_state(int32_t h, const double* T, const double* P, const doub
     return guarded([&]() -> int32_t {
         NetEntry& ne = net(h);
         MechEntry& me = mech(ne.mech);
+        requireMechDevice(me);
         if (!T || !P || !Y) throw std::runtime_error("null array argument");
         const int K = me.m.K, n = ne.n;
         auto kind = (flags & GB_DEVICE_POINTERS) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
@@ -955,6 +989,7 @@ int32_t gb_net_advance(int32_t h, double t) {
     return guarded([&]() -> int32_t {
         NetEntry& ne = net(h);
         MechEntry& me = mech(ne.mech);
+        requireMechDevice(me);
         if (t < ne.time) throw std::runtime_error("cannot integrate backwards in time");
         if (t == ne.time) return 0;
         cudaStream_t s = me.stream;
@@ -988,6 +1023,48 @@ int32_t gb_net_advance(int32_t h, double t) {
     });
 }
 
+int32_t gb_net_step(int32_t h, double* times, int32_t flags) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        MechEntry& me = mech(ne.mech);
+        requireMechDevice(me);
+        cudaStream_t s = me.stream;
+        ne.dTnow.ensure((size_t)ne.n * 8);
+        ck(cudaEventRecord(ne.evA, s), "event record");
+        // one CV_ONE_STEP call per reactor towards time + 1 (the reference's tout), no graph:
+        // the captured advance stays valid for the next gb_net_advance
+        netLaunch(ne, me, ne.time, ne.time + 1.0, true);
+        ck(cudaEventRecord(ne.evB, s), "event record");
+        ck(cudaStreamSynchronize(s), "integrator step");
+        float ms = 0.f;
+        ck(cudaEventElapsedTime(&ms, ne.evA, ne.evB), "event time");
+        ne.lastMs = ms;
+        std::vector<double> tn(ne.n);
+        ck(cudaMemcpy(tn.data(), ne.dTnow.p, (size_t)ne.n * 8, cudaMemcpyDeviceToHost), "copy times");
+        if (times) {
+            auto kind = (flags & GB_DEVICE_POINTERS) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+            ck(cudaMemcpy(times, ne.dTnow.p, (size_t)ne.n * 8, kind), "copy times");
+        }
+        // the network's time: the latest reactor time, from which every reactor can go on
+        // (an advance to an earlier time would have to reach back past a reactor's last step)
+        ne.time = *std::max_element(tn.begin(), tn.end());
+        std::vector<int> st(ne.n);
+        ck(cudaMemcpy(st.data(), ne.dStatus.p, (size_t)ne.n * 4, cudaMemcpyDeviceToHost), "copy status");
+        int bad = 0;
+        for (int v : st) bad += (v != 0);
+        return bad;
+    });
+}
+
+double gb_kin_last_kernel_ms(int32_t h) {
+    try {
+        return mech(h).lastMs;
+    } catch (std::exception& e) {
+        g_error = e.what();
+        return -999.999;
+    }
+}
+
 double gb_net_time(int32_t h) {
     try {
         return net(h).time;
@@ -1010,6 +1087,7 @@ int32_t gb_net_get_state(int32_t h, double* T, double* Y, int32_t flags) {
     return guarded([&]() -> int32_t {
         NetEntry& ne = net(h);
         MechEntry& me = mech(ne.mech);
+        requireMechDevice(me);
         auto kind = (flags & GB_DEVICE_POINTERS) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
         if (T) ck(cudaMemcpy(T, ne.dT.p, (size_t)ne.n * 8, kind), "copy T");
         if (Y) ck(cudaMemcpy(Y, ne.dY.p, (size_t)me.m.K * ne.n * 8, kind), "copy Y");
@@ -1046,6 +1124,7 @@ int32_t gb_reactors_advance_noalloc(int32_t h, int32_t n, double t_end, double* 
                                     void* stream) {
     return guarded([&]() -> int32_t {
         MechEntry& me = mech(h);
+        requireMechDevice(me);
         if (n <= 0) throw std::runtime_error("need n > 0 reactors");
         if (!T || !P || !Y || !status) throw std::runtime_error("null array argument");
         if (!(t_end > 0) || !std::isfinite(t_end)) throw std::runtime_error("t_end must be positive and finite");
@@ -1061,6 +1140,13 @@ int32_t gb_reactors_advance_noalloc(int32_t h, int32_t n, double t_end, double* 
             throw std::runtime_error("gb_reactors_advance_noalloc: n = " + std::to_string(n) +
                                      " exceeds the maximum of " + std::to_string(cap) +
                                      " reactors that its 16 MiB scratch holds for this mechanism");
+        cudaStream_t s = (cudaStream_t)stream;
+        // the call synchronises its stream and queries pointers, neither of which a stream
+        // capture allows: refuse before touching the stream
+        cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+        ck(cudaStreamIsCapturing(s, &cap_status), "cudaStreamIsCapturing");
+        if (cap_status != cudaStreamCaptureStatusNone)
+            throw std::runtime_error("gb_reactors_advance_noalloc cannot be called while its stream is being captured");
         int dev = 0;
         ck(cudaGetDevice(&dev), "cudaGetDevice");
         requireDevicePointer(T, dev, "T");
@@ -1074,8 +1160,10 @@ int32_t gb_reactors_advance_noalloc(int32_t h, int32_t n, double t_end, double* 
         const int recStride = bdfRecordStride(N);
         const int fit = maxSmemPerBlock() / (warpDoubles * 8);
         if (fit < 1) throw std::runtime_error("mechanism too large for one warp's shared memory");
-        const int wpb = std::min(o.warps_per_block > 0 ? o.warps_per_block : 8, fit);
-        const int blocksPerSm = std::max(1, (228 * 1024) / (warpDoubles * 8 * wpb));
+        const int wpb = std::min(std::min(o.warps_per_block > 0 ? o.warps_per_block : 8, kBdfMaxThreads / 32), fit);
+        // resident blocks per SM from the occupancy calculator (registers included), as the
+        // network path chooses its grid
+        const int blocksPerSm = bdfBlocksPerSm(N, fp32, wpb, (size_t)warpDoubles * 8 * wpb, me.dm.NX > 0);
         const int blocks = std::min(me.smCount * blocksPerSm, (n + wpb - 1) / wpb);
 
         std::lock_guard<std::mutex> lk(g_noallocMu);
@@ -1085,7 +1173,6 @@ int32_t gb_reactors_advance_noalloc(int32_t h, int32_t n, double t_end, double* 
         double* rec = (double*)(base + 256);
         long long* stats = (long long*)(base + 256 + alignUp256(recBytes));
         double* tign = (double*)((char*)stats + alignUp256((size_t)n * 64));
-        cudaStream_t s = (cudaStream_t)stream;
         // Must start at zero: the work counter, and each record (a record whose flags
         // word is zero makes the kernel start that reactor from T, P, Y at time 0).
         ck(cudaMemsetAsync(counter, 0, sizeof(int), s), "reset counter");
@@ -1111,6 +1198,7 @@ int32_t gb_reactor_rhs(int32_t h, int32_t n, const double* T, const double* P, c
                        double* dYdt, int32_t flags) {
     return guarded([&]() -> int32_t {
         MechEntry& e = mech(h);
+        requireMechDevice(e);
         if (n < 0) throw std::runtime_error("negative number of states");
         if (n == 0) return 0;
         if (!T || !P || !Y || !dTdt || !dYdt) throw std::runtime_error("null array argument");
@@ -1216,6 +1304,7 @@ int32_t gb_nn_features(int32_t h, int32_t n, const double* T, const double* P, c
                        const float* sd, void* X, int32_t ldx) {
     return guarded([&]() -> int32_t {
         MechEntry& e = mech(h);
+        requireMechDevice(e);
         if (n < 0 || ldx < e.m.K + 2 || !T || !P || !Y || !mu || !sd || !X) throw std::runtime_error("features: bad arguments");
         ck(launchFeatures(n, e.m.K, T, P, Y, mu, sd, (__nv_bfloat16*)X, ldx, 0), "features launch");
         ck(cudaStreamSynchronize(0), "features");
@@ -1228,6 +1317,7 @@ int32_t gb_nn_apply(int32_t h, int32_t n, const float* O, int32_t ldo, const flo
                     double* Yn) {
     return guarded([&]() -> int32_t {
         MechEntry& e = mech(h);
+        requireMechDevice(e);
         if (n < 0 || ldo < e.m.K + 1 || !O || !mu || !sd || !T || !Y || !Tn || !Yn) throw std::runtime_error("apply: bad arguments");
         if ((f0T == nullptr) != (f0Y == nullptr)) throw std::runtime_error("apply: give both f0T and f0Y or neither");
         ck(launchApplyDelta(n, e.m.K, O, ldo, mu, sd, T, Y, dt, f0T, f0Y, Tn, Yn, 0), "apply launch");
@@ -1242,6 +1332,7 @@ int32_t gb_nn_gate(int32_t h, int32_t n, double dt, const double* T0, const doub
                    int32_t* accept, double* score) {
     return guarded([&]() -> int32_t {
         MechEntry& e = mech(h);
+        requireMechDevice(e);
         if (n < 0 || !T0 || !Y0 || !T1 || !Y1 || !f0T || !f0Y || !f1T || !f1Y || !elem_mass || !accept || !score)
             throw std::runtime_error("gate: bad arguments");
         GateArgs a{};

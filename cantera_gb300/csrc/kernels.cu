@@ -1152,9 +1152,11 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
             if (count >= p.maxSteps) { status = ST_MAX_STEPS; break; }
             status = W.template step<MT, NS>(M, S);
             count++;
+            if (p.oneStep) break;
         }
-        // output: interpolate to tout (or the last state on failure)
-        const double sfac = (status == ST_OK && S.h != 0.0) ? ddiv(p.tout - S.tn, S.h) : 0.0;
+        // output: interpolate to tout (or the last state on failure; the state at the new
+        // internal time after one step)
+        const double sfac = (status == ST_OK && S.h != 0.0 && !p.oneStep) ? ddiv(p.tout - S.tn, S.h) : 0.0;
 #pragma unroll 1
         for (int i = lane; i < N; i += 32) {
             double v = W.zn[(size_t)S.q * N + i];
@@ -1187,6 +1189,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
             stt[5] = A.netf; stt[6] = A.ncfn; stt[7] = S.q;
             p.status[r] = status;
             p.tign[r] = W.ignitionTime();
+            if (p.tnow) p.tnow[r] = S.tn;
         }
         __syncwarp();
     }

@@ -64,6 +64,9 @@ struct BdfParams {
     void* Jbuf;           // kept Jacobians (FP64), one slot of Jstride bytes per resident warp;
                           // null: a new Jacobian at every linear-solver setup
     long long Jstride;
+    int oneStep;          // 1: each reactor takes one internal step (its state at the new
+                          // internal time is written, no interpolation); 0: step past tout
+    double* tnow;         // [n] internal time of each reactor after the launch (or null)
 };
 
 constexpr int kBdfMaxThreads = 256;   // at most 8 warps per block

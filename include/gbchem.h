@@ -72,6 +72,11 @@ int32_t gb_kin_net_production_rates_ddCi(int32_t mech, int32_t n, const double* 
                                          const double* Y, int32_t nnz, double* vals, double* wdot,
                                          int32_t flags);
 
+/* Device time in ms of the kernel launch of the last rates or ddCi call on this mechanism
+ * (CUDA events on the engine's stream around the launch; no counterpart in the
+ * reference), or -999.999 with an invalid handle. */
+double gb_kin_last_kernel_ms(int32_t mech);
+
 /* ---- batched reactor network ------------------------------------------------------------
  * gb_net_* replace ReactorNet over IdealGasConstPressureReactor (src/zeroD/ReactorNet.cpp:
  * 37-357; CLib reactornet_advance, headers/ctreactornet.yaml:19-20): n independent reactors,
@@ -122,6 +127,16 @@ int32_t gb_net_set_max_time_step(int32_t net, double max_time_step);
 /* Advance every reactor to time t (ReactorNet::advance: step past t, interpolate back).
  * Returns the number of reactors whose integration failed (status != 0), or GB_ERR. */
 int32_t gb_net_advance(int32_t net, double t);
+/* One internal step of every reactor (ReactorNet::step, src/zeroD/ReactorNet.cpp:435-441,
+ * which makes one CV_ONE_STEP call towards time + 1: CVodesIntegrator::step,
+ * src/numerics/CVodesIntegrator.cpp:531-549; Python ReactorNet.step,
+ * interfaces/cython/cantera/reactor.py:1822).  Each reactor's state becomes its state at its
+ * new internal time, written to times[n] (host, or device with GB_DEVICE_POINTERS; may be
+ * NULL).  The reactors are independent, so their times differ; the network's time
+ * (gb_net_time) becomes the latest of them, and a later gb_net_advance(t) needs t >= that
+ * time (reactors behind it step on, the others interpolate back within their last step).
+ * Returns the number of reactors whose step failed, or GB_ERR. */
+int32_t gb_net_step(int32_t net, double* times, int32_t flags);
 double gb_net_time(int32_t net);
 /* Device time of the integrator launch of the last gb_net_advance, in ms (CUDA events on
  * the engine's stream around the launch). */
@@ -160,8 +175,10 @@ int32_t gb_net_ignition_times(int32_t net, double* tign);
  * cudaStream_t; NULL is the default stream) and synchronises it before returning.  Every
  * call on a device shares that one array: calls of this process are serialised by a lock,
  * and calls that overlap on one device from other code that bypasses it would race.  The
- * first call on each device looks the array up (and may load the module), so make it
- * before any stream capture. */
+ * call queries its pointers and synchronises its stream, so it cannot be made while that
+ * stream is being captured (it returns GB_ERR then); its first call on each device looks the
+ * array up and may load the module.  The mechanism must have been loaded with the same
+ * device current (GB_ERR otherwise), as for every call that launches work. */
 int32_t gb_reactors_advance_noalloc(int32_t mech, int32_t n, double t_end, double* T, const double* P,
                                     double* Y, int32_t* status, const gb_net_options* opts,
                                     void* stream);

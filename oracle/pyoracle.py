@@ -13,6 +13,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "_build", "liboracle.so")
+# the same sources built with the reference's release flags (SConstruct:608-610: -O3, the
+# compiler's default floating-point contraction): the timed CPU baseline, not the checker
+LIB_FAST = os.path.join(HERE, "_build", "liboracle_fast.so")
 SOURCES = [
     os.path.join(HERE, "oracle.cpp"),
     os.path.join(ROOT, "cantera_gb300", "csrc", "mechanism.cpp"),
@@ -24,16 +27,24 @@ STAT_NAMES = ["steps", "rhs_evals", "newton_iters", "lin_setups", "jac_evals",
               "jtimes_evals"]
 
 
-def build(force=False):
-    """Compile the oracle (-ffp-contract=off so x86 and Arm agree bit for bit)."""
-    os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    newest = max(os.path.getmtime(s) for s in SOURCES + [os.path.join(HERE, "oracle.h")])
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
-        return LIB
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
-           "-o", LIB] + SOURCES + ["-lpthread"]
+def build(force=False, fast=False):
+    """Compile the oracle.  The checker (fast=False) is built with -O2 -ffp-contract=off so
+    that x86 and Arm agree bit for bit; the timing build (fast=True) with the reference's
+    release flags, -O3 and the compiler's default contraction (fused multiply-adds on Arm)."""
+    out = LIB_FAST if fast else LIB
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    newest = max(os.path.getmtime(s) for s in SOURCES + [os.path.join(HERE, "oracle.h"), __file__])
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
+        return out
+    flags = ["-O3"] if fast else ["-O2", "-ffp-contract=off"]
+    tmp = out + ".tmp%d" % os.getpid()
+    cmd = ["g++"] + flags + ["-std=c++17", "-fPIC", "-shared", "-o", tmp] + SOURCES + ["-lpthread"]
     subprocess.check_call(cmd)
-    return LIB
+    os.replace(tmp, out)
+    return out
+
+
+FLAGS = {False: "g++ -O2 -ffp-contract=off", True: "g++ -O3 (default FP contraction)"}
 
 
 class BdfOpts(ctypes.Structure):
@@ -58,14 +69,13 @@ def opts(rtol=1e-9, atol=1e-15, max_steps=20000, max_order=5, analytic=False,
                    int(jac_reuse), int(mole_reactor or gmres), int(gmres))
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        build()
-        L = ctypes.CDLL(LIB)
+def lib(fast=False):
+    """The oracle library: the checker build, or with fast=True the timing build."""
+    if fast not in _libs:
+        L = ctypes.CDLL(build(fast=fast))
         D = ctypes.POINTER(ctypes.c_double)
         I32 = ctypes.c_int32
         L.or_mech_load.restype = I32
@@ -95,8 +105,8 @@ def lib():
         L.or_add_data_directory.argtypes = [ctypes.c_char_p]
         # files that other mechanism files reference (e.g. "gri30.yaml/species")
         L.or_add_data_directory(os.path.join(ROOT, "cantera_gb300", "data").encode())
-        _lib = L
-    return _lib
+        _libs[fast] = L
+    return _libs[fast]
 
 
 def _p(a):
@@ -112,8 +122,10 @@ def _c(a):
 class Mech:
     """A mechanism loaded into the oracle."""
 
-    def __init__(self, path, phase=""):
-        L = lib()
+    def __init__(self, path, phase="", fast=False):
+        """fast=True: the timing build (the reference's compiler flags) instead of the checker."""
+        self.L = L = lib(fast)
+        self.fast = fast
         self.h = L.or_mech_load(path.encode(), phase.encode())
         if self.h < 0:
             raise RuntimeError(L.or_last_error().decode())
@@ -125,7 +137,7 @@ class Mech:
         L.or_molecular_weights(self.h, _p(self.mw))
 
     def species_index(self, name):
-        return lib().or_species_index(self.h, name.encode())
+        return self.L.or_species_index(self.h, name.encode())
 
     def composition(self, spec):
         """'H2:2, O2:1' -> normalised array over species (mole basis)."""
@@ -140,31 +152,31 @@ class Mech:
 
     def mole_to_mass(self, X):
         Y = np.zeros(self.K)
-        lib().or_mole_to_mass(self.h, _p(_c(X)), _p(Y))
+        self.L.or_mole_to_mass(self.h, _p(_c(X)), _p(Y))
         return Y
 
     def equivalence_ratio(self, phi, fuel, oxidizer):
         Y = np.zeros(self.K)
-        lib().or_equivalence_ratio(self.h, phi, _p(_c(self.composition(fuel))),
+        self.L.or_equivalence_ratio(self.h, phi, _p(_c(self.composition(fuel))),
                                    _p(_c(self.composition(oxidizer))), _p(Y))
         return Y
 
     def thermo(self, T):
         cp, h, s = np.zeros(self.K), np.zeros(self.K), np.zeros(self.K)
-        lib().or_thermo(self.h, T, _p(cp), _p(h), _p(s))
+        self.L.or_thermo(self.h, T, _p(cp), _p(h), _p(s))
         return cp, h, s
 
     def rates(self, T, P, Y):
         out = {k: np.zeros(self.R) for k in ("kf", "rkc", "ropf", "ropr", "ropnet")}
         wdot = np.zeros(self.K)
-        lib().or_rates(self.h, T, P, _p(_c(Y)), _p(out["kf"]), _p(out["rkc"]), _p(out["ropf"]),
+        self.L.or_rates(self.h, T, P, _p(_c(Y)), _p(out["kf"]), _p(out["rkc"]), _p(out["ropf"]),
                        _p(out["ropr"]), _p(out["ropnet"]), _p(wdot))
         out["wdot"] = wdot
         return out
 
     def ddci(self, T, P, Y, mode=0):
         J = np.zeros((self.K, self.K))
-        lib().or_ddci(self.h, T, P, _p(_c(Y)), mode, _p(J))
+        self.L.or_ddci(self.h, T, P, _p(_c(Y)), mode, _p(J))
         return J
 
     def rates_batch(self, T, P, Y_sm, mode=1, pattern=None, threads=None, gross=False):
@@ -182,7 +194,7 @@ class Mech:
             ri = np.ascontiguousarray(rowidx, dtype=np.int32)
             jac = np.zeros((len(ri), n))
         I = ctypes.POINTER(ctypes.c_int32)
-        lib().or_rates_batch(self.h, n, _p(_c(T)), _p(_c(P)), _p(_c(Y_sm)), _p(wdot), mode,
+        self.L.or_rates_batch(self.h, n, _p(_c(T)), _p(_c(P)), _p(_c(Y_sm)), _p(wdot), mode,
                              cp.ctypes.data_as(I) if cp is not None else None,
                              ri.ctypes.data_as(I) if ri is not None else None,
                              _p(jac) if jac is not None else None, _p(gr), threads)
@@ -192,19 +204,19 @@ class Mech:
 
     def reactor_rhs(self, P, y):
         ydot = np.zeros(self.K + 2)
-        lib().or_reactor_rhs(self.h, P, _p(_c(y)), _p(ydot))
+        self.L.or_reactor_rhs(self.h, P, _p(_c(y)), _p(ydot))
         return ydot
 
     def mole_reactor_rhs(self, P, z):
         """Mole-reactor right-hand side for z = [T, n_1..n_K] (kmol) at pressure P."""
         zdot = np.zeros(self.K + 1)
-        st = lib().or_mole_reactor_rhs(self.h, P, _p(_c(z)), _p(zdot))
+        st = self.L.or_mole_reactor_rhs(self.h, P, _p(_c(z)), _p(zdot))
         return zdot, st
 
     def mole_precond_jacobian(self, P, z, atol=1e-15):
         """The adaptive preconditioner's Jacobian elements [K+1, K+1] at z."""
         J = np.zeros((self.K + 1, self.K + 1))
-        st = lib().or_mole_precond_jacobian(self.h, P, _p(_c(z)), atol, _p(J))
+        st = self.L.or_mole_precond_jacobian(self.h, P, _p(_c(z)), atol, _p(J))
         return J, st
 
     def advance_batch(self, T0, P, Y0, t_end, o=None, threads=None):
@@ -216,7 +228,7 @@ class Mech:
         Y = np.zeros((n, self.K))
         st = np.zeros((n, NSTAT), dtype=np.int64)
         tig = np.zeros(n)
-        lib().or_advance_batch(self.h, n, _p(_c(T0)), _p(_c(P)), _p(_c(Y0)), t_end,
+        self.L.or_advance_batch(self.h, n, _p(_c(T0)), _p(_c(P)), _p(_c(Y0)), t_end,
                                ctypes.byref(o), _p(T), _p(Y),
                                st.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _p(tig), threads)
         return T, Y, st, tig
@@ -226,7 +238,7 @@ class Mech:
         times = _c(times)
         out = np.zeros((len(times), self.K + 1))
         st = np.zeros(NSTAT, dtype=np.int64)
-        rc = lib().or_advance_trajectory(self.h, T0, P, _p(_c(Y0)), len(times), _p(times),
+        rc = self.L.or_advance_trajectory(self.h, T0, P, _p(_c(Y0)), len(times), _p(times),
                                          ctypes.byref(o), _p(out),
                                          st.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
         return out, st, rc
@@ -235,7 +247,7 @@ class Mech:
         o = o or opts()
         t = ctypes.c_double()
         st = np.zeros(NSTAT, dtype=np.int64)
-        rc = lib().or_ignition_by_steps(self.h, T0, P, _p(_c(Y0)), dT, ctypes.byref(o),
+        rc = self.L.or_ignition_by_steps(self.h, T0, P, _p(_c(Y0)), dT, ctypes.byref(o),
                                         ctypes.byref(t),
                                         st.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
         return t.value, st, rc

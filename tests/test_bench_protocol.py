@@ -1,0 +1,82 @@
+"""The benchmark's CPU-side arithmetic (no GPU): the error protocol of the integrator
+workloads, the FLOP model behind the roofline, and the timing build of the oracle."""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+from oracle import pyoracle as po  # noqa: E402
+
+DATA = os.path.join(ROOT, "cantera_gb300", "data")
+
+
+def h2o2_sample(n=8):
+    m = po.Mech(os.path.join(DATA, "h2o2.yaml"), "ohmech")
+    rng = np.random.default_rng(7)
+    T0 = rng.uniform(1000.0, 1600.0, n)
+    P = np.full(n, 101325.0)
+    Y0 = np.array([m.equivalence_ratio(p, "H2:1", "O2:1, N2:3.76") for p in rng.uniform(0.5, 2.0, n)])
+    return m, T0, P, Y0
+
+
+def test_error_protocol_fields_and_self_consistency():
+    m, T0, P, Y0 = h2o2_sample()
+    t_end, rtol, atol = 1e-3, 1e-8, 1e-15
+    # the reference-configured oracle stands in for the GPU: its errors against the oracle
+    # are zero and against the tight run equal the oracle's own
+    To, Yo, _, tio = m.advance_batch(T0, P, Y0, t_end, bench.oracle_opts(po, rtol, atol), threads=2)
+    e = bench.error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, {"same": (To, Yo, tio)}, threads=2)
+    assert e["reactors"] == len(T0) and e["oracle_failed"] == 0
+    assert e["igniting"] > 0
+    s = e["same"]
+    assert s["vs_oracle"]["T_max_rel"] == 0.0 and s["vs_oracle"]["major_species_max_rel"] == 0.0
+    assert s["ignition_delay_max_rel_vs_oracle"] == 0.0
+    assert s["vs_tight"]["all"] == e["oracle_vs_tight"]["all"]
+    assert s["T_within_oracle_error"] and s["major_species_within_oracle_error"]
+    # the tight run is closer to the truth than rtol 1e-8: the oracle's own error is small
+    assert e["oracle_vs_tight"]["all"]["T_max_rel"] < 1e-5
+
+
+def test_error_protocol_flags_a_shifted_result():
+    m, T0, P, Y0 = h2o2_sample(4)
+    t_end, rtol, atol = 1e-3, 1e-8, 1e-15
+    To, Yo, _, tio = m.advance_batch(T0, P, Y0, t_end, bench.oracle_opts(po, rtol, atol), threads=2)
+    e = bench.error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, {"off": (To * (1 + 1e-4), Yo, tio * 1.01)}, threads=2)
+    assert not e["off"]["T_within_bar"] and not e["off"]["T_within_oracle_error"]
+    assert e["off"]["ignition_delay_max_rel_vs_oracle"] > 9e-3 and not e["off"]["ignition_within_1e-3"]
+
+
+def test_flop_model_and_roofline_arithmetic():
+    st = {"K": 53, "R": 325, "reversible": 309, "falloff": 29, "troe": 26, "three_body": 41,
+          "tb_entries": 300, "gather_entries": 1500, "jac_col_entries": 2000, "jac_scatter_entries": 3000}
+    fm = bench.flop_model(st, 54)
+    assert fm["rates"] < fm["rhs"] and fm["ddci"] > 0
+    assert abs(fm["lu"] - (2.0 / 3.0) * 54 ** 3 - 54 * 8.0) < 1e-9
+    n = 10
+    stats = {"rhs_evals": np.full(n, 100), "lin_setups": np.full(n, 10), "newton_iters": np.full(n, 90),
+             "steps": np.full(n, 80)}
+    f64, f32 = bench.algorithmic_flops(stats, fm, False)
+    expect = n * (100 * fm["rhs"] + 10 * (fm["jac"] + fm["lu"]) + 90 * fm["newton"] + 80 * fm["step"])
+    assert abs(f64 - expect) <= 1e-9 * expect and f32 == 0.0
+    f64b, f32b = bench.algorithmic_flops(stats, fm, True)
+    assert abs(f64b + f32b - f64) <= 1e-9 * f64 and f32b > 0
+
+
+def test_timing_build_agrees_with_checker():
+    """The timing build (-O3, default contraction) computes the same rates as the checker
+    to rounding level, so its time is the time of the same work."""
+    m = po.Mech(os.path.join(DATA, "gri30.yaml"), "gri30")
+    mf = po.Mech(os.path.join(DATA, "gri30.yaml"), "gri30", fast=True)
+    assert mf.L is not m.L
+    rng = np.random.default_rng(3)
+    n = 64
+    T = rng.uniform(300, 3000, n)
+    P = 101325.0 * 10 ** rng.uniform(-1, 2, n)
+    Y = rng.dirichlet(0.5 * np.ones(m.K), n).T.copy()
+    w, _, gross = m.rates_batch(T, P, Y, mode=0, threads=2, gross=True)
+    wf, _ = mf.rates_batch(T, P, Y, mode=0, threads=2)
+    assert np.all(np.abs(w - wf) <= 1e-12 * gross + 1e-300)

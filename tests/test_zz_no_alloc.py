@@ -117,3 +117,37 @@ def test_noalloc_rejects_oversize_and_host_pointers():
     rc = L.gb_reactors_advance_noalloc(sol._h, 4, 1e-3, h.ctypes.data_as(ctypes.c_void_p), d(T),
                                        d(Y), d(st), None, None)
     assert rc == -999 and "device pointer" in _errmsg(L)
+
+
+def test_noalloc_clamps_block_size_and_refuses_capture():
+    """More than 8 reactors per block are clamped to the kernel's limit, as the network
+    path does; a call on a stream that is being captured is refused with an error (the call
+    synchronises its stream), and the stream stays usable."""
+    import torch
+    import cantera_gb300 as gb
+    L = gb.library()
+    sol = gpu_solution("h2o2")
+    T0, P, Y0 = _workload(sol, 40, 5)
+    opts = dict(rtol=1e-9, atol=1e-15, warps_per_block=16)
+    Tr, Yr, sr = _reference(gb, sol, T0, P, Y0, 2e-4, dict(opts, warps_per_block=8))
+    Tn, Yn, sn = _noalloc(gb, sol, T0, P, Y0, 2e-4, opts)
+    np.testing.assert_array_equal(sn, sr)
+    np.testing.assert_array_equal(Tn, Tr)
+    np.testing.assert_array_equal(Yn, Yr)
+    dev = torch.device("cuda:0")
+    T = torch.tensor(T0, device=dev)
+    Pd = torch.tensor(P, device=dev)
+    Y = torch.tensor(Y0, device=dev).contiguous()
+    st = torch.zeros(40, dtype=torch.int32, device=dev)
+    d = lambda t: ctypes.c_void_p(t.data_ptr())
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s):
+        rc = L.gb_reactors_advance_noalloc(sol._h, 40, 2e-4, d(T), d(Pd), d(Y), d(st), None,
+                                           ctypes.c_void_p(s.cuda_stream))
+        T.add_(0.0)   # a captured node, so that the graph is not empty
+    assert rc == -999 and "captured" in _errmsg(L)
+    torch.cuda.synchronize()
+    Tn2, _, sn2 = _noalloc(gb, sol, T0, P, Y0, 2e-4, opts)
+    np.testing.assert_array_equal(Tn2, Tr)
