@@ -96,6 +96,11 @@ def library():
         "gb_nn_gemm": (I32, [I32, I32, I32, P, ctypes.c_int64, ctypes.c_int64, P, ctypes.c_int64, ctypes.c_int64,
                              P, ctypes.c_int64, ctypes.c_int64, I32, ctypes.c_float, P, I32, P, ctypes.c_int64,
                              ctypes.c_int64, I32]),
+        "gb_nn_gemm_tc": (I32, [I32, I32, I32, P, ctypes.c_int64, P, ctypes.c_int64, P, ctypes.c_int64, I32,
+                                ctypes.c_float, P, I32, P, ctypes.c_int64, I32, P, ctypes.c_int64, I32, P]),
+        "gb_nn_transpose": (I32, [I32, I32, P, ctypes.c_int64, P, ctypes.c_int64, P]),
+        "gb_nn_sync": (I32, [P]),
+        "gb_nn_set_stream": (I32, [P, I32]),
         "gb_nn_adam": (I32, [I32, P, P, P, P, P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, I32]),
         "gb_nn_colsum": (I32, [I32, I32, P, I32, ctypes.c_float, P]),
         "gb_nn_mse": (I32, [I32, I32, I32, P, P, P, P]),
@@ -164,6 +169,7 @@ class Solution:
             if os.path.exists(cand):
                 path = cand
         self._h = _check(library().gb_mech_load(path.encode(), name.encode()))
+        self.source = (os.path.abspath(path), name)
         L = library()
         self.n_species = _check(L.gb_mech_n_species(self._h))
         self.n_reactions = _check(L.gb_mech_n_reactions(self._h))

@@ -12,8 +12,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgbchem.so")
-SOURCES = ["capi.cu", "kernels.cu", "kernels_x.cu", "surrogate.cu", "mechanism.cpp", "yaml_lite.cpp"]
-HEADERS = ["devmech.h", "fastexp.h", "kernels.h", "kinetics.cuh", "mechanism.h", "surrogate.h", "yaml_lite.h"]
+SOURCES = ["capi.cu", "kernels.cu", "kernels_x.cu", "surrogate.cu", "umma.cu", "mechanism.cpp", "yaml_lite.cpp"]
+HEADERS = ["devmech.h", "fastexp.h", "kernels.h", "kinetics.cuh", "mechanism.h", "nnmath.cuh", "surrogate.h",
+           "yaml_lite.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -28,6 +28,10 @@ using namespace gbchem;
 namespace {
 
 thread_local std::string g_error;
+// the stream of the surrogate's calls (gb_nn_*) on this host thread, and whether they
+// return without waiting for their work (gb_nn_set_stream)
+thread_local cudaStream_t g_nnStream = nullptr;
+thread_local bool g_nnAsync = false;
 
 struct CudaError : std::runtime_error {
     explicit CudaError(const std::string& m) : std::runtime_error(m) {}
@@ -394,6 +398,22 @@ void packDevMech(MechEntry& e) {
     for (int c = 0; c < K; c++)
         for (int q = e.jcPtr[c]; q < e.jcPtr[c + 1]; q++) jpCol[q] = c;
     std::vector<int> jcPtr(e.jcPtr.begin(), e.jcPtr.end()), jrIdx(e.jrIdx.begin(), e.jrIdx.end());
+    // the pattern slot of every scatter of a column entry: column j, its entries e (reaction
+    // i) in order, the species r of reaction i with a net coefficient in order ->
+    // slot of (r, j), or -1 (not a structural nonzero)
+    std::vector<int> colSlotStart(1, 0), colSlot;
+    for (int j = 0; j < K; j++) {
+        std::map<int, int> slotOfRow;
+        for (int q = jcPtr[j]; q < jcPtr[j + 1]; q++) slotOfRow[jrIdx[q]] = q;
+        for (int e2 = colPtr[j]; e2 < colPtr[j + 1]; e2++) {
+            const int i = colRxn[e2];
+            for (int r = rsPtr[i]; r < rsPtr[i + 1]; r++) {
+                auto it = slotOfRow.find(rsK[r]);
+                colSlot.push_back(it == slotOfRow.end() ? -1 : it->second);
+            }
+        }
+        colSlotStart.push_back((int)colSlot.size());
+    }
 
     // Arena order by use: what every right-hand side reads, then what a Jacobian reads,
     // then the general (CN) side lists, then the rest.  Kernels copy a prefix of the arena
@@ -411,6 +431,7 @@ void packDevMech(MechEntry& e) {
     size_t o_colPtr = a.add(colPtr), o_colRxn = a.add(colRxn), o_colE = a.add(colE);
     size_t o_rsPtr = a.add(rsPtr), o_rsK = a.add(rsK), o_rsNu = a.add(rsNu);
     size_t o_gsPtr = a.add(gsPtr), o_gsTb = a.add(gsTb), o_gsCoef = a.add(gsCoef);
+    size_t o_colSlotStart = a.add(colSlotStart), o_colSlot = a.add(colSlot);
     const size_t jacEnd = a.data.size();
     size_t o_sidePtr = a.add(sidePtr), o_sideK = a.add(sideK), o_sideNu = a.add(sideNu), o_sideOrd = a.add(sideOrd);
     const size_t sideEnd = a.data.size();
@@ -446,6 +467,7 @@ void packDevMech(MechEntry& e) {
     d.gsPtr = (const int*)(b + o_gsPtr); d.gsTb = (const int*)(b + o_gsTb); d.gsCoef = (const double*)(b + o_gsCoef);
     d.jcPtr = (const int*)(b + o_jcPtr); d.jrIdx = (const int*)(b + o_jrIdx); d.jpCol = (const int*)(b + o_jpCol);
     d.pdep = (const double*)(b + o_pdep);
+    d.colSlotStart = (const int*)(b + o_colSlotStart); d.colSlot = (const int*)(b + o_colSlot);
 }
 
 // dynamic shared memory a block may use: the opt-in maximum less the kernels' static
@@ -487,19 +509,23 @@ int32_t runRates(int32_t h, int32_t n, const double* T, const double* P, const d
         if (dev) dJ = vals;
         else { e.dJ.ensure((size_t)e.dm.nnz * n * 8); dJ = e.dJ.as<double>(); }
     }
-    e.dCounter.ensure(sizeof(int));
-    ck(cudaMemsetAsync(e.dCounter.p, 0, sizeof(int), s), "memset");
+    e.dCounter.ensure(2 * sizeof(int));
+    ck(cudaMemsetAsync(e.dCounter.p, 0, 2 * sizeof(int), s), "memset");
     RatesParams p{};
     p.m = e.dm; p.n = n; p.T = dT; p.P = dP; p.Y = dY; p.wdot = dW; p.jac = dJ;
     p.counter = e.dCounter.as<int>();
     p.warpDoubles = ratesWarpDoubles(e.dm, dJ != nullptr);
     // the mechanism data the call reads goes into shared memory when 8 warps still fit
-    const int budget = maxSmemPerBlock();
+    // next to the block's state tile
+    const int budget = maxSmemPerBlock() - ratesTileDoubles(e.dm) * 8;
     const int want = dJ ? e.dm.sideBytes : e.dm.hotBytes;
     p.mechSmem = (budget - want) / (p.warpDoubles * 8) >= 8 ? want : 0;
     int wpb = std::max(1, std::min(8, (budget - p.mechSmem) / (p.warpDoubles * 8)));
-    int blocksPerSm = std::max(1, (228 * 1024) / (p.mechSmem + p.warpDoubles * 8 * wpb + 1024));
-    int blocks = std::min(e.smCount * blocksPerSm, (n + wpb - 1) / wpb);
+    if (budget - p.mechSmem < p.warpDoubles * 8) throw std::runtime_error("mechanism too large for the rates kernel's shared memory");
+    const int perBlock = p.mechSmem + ratesTileDoubles(e.dm) * 8 + p.warpDoubles * 8 * wpb + 1024;
+    int blocksPerSm = std::max(1, (228 * 1024) / perBlock);
+    const int tiles = (int)(((long long)n + kRatesTile - 1) / kRatesTile);
+    int blocks = std::min(e.smCount * blocksPerSm, tiles);
     if (!e.evA) {
         ck(cudaEventCreate(&e.evA), "event");
         ck(cudaEventCreate(&e.evB), "event");
@@ -513,6 +539,9 @@ int32_t runRates(int32_t h, int32_t n, const double* T, const double* P, const d
     float ms = 0.f;
     ck(cudaEventElapsedTime(&ms, e.evA, e.evB), "event time");
     e.lastMs = ms;
+    int flags2[2] = {0, 0};
+    ck(cudaMemcpy(flags2, e.dCounter.p, sizeof(flags2), cudaMemcpyDeviceToHost), "copy flags");
+    if (flags2[1]) throw std::runtime_error("rates kernel: the bulk copy of the mechanism into shared memory did not complete");
     return 0;
 }
 
@@ -643,6 +672,10 @@ void requireDevicePointer(const void* ptr, int dev, const char* what) {
     ck(cudaPointerGetAttributes(&a, ptr), what);
     const bool ok = (a.type == cudaMemoryTypeDevice && a.device == dev) || a.type == cudaMemoryTypeManaged;
     if (!ok) throw std::runtime_error(std::string(what) + " must be a device pointer on the current device");
+}
+// end of a surrogate call: wait for its work unless this thread asked for asynchronous calls
+void nnFinish(const char* what) {
+    if (!g_nnAsync) ck(cudaStreamSynchronize(g_nnStream), what);
 }
 }  // namespace
 
@@ -1266,8 +1299,59 @@ int32_t gb_nn_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, 
         g.B = (const __nv_bfloat16*)B; g.sbn = sbn; g.sbk = sbk;
         g.C = C; g.scm = scm; g.scn = scn; g.cFloat = c_float;
         g.alpha = alpha; g.bias = bias; g.act = act; g.Z = Z; g.szm = szm; g.szn = szn; g.zFloat = z_float;
-        ck(launchGemm(g, 0), "gemm launch");
-        ck(cudaStreamSynchronize(0), "gemm");
+        ck(launchGemm(g, g_nnStream), "gemm launch");
+        nnFinish("gemm");
+        return 0;
+    });
+}
+
+int32_t gb_nn_set_stream(void* stream, int32_t async) {
+    return guarded([&]() -> int32_t {
+        g_nnStream = (cudaStream_t)stream;
+        g_nnAsync = async != 0;
+        return 0;
+    });
+}
+
+int32_t gb_nn_gemm_tc(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda, const void* B, int64_t ldb,
+                      void* C, int64_t ldc, int32_t c_float, float alpha, const float* bias, int32_t act, void* Z,
+                      int64_t ldz, int32_t z_float, void* CT, int64_t ldct, int32_t splits, void* stream) {
+    return guarded([&]() -> int32_t {
+        if (!A || !B || !C) throw std::runtime_error("gemm_tc: null operand");
+        if (act < 0 || act > 2) throw std::runtime_error("gemm_tc: act must be 0, 1 or 2");
+        UmmaArgs g{};
+        g.M = M; g.N = N; g.K = K;
+        g.A = (const __nv_bfloat16*)A; g.lda = lda;
+        g.B = (const __nv_bfloat16*)B; g.ldb = ldb;
+        g.C = C; g.ldc = ldc; g.cFloat = c_float;
+        g.alpha = alpha; g.bias = bias; g.act = act; g.Z = Z; g.ldz = ldz; g.zFloat = z_float;
+        g.CT = (__nv_bfloat16*)CT; g.ldct = ldct;
+        if (const char* why = checkUmmaArgs(g, splits)) throw std::runtime_error(std::string("gemm_tc: ") + why);
+        cudaStream_t s = (cudaStream_t)stream;
+        if (splits > 1)   // the CTAs add their partial tiles into C
+            ck(cudaMemset2DAsync(C, (size_t)ldc * 4, 0, (size_t)N * 4, (size_t)M, s), "gemm_tc: clear C");
+        ck(launchUmma(g, splits, s), "gemm_tc launch");
+        return 0;
+    });
+}
+
+int32_t gb_nn_transpose(int32_t M, int32_t N, const void* src, int64_t lds, void* dst, int64_t ldd, void* stream) {
+    return guarded([&]() -> int32_t {
+        if (M < 0 || N < 0 || lds < N || ldd < M) throw std::runtime_error("transpose: bad sizes");
+        if (M && N && (!src || !dst)) throw std::runtime_error("transpose: null array");
+        ck(launchTranspose(M, N, (const __nv_bfloat16*)src, lds, (__nv_bfloat16*)dst, ldd, (cudaStream_t)stream),
+           "transpose launch");
+        return 0;
+    });
+}
+
+int32_t gb_nn_sync(void* stream) {
+    return guarded([&]() -> int32_t {
+        ck(cudaStreamSynchronize((cudaStream_t)stream), "surrogate stream");
+        const int e = ummaTakeError();
+        if (e < 0) throw std::runtime_error("gemm_tc: cannot read the error flag");
+        if (e) throw std::runtime_error("gemm_tc: a tensor-core GEMM block gave up waiting for its operands or "
+                                        "its accumulator (bounded wait ran out); its output tile is not written");
         return 0;
     });
 }
@@ -1276,8 +1360,8 @@ int32_t gb_nn_adam(int32_t n, float* w, float* m, float* v, const float* g, void
                    float beta2, float eps, int32_t step) {
     return guarded([&]() -> int32_t {
         if (n < 0 || !w || !m || !v || !g || !wb || step < 1) throw std::runtime_error("adam: bad arguments");
-        ck(launchAdam(n, w, m, v, g, (__nv_bfloat16*)wb, lr, beta1, beta2, eps, step, 0), "adam launch");
-        ck(cudaStreamSynchronize(0), "adam");
+        ck(launchAdam(n, w, m, v, g, (__nv_bfloat16*)wb, lr, beta1, beta2, eps, step, g_nnStream), "adam launch");
+        nnFinish("adam");
         return 0;
     });
 }
@@ -1285,8 +1369,8 @@ int32_t gb_nn_adam(int32_t n, float* w, float* m, float* v, const float* g, void
 int32_t gb_nn_colsum(int32_t M, int32_t N, const void* X, int32_t ld, float alpha, float* out) {
     return guarded([&]() -> int32_t {
         if (M < 0 || N < 0 || ld < N || !X || !out) throw std::runtime_error("colsum: bad arguments");
-        ck(launchColSum(M, N, (const __nv_bfloat16*)X, ld, alpha, out, 0), "colsum launch");
-        ck(cudaStreamSynchronize(0), "colsum");
+        ck(launchColSum(M, N, (const __nv_bfloat16*)X, ld, alpha, out, g_nnStream), "colsum launch");
+        nnFinish("colsum");
         return 0;
     });
 }
@@ -1294,8 +1378,8 @@ int32_t gb_nn_colsum(int32_t M, int32_t N, const void* X, int32_t ld, float alph
 int32_t gb_nn_mse(int32_t M, int32_t nout, int32_t ld, const float* P, const float* Y, void* dY, float* loss) {
     return guarded([&]() -> int32_t {
         if (M < 0 || nout < 0 || ld < nout || !P || !Y || !dY || !loss) throw std::runtime_error("mse: bad arguments");
-        ck(launchMseGrad(M, nout, ld, P, Y, (__nv_bfloat16*)dY, loss, 0), "mse launch");
-        ck(cudaStreamSynchronize(0), "mse");
+        ck(launchMseGrad(M, nout, ld, P, Y, (__nv_bfloat16*)dY, loss, g_nnStream), "mse launch");
+        nnFinish("mse");
         return 0;
     });
 }
@@ -1306,8 +1390,8 @@ int32_t gb_nn_features(int32_t h, int32_t n, const double* T, const double* P, c
         MechEntry& e = mech(h);
         requireMechDevice(e);
         if (n < 0 || ldx < e.m.K + 2 || !T || !P || !Y || !mu || !sd || !X) throw std::runtime_error("features: bad arguments");
-        ck(launchFeatures(n, e.m.K, T, P, Y, mu, sd, (__nv_bfloat16*)X, ldx, 0), "features launch");
-        ck(cudaStreamSynchronize(0), "features");
+        ck(launchFeatures(n, e.m.K, T, P, Y, mu, sd, (__nv_bfloat16*)X, ldx, g_nnStream), "features launch");
+        nnFinish("features");
         return 0;
     });
 }
@@ -1320,8 +1404,8 @@ int32_t gb_nn_apply(int32_t h, int32_t n, const float* O, int32_t ldo, const flo
         requireMechDevice(e);
         if (n < 0 || ldo < e.m.K + 1 || !O || !mu || !sd || !T || !Y || !Tn || !Yn) throw std::runtime_error("apply: bad arguments");
         if ((f0T == nullptr) != (f0Y == nullptr)) throw std::runtime_error("apply: give both f0T and f0Y or neither");
-        ck(launchApplyDelta(n, e.m.K, O, ldo, mu, sd, T, Y, dt, f0T, f0Y, Tn, Yn, 0), "apply launch");
-        ck(cudaStreamSynchronize(0), "apply");
+        ck(launchApplyDelta(n, e.m.K, O, ldo, mu, sd, T, Y, dt, f0T, f0Y, Tn, Yn, g_nnStream), "apply launch");
+        nnFinish("apply");
         return 0;
     });
 }

@@ -106,6 +106,13 @@ struct DevMech {
     //              last levels are the sentinels at ln P = -1000 and +1000
     //   Chebyshev: nT, nP, TrNum, TrDen, PrNum, PrDen, then nT x nP coefficients (row-major)
     const double* pdep;
+    // the pattern slot of each scatter of the column lists (the rates kernel accumulates
+    // d(wdot)/dc directly on the output pattern): column j's scatters start at
+    // colSlotStart[j]; then, for each entry e of column j in order and each species of
+    // reaction colRxn[e] with a net coefficient (rsPtr order), the slot of (species, j) in
+    // jcPtr/jrIdx, or -1
+    const int* colSlotStart;     // [K+1]
+    const int* colSlot;
 };
 
 // every array of a DevMech
@@ -114,7 +121,7 @@ struct DevMech {
     X(rsPtr) X(rsK) X(rsNu) X(fo1) X(fo2) X(tbRxn) X(tbDef) X(tbMA) X(tbPtr) X(tbK) X(tbE) \
     X(spPtr) X(spRxn) X(spNu) X(taskPtr) X(laneTaskPtr) X(laneTasks) X(spTaskPtr) X(spTasks) \
     X(colPtr) X(colRxn) X(colE) X(laneColPtr) X(laneCols) X(gsPtr) X(gsTb) X(gsCoef) \
-    X(jcPtr) X(jrIdx) X(jpCol) X(pdep)
+    X(jcPtr) X(jrIdx) X(jpCol) X(pdep) X(colSlotStart) X(colSlot)
 
 #ifdef __CUDACC__
 // Point the arrays that lie in the first `bytes` of the arena at a copy of that prefix
@@ -140,6 +147,56 @@ __device__ __forceinline__ void loadMech(const DevMech& src, DevMech& sm, char* 
         sm = src;
         if (bytes > 0) rebaseMech(sm, dyn, bytes);
     }
+}
+
+// Bounded wait for phase `parity` of the mbarrier at shared address `mbar`; false when
+// `limit` polls pass without it (each poll may suspend the thread briefly in hardware).
+__device__ __forceinline__ bool mbarWaitBounded(uint32_t mbar, uint32_t parity, int limit) {
+    for (int it = 0; it < limit; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done) : "r"(mbar), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+constexpr int kBulkChunk = 32768;          // bytes per bulk copy instruction
+constexpr int kBulkWaitPolls = 1 << 22;    // polls before a block gives up on its copy
+
+// Block prologue with the bulk-copy (TMA) engine: one thread arms the block's mbarrier with
+// the byte count and issues cp.async.bulk copies of the arena prefix [0, bytes) (a
+// multiple of 16; the arena is 256-byte aligned, `dyn` 128-byte aligned) into shared
+// memory; every thread waits (bounded) for the mbarrier's first phase.  Builds the block's
+// DevMech in `sm` as loadMech does.  Returns false in every thread of the block when the
+// copy did not complete within the limit.
+__device__ __forceinline__ bool loadMechBulk(const DevMech& src, DevMech& sm, char* dyn, int bytes,
+                                             uint64_t* mbar) {
+    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(mbar);
+    if (threadIdx.x == 0) {
+        sm = src;
+        if (bytes > 0) {
+            rebaseMech(sm, dyn, bytes);
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(dyn);
+            for (int off = 0; off < bytes; off += kBulkChunk) {
+                const int sz = bytes - off < kBulkChunk ? bytes - off : kBulkChunk;
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                    ::"r"(dst + off), "l"(src.arena + off), "r"(sz), "r"(mb) : "memory");
+            }
+        }
+    }
+    __syncthreads();
+    bool ok = true;
+    if (bytes > 0) ok = mbarWaitBounded(mb, 0, kBulkWaitPolls);
+    return __syncthreads_and(ok) != 0;
 }
 #endif
 

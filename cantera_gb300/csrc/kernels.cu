@@ -19,50 +19,102 @@ namespace gbchem {
 // Rates and d(wdot)/dc over a batch of states (Kinetics::getNetProductionRates,
 // Kinetics::netProductionRates_ddCi)
 // =============================================================================
+// A block takes tiles of kRatesTile consecutive states from an atomic counter.  The tile's
+// T, P and Y[K] rows are loaded into shared memory with one coalesced 256-byte request per
+// row (lanes across states); each warp then evaluates whole states (lanes across species,
+// reactions and Jacobian columns) and writes wdot back into its state's column of the
+// tile, which the block stores with coalesced rows.  d(wdot)/dc is accumulated per warp
+// directly on the output pattern (nnz doubles) and written by the whole block for W
+// consecutive states at a time, so that each pattern slot is one contiguous run of W
+// doubles in the [nnz][n] output.  The mechanism prefix the call reads is staged into
+// shared memory by the bulk-copy engine.
 template <bool kX>
 __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
     extern __shared__ __align__(128) double smem[];
     __shared__ uint64_t s_tab[kGbxTableWords];
     __shared__ DevMech s_mech;
-    loadMech(p.m, s_mech, (char*)smem, p.mechSmem);
-    gbx_load_table(s_tab);   // (its barrier also completes the mechanism copy)
+    __shared__ __align__(8) uint64_t s_mbar;
+    __shared__ int s_tile;
+    if (!loadMechBulk(p.m, s_mech, (char*)smem, p.mechSmem, &s_mbar)) {
+        if (threadIdx.x == 0) atomicExch(p.counter + 1, 1);
+        return;
+    }
+    gbx_load_table(s_tab);   // (its barrier also publishes s_mech)
     const DevMech& m = s_mech;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    double* base = smem + p.mechSmem / 8 + (size_t)warp * p.warpDoubles;
+    const int W = blockDim.x >> 5;
+    const int K = m.K, n = p.n;
+    constexpr int LD = kRatesTile + 1;        // padded row: column reads hit distinct banks
+    double* tile = smem + p.mechSmem / 8;     // rows: T, P, then Y_k / wdot_k, each LD doubles
+    double* base = tile + ratesTileDoubles(m) + (size_t)warp * p.warpDoubles;
     KinScratch s;
     const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
     s.carve(base, m.K, m.R, m.NTB, m.NF, m.NT);
     s.tab = s_tab;
     double* Yl = base + kinD;
-    double* gk = Yl + m.K;
-    double* Jc = gk + m.K;
-    const int ld = m.K + 1;
+    double* gk = Yl + K;
+    double* Js = gk + K;                      // [nnz] this warp's d(wdot)/dc on the pattern
+    const bool jac = p.jac != nullptr;
     KinState st;
     for (;;) {
-        int idx = 0;
-        if (lane == 0) idx = atomicAdd(p.counter, 1);
-        idx = __shfl_sync(0xffffffffu, idx, 0);
-        if (idx >= p.n) break;
-        for (int k = lane; k < m.K; k += 32) Yl[k] = p.Y[(size_t)k * p.n + idx];
-        double T = p.T[idx], P = p.P[idx];
-        __syncwarp();
-        warpState(m, T, P, Yl, s, st, lane);
-        __syncwarp();
-        warpRates<kX>(m, s, st, lane, p.jac != nullptr);
-        if (p.wdot)
-            for (int k = lane; k < m.K; k += 32) p.wdot[(size_t)k * p.n + idx] = s.wdot[k];
-        if (p.jac) {
-            for (int q = lane; q < m.K * ld; q += 32) Jc[q] = 0.0;
-            __syncwarp();
-            warpJacC<double, false>(m, s, Jc, ld, lane);
-            warpDenseG(m, s, gk, lane);
-            for (int q = lane; q < m.nnz; q += 32) {
-                int r = m.jrIdx[q], c = m.jpCol[q];
-                p.jac[(size_t)q * p.n + idx] = Jc[(size_t)r * ld + c] + gk[r];
+        if (threadIdx.x == 0) s_tile = atomicAdd(p.counter, 1);
+        __syncthreads();
+        const long long s0 = (long long)s_tile * kRatesTile;
+        if (s0 >= n) break;
+        const int ns = (int)min((long long)kRatesTile, (long long)n - s0);
+        // coalesced tile load: row r by warp r mod W, lane = state
+#pragma unroll 1
+        for (int r = warp; r < K + 2; r += W) {
+            const double* src = r == 0 ? p.T : (r == 1 ? p.P : p.Y + (size_t)(r - 2) * n);
+            if (lane < ns) tile[r * LD + lane] = src[s0 + lane];
+        }
+        __syncthreads();
+        // jac: rounds of W states, warp w on state round + w; else warp w on states w, w+W, ...
+#pragma unroll 1
+        for (int r0 = 0; r0 < ns; r0 += (jac ? W : ns)) {
+#pragma unroll 1
+            for (int j = r0 + warp; j < (jac ? min(r0 + W, ns) : ns); j += W) {
+                for (int k = lane; k < K; k += 32) Yl[k] = tile[(2 + k) * LD + j];
+                const double T = tile[j], P = tile[LD + j];
+                __syncwarp();
+                warpState(m, T, P, Yl, s, st, lane);
+                __syncwarp();
+                warpRates<kX>(m, s, st, lane, jac);
+                for (int k = lane; k < K; k += 32) tile[(2 + k) * LD + j] = s.wdot[k];
+                if (jac) {
+                    for (int q = lane; q < m.nnz; q += 32) Js[q] = 0.0;
+                    __syncwarp();
+                    warpJacSparse(m, s, Js, lane);
+                    warpDenseG(m, s, gk, lane);
+                    for (int q = lane; q < m.nnz; q += 32) Js[q] = Js[q] + gk[m.jrIdx[q]];
+                }
+                __syncwarp();
+            }
+            if (jac) {
+                // the block writes the round's states: slot q of state r0 + w is thread
+                // (q * W + w) of a sweep, so W consecutive states of a slot are contiguous
+                __syncthreads();
+                const int nr = min(W, ns - r0);
+                const int tot = m.nnz * W;
+#pragma unroll 1
+                for (int x = threadIdx.x; x < tot; x += blockDim.x) {
+                    const int q = x / W, w = x - q * W;
+                    if (w < nr) {
+                        const double* Jw = tile + ratesTileDoubles(m) + (size_t)w * p.warpDoubles + kinD + 2 * K;
+                        p.jac[(size_t)q * n + s0 + r0 + w] = Jw[q];
+                    }
+                }
+                __syncthreads();
             }
         }
-        __syncwarp();
+        __syncthreads();
+        if (p.wdot) {
+#pragma unroll 1
+            for (int r = warp; r < K; r += W)
+                if (lane < ns) p.wdot[(size_t)r * n + s0 + lane] = tile[(2 + r) * LD + lane];
+        }
+        __syncthreads();
     }
 }
 
@@ -1253,7 +1305,7 @@ cudaError_t launchBdfT(const BdfParams& p, int blocks, int warpsPerBlock, cudaSt
 
 template <bool kX>
 cudaError_t launchRatesT(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
-    size_t smem = (size_t)p.mechSmem + (size_t)p.warpDoubles * 8 * warpsPerBlock;
+    size_t smem = (size_t)p.mechSmem + (size_t)ratesTileDoubles(p.m) * 8 + (size_t)p.warpDoubles * 8 * warpsPerBlock;
     cudaError_t e = cudaFuncSetAttribute(k_rates<kX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_rates<kX><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
@@ -1321,7 +1373,7 @@ int bdfWarpDoublesNoMatrix(const DevMech& m) {
 
 int ratesWarpDoubles(const DevMech& m, bool jac) {
     int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
-    int tot = kinD + 2 * m.K + (jac ? m.K * (m.K + 1) : 0);
+    int tot = kinD + 2 * m.K + (jac ? m.nnz : 0);
     return (tot + 1) & ~1;
 }
 

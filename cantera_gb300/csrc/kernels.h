@@ -15,10 +15,17 @@ struct RatesParams {
     const double* Y;      // [K][n]
     double* wdot;         // [K][n] or null
     double* jac;          // [nnz][n] or null
-    int* counter;         // work counter (zeroed before launch)
+    int* counter;         // [2]: tile counter, then an error flag (both zeroed before launch;
+                          // the flag is set when a block's bulk copy of the mechanism did
+                          // not complete)
     int warpDoubles;      // shared-memory doubles per warp
     int mechSmem;         // bytes of the mechanism arena copied into shared memory
 };
+constexpr int kRatesTile = 32;   // consecutive states per block tile of the rates kernel
+// the block's state tile in shared memory: rows T, P, Y_0..Y_{K-1} of kRatesTile + 1 doubles
+__host__ __device__ inline int ratesTileDoubles(const DevMech& m) {
+    return ((m.K + 2) * (kRatesTile + 1) + 1) & ~1;
+}
 
 // batched reactor right-hand side (IdealGasConstPressureReactor::eval over [T, Y])
 struct RhsParams {
@@ -76,7 +83,7 @@ int bdfNordsieckDoubles(int N);
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32);
 int bdfWarpDoublesNoMatrix(const DevMech& m);   // the slice when the matrix (and the Jacobian
                                                  // scratch kfe, rkc) are in global memory
-int ratesWarpDoubles(const DevMech& m, bool jac);   // dense Jacobian scratch only with jac
+int ratesWarpDoubles(const DevMech& m, bool jac);   // the pattern-sized Jacobian only with jac
 cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
 cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream);
 // resident blocks per SM of the integrator kernel for this launch shape (registers included)

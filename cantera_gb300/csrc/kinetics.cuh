@@ -591,6 +591,52 @@ __device__ __noinline__ void warpJacC(const DevMech& m, const KinScratch& s, MT*
     __syncwarp();
 }
 
+// d(wdot)/dc without the dense default-efficiency part, accumulated directly on the
+// output pattern: Js[slot] (+)= ..., slots from DevMech::colSlot (same entries, same order
+// of accumulation per element as warpJacC).  The caller zeroes Js[nnz].
+GB_TU_LOCAL __device__ __noinline__ void warpJacSparse(const DevMech& m, const KinScratch& s, double* Js, int lane) {
+#pragma unroll 1
+    for (int q = m.laneColPtr[lane]; q < m.laneColPtr[lane + 1]; q++) {
+        const int j = m.laneCols[q];
+        const int e0 = m.colPtr[j], e1 = m.colPtr[j + 1];
+        int slot = m.colSlotStart[j];
+        int iN = 0, rs0N = 0, rs1N = 0;
+        int4 infoN = make_int4(0, 0, 0, 0), rkN = infoN, pkN = infoN;
+        double epN = 0.0;
+        if (e0 < e1) {
+            iN = m.colRxn[e0];
+            infoN = m.rinfo[iN]; rkN = m.rk[iN]; pkN = m.pk[iN]; epN = m.colE[e0];
+            rs0N = m.rsPtr[iN]; rs1N = m.rsPtr[iN + 1];
+        }
+#pragma unroll 1
+        for (int e = e0; e < e1; e++) {
+            const int i = iN, rs0 = rs0N, rs1 = rs1N;
+            const int4 info = infoN, rki = rkN, pki = pkN;
+            const double ep = epN;
+            if (e + 1 < e1) {
+                iN = m.colRxn[e + 1];
+                infoN = m.rinfo[iN]; rkN = m.rk[iN]; pkN = m.pk[iN]; epN = m.colE[e + 1];
+                rs0N = m.rsPtr[iN]; rs1N = m.rsPtr[iN + 1];
+            }
+            const int rb = (info.x >> kRBucketShift) & 7, pb = (info.x >> kPBucketShift) & 7;
+            const double kfe = s.kfe[i];
+            double dF = kfe * massActionDeriv(m, rb, rki, 2 * i, s.c, j);
+            if (info.x & kRevBit) dF -= (kfe * s.rkc[i]) * massActionDeriv(m, pb, pki, 2 * i + 1, s.c, j);
+            if (ep != 0.0) dF += ep * s.Qtb[info.y];
+            if (dF == 0.0) {
+                slot += rs1 - rs0;
+                continue;
+            }
+#pragma unroll 1
+            for (int r = rs0; r < rs1; r++, slot++) {
+                const int t = m.colSlot[slot];
+                if (t >= 0) Js[t] = Js[t] + m.rsNu[r] * dF;
+            }
+        }
+    }
+    __syncwarp();
+}
+
 // g_k = sum over third-body reactions i with default efficiency d_i of S_net[k][i]*d_i*Q_i:
 // the part of d(wdot_k)/dc_j that is the same for every column j.
 __device__ __forceinline__ void warpDenseG(const DevMech& m, const KinScratch& s, double* gout, int lane) {

@@ -6,6 +6,7 @@
 // X W^T, dZ W and dZ^T X; the epilogue adds the bias and applies GELU (keeping the pre-
 // activation for the backward pass) or multiplies by GELU' of a stored pre-activation.
 #include "surrogate.h"
+#include "nnmath.cuh"
 
 #include <math.h>
 
@@ -16,16 +17,6 @@ namespace {
 constexpr int BM = 128, BN = 128, BK = 32, PADK = BK + 8;   // padded rows: conflict-free fragment loads
 constexpr int kGemmThreads = 256;
 
-// GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3)))
-__device__ __forceinline__ float gelu(float x) {
-    const float u = 0.7978845608028654f * fmaf(0.044715f * x, x * x, x);
-    return 0.5f * x * (1.0f + tanhf(u));
-}
-__device__ __forceinline__ float geluGrad(float x) {
-    const float u = 0.7978845608028654f * fmaf(0.044715f * x, x * x, x);
-    const float t = tanhf(u);
-    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * 0.7978845608028654f * fmaf(0.134145f, x * x, 1.0f);
-}
 
 // Load a BMxBK (or BNxBK) tile of an operand, element (row, k) at G[row * srow + k * sk],
 // into shared memory rows [row][k].  kContig: sk == 1 (16-byte vectors along k);
@@ -273,6 +264,30 @@ __global__ void k_gate(GateArgs a) {
 }
 
 }  // namespace
+
+// 32 x 32 tiles through padded shared memory: coalesced reads of src rows, coalesced
+// writes of dst rows
+__global__ void k_transpose(int M, int N, const __nv_bfloat16* src, long long lds, __nv_bfloat16* dst,
+                            long long ldd) {
+    __shared__ __nv_bfloat16 t[32][34];
+    const int m0 = blockIdx.y * 32, n0 = blockIdx.x * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
+#pragma unroll
+    for (int i = ty; i < 32; i += 8)
+        if (m0 + i < M && n0 + tx < N) t[i][tx] = src[(size_t)(m0 + i) * lds + n0 + tx];
+    __syncthreads();
+#pragma unroll
+    for (int i = ty; i < 32; i += 8)
+        if (n0 + i < N && m0 + tx < M) dst[(size_t)(n0 + i) * ldd + m0 + tx] = t[tx][i];
+}
+
+cudaError_t launchTranspose(int M, int N, const __nv_bfloat16* src, long long lds, __nv_bfloat16* dst,
+                            long long ldd, cudaStream_t s) {
+    if (M <= 0 || N <= 0) return cudaSuccess;
+    dim3 grid((N + 31) / 32, (M + 31) / 32);
+    k_transpose<<<grid, 256, 0, s>>>(M, N, src, lds, dst, ldd);
+    return cudaGetLastError();
+}
 
 cudaError_t launchGemm(const GemmArgs& g, cudaStream_t s) {
     dim3 grid(g.N / BN, g.M / BM);

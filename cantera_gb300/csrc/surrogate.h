@@ -34,6 +34,40 @@ struct GemmArgs {
 };
 cudaError_t launchGemm(const GemmArgs& g, cudaStream_t s);
 
+// The tcgen05 GEMM (umma.cu): C[m][n] = epilogue(alpha * sum_k A[m][k] B[n][k]), A [M][K]
+// and B [N][K] BF16, K-major (row strides lda, ldb elements, multiples of 8), FP32
+// accumulation in tensor memory; M, N multiples of 128, K of 64 * splits.  Epilogue: + bias
+// (float [N]); act 1 = GELU with the pre-activation written to Z (float or bf16, row stride
+// ldz) when Z is given, act 2 = multiply by GELU'(Z); C float or bf16 (row stride ldc);
+// CT (bf16, may be null) receives C transposed, CT[n * ldct + m].  splits > 1: each CTA
+// sums K / splits of the products and adds its tile into FP32 C (zeroed by the caller).
+struct UmmaArgs {
+    int M, N, K;
+    const __nv_bfloat16* A;
+    long long lda;
+    const __nv_bfloat16* B;
+    long long ldb;
+    void* C;
+    long long ldc;
+    int cFloat;
+    float alpha;
+    const float* bias;
+    int act;
+    void* Z;
+    long long ldz;
+    int zFloat;
+    __nv_bfloat16* CT;
+    long long ldct;
+    int splitK;        // set by launchUmma
+};
+const char* checkUmmaArgs(const UmmaArgs& g, int splits);   // null when the call is valid
+cudaError_t launchUmma(const UmmaArgs& g, int splits, cudaStream_t s);
+int ummaTakeError();   // 1 if a CTA gave up a bounded wait since the last call (and clears it)
+
+// dst[n * ldd + m] = src[m * lds + n] for m < M, n < N (BF16 transpose through shared memory)
+cudaError_t launchTranspose(int M, int N, const __nv_bfloat16* src, long long lds, __nv_bfloat16* dst,
+                            long long ldd, cudaStream_t s);
+
 // Adam on FP32 master weights (w, m, v, gradient g, n values); writes the BF16 copy wb.
 cudaError_t launchAdam(int n, float* w, float* m, float* v, const float* g, __nv_bfloat16* wb, float lr,
                        float beta1, float beta2, float eps, int step, cudaStream_t s);

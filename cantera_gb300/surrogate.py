@@ -5,7 +5,8 @@ change over a fixed step dt (dY, dT, each standardised), learned as the correcti
 explicit step dt f(x0) (f the reactor right-hand side), relative to that step's size:
 slow states need almost none.  Training pairs come from the
 batched integrator; training and inference run on the engine's own kernels (BF16
-tensor-core GEMMs accumulating in FP32 with fused bias/GELU epilogues, the MSE gradient,
+GEMMs on the tcgen05 tensor cores accumulating in FP32 tensor memory, with fused bias/GELU
+epilogues that also write the transposed copies the backward pass reads; the MSE gradient,
 bias-gradient sums and Adam; ``gb_nn_*`` in include/gbchem.h).  Each prediction is gated by
 element and enthalpy conservation and by the trapezoidal rule with the reactor right-hand
 sides at both ends; reactors that fail fall back to the FP64 BDF integrator.
@@ -47,7 +48,7 @@ class Surrogate:
         real_in = [self.K + 2] + [hidden] * layers
         real_out = [hidden] * layers + [self.K + 1]
         g = torch.Generator().manual_seed(seed)
-        self.W, self.Wb, self.b, self.mW, self.vW, self.mb, self.vb = [], [], [], [], [], [], []
+        self.W, self.Wb, self.WbT, self.b, self.mW, self.vW, self.mb, self.vb = [], [], [], [], [], [], [], []
         for l in range(len(dims) - 1):
             n_out, n_in = dims[l + 1], dims[l]
             w = torch.zeros(n_out, n_in)
@@ -56,6 +57,7 @@ class Surrogate:
             w = w.to(self.dev)
             self.W.append(w)
             self.Wb.append(w.to(torch.bfloat16))
+            self.WbT.append(self.Wb[-1].T.contiguous())
             self.b.append(torch.zeros(n_out, device=self.dev))
             self.mW.append(torch.zeros_like(w))
             self.vW.append(torch.zeros_like(w))
@@ -113,97 +115,175 @@ class Surrogate:
         return ((n + 127) // 128) * 128
 
     # ---- network ---------------------------------------------------------------------
-    def _gemm(self, M, N, K, A, sam, sak, B, sbn, sbk, C, scm, scn, c_float, alpha=1.0, bias=None, act=0,
-              Z=None, szm=0, szn=0, z_float=1):
-        _check(library().gb_nn_gemm(M, N, K, _p(A), sam, sak, _p(B), sbn, sbk, _p(C), scm, scn, c_float, alpha,
-                                    _p(bias), act, _p(Z), szm, szn, z_float))
+    # Every product is one call of the tensor-core GEMM (gb_nn_gemm_tc: tcgen05.mma with
+    # TMEM accumulators, TMA-staged K-major operands).  The backward pass needs the layer
+    # inputs and the output gradients transposed (the weight gradient dW = dZ^T X reduces
+    # over the batch, which must be the K-major dimension of both operands): the forward
+    # epilogues write X^T next to X, the backward epilogues dZ^T next to dZ, and W^T is kept
+    # beside W.
+    def _tc(self, A, B, C, alpha=1.0, bias=None, act=0, Z=None, CT=None, splits=1):
+        M, K = A.shape
+        N = B.shape[0]
+        _check(library().gb_nn_gemm_tc(M, N, K, _p(A), A.stride(0), _p(B), B.stride(0), _p(C), C.stride(0),
+                                       int(C.dtype.itemsize == 4), alpha, _p(bias), act, _p(Z),
+                                       Z.stride(0) if Z is not None else 0,
+                                       int(Z is not None and Z.dtype.itemsize == 4), _p(CT),
+                                       CT.stride(0) if CT is not None else 0, splits, self._stream()))
 
-    def forward(self, X, keep=False):
-        """Output [M, PAD_OUT] (float) of a padded input batch X [M, PAD_IN] (bf16)."""
+    def _stream(self):
+        return ctypes.c_void_p(self.torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def _transpose(self, X, XT):
+        _check(library().gb_nn_transpose(X.shape[0], X.shape[1], _p(X), X.stride(0), _p(XT), XT.stride(0),
+                                         self._stream()))
+
+    def _refresh_transposed_weights(self):
+        for l in range(len(self.Wb)):
+            self._transpose(self.Wb[l], self.WbT[l])
+
+    @staticmethod
+    def _splits(M, tiles):
+        """K-splits of a weight-gradient product (K = batch rows): about one block per SM."""
+        s = 1
+        while s * 2 * tiles <= 148 and M % (64 * s * 2) == 0:
+            s *= 2
+        return s
+
+    def forward(self, X, keep=False, buf=None):
+        """Output [M, PAD_OUT] (float) of a padded input batch X [M, PAD_IN] (bf16).  keep:
+        also the pre-activations and the transposed layer inputs of the backward pass (in
+        the training buffers `buf`)."""
         torch = self.torch
         M = X.shape[0]
         A = X
-        cache = []
         nl = len(self.W)
         for l in range(nl):
-            n_out, n_in = self.dims[l + 1], self.dims[l]
+            n_out = self.dims[l + 1]
             if l < nl - 1:
-                Z = torch.empty(M, n_out, device=self.dev) if keep else None
-                C = torch.empty(M, n_out, dtype=torch.bfloat16, device=self.dev)
-                self._gemm(M, n_out, n_in, A, n_in, 1, self.Wb[l], n_in, 1, C, n_out, 1, 0, 1.0, self.b[l], 1,
-                           Z, n_out, 1, 1)
+                C = buf["act"][l + 1] if keep else torch.empty(M, n_out, dtype=torch.bfloat16, device=self.dev)
+                self._tc(A, self.Wb[l], C, bias=self.b[l], act=1, Z=buf["Z"][l] if keep else None,
+                         CT=buf["actT"][l + 1] if keep else None)
             else:
-                Z = None
-                C = torch.empty(M, n_out, device=self.dev)
-                self._gemm(M, n_out, n_in, A, n_in, 1, self.Wb[l], n_in, 1, C, n_out, 1, 1, 1.0, self.b[l], 0)
-            cache.append((A, Z))
+                C = buf["out"] if keep else torch.empty(M, n_out, device=self.dev)
+                self._tc(A, self.Wb[l], C, bias=self.b[l], act=0)
             A = C
-        return (A, cache) if keep else A
+        return A
+
+    def _buffers(self, M):
+        """Device buffers of one training batch of M rows (reused across steps)."""
+        torch = self.torch
+        bf = torch.bfloat16
+        nl = len(self.W)
+        d = self.dims
+        hid = max(d[1:-1])
+        return {"X": torch.zeros(M, PAD_IN, dtype=bf, device=self.dev),
+                "Y": torch.zeros(M, PAD_OUT, device=self.dev),
+                "act": [None] + [torch.empty(M, d[l], dtype=bf, device=self.dev) for l in range(1, nl)],
+                "actT": [torch.empty(d[l], M, dtype=bf, device=self.dev) for l in range(nl)],
+                "Z": [torch.empty(M, d[l + 1], device=self.dev) for l in range(nl - 1)],
+                "out": torch.empty(M, PAD_OUT, device=self.dev),
+                "dZ": [torch.empty(M, max(hid, PAD_OUT), dtype=bf, device=self.dev) for _ in range(2)],
+                "dZT": [torch.empty(max(hid, PAD_OUT), M, dtype=bf, device=self.dev) for _ in range(2)],
+                "gW": [torch.empty_like(w) for w in self.W],
+                "gb": [torch.empty_like(b) for b in self.b],
+                "bb": [torch.empty(b.shape, dtype=bf, device=self.dev) for b in self.b],
+                "loss": torch.zeros(1, device=self.dev)}
+
+    def _backward(self, buf, n_real):
+        """Parameter gradients of the batch in buf (forward pass already run, the rows beyond
+        n_real being padding with zero inputs and targets); the batch loss is added to
+        buf["loss"] as the mean over all M rows."""
+        M = buf["X"].shape[0]
+        L = library()
+        out = buf["out"]
+        if n_real < M:
+            out[n_real:] = 0.0
+        nl = len(self.W)
+        dZ = buf["dZ"][0][:, :PAD_OUT]
+        dZT = buf["dZT"][0][:PAD_OUT]
+        _check(L.gb_nn_mse(M, self.K + 1, PAD_OUT, _p(out), _p(buf["Y"]), _p(dZ), _p(buf["loss"])))
+        self._transpose(dZ, dZT)
+        scale = M / float(n_real)            # the loss is the mean over the n_real rows
+        for l in range(nl - 1, -1, -1):
+            n_out, n_in = self.dims[l + 1], self.dims[l]
+            tiles = (n_out // 128) * (n_in // (256 if n_in % 256 == 0 else 128))
+            # dW = dZ^T X: (n_out x M)(M x n_in), reduced over the batch in K-splits
+            self._tc(dZT, buf["actT"][l], buf["gW"][l], alpha=scale, splits=self._splits(M, tiles))
+            _check(L.gb_nn_colsum(M, n_out, _p(dZ), dZ.stride(0), scale, _p(buf["gb"][l])))
+            if l > 0:
+                k = (nl - l) % 2
+                dprev = buf["dZ"][k][:, :n_in]
+                dprevT = buf["dZT"][k][:n_in]
+                # dZ_prev = (dZ W) * GELU'(Z_prev): (M x n_out)(n_out x n_in) with W^T K-major
+                self._tc(dZ, self.WbT[l], dprev, act=2, Z=buf["Z"][l - 1], CT=dprevT)
+                dZ, dZT = dprev, dprevT
 
     def gradients(self, X, Ytarget, n_real):
         """Loss and parameter gradients of a batch (the rows beyond n_real are padding and
         must carry zero targets and zero inputs)."""
-        torch = self.torch
         M = X.shape[0]
-        out, cache = self.forward(X, keep=True)
-        if n_real < M:
-            out[n_real:] = 0.0
-        loss = torch.zeros(1, device=self.dev)
-        dZ = torch.empty(M, PAD_OUT, dtype=torch.bfloat16, device=self.dev)
-        _check(library().gb_nn_mse(M, self.K + 1, PAD_OUT, _p(out), _p(Ytarget), _p(dZ), _p(loss)))
-        # the loss is averaged over the n_real rows
-        scale = M / float(n_real)
-        gW, gb = [None] * len(self.W), [None] * len(self.W)
-        for l in range(len(self.W) - 1, -1, -1):
-            n_out, n_in = self.dims[l + 1], self.dims[l]
-            A, _ = cache[l]
-            gW[l] = torch.empty(n_out, n_in, device=self.dev)
-            # dW = dZ^T A: (n_out x M) (M x n_in)
-            self._gemm(n_out, n_in, M, dZ, 1, n_out, A, 1, n_in, gW[l], n_in, 1, 1, scale)
-            gb[l] = torch.empty(n_out, device=self.dev)
-            _check(library().gb_nn_colsum(M, n_out, _p(dZ), n_out, scale, _p(gb[l])))
-            if l > 0:
-                _, Zp = cache[l - 1]
-                dprev = torch.empty(M, n_in, dtype=torch.bfloat16, device=self.dev)
-                # dZ_prev = (dZ W) * GELU'(Z_prev): (M x n_out)(n_out x n_in)
-                self._gemm(M, n_in, n_out, dZ, n_out, 1, self.Wb[l], 1, n_in, dprev, n_in, 1, 0, 1.0, None, 2,
-                           Zp, n_in, 1, 1)
-                dZ = dprev
-        return float(loss.item()) * scale, gW, gb
+        buf = self._buffers(M)
+        buf["X"].copy_(X)
+        buf["Y"].copy_(Ytarget)
+        self._transpose(buf["X"], buf["actT"][0])
+        self.forward(buf["X"], keep=True, buf=buf)
+        self._backward(buf, n_real)
+        self.torch.cuda.synchronize()
+        _check(library().gb_nn_sync(self._stream()))
+        return float(buf["loss"].item()) * M / float(n_real), buf["gW"], buf["gb"]
 
-    def adam_step(self, gW, gb, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+    def adam_step(self, gW, gb, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, bb=None):
         self.step_count += 1
         L = library()
         for l in range(len(self.W)):
             _check(L.gb_nn_adam(self.W[l].numel(), _p(self.W[l]), _p(self.mW[l]), _p(self.vW[l]), _p(gW[l]),
                                 _p(self.Wb[l]), lr, beta1, beta2, eps, self.step_count))
-            bb = self.torch.empty(self.b[l].shape, dtype=self.torch.bfloat16, device=self.dev)
+            b16 = bb[l] if bb is not None else self.torch.empty(self.b[l].shape, dtype=self.torch.bfloat16,
+                                                                 device=self.dev)
             _check(L.gb_nn_adam(self.b[l].numel(), _p(self.b[l]), _p(self.mb[l]), _p(self.vb[l]), _p(gb[l]),
-                                _p(bb), lr, beta1, beta2, eps, self.step_count))
+                                _p(b16), lr, beta1, beta2, eps, self.step_count))
+        self._refresh_transposed_weights()
 
-    def train(self, X, Yt, n, epochs=10, batch=8192, lr=1e-3, seed=0, log=None):
-        """Mini-batch Adam over the n training rows of X [>=n, PAD_IN], Yt [>=n, PAD_OUT]."""
+    def train(self, X, Yt, n, epochs=10, batch=16384, lr=1e-3, warmup=0.05, seed=0, log=None):
+        """Mini-batch Adam over the n training rows of X [>=n, PAD_IN], Yt [>=n, PAD_OUT]:
+        learning rate ramped up linearly over the first `warmup` fraction of the steps, then
+        cosine-decayed to zero.  The steps are queued on the current stream without host
+        synchronisation; the mean loss of each epoch is read once at its end."""
         torch = self.torch
         batch = min(self._rows(batch), self._rows(n))
         g = torch.Generator(device=self.dev).manual_seed(seed)
+        buf = self._buffers(batch)
+        L = library()
+        _check(L.gb_nn_set_stream(self._stream(), 1))
         losses = []
-        for ep in range(epochs):
-            perm = torch.randperm(n, device=self.dev, generator=g)
-            tot, cnt = 0.0, 0
-            for s in range(0, n, batch):
-                idx = perm[s:s + batch]
-                m = idx.numel()
-                Xb = torch.zeros(batch, PAD_IN, dtype=torch.bfloat16, device=self.dev)
-                Yb = torch.zeros(batch, PAD_OUT, device=self.dev)
-                Xb[:m] = X[idx]
-                Yb[:m] = Yt[idx]
-                loss, gW, gb = self.gradients(Xb, Yb, m)
-                self.adam_step(gW, gb, lr=lr * (0.5 * (1 + math.cos(math.pi * ep / max(1, epochs)))))
-                tot += loss * m
-                cnt += m
-            losses.append(tot / cnt)
-            if log:
-                log(ep, losses[-1])
+        steps_per_epoch = (n + batch - 1) // batch
+        total = epochs * steps_per_epoch
+        nwarm = max(1, int(warmup * total))
+        step = 0
+        try:
+            for ep in range(epochs):
+                perm = torch.randperm(n, device=self.dev, generator=g)
+                buf["loss"].zero_()
+                for s0 in range(0, n, batch):
+                    idx = perm[s0:s0 + batch]
+                    m = idx.numel()
+                    torch.index_select(X, 0, idx, out=buf["X"][:m])
+                    torch.index_select(Yt, 0, idx, out=buf["Y"][:m])
+                    if m < batch:
+                        buf["X"][m:] = 0
+                        buf["Y"][m:] = 0
+                    self._transpose(buf["X"], buf["actT"][0])
+                    self.forward(buf["X"], keep=True, buf=buf)
+                    self._backward(buf, m)
+                    step += 1
+                    f = step / nwarm if step <= nwarm else 0.5 * (1 + math.cos(math.pi * (step - nwarm) / max(1, total - nwarm)))
+                    self.adam_step(buf["gW"], buf["gb"], lr=lr * f, bb=buf["bb"])
+                _check(L.gb_nn_sync(self._stream()))
+                losses.append(float(buf["loss"].item()) * batch / float(n))
+                if log:
+                    log(ep, losses[-1])
+        finally:
+            L.gb_nn_set_stream(None, 0)
         return losses
 
     # ---- inference with the gate and the fallback -------------------------------------

@@ -9,13 +9,73 @@ waves of its own resident capacity (blocks x reactors per block), and candidates
 by time per reactor: a sample of a fixed size would favour the shape whose capacity happens
 to divide it well (the tail of a partial wave dominates a short run).  Within ``margin`` of
 the fastest, the shape with more resident reactors wins (more latency hiding on the long
-runs the tuner stands in for).  Results are cached per (mechanism, options).
+runs the tuner stands in for).  Results are cached per (mechanism, options) in the process
+and persisted in a JSON file keyed by the mechanism's content, the GPU and the options
+(``GBCHEM_TUNING_CACHE`` names the file; default ``~/.cache/cantera_gb300/launch_shapes.json``;
+an empty value turns the file off), so a later process on the same kind of GPU skips the
+measurement.
 """
+import hashlib
+import json
+import os
 import time
 
 from . import ReactorNet
 
 _cache = {}
+
+
+def cache_path():
+    p = os.environ.get("GBCHEM_TUNING_CACHE")
+    if p is None:
+        p = os.path.join(os.path.expanduser("~"), ".cache", "cantera_gb300", "launch_shapes.json")
+    return p or None
+
+
+def mechanism_key(solution):
+    """Content hash of the mechanism: its file, phase and structure counts (which also cover
+    species and reactions drawn from other files)."""
+    h = hashlib.sha256()
+    path, phase = getattr(solution, "source", ("", ""))
+    try:
+        with open(path, "rb") as f:
+            h.update(f.read())
+    except OSError:
+        h.update(path.encode())
+    h.update(phase.encode())
+    h.update(json.dumps(solution.structure(), sort_keys=True).encode())
+    return h.hexdigest()[:24]
+
+
+def gpu_key():
+    try:
+        import torch
+        d = torch.cuda.current_device()
+        p = torch.cuda.get_device_properties(d)
+        return "%s|sm%d%d|%dSM" % (p.name, p.major, p.minor, p.multi_processor_count)
+    except Exception:
+        return "unknown-gpu"
+
+
+def _load(path):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(path, key, value):
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        data = _load(path)
+        data[key] = value
+        tmp = "%s.%d.tmp" % (path, os.getpid())
+        with open(tmp, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+    except OSError:
+        pass
 
 
 def candidates(max_warps=8):
@@ -39,9 +99,18 @@ def autotune(solution, T, P, Y, t_probe, waves=3, pool=8192, rtol=1e-8, atol=1e-
     Each candidate advances `waves` full waves of its resident capacity, drawn with a stride
     from the caller's reactors (at most `pool` of them).  Also returns every candidate's
     timing (seconds per reactor)."""
-    key = (solution._h, lu_precision, waves, pool, float(t_probe))
+    key = (solution._h, lu_precision, waves, pool, float(t_probe), rtol, atol)
     if use_cache and key in _cache:
         return _cache[key]
+    path = cache_path() if use_cache else None
+    pkey = "|".join([mechanism_key(solution), gpu_key(), "lu%d" % lu_precision, "w%d" % waves, "p%d" % pool,
+                     "t%.6g" % t_probe, "r%.3g" % rtol, "a%.3g" % atol])
+    if path:
+        hit = _load(path).get(pkey)
+        if hit:
+            result = (dict(hit["pick"]), hit["log"])
+            _cache[key] = result
+            return result
     n = T.shape[0]
     npool = min(n, pool)
     Tp, Pp, Yp = _subset(T, P, Y, max(1, n // npool), npool)
@@ -73,4 +142,6 @@ def autotune(solution, T, P, Y, t_probe, waves=3, pool=8192, rtol=1e-8, atol=1e-
     pick = max(near, key=lambda t: t[2]["blocks"] * t[2]["warps_per_block"])
     result = (dict(pick[1]), [{"seconds": t, "options": c, "shape": s} for t, c, s in timings])
     _cache[key] = result
+    if path:
+        _store(path, pkey, {"pick": result[0], "log": result[1], "measured": time.strftime("%Y-%m-%d %H:%M:%S")})
     return result

@@ -193,8 +193,9 @@ int32_t gb_mech_n_elements(int32_t mech);
 int32_t gb_mech_element_mass(int32_t mech, int32_t buflen, double* out);
 
 /* ---- learned surrogate (no counterpart in the reference) -------------------------------
- * Device-pointer operations of the MLP surrogate, each on the default stream and finished
- * on return.  gb_nn_gemm: C(m,n) = epilogue(alpha * sum_k A(m,k) B(n,k)) with BF16 A, B on
+ * Device-pointer operations of the MLP surrogate, on the calling thread's surrogate stream
+ * (gb_nn_set_stream; the default stream until set) and finished on return unless that
+ * thread asked for asynchronous calls.  gb_nn_gemm: C(m,n) = epilogue(alpha * sum_k A(m,k) B(n,k)) with BF16 A, B on
  * the tensor cores, FP32 accumulation; element (i,j) of X at X[i*s_i + j*s_j]; M, N multiples
  * of 128, K of 32; epilogue: + bias[n] (float, may be NULL), act 1 = GELU (tanh form) with the
  * pre-activation written to Z (unless Z is NULL), act 2 = multiply by GELU'(Z); C and Z float
@@ -203,6 +204,27 @@ int32_t gb_nn_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, 
                    const void* B, int64_t sbn, int64_t sbk, void* C, int64_t scm, int64_t scn,
                    int32_t c_float, float alpha, const float* bias, int32_t act, void* Z, int64_t szm,
                    int64_t szn, int32_t z_float);
+/* The same products on the 5th-generation tensor cores (tcgen05.mma, accumulators in tensor
+ * memory, operands staged by TMA), the surrogate's GEMM: C(m,n) = epilogue(alpha * sum_k
+ * A[m*lda + k] B[n*ldb + k]) with BF16 A [M][K] and B [N][K] both K-major (lda, ldb >= K,
+ * multiples of 8), M and N multiples of 128, K a multiple of 64 * splits; epilogue as
+ * gb_nn_gemm (bias, act 1 GELU keeping the pre-activation in Z, act 2 times GELU'(Z); Z float
+ * or bf16 with row stride ldz); C float (c_float 1) or bf16, row stride ldc; CT (bf16, may be
+ * NULL) receives C transposed, CT[n*ldct + m].  splits > 1 divides K among blocks that add
+ * their partial products into FP32 C (the call clears C first; no bias, act or CT then).
+ * Ordered on `stream` (a cudaStream_t, NULL the default stream), not synchronised: call
+ * gb_nn_sync to wait and to collect errors. */
+int32_t gb_nn_gemm_tc(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda, const void* B, int64_t ldb,
+                      void* C, int64_t ldc, int32_t c_float, float alpha, const float* bias, int32_t act, void* Z,
+                      int64_t ldz, int32_t z_float, void* CT, int64_t ldct, int32_t splits, void* stream);
+/* dst[n*ldd + m] = src[m*lds + n] for m < M, n < N (bf16), ordered on `stream`. */
+int32_t gb_nn_transpose(int32_t M, int32_t N, const void* src, int64_t lds, void* dst, int64_t ldd, void* stream);
+/* Stream of this host thread's gb_nn_* calls (NULL: the default stream); async = 1: they
+ * return without waiting for their work (gb_nn_sync waits). */
+int32_t gb_nn_set_stream(void* stream, int32_t async);
+/* Wait for `stream`; GB_ERR if a tensor-core GEMM block gave up a bounded wait since the
+ * last call (its tile is then not written). */
+int32_t gb_nn_sync(void* stream);
 /* Adam step on FP32 master weights w with moments m, v and gradient g; writes the bf16 copy. */
 int32_t gb_nn_adam(int32_t n, float* w, float* m, float* v, const float* g, void* wb, float lr,
                    float beta1, float beta2, float eps, int32_t step);

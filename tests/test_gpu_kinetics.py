@@ -138,3 +138,24 @@ def test_engine_log_against_library_log():
     small = fin & ~big
     assert np.max(np.abs(a - b)[small]) < 2 ** -60 + np.max(np.spacing(np.abs(b[small])))
     assert np.all((a == b)[~fin] | both_nan[~fin])
+
+
+@pytest.mark.parametrize("name", ["h2o2", "gri30"])
+def test_state_tiles_do_not_change_results(name):
+    """The kernel works on tiles of 32 consecutive states: any batch size, and any position
+    of a state in its batch, gives the same bits (wdot and ddCi), also through device
+    pointers."""
+    import torch
+    sol, m = gpu_solution(name), oracle_mech(name)
+    T, P, Y = random_states(m.K, 100, seed=21)
+    w = sol.net_production_rates(T, P, Y)
+    J = sol.net_production_rates_ddCi(T, P, Y)
+    for a, b in ((0, 1), (5, 38), (31, 64), (67, 100), (3, 35)):
+        sl = slice(a, b)
+        Ys = np.ascontiguousarray(Y[:, sl])
+        assert np.array_equal(sol.net_production_rates(T[sl], P[sl], Ys), w[:, sl])
+        assert np.array_equal(sol.net_production_rates_ddCi(T[sl], P[sl], Ys), J[:, sl])
+    d = lambda x: torch.tensor(x, device="cuda")
+    wd = torch.empty((m.K, 100), dtype=torch.float64, device="cuda")
+    Jd = sol.net_production_rates_ddCi(d(T), d(P), d(Y), wdot=wd)
+    assert np.array_equal(Jd.cpu().numpy(), J) and np.array_equal(wd.cpu().numpy(), w)
