@@ -82,6 +82,9 @@ def library():
         "gb_net_set_max_time_step": (I32, [I32, D]),
         "gb_net_advance": (I32, [I32, D]),
         "gb_net_step": (I32, [I32, P, I32]),
+        "gb_net_checkpoint_bytes": (ctypes.c_int64, [I32]),
+        "gb_net_checkpoint": (I32, [I32, P, ctypes.c_int64]),
+        "gb_net_restore": (I32, [I32, P, ctypes.c_int64]),
         "gb_net_time": (D, [I32]),
         "gb_kin_last_kernel_ms": (D, [I32]),
         "gb_net_last_advance_ms": (D, [I32]),
@@ -367,6 +370,20 @@ class ReactorNet:
             times = np.empty(self.n)
         self.last_step_failures = _check(library().gb_net_step(self._h, _ptr(times), flags))
         return times
+
+    def checkpoint(self):
+        """The network's integrator state (time, records, counters, state) as bytes."""
+        L = library()
+        nb = L.gb_net_checkpoint_bytes(self._h)
+        _check(nb)
+        buf = np.empty(nb, dtype=np.uint8)
+        _check(L.gb_net_checkpoint(self._h, _ptr(buf), nb))
+        return buf.tobytes()
+
+    def restore(self, data):
+        """Continue from a checkpoint of a network of the same size and mechanism."""
+        buf = np.frombuffer(data, dtype=np.uint8).copy()
+        _check(library().gb_net_restore(self._h, _ptr(buf), buf.size))
 
     @property
     def launch_info(self):

@@ -1089,6 +1089,107 @@ int32_t gb_net_step(int32_t h, double* times, int32_t flags) {
     });
 }
 
+/* ---- checkpoint / restore of a network's integrator records ------------------------- */
+namespace {
+constexpr int64_t kCkptMagic = 0x4B43504B43424747LL;   // "GGBCKPCK"
+constexpr int64_t kCkptVersion = 1;
+struct CkptLayout {
+    size_t header, rec, stats, status, tign, T, P, Y, total;
+};
+CkptLayout ckptLayout(const NetEntry& ne, int K) {
+    CkptLayout L{};
+    const size_t n = (size_t)ne.n;
+    auto up8 = [](size_t b) { return (b + 7) & ~size_t(7); };
+    L.header = 8 * 8 + 8;                               // 8 int64 fields, then the time
+    L.rec = L.header;
+    L.stats = L.rec + n * ne.recStride * 8;
+    L.status = L.stats + n * 64;
+    L.tign = L.status + up8(n * 4);
+    L.T = L.tign + n * 8;
+    L.P = L.T + n * 8;
+    L.Y = L.P + n * 8;
+    L.total = L.Y + (size_t)K * n * 8;
+    return L;
+}
+}  // namespace
+
+int64_t gb_net_checkpoint_bytes(int32_t h) {
+    try {
+        NetEntry& ne = net(h);
+        return (int64_t)ckptLayout(ne, mech(ne.mech).m.K).total;
+    } catch (std::exception& e) {
+        g_error = e.what();
+        return GB_ERR;
+    }
+}
+
+int32_t gb_net_checkpoint(int32_t h, void* buf, int64_t bytes) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        MechEntry& me = mech(ne.mech);
+        requireMechDevice(me);
+        const int K = me.m.K;
+        const CkptLayout L = ckptLayout(ne, K);
+        if (!buf || bytes < (int64_t)L.total) throw std::runtime_error("checkpoint buffer smaller than gb_net_checkpoint_bytes");
+        char* b = (char*)buf;
+        int64_t hd[8] = {kCkptMagic, kCkptVersion, ne.n, me.dm.N, ne.recStride, K, 0, 0};
+        std::memcpy(b, hd, sizeof(hd));
+        std::memcpy(b + 64, &ne.time, 8);
+        const size_t n = (size_t)ne.n;
+        ck(cudaStreamSynchronize(me.stream), "checkpoint");
+        ck(cudaMemcpy(b + L.rec, ne.dRec.p, n * ne.recStride * 8, cudaMemcpyDeviceToHost), "checkpoint records");
+        ck(cudaMemcpy(b + L.stats, ne.dStats.p, n * 64, cudaMemcpyDeviceToHost), "checkpoint stats");
+        ck(cudaMemcpy(b + L.status, ne.dStatus.p, n * 4, cudaMemcpyDeviceToHost), "checkpoint status");
+        ck(cudaMemcpy(b + L.tign, ne.dTign.p, n * 8, cudaMemcpyDeviceToHost), "checkpoint ignition");
+        ck(cudaMemcpy(b + L.T, ne.dT.p, n * 8, cudaMemcpyDeviceToHost), "checkpoint T");
+        ck(cudaMemcpy(b + L.P, ne.dP.p, n * 8, cudaMemcpyDeviceToHost), "checkpoint P");
+        ck(cudaMemcpy(b + L.Y, ne.dY.p, (size_t)K * n * 8, cudaMemcpyDeviceToHost), "checkpoint Y");
+        return 0;
+    });
+}
+
+int32_t gb_net_restore(int32_t h, const void* buf, int64_t bytes) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        MechEntry& me = mech(ne.mech);
+        requireMechDevice(me);
+        const int K = me.m.K;
+        const CkptLayout L = ckptLayout(ne, K);
+        if (!buf || bytes < (int64_t)L.total) throw std::runtime_error("checkpoint buffer too small for this network");
+        const char* b = (const char*)buf;
+        int64_t hd[8];
+        std::memcpy(hd, b, sizeof(hd));
+        if (hd[0] != kCkptMagic || hd[1] != kCkptVersion) throw std::runtime_error("not a reactor-network checkpoint");
+        if (hd[2] != ne.n || hd[3] != me.dm.N || hd[4] != ne.recStride || hd[5] != K)
+            throw std::runtime_error("checkpoint of a network of another size or mechanism");
+        double t = 0.0;
+        std::memcpy(&t, b + 64, 8);
+        if (!std::isfinite(t) || t < 0.0) throw std::runtime_error("checkpoint time is not valid");
+        const size_t n = (size_t)ne.n;
+        cudaStream_t s = me.stream;
+        ck(cudaStreamSynchronize(s), "restore");
+        ck(cudaMemcpy(ne.dRec.p, b + L.rec, n * ne.recStride * 8, cudaMemcpyHostToDevice), "restore records");
+        ck(cudaMemcpy(ne.dStats.p, b + L.stats, n * 64, cudaMemcpyHostToDevice), "restore stats");
+        ck(cudaMemcpy(ne.dStatus.p, b + L.status, n * 4, cudaMemcpyHostToDevice), "restore status");
+        ck(cudaMemcpy(ne.dTign.p, b + L.tign, n * 8, cudaMemcpyHostToDevice), "restore ignition");
+        ck(cudaMemcpy(ne.dT.p, b + L.T, n * 8, cudaMemcpyHostToDevice), "restore T");
+        ck(cudaMemcpy(ne.dP.p, b + L.P, n * 8, cudaMemcpyHostToDevice), "restore P");
+        ck(cudaMemcpy(ne.dY.p, b + L.Y, (size_t)K * n * 8, cudaMemcpyHostToDevice), "restore Y");
+        // queue order as gb_net_set_state makes it (hottest first); it only schedules
+        std::vector<double> hT(n);
+        std::memcpy(hT.data(), b + L.T, n * 8);
+        std::vector<int> ord(n);
+        std::iota(ord.begin(), ord.end(), 0);
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return hT[a] > hT[c]; });
+        ne.dOrder.ensure(n * 4);
+        ck(cudaMemcpy(ne.dOrder.p, ord.data(), n * 4, cudaMemcpyHostToDevice), "restore order");
+        ne.haveOrder = true;
+        ne.time = t;
+        dropGraph(ne);
+        return 0;
+    });
+}
+
 double gb_kin_last_kernel_ms(int32_t h) {
     try {
         return mech(h).lastMs;

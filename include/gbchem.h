@@ -143,6 +143,18 @@ double gb_net_time(int32_t net);
 double gb_net_last_advance_ms(int32_t net);
 int32_t gb_net_get_state(int32_t net, double* T, double* Y, int32_t flags);
 
+/* Checkpoint of a network (no counterpart in the reference, whose CVODES state cannot be
+ * saved; the nearest is ReactorNet::reinitialize from the reactors' states,
+ * src/zeroD/ReactorNet.cpp:306-322): its time, every reactor's integrator record (Nordsieck
+ * array, step size, order, error-test history, ignition marker), counters, status and the
+ * state at the network's time, into a host buffer of gb_net_checkpoint_bytes bytes.
+ * gb_net_restore puts such a checkpoint into a network of the same size and mechanism;
+ * advancing it then continues the saved integration exactly (bit for bit).  The returned size
+ * is an int64, or GB_ERR. */
+int64_t gb_net_checkpoint_bytes(int32_t net);
+int32_t gb_net_checkpoint(int32_t net, void* buf, int64_t bytes);
+int32_t gb_net_restore(int32_t net, const void* buf, int64_t bytes);
+
 /* Launch shape of the integrator: info[0..5] = blocks, reactors (warps) per block, shared
  * bytes per warp, mechanism bytes in shared memory per block, Newton matrices in shared (1)
  * or global (2) memory, factorisation buffers per block.  (No counterpart in the reference.) */

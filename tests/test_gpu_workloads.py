@@ -239,3 +239,31 @@ def test_net_step_device_times_and_facade():
     assert 0 < t1 < t2 == rn.time
     rn.advance(1e-3)
     assert r.T > 2000.0
+
+
+def test_checkpoint_restore_continues_bit_for_bit():
+    """A network checkpointed mid-integration and restored into a new network continues the
+    same integration: bit-identical states, counters and ignition times; checkpoints of
+    another network size are refused."""
+    import cantera_gb300 as gb
+    sol = gpu_solution("gri30")
+    T0, P, Y0 = gri30_sample(40, seed_offset=11)
+    a = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=RTOL, atol=ATOL)
+    assert a.advance(2e-3) == 0
+    ck = a.checkpoint()
+    assert a.advance(1e-2) == 0
+    b = gb.ReactorNet(sol, T0 + 100.0, P, Y0.T.copy(), rtol=RTOL, atol=ATOL, use_graph=True)
+    b.restore(ck)
+    assert b.time == 2e-3
+    assert b.advance(1e-2) == 0
+    Ta, Ya = a.get_state()
+    Tb, Yb = b.get_state()
+    assert np.array_equal(Ta, Tb) and np.array_equal(Ya, Yb)
+    assert np.array_equal(a.ignition_times, b.ignition_times)
+    for k, v in a.solver_stats.items():
+        assert np.array_equal(v, b.solver_stats[k]), k
+    c = gb.ReactorNet(sol, T0[:20], P[:20], Y0[:20].T.copy())
+    with pytest.raises(gb.GBError, match="another size"):
+        c.restore(ck)
+    with pytest.raises(gb.GBError, match="not a reactor-network checkpoint"):
+        b.restore(bytes(len(ck)))
