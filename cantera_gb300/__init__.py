@@ -25,7 +25,9 @@ __all__ = ["Solution", "ReactorNet", "library", "DATA_DIR", "GBError"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DATA_DIR = os.path.join(HERE, "data")
-LIB_PATH = os.environ.get("GBCHEM_LIB", os.path.join(HERE, "_build", "libgbchem.so"))
+# GBCHEM_CHECKED=1 loads the bounds-checked build (gb_check_status); GBCHEM_LIB names a library
+CHECKED = os.environ.get("GBCHEM_CHECKED", "") not in ("", "0")
+LIB_PATH = os.environ.get("GBCHEM_LIB", os.path.join(HERE, "_build_checked" if CHECKED else "_build", "libgbchem.so"))
 GB_ERR = -999
 GB_DEVICE_POINTERS = 1
 STAT_NAMES = ["steps", "rhs_evals", "newton_iters", "lin_setups", "jac_evals",
@@ -57,7 +59,7 @@ def library():
         return _lib
     if not os.path.exists(LIB_PATH) or os.environ.get("GBCHEM_REBUILD"):
         from . import build as _build
-        _build.build()
+        _build.build(checked=CHECKED and "GBCHEM_LIB" not in os.environ)
     L = ctypes.CDLL(LIB_PATH)
     I32, D, P = ctypes.c_int32, ctypes.c_double, ctypes.c_void_p
     sig = {
@@ -87,6 +89,7 @@ def library():
         "gb_net_restore": (I32, [I32, P, ctypes.c_int64]),
         "gb_net_time": (D, [I32]),
         "gb_kin_last_kernel_ms": (D, [I32]),
+        "gb_check_status": (I32, [I32, P]),
         "gb_net_last_advance_ms": (D, [I32]),
         "gb_net_get_state": (I32, [I32, P, P, I32]),
         "gb_net_get_status": (I32, [I32, P]),

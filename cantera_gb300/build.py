@@ -12,6 +12,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgbchem.so")
+OUT_CHECKED = os.path.join(HERE, "_build_checked")
+LIB_CHECKED = os.path.join(OUT_CHECKED, "libgbchem.so")
 SOURCES = ["capi.cu", "kernels.cu", "kernels_x.cu", "surrogate.cu", "umma.cu", "mechanism.cpp", "yaml_lite.cpp"]
 HEADERS = ["devmech.h", "fastexp.h", "kernels.h", "kinetics.cuh", "mechanism.h", "nnmath.cuh", "surrogate.h",
            "yaml_lite.h"]
@@ -28,7 +30,7 @@ def _nvcc():
     raise RuntimeError("nvcc not found")
 
 
-def _compile(nvcc, src, extra):
+def _compile(nvcc, src, extra, OUT):
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
     cmd = [nvcc] + ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
                            "-I", os.path.join(HERE, "..", "include"), "-c", src, "-o", obj] + extra
@@ -38,7 +40,14 @@ def _compile(nvcc, src, extra):
     return obj, r.stderr
 
 
-def build(force=False, verbose=False, extra=None):
+def build(force=False, verbose=False, extra=None, checked=False):
+    """Build the library (the bounds-checked variant with checked=True, into _build_checked)."""
+    if checked:
+        return _build(OUT_CHECKED, LIB_CHECKED, force, verbose, list(extra or []) + ["-DGBCHEM_CHECKED"])
+    return _build(OUT, LIB, force, verbose, extra)
+
+
+def _build(OUT, LIB, force, verbose, extra):
     os.makedirs(OUT, exist_ok=True)
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     deps = srcs + [os.path.join(CSRC, h) for h in HEADERS] + [
@@ -49,7 +58,7 @@ def build(force=False, verbose=False, extra=None):
     nvcc = _nvcc()
     extra = list(extra or [])
     with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
-        results = list(ex.map(lambda s: _compile(nvcc, s, extra), srcs))
+        results = list(ex.map(lambda s: _compile(nvcc, s, extra, OUT), srcs))
     if verbose:
         for _, err in results:
             if err:

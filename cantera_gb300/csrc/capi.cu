@@ -80,6 +80,7 @@ struct MechEntry {
     int device = -1;      // the CUDA device the mechanism's arena and stream live on
     // kinetics workspace
     DBuf dT, dP, dY, dW, dJ, dCounter;
+    DBuf dChk;                                  // bounds-check record (checked build)
     cudaEvent_t evA = nullptr, evB = nullptr;   // around the last kinetics kernel launch
     double lastMs = 0.0;
     ~MechEntry() {
@@ -708,6 +709,9 @@ int32_t gb_mech_load(const char* path, const char* phase) {
         e->device = dev;
         ck(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
         packDevMech(*e);
+        e->dChk.ensure(4 * sizeof(int));
+        ck(cudaMemset(e->dChk.p, 0, 4 * sizeof(int)), "memset");
+        e->dm.chk = e->dChk.as<int>();
         std::lock_guard<std::mutex> lk(g_mu);
         g_mechs.push_back(std::move(e));
         return (int32_t)g_mechs.size() - 1;
@@ -1187,6 +1191,24 @@ int32_t gb_net_restore(int32_t h, const void* buf, int64_t bytes) {
         ne.time = t;
         dropGraph(ne);
         return 0;
+    });
+}
+
+int32_t gb_check_status(int32_t h, int32_t* out) {
+    return guarded([&]() -> int32_t {
+        MechEntry& me = mech(h);
+        requireMechDevice(me);
+        if (!out) throw std::runtime_error("null array argument");
+        int v[4] = {0, 0, 0, 0};
+        ck(cudaDeviceSynchronize(), "check status");
+        ck(cudaMemcpy(v, me.dChk.p, sizeof(v), cudaMemcpyDeviceToHost), "check status");
+        ck(cudaMemset(me.dChk.p, 0, sizeof(v)), "check status");
+        out[0] = v[0]; out[1] = v[1]; out[2] = v[2];
+#ifdef GBCHEM_CHECKED
+        return 1;
+#else
+        return 0;
+#endif
     });
 }
 

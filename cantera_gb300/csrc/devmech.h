@@ -113,7 +113,42 @@ struct DevMech {
     // jcPtr/jrIdx, or -1
     const int* colSlotStart;     // [K+1]
     const int* colSlot;
+    // bounds-check record of the checked build (GBCHEM_CHECKED): first failing site, its
+    // index, its bound; written only by the checked build's kernels
+    int* chk;
 };
+
+// Bounds-checked build.  Every index that comes from the mechanism's tables (species,
+// reactions, third bodies, falloff records, gather tasks, Jacobian columns and slots) or
+// from a queue passes through GB_IX(m, i, n, site).  In the normal build that is just i.
+// With GBCHEM_CHECKED an index outside [0, n) records (site, i, n) in m.chk (the first
+// violation wins) and is replaced by 0, so that the access itself stays in bounds and the
+// kernel runs on; the host reads the record with gb_check_status.
+#if defined(__CUDACC__) && defined(GBCHEM_CHECKED)
+__device__ __forceinline__ int gbCheckIx(const DevMech& m, long long i, long long n, int site) {
+    if ((unsigned long long)i < (unsigned long long)n) return (int)i;
+    if (m.chk && atomicCAS(m.chk, 0, site) == 0) {
+        m.chk[1] = (int)i;
+        m.chk[2] = (int)n;
+    }
+    return 0;
+}
+// the used fields (the first min(w, 3)) of an expanded species list
+__device__ __forceinline__ int4 gbCheckIx4(const DevMech& m, int4 e, int n, int site) {
+    if (e.w > 0) e.x = gbCheckIx(m, e.x, n, site);
+    if (e.w > 1) e.y = gbCheckIx(m, e.y, n, site);
+    if (e.w > 2) e.z = gbCheckIx(m, e.z, n, site);
+    return e;
+}
+#define GB_IX(m, i, n, site) gbCheckIx((m), (i), (n), (site))
+#define GB_IX4(m, e, n, site) gbCheckIx4((m), (e), (n), (site))
+#else
+#define GB_IX(m, i, n, site) (i)
+#define GB_IX4(m, e, n, site) (e)
+#endif
+enum { GB_SITE_SPECIES = 1, GB_SITE_SIDE = 2, GB_SITE_TB_SPECIES = 3, GB_SITE_TB = 4, GB_SITE_FALLOFF = 5,
+       GB_SITE_GATHER_RXN = 6, GB_SITE_TASK = 7, GB_SITE_COLUMN = 8, GB_SITE_COL_RXN = 9, GB_SITE_SLOT = 10,
+       GB_SITE_NET_SPECIES = 11, GB_SITE_DENSE_TB = 12, GB_SITE_PATTERN_ROW = 13, GB_SITE_QUEUE = 14 };
 
 // every array of a DevMech
 #define GB_DEVMECH_ARRAYS(X) \

@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
                     __syncwarp();
                     warpJacSparse(m, s, Js, lane);
                     warpDenseG(m, s, gk, lane);
-                    for (int q = lane; q < m.nnz; q += 32) Js[q] = Js[q] + gk[m.jrIdx[q]];
+                    for (int q = lane; q < m.nnz; q += 32) Js[q] = Js[q] + gk[GB_IX(m, m.jrIdx[q], K, GB_SITE_PATTERN_ROW)];
                 }
                 __syncwarp();
             }
@@ -1115,7 +1115,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
         if (lane == 0) idx = atomicAdd(p.counter, 1);
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= p.n) break;
-        const int r = p.order ? p.order[idx] : idx;
+        const int r = p.order ? GB_IX(m, p.order[idx], p.n, GB_SITE_QUEUE) : idx;
         double* rec = p.rec + (size_t)r * p.recStride;
         const double* rs = rec + (QMAX + 1) * N;
         long long* stt = p.stats + (size_t)r * 8;

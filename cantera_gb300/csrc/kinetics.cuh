@@ -117,7 +117,7 @@ __device__ __forceinline__ double massAction(const DevMech& m, int bucket, int4 
     for (int q = m.sidePtr[side]; q < m.sidePtr[side + 1]; q++) {
         double o = m.sideOrd[q];
         if (o != 0.0) {
-            double x = c[m.sideK[q]];
+            double x = c[GB_IX(m, m.sideK[q], m.K, GB_SITE_SIDE)];
             if (!(x > 0.0)) return 0.0;
             // pow(x, 1) = x and pow(x, 2) = x*x up to rounding
             r *= (o == 1.0) ? x : ((o == 2.0) ? x * x : pow(x, o));
@@ -155,7 +155,7 @@ __device__ __forceinline__ double massActionDeriv(const DevMech& m, int bucket, 
 #pragma unroll 1
         for (int p = q0; p < q1; p++) {
             if (p == q) continue;
-            double y = c[m.sideK[p]];
+            double y = c[GB_IX(m, m.sideK[p], m.K, GB_SITE_SIDE)];
             if (y > 0) prod *= pow(y, m.sideOrd[p]);
             else { prod = 0.0; break; }
         }
@@ -421,7 +421,7 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
     for (int t = lane; t < m.NTB; t += 32) {
         double sum = 0.0;
 #pragma unroll 1
-        for (int q = m.tbPtr[t]; q < m.tbPtr[t + 1]; q++) sum += m.tbE[q] * s.c[m.tbK[q]];
+        for (int q = m.tbPtr[t]; q < m.tbPtr[t + 1]; q++) sum += m.tbE[q] * s.c[GB_IX(m, m.tbK[q], m.K, GB_SITE_TB_SPECIES)];
         s.Mtb[t] = m.tbDef[t] * st.ctot + sum;
     }
     __syncwarp();
@@ -433,9 +433,15 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
     if (lane < m.R) { nInfo = m.rinfo[lane]; nAr = m.rarr[lane]; nRe = m.rk[lane]; nPe = m.pk[lane]; }
 #pragma unroll 1
     for (int i = lane; i < m.R; i += 32) {
+#ifdef GBCHEM_CHECKED
+        int4 info = nInfo;
+        if (info.y >= 0) info.y = GB_IX(m, info.y, m.NTB, GB_SITE_TB);
+        if (info.z >= 0) info.z = GB_IX(m, info.z, m.NF, GB_SITE_FALLOFF);
+#else
         const int4 info = nInfo;
+#endif
         const D4 ar = nAr;
-        const int4 re = nRe, pe = nPe;
+        const int4 re = GB_IX4(m, nRe, m.K, GB_SITE_SPECIES), pe = GB_IX4(m, nPe, m.K, GB_SITE_SPECIES);
         if (i + 32 < m.R) {
             nInfo = m.rinfo[i + 32]; nAr = m.rarr[i + 32]; nRe = m.rk[i + 32]; nPe = m.pk[i + 32];
         }
@@ -499,7 +505,7 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
                 if (pe.w > 2) dG += s.g[pe.z];
             } else {
 #pragma unroll 1
-                for (int q = m.sidePtr[2 * i + 1]; q < m.sidePtr[2 * i + 2]; q++) dG += m.sideNu[q] * s.g[m.sideK[q]];
+                for (int q = m.sidePtr[2 * i + 1]; q < m.sidePtr[2 * i + 2]; q++) dG += m.sideNu[q] * s.g[GB_IX(m, m.sideK[q], m.K, GB_SITE_SIDE)];
             }
             double dr = 0.0;
             if (rb != 0) {
@@ -508,7 +514,7 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
                 if (re.w > 2) dr += s.g[re.z];
             } else {
 #pragma unroll 1
-                for (int q = m.sidePtr[2 * i]; q < m.sidePtr[2 * i + 1]; q++) dr += m.sideNu[q] * s.g[m.sideK[q]];
+                for (int q = m.sidePtr[2 * i]; q < m.sidePtr[2 * i + 1]; q++) dr += m.sideNu[q] * s.g[GB_IX(m, m.sideK[q], m.K, GB_SITE_SIDE)];
             }
             dG -= dr;
             rkc = fmin(fexp(dG - ar.w * logStandConc, s.tab), 1e300);
@@ -529,10 +535,10 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
     // wdot_k = sum_i nu_ki rop_i: balanced tasks, then a fixed-order sum per species
 #pragma unroll 1
     for (int q = m.laneTaskPtr[lane]; q < m.laneTaskPtr[lane + 1]; q++) {
-        const int t = m.laneTasks[q];
+        const int t = GB_IX(m, m.laneTasks[q], m.NT, GB_SITE_TASK);
         double w = 0.0;
 #pragma unroll 1
-        for (int e = m.taskPtr[t]; e < m.taskPtr[t + 1]; e++) w = fma(m.spNu[e], s.rop[m.spRxn[e]], w);
+        for (int e = m.taskPtr[t]; e < m.taskPtr[t + 1]; e++) w = fma(m.spNu[e], s.rop[GB_IX(m, m.spRxn[e], m.R, GB_SITE_GATHER_RXN)], w);
         s.part[t] = w;
     }
     __syncwarp();
@@ -540,7 +546,7 @@ __device__ __noinline__ void warpRates(const DevMech& m, KinScratch& s, const Ki
     for (int k = lane; k < m.K; k += 32) {
         double w = 0.0;
 #pragma unroll 1
-        for (int q = m.spTaskPtr[k]; q < m.spTaskPtr[k + 1]; q++) w += s.part[m.spTasks[q]];
+        for (int q = m.spTaskPtr[k]; q < m.spTaskPtr[k + 1]; q++) w += s.part[GB_IX(m, m.spTasks[q], m.NT, GB_SITE_TASK)];
         s.wdot[k] = w;
     }
     __syncwarp();
@@ -554,15 +560,15 @@ template <typename MT, bool kT>
 __device__ __noinline__ void warpJacC(const DevMech& m, const KinScratch& s, MT* Jc, int ld, int lane) {
 #pragma unroll 1
     for (int q = m.laneColPtr[lane]; q < m.laneColPtr[lane + 1]; q++) {
-        const int j = m.laneCols[q];
+        const int j = GB_IX(m, m.laneCols[q], m.K, GB_SITE_COLUMN);
         const int e0 = m.colPtr[j], e1 = m.colPtr[j + 1];
         // the next entry's reaction data are loaded one iteration ahead
         int iN = 0, rs0N = 0, rs1N = 0;
         int4 infoN = make_int4(0, 0, 0, 0), rkN = infoN, pkN = infoN;
         double epN = 0.0;
         if (e0 < e1) {
-            iN = m.colRxn[e0];
-            infoN = m.rinfo[iN]; rkN = m.rk[iN]; pkN = m.pk[iN]; epN = m.colE[e0];
+            iN = GB_IX(m, m.colRxn[e0], m.R, GB_SITE_COL_RXN);
+            infoN = m.rinfo[iN]; rkN = GB_IX4(m, m.rk[iN], m.K, GB_SITE_SPECIES); pkN = GB_IX4(m, m.pk[iN], m.K, GB_SITE_SPECIES); epN = m.colE[e0];
             rs0N = m.rsPtr[iN]; rs1N = m.rsPtr[iN + 1];
         }
 #pragma unroll 1
@@ -571,19 +577,20 @@ __device__ __noinline__ void warpJacC(const DevMech& m, const KinScratch& s, MT*
             const int4 info = infoN, rki = rkN, pki = pkN;
             const double ep = epN;
             if (e + 1 < e1) {
-                iN = m.colRxn[e + 1];
-                infoN = m.rinfo[iN]; rkN = m.rk[iN]; pkN = m.pk[iN]; epN = m.colE[e + 1];
+                iN = GB_IX(m, m.colRxn[e + 1], m.R, GB_SITE_COL_RXN);
+                infoN = m.rinfo[iN]; rkN = GB_IX4(m, m.rk[iN], m.K, GB_SITE_SPECIES); pkN = GB_IX4(m, m.pk[iN], m.K, GB_SITE_SPECIES); epN = m.colE[e + 1];
                 rs0N = m.rsPtr[iN]; rs1N = m.rsPtr[iN + 1];
             }
             const int rb = (info.x >> kRBucketShift) & 7, pb = (info.x >> kPBucketShift) & 7;
             const double kfe = s.kfe[i];
             double dF = kfe * massActionDeriv(m, rb, rki, 2 * i, s.c, j);
             if (info.x & kRevBit) dF -= (kfe * s.rkc[i]) * massActionDeriv(m, pb, pki, 2 * i + 1, s.c, j);
-            if (ep != 0.0) dF += ep * s.Qtb[info.y];
+            if (ep != 0.0) dF += ep * s.Qtb[GB_IX(m, info.y, m.NTB, GB_SITE_TB)];
             if (dF == 0.0) continue;
 #pragma unroll 1
             for (int r = rs0; r < rs1; r++) {
-                MT* p = kT ? Jc + (size_t)j * ld + m.rsK[r] : Jc + (size_t)m.rsK[r] * ld + j;
+                const int kr = GB_IX(m, m.rsK[r], m.K, GB_SITE_NET_SPECIES);
+                MT* p = kT ? Jc + (size_t)j * ld + kr : Jc + (size_t)kr * ld + j;
                 *p = (MT)((double)*p + m.rsNu[r] * dF);
             }
         }
@@ -597,15 +604,15 @@ __device__ __noinline__ void warpJacC(const DevMech& m, const KinScratch& s, MT*
 GB_TU_LOCAL __device__ __noinline__ void warpJacSparse(const DevMech& m, const KinScratch& s, double* Js, int lane) {
 #pragma unroll 1
     for (int q = m.laneColPtr[lane]; q < m.laneColPtr[lane + 1]; q++) {
-        const int j = m.laneCols[q];
+        const int j = GB_IX(m, m.laneCols[q], m.K, GB_SITE_COLUMN);
         const int e0 = m.colPtr[j], e1 = m.colPtr[j + 1];
         int slot = m.colSlotStart[j];
         int iN = 0, rs0N = 0, rs1N = 0;
         int4 infoN = make_int4(0, 0, 0, 0), rkN = infoN, pkN = infoN;
         double epN = 0.0;
         if (e0 < e1) {
-            iN = m.colRxn[e0];
-            infoN = m.rinfo[iN]; rkN = m.rk[iN]; pkN = m.pk[iN]; epN = m.colE[e0];
+            iN = GB_IX(m, m.colRxn[e0], m.R, GB_SITE_COL_RXN);
+            infoN = m.rinfo[iN]; rkN = GB_IX4(m, m.rk[iN], m.K, GB_SITE_SPECIES); pkN = GB_IX4(m, m.pk[iN], m.K, GB_SITE_SPECIES); epN = m.colE[e0];
             rs0N = m.rsPtr[iN]; rs1N = m.rsPtr[iN + 1];
         }
 #pragma unroll 1
@@ -614,15 +621,15 @@ GB_TU_LOCAL __device__ __noinline__ void warpJacSparse(const DevMech& m, const K
             const int4 info = infoN, rki = rkN, pki = pkN;
             const double ep = epN;
             if (e + 1 < e1) {
-                iN = m.colRxn[e + 1];
-                infoN = m.rinfo[iN]; rkN = m.rk[iN]; pkN = m.pk[iN]; epN = m.colE[e + 1];
+                iN = GB_IX(m, m.colRxn[e + 1], m.R, GB_SITE_COL_RXN);
+                infoN = m.rinfo[iN]; rkN = GB_IX4(m, m.rk[iN], m.K, GB_SITE_SPECIES); pkN = GB_IX4(m, m.pk[iN], m.K, GB_SITE_SPECIES); epN = m.colE[e + 1];
                 rs0N = m.rsPtr[iN]; rs1N = m.rsPtr[iN + 1];
             }
             const int rb = (info.x >> kRBucketShift) & 7, pb = (info.x >> kPBucketShift) & 7;
             const double kfe = s.kfe[i];
             double dF = kfe * massActionDeriv(m, rb, rki, 2 * i, s.c, j);
             if (info.x & kRevBit) dF -= (kfe * s.rkc[i]) * massActionDeriv(m, pb, pki, 2 * i + 1, s.c, j);
-            if (ep != 0.0) dF += ep * s.Qtb[info.y];
+            if (ep != 0.0) dF += ep * s.Qtb[GB_IX(m, info.y, m.NTB, GB_SITE_TB)];
             if (dF == 0.0) {
                 slot += rs1 - rs0;
                 continue;
@@ -630,7 +637,10 @@ GB_TU_LOCAL __device__ __noinline__ void warpJacSparse(const DevMech& m, const K
 #pragma unroll 1
             for (int r = rs0; r < rs1; r++, slot++) {
                 const int t = m.colSlot[slot];
-                if (t >= 0) Js[t] = Js[t] + m.rsNu[r] * dF;
+                if (t >= 0) {
+                    const int tt = GB_IX(m, t, m.nnz, GB_SITE_SLOT);
+                    Js[tt] = Js[tt] + m.rsNu[r] * dF;
+                }
             }
         }
     }
@@ -644,7 +654,7 @@ __device__ __forceinline__ void warpDenseG(const DevMech& m, const KinScratch& s
     for (int k = lane; k < m.K; k += 32) {
         double g = 0.0;
 #pragma unroll 1
-        for (int q = m.gsPtr[k]; q < m.gsPtr[k + 1]; q++) g += m.gsCoef[q] * s.Qtb[m.gsTb[q]];
+        for (int q = m.gsPtr[k]; q < m.gsPtr[k + 1]; q++) g += m.gsCoef[q] * s.Qtb[GB_IX(m, m.gsTb[q], m.NTB, GB_SITE_DENSE_TB)];
         gout[k] = g;
     }
     __syncwarp();

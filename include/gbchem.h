@@ -278,6 +278,16 @@ int32_t gb_check_exp(int32_t n, const double* x, double* out_engine, double* out
 /* The same for the engine's logarithm against the CUDA library log. */
 int32_t gb_check_log(int32_t n, const double* x, double* out_engine, double* out_library);
 
+/* Bounds checks (no counterpart in the reference): a library built with GBCHEM_CHECKED
+ * (python -c "from cantera_gb300 import build; build.build(checked=True)", loaded with
+ * GBCHEM_CHECKED=1) checks every index its kernels take from the mechanism's tables or
+ * queues; an index out of range is recorded and replaced by 0, so the kernel stays in
+ * bounds.  out[0..2] = the first failing check site (0: none), its index and its bound,
+ * for the kernels run on this mechanism since the last call (the record is then cleared).
+ * Returns 1 for a checked build, 0 for the normal one (whose kernels record nothing), or
+ * GB_ERR. */
+int32_t gb_check_status(int32_t mech, int32_t* out);
+
 /* Copy the most recent error message (thread-local) into buf; returns its length. */
 int32_t gb_get_error(int32_t buflen, char* buf);
 
