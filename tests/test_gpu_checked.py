@@ -15,7 +15,7 @@ from conftest import DATA, MECHS, ROOT, gpu_solution, random_states
 pytestmark = pytest.mark.gpu
 
 SCRIPT = r'''
-import os, sys
+import ctypes, os, sys
 import numpy as np
 sys.path.insert(0, {root!r})
 sys.path.insert(0, os.path.join({root!r}, "tests"))
@@ -45,7 +45,7 @@ for name in ("gri30", "nDodecane", "pdep"):
         T1, Y1 = net.get_state()
         out["%s_T%d" % (name, lu)], out["%s_Y%d" % (name, lu)] = T1, Y1
     st = np.zeros(3, dtype=np.int32)
-    rc = L.gb_check_status(sol._h, st.ctypes.data_as(gb.ctypes.c_void_p) if hasattr(gb, "ctypes") else None)
+    rc = L.gb_check_status(sol._h, st.ctypes.data_as(ctypes.c_void_p))
     out[name + "_chk"] = np.array([rc] + st.tolist())
 np.savez({out!r}, **out)
 '''
@@ -81,8 +81,7 @@ def test_checked_build_records_nothing_and_changes_nothing(tmp_path):
     build.build(checked=True)
     out = str(tmp_path / "checked.npz")
     script = tmp_path / "run_checked.py"
-    script.write_text("import ctypes\n" + SCRIPT.format(root=ROOT, out=out).replace(
-        'st.ctypes.data_as(gb.ctypes.c_void_p) if hasattr(gb, "ctypes") else None', "st.ctypes.data_as(ctypes.c_void_p)"))
+    script.write_text(SCRIPT.format(root=ROOT, out=out))
     env = dict(os.environ, GBCHEM_CHECKED="1")
     env.pop("GBCHEM_LIB", None)
     r = subprocess.run([sys.executable, str(script)], env=env, capture_output=True, text=True, timeout=900)
