@@ -19,7 +19,7 @@ and `error_protocol` (against the oracle configured as the reference's ReactorNe
 against its tight run at rtol 1e-12, atol 1e-20, with ignition delays).
 
 Usage:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-        python bench.py --workload rates|ndodecane|h2o2      (one workload's line alone)
+        python bench.py --workload rates|ndodecane|h2o2|gemm (one workload's line alone)
 Under torchrun each rank takes a contiguous shard of the reactors (no collective on the
 data path); the time is the maximum over ranks.
 """
@@ -543,8 +543,19 @@ def run_workload(args):
     torch.cuda.set_device(0)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     threads = os.cpu_count()
-    fn = {"rates": lambda: variant_rates(dev, torch, flush, threads, peaks=measured_peaks()),
-          "ndodecane": lambda: variant_ndodecane(dev, torch, flush, threads),
+    if args.workload == "gemm":
+        import cantera_gb300 as gb
+        from cantera_gb300.surrogate import Surrogate
+        sur = Surrogate(gb.Solution("gri30.yaml", "gri30"), hidden=SUR["hidden"], layers=SUR["layers"], seed=0,
+                        device=str(dev))
+        line = dict(workload="gemm", n_gpus=1, dtype="bf16", data="synthetic", higher_is_better=True)
+        line.update(gemm_roofline(sur, torch, M=args.n if args.n != WL["n"] else 65536))
+        print(json.dumps(line))
+        return
+    custom = args.n != WL["n"]
+    fn = {"rates": lambda: variant_rates(dev, torch, flush, threads, n=args.n if custom else 1 << 20,
+                                         peaks=measured_peaks()),
+          "ndodecane": lambda: variant_ndodecane(dev, torch, flush, threads, n=args.n if custom else 16384),
           "h2o2": lambda: variant_h2o2(dev, torch, flush, threads)}[args.workload]
     line = dict(workload=args.workload, n_gpus=1, dtype="f64", data="synthetic", higher_is_better=True)
     line.update(fn())
@@ -601,7 +612,7 @@ def main():
                     help="skip the launch-shape autotuner (use the engine's rule)")
     ap.add_argument("--lu-staging", type=int, default=0,
                     help="shared-memory factorisation buffers per block: -1 none, 0 automatic, k at most k")
-    ap.add_argument("--workload", default="uneven", choices=["uneven", "rates", "ndodecane", "h2o2"],
+    ap.add_argument("--workload", default="uneven", choices=["uneven", "rates", "ndodecane", "h2o2", "gemm"],
                     help="uneven: the headline workload; the others print their own measurement line")
     ap.add_argument("--matrix-placement", type=int, default=0, choices=[0, 1, 2],
                     help="Newton matrix: 0 automatic, 1 shared memory, 2 global slot per warp")
