@@ -161,18 +161,23 @@ def algorithmic_flops(stats, fm, fp32_lu):
     return float(f64), float(f32)
 
 
-def read_traffic():
-    """DRAM bytes per launch of the integrator kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_bdf_gri30_uneven.md")
+def read_profile_value(key, name="k_bdf_gri30_uneven.md"):
+    """A `key: value ...` figure of a committed ncu summary (None if absent)."""
+    path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith("traffic_bytes_per_launch:"):
+        if line.startswith(key + ":"):
             try:
                 return float(line.split(":")[1].split()[0])
             except (IndexError, ValueError):
                 return None
     return None
+
+
+def read_traffic():
+    """DRAM bytes per launch of the integrator kernel from the committed ncu summary."""
+    return read_profile_value("traffic_bytes_per_launch")
 
 
 SUR = dict(dt=1e-6, train_reactors=65536, held_reactors=65536, hidden=512, layers=4, epochs=6, batch=16384,
@@ -753,6 +758,11 @@ def main():
                          "peak_source": "FP64 FMA rate measured live by this run (MEASURED_PEAKS.json has no FP64 figure)",
                          "flops_per_reactor": fpr, "kernel_ms_mean": kernel_s * 1e3,
                          "ceiling_reactors_per_s": peak * 1e12 / fpr,
+                         # FP64 pipe work counted by ncu (DFMA x 2 + DADD + DMUL thread instructions
+                         # per cycle over all SMs) at this run's SM clock: the FP64 arithmetic the
+                         # kernel issues, beside the algorithm's operation model above
+                         "ncu_fp64_tflops": (read_profile_value("fp64_flops_per_cycle") or 0.0) *
+                                            (r64["clocks"].get("sm_mhz") or 0.0) * 1e6 / 1e12 or None,
                          "exp_fma_declared": EXP_FMA, "log_fma_declared": LOG_FMA,
                          "exp_fma_measured": fp["exp_fma"], "log_fma_measured": fp["log_fma"]},
             "clocks": r64["clocks"], "gpu_launches": args.steps,
