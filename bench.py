@@ -294,12 +294,14 @@ def gemm_roofline(sur, torch, M=65536):
     flops = 2.0 * M * hid * hid
     peaks = measured_peaks()
     peak = peaks.get("bf16_tflops")
+    source = "MEASURED_PEAKS.json bf16_tflops (burst)"
+    if not peak:
+        peak, source = 1900.0, "fallback: 1.9 PFLOP/s dense BF16 burst, an earlier measurement on a GB300"
     tf = flops / (ms / 1e3) / 1e12
     # bytes: X, W in; C (bf16) and Z (fp32) out
     byt = M * hid * 2 + hid * hid * 2 + M * hid * (2 + 4)
     return {"shape": [M, hid, hid], "ms": ms, "tflops": tf, "peak_tflops": peak,
-            "frac": tf / peak if peak else None, "hbm_gbs": byt / (ms / 1e3) / 1e9,
-            "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peak else None,
+            "frac": tf / peak, "hbm_gbs": byt / (ms / 1e3) / 1e9, "peak_source": source,
             "kernel": "k_umma_gemm (tcgen05.mma kind::f16, TMEM accumulator, TMA 128B-swizzled operands)"}
 
 
@@ -335,6 +337,21 @@ def settled_mask(m, P, Tt, Yt, t_end, rtol):
     return np.abs(dTdt) * 1e-4 * t_end < 10 * rtol * Tt
 
 
+def tight_run(m, po, T0, P, Y0, t_end, threads):
+    """The tight solution: the reference's method at rtol 1e-12, atol 1e-20; a reactor whose
+    run stops (the difference-quotient Jacobian can stall at the 1000 K midpoint of the NASA7
+    fits at this tolerance) is re-run with the analytic Jacobian.  Returns T, Y, stats,
+    ignition times, the re-run count and the mask of reactors still without a solution."""
+    Tt, Yt, stt, tit = m.advance_batch(T0, P, Y0, t_end, oracle_opts(po, 0, 0, tight=True), threads=threads)
+    bad = stt[:, 8] != 0
+    rerun = int(bad.sum())
+    if rerun:
+        o = po.opts(rtol=TIGHT["rtol"], atol=TIGHT["atol"], analytic=True)
+        T2, Y2, st2, ti2 = m.advance_batch(T0[bad], P[bad], Y0[bad], t_end, o, threads=threads)
+        Tt[bad], Yt[bad], stt[bad], tit[bad] = T2, Y2, st2, ti2
+    return Tt, Yt, stt, tit, rerun, stt[:, 8] != 0
+
+
 def error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, gpu, threads):
     """Error protocol of the integrator workloads on one sample: (i) against the CPU oracle
     configured as the reference's ReactorNet at the same tolerances, (ii) against a tight
@@ -343,29 +360,35 @@ def error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, gpu, threads):
     reactor.  gpu: {variant: (T [n], Y [n][K], tign [n])} on the same sample."""
     t0 = time.perf_counter()
     To, Yo, sto, tio = m.advance_batch(T0, P, Y0, t_end, oracle_opts(po, rtol, atol), threads=threads)
-    Tt, Yt, stt, tit = m.advance_batch(T0, P, Y0, t_end, oracle_opts(po, rtol, atol, tight=True), threads=threads)
+    Tt, Yt, stt, tit, rerun, tfail = tight_run(m, po, T0, P, Y0, t_end, threads)
     secs = time.perf_counter() - t0
-    settled = settled_mask(m, P, Tt, Yt, t_end, rtol)
-    ign = (Tt > T0 + 400.0) & (tit > 0) & (tit < t_end)
+    use = (sto[:, 8] == 0) & ~tfail           # reactors with both oracle solutions
+    settled = settled_mask(m, P, Tt, Yt, t_end, rtol) & use
+    ign = (Tt > T0 + 400.0) & (tit > 0) & (tit < t_end) & use
     bar = 10 * rtol
-    out = {"reactors": int(len(T0)), "igniting": int(ign.sum()), "settled": int(settled.sum()),
-           "bar_10rtol": bar, "tight": dict(TIGHT), "oracle_seconds": secs,
-           "oracle_vs_tight": {"all": state_errors(To, Yo, Tt, Yt),
-                               "settled": state_errors(To[settled], Yo[settled], Tt[settled], Yt[settled])},
-           "oracle_failed": int(np.sum(sto[:, 8] != 0) + np.sum(stt[:, 8] != 0))}
+    out = {"reactors": int(len(T0)), "compared": int(use.sum()), "igniting": int(ign.sum()),
+           "settled": int(settled.sum()), "bar_10rtol": bar, "tight": dict(TIGHT),
+           "tight_rerun_with_analytic_jacobian": rerun, "tight_failed": int(tfail.sum()),
+           "oracle_failed": int(np.sum(sto[:, 8] != 0)), "oracle_seconds": secs,
+           "oracle_vs_tight": {"all": state_errors(To[use], Yo[use], Tt[use], Yt[use]),
+                               "settled": state_errors(To[settled], Yo[settled], Tt[settled], Yt[settled])}}
     if ign.any():
         out["oracle_vs_tight"]["ignition_delay_max_rel"] = float(np.max(np.abs(tio[ign] - tit[ign]) / tit[ign]))
     for name, (Tg, Yg, tg) in gpu.items():
-        e = {"vs_tight": {"all": state_errors(Tg, Yg, Tt, Yt),
+        e = {"vs_tight": {"all": state_errors(Tg[use], Yg[use], Tt[use], Yt[use]),
                           "settled": state_errors(Tg[settled], Yg[settled], Tt[settled], Yt[settled])},
-             "vs_oracle": state_errors(Tg, Yg, To, Yo)}
+             "vs_oracle": state_errors(Tg[use], Yg[use], To[use], Yo[use])}
         if ign.any():
             e["ignition_delay_max_rel_vs_oracle"] = float(np.max(np.abs(tg[ign] - tio[ign]) / tio[ign]))
             e["ignition_delay_max_rel_vs_tight"] = float(np.max(np.abs(tg[ign] - tit[ign]) / tit[ign]))
         a, o_ = e["vs_tight"]["all"], out["oracle_vs_tight"]["all"]
+        # two correct integrations at the same tolerance differ in their error by O(1)
+        # factors (different Jacobians, different steps): the ratio of the GPU's error to the
+        # reference configuration's own, and the 3x bar the tests hold
+        e["T_error_ratio_to_oracle"] = a["T_max_rel"] / max(o_["T_max_rel"], 1e-300)
         e["T_within_bar"] = a["T_max_rel"] <= bar
-        e["T_within_oracle_error"] = a["T_max_rel"] <= max(bar, o_["T_max_rel"])
-        e["major_species_within_oracle_error"] = a["major_species_max_rel"] <= max(bar, o_["major_species_max_rel"])
+        e["T_within_3x_oracle_error"] = a["T_max_rel"] <= max(bar, 3 * o_["T_max_rel"])
+        e["major_species_within_3x_oracle_error"] = a["major_species_max_rel"] <= max(bar, 3 * o_["major_species_max_rel"])
         e["settled_T_within_bar"] = e["vs_tight"]["settled"]["T_max_rel"] <= bar
         if ign.any():
             e["ignition_within_1e-3"] = e["ignition_delay_max_rel_vs_oracle"] <= 1e-3
@@ -485,12 +508,14 @@ def variant_rates(dev, torch, flush, threads, n=1 << 20, peaks=None):
                    pattern=(sol.jac_colptr, sol.jac_rowidx), threads=threads)
     cpu_j = ns / (time.perf_counter() - t0)
     hbm = (peaks or {}).get("hbm_gbs")
+    hbm_source = "MEASURED_PEAKS.json hbm_gbs"
+    if not hbm:
+        hbm, hbm_source = 6800.0, "fallback: 6.8 TB/s, an earlier copy measurement on a GB300"
     return {"value": out["wdot"]["states_per_s"], "unit": "states/s", "modes": out,
             "config": {"workload": "gri30, %d states, T U[300,3000] K, P log-U[0.1,100] atm, Y Dirichlet(0.5)" % n,
                        "seed": 20261204, "l2": "flushed (256 MB write) before every timed call"},
-            "hbm_roofline": {"peak_gbs": hbm, "frac_wdot": out["wdot"]["hbm_gbs"] / hbm if hbm else None,
-                             "frac_jacobian": out["wdot+jacobian"]["hbm_gbs"] / hbm if hbm else None,
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else None},
+            "hbm_roofline": {"peak_gbs": hbm, "frac_wdot": out["wdot"]["hbm_gbs"] / hbm,
+                             "frac_jacobian": out["wdot+jacobian"]["hbm_gbs"] / hbm, "peak_source": hbm_source},
             "parity_vs_oracle": parity,
             "cpu_baseline": {"value": cpu_w, "unit": "states/s (wdot)", "value_jacobian": cpu_j, "cores": threads,
                              "kind": "port", "sample": "%d of the states, oracle restatement built with %s"

@@ -525,8 +525,9 @@ int32_t runRates(int32_t h, int32_t n, const double* T, const double* P, const d
     if (budget - p.mechSmem < p.warpDoubles * 8) throw std::runtime_error("mechanism too large for the rates kernel's shared memory");
     const int perBlock = p.mechSmem + ratesTileDoubles(e.dm) * 8 + p.warpDoubles * 8 * wpb + 1024;
     int blocksPerSm = std::max(1, (228 * 1024) / perBlock);
-    const int tiles = (int)(((long long)n + kRatesTile - 1) / kRatesTile);
-    int blocks = std::min(e.smCount * blocksPerSm, tiles);
+    // wdot alone: a tile of 32 states per block at a time; with the Jacobian: a state per warp
+    const long long units = dJ ? ((long long)n + wpb - 1) / wpb : ((long long)n + kRatesTile - 1) / kRatesTile;
+    int blocks = (int)std::min<long long>((long long)e.smCount * blocksPerSm, units);
     if (!e.evA) {
         ck(cudaEventCreate(&e.evA), "event");
         ck(cudaEventCreate(&e.evB), "event");

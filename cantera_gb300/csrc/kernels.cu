@@ -23,11 +23,10 @@ namespace gbchem {
 // T, P and Y[K] rows are loaded into shared memory with one coalesced 256-byte request per
 // row (lanes across states); each warp then evaluates whole states (lanes across species,
 // reactions and Jacobian columns) and writes wdot back into its state's column of the
-// tile, which the block stores with coalesced rows.  d(wdot)/dc is accumulated per warp
-// directly on the output pattern (nnz doubles) and written by the whole block for W
-// consecutive states at a time, so that each pattern slot is one contiguous run of W
-// doubles in the [nnz][n] output.  The mechanism prefix the call reads is staged into
-// shared memory by the bulk-copy engine.
+// tile, which the block stores with coalesced rows.  With d(wdot)/dc (several times the work
+// of a state's wdot) warps take single states instead, and the Jacobian is accumulated per
+// warp directly on the output pattern (nnz doubles: no dense K x K scratch, no gather).  The
+// mechanism prefix the call reads is staged into shared memory by the bulk-copy engine.
 template <bool kX>
 __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
     extern __shared__ __align__(128) double smem[];
@@ -57,6 +56,36 @@ __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
     double* Js = gk + K;                      // [nnz] this warp's d(wdot)/dc on the pattern
     const bool jac = p.jac != nullptr;
     KinState st;
+    if (jac) {
+        // d(wdot)/dc: a state costs several wdot evaluations, so keeping every warp busy
+        // matters more than coalesced input rows: each warp takes single states from the
+        // counter and writes its state's wdot and pattern values itself (the warps of a block
+        // work on neighbouring states at the same time, so a slot's neighbouring values merge
+        // in L2 before they are written back)
+        for (;;) {
+            int idx = 0;
+            if (lane == 0) idx = atomicAdd(p.counter, 1);
+            idx = __shfl_sync(0xffffffffu, idx, 0);
+            if (idx >= n) break;
+            for (int k = lane; k < K; k += 32) Yl[k] = p.Y[(size_t)k * n + idx];
+            const double T = p.T[idx], P = p.P[idx];
+            __syncwarp();
+            warpState(m, T, P, Yl, s, st, lane);
+            __syncwarp();
+            warpRates<kX>(m, s, st, lane, true);
+            if (p.wdot)
+                for (int k = lane; k < K; k += 32) p.wdot[(size_t)k * n + idx] = s.wdot[k];
+            for (int q = lane; q < m.nnz; q += 32) Js[q] = 0.0;
+            __syncwarp();
+            warpJacSparse(m, s, Js, lane);
+            warpDenseG(m, s, gk, lane);
+            double* out = p.jac + idx;
+            for (int q = lane; q < m.nnz; q += 32)
+                out[(size_t)q * n] = Js[q] + gk[GB_IX(m, m.jrIdx[q], K, GB_SITE_PATTERN_ROW)];
+            __syncwarp();
+        }
+        return;
+    }
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(p.counter, 1);
         __syncthreads();
@@ -70,43 +99,17 @@ __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
             if (lane < ns) tile[r * LD + lane] = src[s0 + lane];
         }
         __syncthreads();
-        // jac: rounds of W states, warp w on state round + w; else warp w on states w, w+W, ...
+        // warp w on states w, w+W, ... of the tile
 #pragma unroll 1
-        for (int r0 = 0; r0 < ns; r0 += (jac ? W : ns)) {
-#pragma unroll 1
-            for (int j = r0 + warp; j < (jac ? min(r0 + W, ns) : ns); j += W) {
-                for (int k = lane; k < K; k += 32) Yl[k] = tile[(2 + k) * LD + j];
-                const double T = tile[j], P = tile[LD + j];
-                __syncwarp();
-                warpState(m, T, P, Yl, s, st, lane);
-                __syncwarp();
-                warpRates<kX>(m, s, st, lane, jac);
-                for (int k = lane; k < K; k += 32) tile[(2 + k) * LD + j] = s.wdot[k];
-                if (jac) {
-                    for (int q = lane; q < m.nnz; q += 32) Js[q] = 0.0;
-                    __syncwarp();
-                    warpJacSparse(m, s, Js, lane);
-                    warpDenseG(m, s, gk, lane);
-                    for (int q = lane; q < m.nnz; q += 32) Js[q] = Js[q] + gk[GB_IX(m, m.jrIdx[q], K, GB_SITE_PATTERN_ROW)];
-                }
-                __syncwarp();
-            }
-            if (jac) {
-                // the block writes the round's states: slot q of state r0 + w is thread
-                // (q * W + w) of a sweep, so W consecutive states of a slot are contiguous
-                __syncthreads();
-                const int nr = min(W, ns - r0);
-                const int tot = m.nnz * W;
-#pragma unroll 1
-                for (int x = threadIdx.x; x < tot; x += blockDim.x) {
-                    const int q = x / W, w = x - q * W;
-                    if (w < nr) {
-                        const double* Jw = tile + ratesTileDoubles(m) + (size_t)w * p.warpDoubles + kinD + 2 * K;
-                        p.jac[(size_t)q * n + s0 + r0 + w] = Jw[q];
-                    }
-                }
-                __syncthreads();
-            }
+        for (int j = warp; j < ns; j += W) {
+            for (int k = lane; k < K; k += 32) Yl[k] = tile[(2 + k) * LD + j];
+            const double T = tile[j], P = tile[LD + j];
+            __syncwarp();
+            warpState(m, T, P, Yl, s, st, lane);
+            __syncwarp();
+            warpRates<kX>(m, s, st, lane, false);
+            for (int k = lane; k < K; k += 32) tile[(2 + k) * LD + j] = s.wdot[k];
+            __syncwarp();
         }
         __syncthreads();
         if (p.wdot) {

@@ -15,9 +15,9 @@ struct RatesParams {
     const double* Y;      // [K][n]
     double* wdot;         // [K][n] or null
     double* jac;          // [nnz][n] or null
-    int* counter;         // [2]: tile counter, then an error flag (both zeroed before launch;
-                          // the flag is set when a block's bulk copy of the mechanism did
-                          // not complete)
+    int* counter;         // [2]: tile (wdot) or state (Jacobian) counter, then an error
+                          // flag, both zeroed before launch (the flag is set when a block's
+                          // bulk copy of the mechanism did not complete)
     int warpDoubles;      // shared-memory doubles per warp
     int mechSmem;         // bytes of the mechanism arena copied into shared memory
 };

@@ -182,8 +182,13 @@ class Surrogate:
                 "actT": [torch.empty(d[l], M, dtype=bf, device=self.dev) for l in range(nl)],
                 "Z": [torch.empty(M, d[l + 1], device=self.dev) for l in range(nl - 1)],
                 "out": torch.empty(M, PAD_OUT, device=self.dev),
-                "dZ": [torch.empty(M, max(hid, PAD_OUT), dtype=bf, device=self.dev) for _ in range(2)],
-                "dZT": [torch.empty(max(hid, PAD_OUT), M, dtype=bf, device=self.dev) for _ in range(2)],
+                # output-layer gradient (contiguous [M][PAD_OUT]: the MSE kernel's row stride is
+                # that of the outputs) and the hidden layers' ping-pong gradients, each with its
+                # transposed copy
+                "dZo": torch.empty(M, PAD_OUT, dtype=bf, device=self.dev),
+                "dZoT": torch.empty(PAD_OUT, M, dtype=bf, device=self.dev),
+                "dZ": [torch.empty(M, hid, dtype=bf, device=self.dev) for _ in range(2)],
+                "dZT": [torch.empty(hid, M, dtype=bf, device=self.dev) for _ in range(2)],
                 "gW": [torch.empty_like(w) for w in self.W],
                 "gb": [torch.empty_like(b) for b in self.b],
                 "bb": [torch.empty(b.shape, dtype=bf, device=self.dev) for b in self.b],
@@ -199,8 +204,7 @@ class Surrogate:
         if n_real < M:
             out[n_real:] = 0.0
         nl = len(self.W)
-        dZ = buf["dZ"][0][:, :PAD_OUT]
-        dZT = buf["dZT"][0][:PAD_OUT]
+        dZ, dZT = buf["dZo"], buf["dZoT"]
         _check(L.gb_nn_mse(M, self.K + 1, PAD_OUT, _p(out), _p(buf["Y"]), _p(dZ), _p(buf["loss"])))
         self._transpose(dZ, dZT)
         scale = M / float(n_real)            # the loss is the mean over the n_real rows
@@ -212,8 +216,7 @@ class Surrogate:
             _check(L.gb_nn_colsum(M, n_out, _p(dZ), dZ.stride(0), scale, _p(buf["gb"][l])))
             if l > 0:
                 k = (nl - l) % 2
-                dprev = buf["dZ"][k][:, :n_in]
-                dprevT = buf["dZT"][k][:n_in]
+                dprev, dprevT = buf["dZ"][k], buf["dZT"][k]
                 # dZ_prev = (dZ W) * GELU'(Z_prev): (M x n_out)(n_out x n_in) with W^T K-major
                 self._tc(dZ, self.WbT[l], dprev, act=2, Z=buf["Z"][l - 1], CT=dprevT)
                 dZ, dZT = dprev, dprevT

@@ -30,13 +30,13 @@ def test_error_protocol_fields_and_self_consistency():
     # are zero and against the tight run equal the oracle's own
     To, Yo, _, tio = m.advance_batch(T0, P, Y0, t_end, bench.oracle_opts(po, rtol, atol), threads=2)
     e = bench.error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, {"same": (To, Yo, tio)}, threads=2)
-    assert e["reactors"] == len(T0) and e["oracle_failed"] == 0
+    assert e["reactors"] == len(T0) and e["oracle_failed"] == 0 and e["tight_failed"] == 0
     assert e["igniting"] > 0
     s = e["same"]
     assert s["vs_oracle"]["T_max_rel"] == 0.0 and s["vs_oracle"]["major_species_max_rel"] == 0.0
     assert s["ignition_delay_max_rel_vs_oracle"] == 0.0
     assert s["vs_tight"]["all"] == e["oracle_vs_tight"]["all"]
-    assert s["T_within_oracle_error"] and s["major_species_within_oracle_error"]
+    assert s["T_within_3x_oracle_error"] and s["major_species_within_3x_oracle_error"]
     # the tight run is closer to the truth than rtol 1e-8: the oracle's own error is small
     assert e["oracle_vs_tight"]["all"]["T_max_rel"] < 1e-5
 
@@ -46,7 +46,7 @@ def test_error_protocol_flags_a_shifted_result():
     t_end, rtol, atol = 1e-3, 1e-8, 1e-15
     To, Yo, _, tio = m.advance_batch(T0, P, Y0, t_end, bench.oracle_opts(po, rtol, atol), threads=2)
     e = bench.error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, {"off": (To * (1 + 1e-4), Yo, tio * 1.01)}, threads=2)
-    assert not e["off"]["T_within_bar"] and not e["off"]["T_within_oracle_error"]
+    assert not e["off"]["T_within_bar"] and not e["off"]["T_within_3x_oracle_error"]
     assert e["off"]["ignition_delay_max_rel_vs_oracle"] > 9e-3 and not e["off"]["ignition_within_1e-3"]
 
 
@@ -80,3 +80,20 @@ def test_timing_build_agrees_with_checker():
     w, _, gross = m.rates_batch(T, P, Y, mode=0, threads=2, gross=True)
     wf, _ = mf.rates_batch(T, P, Y, mode=0, threads=2)
     assert np.all(np.abs(w - wf) <= 1e-12 * gross + 1e-300)
+
+
+def test_tight_run_recovers_a_stalled_reactor():
+    """At rtol 1e-12 / atol 1e-20 the difference-quotient Jacobian stalls on this n-dodecane
+    reactor at the 1000 K midpoint of the NASA7 fits (step size too small); the protocol re-runs
+    it with the analytic Jacobian, which reaches the same ignited state as a looser tight
+    setting."""
+    m = po.Mech(os.path.join(DATA, "nDodecane_Reitz.yaml"), "nDodecane_IG")
+    T0 = np.array([977.6852944187974])
+    P = np.array([2396051.8658179706])
+    Y0 = m.equivalence_ratio(0.9402945673491254, "c12h26:1", "o2:1, n2:3.76")[None, :]
+    _, _, st, _ = m.advance_batch(T0, P, Y0, 5e-3, bench.oracle_opts(po, 0, 0, tight=True), threads=1)
+    assert st[0, 8] == 5
+    Tt, Yt, stt, tit, rerun, failed = bench.tight_run(m, po, T0, P, Y0, 5e-3, threads=1)
+    assert rerun == 1 and not failed.any()
+    To, _, _, _ = m.advance_batch(T0, P, Y0, 5e-3, po.opts(rtol=1e-11, atol=1e-18), threads=1)
+    assert abs(Tt[0] - To[0]) / To[0] < 1e-10 and Tt[0] > 2600.0

@@ -132,8 +132,8 @@ def test_failures_raise(ct):
     with pytest.raises(ct.CanteraError, match="failed"):
         net.advance(1e-3)
     assert net.status[0] != 0
-    with pytest.raises(NotImplementedError):
-        net.step()
+    with pytest.raises(ct.CanteraError, match="failed in their step"):
+        net.step()   # a failed reactor stays failed
     with pytest.raises(ValueError, match="another network"):
         ct.ReactorNet([r])
     other = ct.Solution("h2o2.yaml", "ohmech")

@@ -17,8 +17,14 @@ def ref_opts(po, rtol=RTOL, atol=ATOL):
     return po.opts(rtol=rtol, atol=atol, analytic=False, jac_reuse=True)
 
 
-def tight_opts(po):
-    return po.opts(rtol=1e-12, atol=1e-20, analytic=False, jac_reuse=True)
+def tight(m, T0, P, Y0, t_end):
+    """The tight solution of the bench's error protocol (rtol 1e-12, atol 1e-20; a reactor
+    whose difference-quotient run stalls is re-run with the analytic Jacobian) and the mask
+    of reactors that have one."""
+    import bench
+    from oracle import pyoracle as po
+    Tt, Yt, stt, tit, _, failed = bench.tight_run(m, po, T0, P, Y0, t_end, threads=None)
+    return Tt, Yt, tit, ~failed
 
 
 def major_rel(Y, Yr):
@@ -64,8 +70,8 @@ def test_h2o2_all_1024_reactors(lu):
     assert major_rel(Y, Ya) < 10 * RTOL
     # the reference's configuration and the tight solution
     To, Yo, sto, tio = m.advance_batch(T0, P, Y0, t_end, ref_opts(po))
-    Tt, Yt, stt, tit = m.advance_batch(T0, P, Y0, t_end, tight_opts(po))
-    assert np.all(sto[:, 8] == 0) and np.all(stt[:, 8] == 0)
+    Tt, Yt, tit, have = tight(m, T0, P, Y0, t_end)
+    assert np.all(sto[:, 8] == 0) and np.all(have)
     ign = (Tt > T0 + 400) & (tit > 0) & (tit < t_end)
     assert ign.sum() > 100
     assert np.max(np.abs(tig[ign] - tio[ign]) / tio[ign]) < 1e-3
@@ -105,8 +111,8 @@ def test_gri30_uneven_sample_against_tight_run(lu):
     Y = Y.T
     tig = net.ignition_times
     To, Yo, sto, tio = m.advance_batch(T0, P, Y0, t_end, ref_opts(po))
-    Tt, Yt, stt, tit = m.advance_batch(T0, P, Y0, t_end, tight_opts(po))
-    assert np.all(sto[:, 8] == 0) and np.all(stt[:, 8] == 0)
+    Tt, Yt, tit, have = tight(m, T0, P, Y0, t_end)
+    assert np.all(sto[:, 8] == 0) and np.all(have)
     ign = (Tt > T0 + 400) & (tit > 0) & (tit < t_end)
     assert ign.sum() >= 20 and (~ign).sum() >= 20
     assert np.max(np.abs(tig[ign] - tio[ign]) / tio[ign]) < 1e-3
@@ -152,7 +158,8 @@ def test_ndodecane_256_reactors_to_5ms():
     assert ign.sum() >= 20
     ok = settled(m, P, To, Yo, t_end)
     sub = np.arange(0, 256, 8)
-    Tt, Yt, stt, tit = m.advance_batch(T0[sub], P[sub], Y0[sub], t_end, tight_opts(po))
+    Tt, Yt, tit, have = tight(m, T0[sub], P[sub], Y0[sub], t_end)
+    sub, Tt = sub[have], Tt[have]
     ora_T = np.max(np.abs(To[sub] - Tt) / Tt)
     for lu in (64, 32):
         T, Y, tig, st = out[lu]
