@@ -298,10 +298,14 @@ def gemm_roofline(sur, torch, M=65536):
     if not peak:
         peak, source = 1900.0, "fallback: 1.9 PFLOP/s dense BF16 burst, an earlier measurement on a GB300"
     tf = flops / (ms / 1e3) / 1e12
-    # bytes: X, W in; C (bf16) and Z (fp32) out
+    # bytes: X, W in; C (bf16) and Z (fp32) out.  At 2 M N K / bytes ~ 114 FLOP per byte this
+    # product sits below the ridge of the BF16 roofline (~280 FLOP per byte): its bound is HBM
     byt = M * hid * 2 + hid * hid * 2 + M * hid * (2 + 4)
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    gbs = byt / (ms / 1e3) / 1e9
     return {"shape": [M, hid, hid], "ms": ms, "tflops": tf, "peak_tflops": peak,
-            "frac": tf / peak, "hbm_gbs": byt / (ms / 1e3) / 1e9, "peak_source": source,
+            "frac": tf / peak, "hbm_gbs": gbs, "hbm_peak_gbs": hbm, "hbm_frac": gbs / hbm,
+            "flop_per_byte": flops / byt, "peak_source": source,
             "kernel": "k_umma_gemm (tcgen05.mma kind::f16, TMEM accumulator, TMA 128B-swizzled operands)"}
 
 
