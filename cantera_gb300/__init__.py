@@ -194,10 +194,11 @@ class Solution:
 
     def structure(self):
         """Structure counts used by the FP64 operation model of the benchmark."""
-        c = np.zeros(12, dtype=np.int64)
-        _check(library().gb_mech_structure(self._h, 12, _ptr(c)))
+        c = np.zeros(16, dtype=np.int64)
+        _check(library().gb_mech_structure(self._h, 16, _ptr(c)))
         keys = ["K", "R", "reversible", "falloff", "troe", "three_body", "tb_entries",
-                "gather_entries", "jac_col_entries", "jac_scatter_entries", "reac_slots", "prod_slots"]
+                "gather_entries", "jac_col_entries", "jac_scatter_entries", "reac_slots", "prod_slots",
+                "arena_rhs_bytes", "arena_jacobian_bytes", "arena_side_bytes", "arena_bytes"]
         return dict(zip(keys, (int(v) for v in c)))
 
     def species_index(self, name):

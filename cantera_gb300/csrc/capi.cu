@@ -516,14 +516,15 @@ int32_t runRates(int32_t h, int32_t n, const double* T, const double* P, const d
     p.m = e.dm; p.n = n; p.T = dT; p.P = dP; p.Y = dY; p.wdot = dW; p.jac = dJ;
     p.counter = e.dCounter.as<int>();
     p.warpDoubles = ratesWarpDoubles(e.dm, dJ != nullptr);
+    p.tileDoubles = dJ ? 0 : ratesTileDoubles(e.dm);
     // the mechanism data the call reads goes into shared memory when 8 warps still fit
     // next to the block's state tile
-    const int budget = maxSmemPerBlock() - ratesTileDoubles(e.dm) * 8;
+    const int budget = maxSmemPerBlock() - p.tileDoubles * 8;
     const int want = dJ ? e.dm.sideBytes : e.dm.hotBytes;
     p.mechSmem = (budget - want) / (p.warpDoubles * 8) >= 8 ? want : 0;
     int wpb = std::max(1, std::min(8, (budget - p.mechSmem) / (p.warpDoubles * 8)));
     if (budget - p.mechSmem < p.warpDoubles * 8) throw std::runtime_error("mechanism too large for the rates kernel's shared memory");
-    const int perBlock = p.mechSmem + ratesTileDoubles(e.dm) * 8 + p.warpDoubles * 8 * wpb + 1024;
+    const int perBlock = p.mechSmem + p.tileDoubles * 8 + p.warpDoubles * 8 * wpb + 1024;
     int blocksPerSm = std::max(1, (228 * 1024) / perBlock);
     // wdot alone: a tile of 32 states per block at a time; with the Jacobian: a state per warp
     const long long units = dJ ? ((long long)n + wpb - 1) / wpb : ((long long)n + kRatesTile - 1) / kRatesTile;
@@ -804,6 +805,10 @@ int32_t gb_mech_structure(int32_t h, int32_t ncounts, int64_t* counts) {
         counts[0] = m.K; counts[1] = m.R; counts[2] = rev; counts[3] = fo; counts[4] = troe;
         counts[5] = m.nThirdBody(); counts[6] = (int64_t)m.tbSpecies.size(); counts[7] = spPtr.back();
         counts[8] = colPtr.back(); counts[9] = scatter; counts[10] = rslots; counts[11] = pslots;
+        if (ncounts >= 16) {   // the device arena: what a right-hand side reads, + a Jacobian, + side lists, total
+            counts[12] = e.dm.hotBytes; counts[13] = e.dm.jacBytes; counts[14] = e.dm.sideBytes;
+            counts[15] = (int64_t)e.arena.bytes;
+        }
         return 0;
     });
 }

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
     const int K = m.K, n = p.n;
     constexpr int LD = kRatesTile + 1;        // padded row: column reads hit distinct banks
     double* tile = smem + p.mechSmem / 8;     // rows: T, P, then Y_k / wdot_k, each LD doubles
-    double* base = tile + ratesTileDoubles(m) + (size_t)warp * p.warpDoubles;
+    double* base = tile + p.tileDoubles + (size_t)warp * p.warpDoubles;
     KinScratch s;
     const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
     s.carve(base, m.K, m.R, m.NTB, m.NF, m.NT);
@@ -1308,7 +1308,7 @@ cudaError_t launchBdfT(const BdfParams& p, int blocks, int warpsPerBlock, cudaSt
 
 template <bool kX>
 cudaError_t launchRatesT(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
-    size_t smem = (size_t)p.mechSmem + (size_t)ratesTileDoubles(p.m) * 8 + (size_t)p.warpDoubles * 8 * warpsPerBlock;
+    size_t smem = (size_t)p.mechSmem + (size_t)p.tileDoubles * 8 + (size_t)p.warpDoubles * 8 * warpsPerBlock;
     cudaError_t e = cudaFuncSetAttribute(k_rates<kX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_rates<kX><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);

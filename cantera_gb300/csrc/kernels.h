@@ -20,6 +20,7 @@ struct RatesParams {
                           // bulk copy of the mechanism did not complete)
     int warpDoubles;      // shared-memory doubles per warp
     int mechSmem;         // bytes of the mechanism arena copied into shared memory
+    int tileDoubles;      // the block's state tile (wdot alone; 0 with the Jacobian)
 };
 constexpr int kRatesTile = 32;   // consecutive states per block tile of the rates kernel
 // the block's state tile in shared memory: rows T, P, Y_0..Y_{K-1} of kRatesTile + 1 doubles

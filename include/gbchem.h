@@ -266,7 +266,9 @@ int32_t gb_nn_gate(int32_t mech, int32_t n, double dt, const double* T0, const d
  * Structure counts of a mechanism for the benchmark's FP64 operation model:
  * counts[0..11] = K, R, reversible, falloff, Troe, three-body reactions, third-body
  * efficiency entries, species-gather entries, Jacobian column entries, Jacobian scatter
- * entries, reactant-side species slots, product-side species slots. */
+ * entries, reactant-side species slots, product-side species slots; with ncounts >= 16 also
+ * counts[12..15] = bytes of the device arena a right-hand side reads, + what a Jacobian adds,
+ * + the general side lists, and the whole arena. */
 int32_t gb_mech_structure(int32_t mech, int32_t ncounts, int64_t* counts);
 /* Sustained FP64 FMA rate of the device in GFLOP/s (2 flops per FMA), measured by a
  * dependent-chain kernel over every SM; also the per-call cost of exp and log in
