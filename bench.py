@@ -583,13 +583,12 @@ def run_workload(args):
         sur = Surrogate(gb.Solution("gri30.yaml", "gri30"), hidden=SUR["hidden"], layers=SUR["layers"], seed=0,
                         device=str(dev))
         line = dict(workload="gemm", n_gpus=1, dtype="bf16", data="synthetic", higher_is_better=True)
-        line.update(gemm_roofline(sur, torch, M=args.n if args.n != WL["n"] else 65536))
+        line.update(gemm_roofline(sur, torch, M=args.n or 65536))
         print(json.dumps(line))
         return
-    custom = args.n != WL["n"]
-    fn = {"rates": lambda: variant_rates(dev, torch, flush, threads, n=args.n if custom else 1 << 20,
+    fn = {"rates": lambda: variant_rates(dev, torch, flush, threads, n=args.n or 1 << 20,
                                          peaks=measured_peaks()),
-          "ndodecane": lambda: variant_ndodecane(dev, torch, flush, threads, n=args.n if custom else 16384),
+          "ndodecane": lambda: variant_ndodecane(dev, torch, flush, threads, n=args.n or 16384),
           "h2o2": lambda: variant_h2o2(dev, torch, flush, threads)}[args.workload]
     line = dict(workload=args.workload, n_gpus=1, dtype="f64", data="synthetic", higher_is_better=True)
     line.update(fn())
@@ -636,7 +635,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=WL["n"])
+    ap.add_argument("--n", type=int, default=None,
+                    help="states or reactors of the workload (default: the workload's own size)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
@@ -667,7 +667,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
         pg = dist
-    n_all = args.n
+    n_all = args.n or WL["n"]
     sol = gb.Solution(WL["mechanism"], WL["phase"])
     K = sol.n_species
     T0, P, Y0 = workload_arrays(n_all, WL["seed"],
