@@ -136,9 +136,13 @@ __device__ __forceinline__ void tmemLoad32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// Stages are few enough (2 of 48 KB, or 3 of 32 KB) that two CTAs fit an SM: one CTA's
+// epilogue then overlaps the other's loads and MMAs (measured on 65,536 x 512 x 512: 105 us
+// against 114 us with one CTA of 4 stages per SM); their 2 x BN tensor-memory columns fit the
+// SM's 512.
 template <int BN>
 struct UmmaCfg {
-    static constexpr int kStages = BN == 256 ? 4 : 6;
+    static constexpr int kStages = BN == 256 ? 2 : 3;
     static constexpr int kABytes = 128 * kBK * 2;                 // 16 KB
     static constexpr int kBBytes = BN * kBK * 2;                  // 16 or 32 KB
     static constexpr int kStageBytes = kABytes + kBBytes;
@@ -148,7 +152,7 @@ struct UmmaCfg {
 };
 
 template <int BN>
-__global__ void __launch_bounds__(kUmmaThreads, 1)
+__global__ void __launch_bounds__(kUmmaThreads, 2)
 k_umma_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, UmmaArgs g) {
     using Cfg = UmmaCfg<BN>;
     constexpr int S = Cfg::kStages;
