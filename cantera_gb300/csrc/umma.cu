@@ -25,6 +25,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "nnmath.cuh"
 #include "surrogate.h"
 
@@ -151,6 +153,79 @@ struct UmmaCfg {
     static constexpr int kSmem = 1024 + kStages * kStageBytes + 256;
 };
 
+// One 32-column chunk of a tile row: v = the row's FP32 accumulators of columns n..n+31.
+// alpha, bias, activation; stores of C (and Z, C^T); with split-K an atomic add into C.
+__device__ __forceinline__ void epilogueChunk(const UmmaArgs& g, int row, int n, float* v) {
+    if (g.splitK) {
+        float* C = (float*)g.C + (size_t)row * g.ldc + n;
+#pragma unroll
+        for (int i = 0; i < 32; i += 4)
+            atomicAdd((float4*)(C + i), make_float4(g.alpha * v[i], g.alpha * v[i + 1], g.alpha * v[i + 2],
+                                                    g.alpha * v[i + 3]));
+        return;
+    }
+#pragma unroll
+    for (int i = 0; i < 32; i++) {
+        float x = g.alpha * v[i];
+        if (g.bias) x += g.bias[n + i];
+        v[i] = x;
+    }
+    if (g.act == 1) {
+        if (g.Z) {   // the pre-activation, kept for the backward pass
+            if (g.zFloat) {
+                float4* Z = (float4*)((float*)g.Z + (size_t)row * g.ldz + n);
+#pragma unroll
+                for (int i = 0; i < 8; i++) Z[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+            } else {
+                __nv_bfloat162* Z = (__nv_bfloat162*)((__nv_bfloat16*)g.Z + (size_t)row * g.ldz + n);
+#pragma unroll
+                for (int i = 0; i < 16; i++) Z[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 32; i++) v[i] = gelu(v[i]);
+    } else if (g.act == 2) {
+        if (g.zFloat) {
+            const float4* Z = (const float4*)((const float*)g.Z + (size_t)row * g.ldz + n);
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const float4 z = Z[i];
+                v[4 * i] *= geluGrad(z.x);
+                v[4 * i + 1] *= geluGrad(z.y);
+                v[4 * i + 2] *= geluGrad(z.z);
+                v[4 * i + 3] *= geluGrad(z.w);
+            }
+        } else {
+            const __nv_bfloat162* Z = (const __nv_bfloat162*)((const __nv_bfloat16*)g.Z + (size_t)row * g.ldz + n);
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                const float2 z = __bfloat1622float2(Z[i]);
+                v[2 * i] *= geluGrad(z.x);
+                v[2 * i + 1] *= geluGrad(z.y);
+            }
+        }
+    }
+    if (g.cFloat) {
+        float4* C = (float4*)((float*)g.C + (size_t)row * g.ldc + n);
+#pragma unroll
+        for (int i = 0; i < 8; i++) C[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+    } else {
+        uint4* C = (uint4*)((__nv_bfloat16*)g.C + (size_t)row * g.ldc + n);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            __nv_bfloat162 h[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) h[j] = __floats2bfloat162_rn(v[8 * i + 2 * j], v[8 * i + 2 * j + 1]);
+            C[i] = *(const uint4*)h;
+        }
+    }
+    if (g.CT) {   // transposed copy: lanes hold consecutive rows, so each column is one 64-byte run
+        __nv_bfloat16* CT = (__nv_bfloat16*)g.CT;
+#pragma unroll
+        for (int i = 0; i < 32; i++) CT[(size_t)(n + i) * g.ldct + row] = __float2bfloat16(v[i]);
+    }
+}
+
 template <int BN>
 __global__ void __launch_bounds__(kUmmaThreads, 2)
 k_umma_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, UmmaArgs g) {
@@ -232,75 +307,7 @@ k_umma_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CU
         for (int c0 = 0; c0 < BN; c0 += 32) {
             float v[32];
             tmemLoad32(tbase + (uint32_t)c0, v);
-            const int n = n0 + c0;
-            if (g.splitK) {
-                float* C = (float*)g.C + (size_t)row * g.ldc + n;
-#pragma unroll
-                for (int i = 0; i < 32; i += 4)
-                    atomicAdd((float4*)(C + i), make_float4(g.alpha * v[i], g.alpha * v[i + 1], g.alpha * v[i + 2],
-                                                            g.alpha * v[i + 3]));
-                continue;
-            }
-#pragma unroll
-            for (int i = 0; i < 32; i++) {
-                float x = g.alpha * v[i];
-                if (g.bias) x += g.bias[n + i];
-                v[i] = x;
-            }
-            if (g.act == 1) {
-                if (g.Z) {   // the pre-activation, kept for the backward pass
-                    if (g.zFloat) {
-                        float4* Z = (float4*)((float*)g.Z + (size_t)row * g.ldz + n);
-#pragma unroll
-                        for (int i = 0; i < 8; i++) Z[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-                    } else {
-                        __nv_bfloat162* Z = (__nv_bfloat162*)((__nv_bfloat16*)g.Z + (size_t)row * g.ldz + n);
-#pragma unroll
-                        for (int i = 0; i < 16; i++) Z[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-                    }
-                }
-#pragma unroll
-                for (int i = 0; i < 32; i++) v[i] = gelu(v[i]);
-            } else if (g.act == 2) {
-                if (g.zFloat) {
-                    const float4* Z = (const float4*)((const float*)g.Z + (size_t)row * g.ldz + n);
-#pragma unroll
-                    for (int i = 0; i < 8; i++) {
-                        const float4 z = Z[i];
-                        v[4 * i] *= geluGrad(z.x);
-                        v[4 * i + 1] *= geluGrad(z.y);
-                        v[4 * i + 2] *= geluGrad(z.z);
-                        v[4 * i + 3] *= geluGrad(z.w);
-                    }
-                } else {
-                    const __nv_bfloat162* Z = (const __nv_bfloat162*)((const __nv_bfloat16*)g.Z + (size_t)row * g.ldz + n);
-#pragma unroll
-                    for (int i = 0; i < 16; i++) {
-                        const float2 z = __bfloat1622float2(Z[i]);
-                        v[2 * i] *= geluGrad(z.x);
-                        v[2 * i + 1] *= geluGrad(z.y);
-                    }
-                }
-            }
-            if (g.cFloat) {
-                float4* C = (float4*)((float*)g.C + (size_t)row * g.ldc + n);
-#pragma unroll
-                for (int i = 0; i < 8; i++) C[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-            } else {
-                uint4* C = (uint4*)((__nv_bfloat16*)g.C + (size_t)row * g.ldc + n);
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    __nv_bfloat162 h[4];
-#pragma unroll
-                    for (int j = 0; j < 4; j++) h[j] = __floats2bfloat162_rn(v[8 * i + 2 * j], v[8 * i + 2 * j + 1]);
-                    C[i] = *(const uint4*)h;
-                }
-            }
-            if (g.CT) {   // transposed copy: lanes hold consecutive rows, so each column is one 64-byte run
-                __nv_bfloat16* CT = (__nv_bfloat16*)g.CT;
-#pragma unroll
-                for (int i = 0; i < 32; i++) CT[(size_t)(n + i) * g.ldct + row] = __float2bfloat16(v[i]);
-            }
+            epilogueChunk(g, row, n0 + c0, v);
         }
     } else if (lane == 0) {
         atomicExch(&g_ummaError, 1);
@@ -308,6 +315,157 @@ k_umma_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CU
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 2)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::kTmemCols)
+                     : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Persistent form: one CTA per SM walks the tiles (t = blockIdx.x, + gridDim.x, ...; split-K
+// ranges are tiles too) with warp-specialised roles and two TMEM accumulators, so that the
+// epilogue of one tile overlaps the loads and MMAs of the next:
+//   warp 0, one lane: TMA producer over a 4- or 6-stage ring (as above, the ring's position
+//     running on across tiles);
+//   warp 1, one lane: MMA issuer, accumulating tile i into accumulator i % 2 after the
+//     epilogue has released it (mbarrier accEmpty), signalling accFull when its MMAs complete;
+//   warps 2..5: the epilogue (warp w reads TMEM lanes 32 (w % 4) .. + 31), each warp's first
+//     lane arriving on accEmpty once its rows are read.
+// A wait that runs out sets s_abort: every role stops at its next tile, the MMA warp drains
+// its issued MMAs (a final commit, bounded wait) before the tensor memory is released.
+// ---------------------------------------------------------------------------
+constexpr int kUmmaPThreads = 192;
+
+template <int BN>
+struct UmmaPCfg {
+    static constexpr int kStages = BN == 256 ? 4 : 6;
+    static constexpr int kABytes = 128 * kBK * 2;
+    static constexpr int kBBytes = BN * kBK * 2;
+    static constexpr int kStageBytes = kABytes + kBBytes;
+    static constexpr int kTmemCols = 2 * BN;                      // two accumulators (<= 512)
+    static constexpr int kSmem = 1024 + kStages * kStageBytes + 256;
+};
+
+__device__ __forceinline__ void mbarArrive(uint32_t mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kUmmaPThreads, 1)
+k_umma_gemm_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                       UmmaArgs g, int splits) {
+    using Cfg = UmmaPCfg<BN>;
+    constexpr int S = Cfg::kStages;
+    extern __shared__ __align__(1024) uint8_t dsm[];
+    uint8_t* base = (uint8_t*)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    // barriers: full[S], empty[S], accFull[2], accEmpty[2], drain
+    uint64_t* bars = (uint64_t*)(base + S * Cfg::kStageBytes);
+    uint32_t* tmemSlot = (uint32_t*)(bars + 2 * S + 5);
+    __shared__ int s_abort;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gx = g.N / BN, gy = g.M / 128;
+    const int ntiles = gx * gy * splits;
+    const int kPer = g.K / splits;
+    const int nk = kPer / kBK;
+    const uint32_t fullB = smemAddr(bars), emptyB = smemAddr(bars + S), accFullB = smemAddr(bars + 2 * S),
+                   accEmptyB = smemAddr(bars + 2 * S + 2), drainB = smemAddr(bars + 2 * S + 4);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < S; i++) {
+            mbarInit(fullB + 8 * i, 1);
+            mbarInit(emptyB + 8 * i, 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbarInit(accFullB + 8 * b, 1);
+            mbarInit(accEmptyB + 8 * b, 4);   // one arrival per epilogue warp
+        }
+        mbarInit(drainB, 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&mapA) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&mapB) : "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(tmemSlot)),
+                     "r"(Cfg::kTmemCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmemSlot;
+    volatile int* abortFlag = &s_abort;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int it = 0;
+            for (int t = blockIdx.x; t < ntiles && !*abortFlag; t += gridDim.x) {
+                const int z = t / (gx * gy), r = t - z * gx * gy;
+                const int m0 = (r / gx) * 128, n0 = (r % gx) * BN, kBeg = z * kPer;
+                for (int kb = 0; kb < nk; kb++, it++) {
+                    const int st = it % S;
+                    if (!mbarWait(emptyB + 8 * st, ((it / S) & 1) ^ 1)) { *abortFlag = 1; break; }
+                    const uint32_t a = smemAddr(base + st * Cfg::kStageBytes);
+                    mbarExpectTx(fullB + 8 * st, Cfg::kStageBytes);
+                    tmaLoad2d(a, &mapA, kBeg + kb * kBK, m0, fullB + 8 * st);
+                    tmaLoad2d(a + Cfg::kABytes, &mapB, kBeg + kb * kBK, n0, fullB + 8 * st);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = instrDescBf16(128, BN);
+            int it = 0, i = 0;
+            for (int t = blockIdx.x; t < ntiles && !*abortFlag; t += gridDim.x, i++) {
+                const int b = i & 1;
+                if (!mbarWait(accEmptyB + 8 * b, ((i >> 1) & 1) ^ 1)) { *abortFlag = 1; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc = tmem + (uint32_t)(b * BN);
+                bool fail = false;
+                for (int kb = 0; kb < nk; kb++, it++) {
+                    const int st = it % S;
+                    if (!mbarWait(fullB + 8 * st, (it / S) & 1)) { fail = true; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t a = smemAddr(base + st * Cfg::kStageBytes);
+                    const uint64_t ad = smemDescSw128(a), bd = smemDescSw128(a + Cfg::kABytes);
+#pragma unroll
+                    for (int kk = 0; kk < kBK / 16; kk++)
+                        ummaF16(acc, ad + 2 * kk, bd + 2 * kk, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+                    ummaCommit(emptyB + 8 * st);
+                }
+                if (fail) { *abortFlag = 1; break; }
+                ummaCommit(accFullB + 8 * b);
+            }
+            // every issued MMA has completed before the tensor memory is released
+            ummaCommit(drainB);
+            if (!mbarWait(drainB, 0)) *abortFlag = 1;
+        }
+    } else {
+        const int ew = warp & 3;                       // TMEM lanes 32 ew .. 32 ew + 31
+        int i = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+            const int b = i & 1;
+            const bool ok = mbarWait(accFullB + 8 * b, (i >> 1) & 1);
+            if (__all_sync(0xffffffffu, ok && !*abortFlag) == 0) { if (lane == 0) *abortFlag = 1; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int z = t / (gx * gy), r = t - z * gx * gy;
+            const int m0 = (r / gx) * 128, n0 = (r % gx) * BN;
+            const int row = m0 + ew * 32 + lane;
+            const uint32_t tbase = tmem + ((uint32_t)(ew * 32) << 16) + (uint32_t)(b * BN);
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                float v[32];
+                tmemLoad32(tbase + (uint32_t)c0, v);
+                epilogueChunk(g, row, n0 + c0, v);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbarArrive(accEmptyB + 8 * b);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && *abortFlag) atomicExch(&g_ummaError, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::kTmemCols)
                      : "memory");
 }
@@ -377,10 +535,36 @@ const char* checkUmmaArgs(const UmmaArgs& g, int splits) {
     return nullptr;
 }
 
+namespace {
+template <int BN>
+cudaError_t launchUmmaPersistentT(const UmmaArgs& g, int splits, int ctas, cudaStream_t s) {
+    CUtensorMap ma, mb;
+    if (!makeMap(&ma, g.A, g.M, g.K, g.lda, 128) || !makeMap(&mb, g.B, g.N, g.K, g.ldb, BN))
+        return cudaErrorInvalidValue;
+    constexpr int smem = UmmaPCfg<BN>::kSmem;
+    cudaError_t e = cudaFuncSetAttribute(k_umma_gemm_persistent<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_umma_gemm_persistent<BN><<<ctas, kUmmaPThreads, smem, s>>>(ma, mb, g, splits);
+    return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t launchUmma(const UmmaArgs& g0, int splits, cudaStream_t s) {
     UmmaArgs g = g0;
     g.splitK = splits > 1 ? 1 : 0;
-    if (g.N % 256 == 0) return launchUmmaT<256>(g, splits, s);
+    const int BN = g.N % 256 == 0 ? 256 : 128;
+    const long long tiles = (long long)(g.N / BN) * (g.M / 128) * splits;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    // many tiles: one persistent CTA per SM overlapping each tile's epilogue with the next
+    // tile's mainloop; a grid of at most two waves of the two-CTA kernel does that already
+    if (tiles > 2LL * sms) {
+        const int ctas = (int)std::min<long long>(tiles, sms);
+        return BN == 256 ? launchUmmaPersistentT<256>(g, splits, ctas, s) : launchUmmaPersistentT<128>(g, splits, ctas, s);
+    }
+    if (BN == 256) return launchUmmaT<256>(g, splits, s);
     return launchUmmaT<128>(g, splits, s);
 }
 

@@ -149,3 +149,34 @@ def test_tensor_core_path_matches_legacy_gemm():
     L = _lib()
     assert L.gb_nn_gemm(M, N, K, _p(A), K, 1, _p(B), K, 1, _p(C2), N, 1, 1, 1.0, _p(bias), 0, None, 0, 0, 1) == 0
     assert torch.allclose(C1, C2, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("M,N,K,splits", [(65536, 512, 256, 1), (40960, 128, 512, 1), (512, 512, 65536, 128)])
+def test_persistent_kernel_many_tiles(M, N, K, splits):
+    """Grids of more than two waves run the persistent kernel (one CTA per SM walking the
+    tiles with two tensor-memory accumulators): plain FP32 output, split-K and (below) the
+    full epilogue agree with the FP32 reference."""
+    import torch
+    A, B = _operands(M, N, K, 11 + splits)
+    C = torch.full((M, N), float("nan"), device="cuda")
+    gemm_tc(A, B, C, alpha=0.5, splits=splits)
+    ref = 0.5 * (A.float() @ B.float().T)
+    scale = ref.abs().amax(dim=1, keepdim=True) + 1e-30
+    assert torch.all((C - ref).abs() <= 1e-5 * scale)
+
+
+def test_persistent_kernel_epilogue():
+    import torch
+    M, N, K = 65536, 512, 512
+    A, B = _operands(M, N, K, 5)
+    bias = torch.randn(N, device="cuda")
+    C = torch.empty(M, N, dtype=torch.bfloat16, device="cuda")
+    Z = torch.empty(M, N, device="cuda")
+    CT = torch.empty(N, M, dtype=torch.bfloat16, device="cuda")
+    for _ in range(2):   # the same result on a second call
+        gemm_tc(A, B, C, bias=bias, act=1, Z=Z, CT=CT)
+        z = A.float() @ B.float().T + bias
+        assert torch.all((Z - z).abs() <= 1e-5 * (z.abs().amax(dim=1, keepdim=True) + 1e-30))
+        ref = gelu(Z)
+        assert torch.all((C.float() - ref).abs() <= 2 ** -8 * ref.abs() + 1e-6)
+        assert torch.equal(CT, C.T.contiguous())
