@@ -257,60 +257,100 @@ __device__ __forceinline__ unsigned long long absKey(float x) {
     return (unsigned long long)((unsigned)__float_as_int(x) & 0x7FFFFFFFu);
 }
 
-template <typename MT>
-__device__ __noinline__ bool devLuFactor(MT* a, int N, int ld, int* piv, double* dinv, int lane) {
-    bool nonsingular = true;
-    if (lane == 0)
-        for (int i = 0; i < N; i++) piv[i] = i;
-    __syncwarp();
-    for (int k = 0; k < N; k++) {
-        // pivot search on the integer pipe: for finite values |x| orders like the bits of
-        // x with the sign cleared (the caller has checked that M is finite)
+// Left-looking LU with partial pivoting and lazy row interchanges: P A = L U with row k of
+// P A being the stored (physical) row piv[k].  Column j is computed in registers (lane l holds
+// rows l, l + 32, ... of it): the eliminations of the earlier pivots are applied in pivot order
+// (step k: u = the column's value in row piv[k], broadcast by a shuffle; every row not yet a
+// pivot at step k subtracts its stored multiplier a[r][k] times u), then the pivot is the
+// largest remaining entry and the remaining rows become multipliers.  Each entry of the
+// matrix is stored once (the right-looking form rewrites the trailing submatrix at every
+// pivot, and a global store goes to L2); the multipliers are re-read, from L1.  Row r of the
+// result holds, for r = piv[k], the multipliers L[k][0..k-1] and then U[k][k..N-1].
+template <typename MT, int S>
+__device__ __forceinline__ bool luLeft(MT* a, int N, int ld, int* piv, double* dinv, int lane) {
+    int pidx[S];   // pivot index of the lane's rows (N: not a pivot yet)
+#pragma unroll
+    for (int t = 0; t < S; t++) pidx[t] = N;
+#pragma unroll 1
+    for (int j = 0; j < N; j++) {
+        MT c[S], m1[S], m2[S];
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            const int r = lane + 32 * t;
+            c[t] = r < N ? a[(size_t)r * ld + j] : (MT)0;
+            m1[t] = (r < N && j > 0) ? a[(size_t)r * ld] : (MT)0;
+            m2[t] = (r < N && j > 1) ? a[(size_t)r * ld + 1] : (MT)0;
+        }
+        int p1 = j > 0 ? piv[0] : 0;
+#pragma unroll 1
+        for (int k = 0; k < j; k++) {
+            MT mul[S];
+#pragma unroll
+            for (int t = 0; t < S; t++) {
+                mul[t] = m1[t];
+                m1[t] = m2[t];
+                const int r = lane + 32 * t;
+                if (r < N && k + 2 < j) m2[t] = a[(size_t)r * ld + k + 2];
+            }
+            const int pk = p1;
+            if (k + 1 < j) p1 = piv[k + 1];
+            MT sel = c[0];
+#pragma unroll
+            for (int t = 1; t < S; t++)
+                if ((pk >> 5) == t) sel = c[t];
+            const MT u = __shfl_sync(0xffffffffu, sel, pk & 31);
+#pragma unroll
+            for (int t = 0; t < S; t++)
+                if (pidx[t] > k) c[t] -= mul[t] * u;
+        }
+        // pivot: the largest remaining |entry| (integer compare of the bits with the sign
+        // cleared; the caller has checked that M is finite), lowest row on ties
         unsigned long long bv = 0ULL;
         int bi = N;
-        for (int i = k + lane; i < N; i += 32) {
-            const unsigned long long v = absKey(a[(size_t)i * ld + k]);
-            if (v > bv || bi == N) { bv = v; bi = i; }
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            const int r = lane + 32 * t;
+            if (r < N && pidx[t] == N) {
+                const unsigned long long v = absKey(c[t]);
+                if (v > bv || bi == N) { bv = v; bi = r; }
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
             const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+            if (oi < N && (bi == N || ov > bv || (ov == bv && oi < bi))) { bv = ov; bi = oi; }
         }
-        if (bv == 0ULL) { nonsingular = false; break; }
-        if (bi != k) {
-            for (int j = lane; j < N; j += 32) {
-                MT t = a[(size_t)k * ld + j];
-                a[(size_t)k * ld + j] = a[(size_t)bi * ld + j];
-                a[(size_t)bi * ld + j] = t;
-            }
-            if (lane == 0) { int t = piv[k]; piv[k] = piv[bi]; piv[bi] = t; }
+        if (bv == 0ULL) return false;
+        MT psel = c[0];
+#pragma unroll
+        for (int t = 1; t < S; t++)
+            if ((bi >> 5) == t) psel = c[t];
+        const MT pv = __shfl_sync(0xffffffffu, psel, bi & 31);
+        const MT inv = (MT)1 / pv;
+        if (lane == 0) {
+            piv[j] = bi;
+            dinv[j] = (double)inv;
         }
-        __syncwarp();
-        const MT inv = (MT)1 / a[(size_t)k * ld + k];
-        if (lane == 0) dinv[k] = (double)inv;
-        for (int i = k + 1 + lane; i < N; i += 32) a[(size_t)i * ld + k] *= inv;
-        __syncwarp();
-        // trailing update, eight rows at a time with all loads issued before the stores
-        for (int j = k + 1 + lane; j < N; j += 32) {
-            const MT u = a[(size_t)k * ld + j];
-            int i = k + 1;
-            for (; i + 8 <= N; i += 8) {
-                MT l[8], v[8];
 #pragma unroll
-                for (int r = 0; r < 8; r++) {
-                    l[r] = a[(size_t)(i + r) * ld + k];
-                    v[r] = a[(size_t)(i + r) * ld + j];
-                }
-#pragma unroll
-                for (int r = 0; r < 8; r++) a[(size_t)(i + r) * ld + j] = v[r] - l[r] * u;
-            }
-            for (; i < N; i++) a[(size_t)i * ld + j] -= a[(size_t)i * ld + k] * u;
+        for (int t = 0; t < S; t++) {
+            const int r = lane + 32 * t;
+            if (r == bi) pidx[t] = j;
+            else if (pidx[t] == N) c[t] *= inv;
+            if (r < N) a[(size_t)r * ld + j] = c[t];
         }
         __syncwarp();
     }
-    return nonsingular;
+    return true;
+}
+
+// NS: register slots per lane of the integrator instantiation (N <= 32 NS)
+template <typename MT, int NS>
+__device__ __noinline__ bool devLuFactor(MT* a, int N, int ld, int* piv, double* dinv, int lane) {
+    __syncwarp();
+    const bool ok = luLeft<MT, NS>(a, N, ld, piv, dinv, lane);
+    __syncwarp();
+    return ok;
 }
 
 // Shared-memory staging of a factorisation whose matrix lives in global memory: a block
@@ -324,7 +364,7 @@ struct LuPool {
     int slotBytes;
 };
 
-template <typename MT>
+template <typename MT, int NS>
 __device__ __noinline__ bool devLuStaged(MT* M, int N, int ld, int* piv, double* dinv, int lane, LuPool pool) {
     int slot = -1;
     if (pool.nslots > 0 && lane == 0) {
@@ -332,13 +372,13 @@ __device__ __noinline__ bool devLuStaged(MT* M, int N, int ld, int* piv, double*
             if (atomicCAS(&pool.flags[q], 0, 1) == 0) slot = q;
     }
     slot = __shfl_sync(0xffffffffu, slot, 0);
-    if (slot < 0) return devLuFactor<MT>(M, N, ld, piv, dinv, lane);
+    if (slot < 0) return devLuFactor<MT, NS>(M, N, ld, piv, dinv, lane);
     MT* S = (MT*)(pool.buf + (size_t)slot * pool.slotBytes);
     const int n = N * ld;
 #pragma unroll 1
     for (int q = lane; q < n; q += 32) S[q] = M[q];
     __syncwarp();
-    const bool ok = devLuFactor<MT>(S, N, ld, piv, dinv, lane);
+    const bool ok = devLuFactor<MT, NS>(S, N, ld, piv, dinv, lane);
 #pragma unroll 1
     for (int q = lane; q < n; q += 32) M[q] = S[q];
     __syncwarp();
@@ -355,7 +395,7 @@ __device__ __noinline__ bool devLuStaged(MT* M, int N, int ld, int* piv, double*
 // The kinetics scratch must hold the state y (the last right-hand side was evaluated at y,
 // giving ftemp).  kJacOnly: store J (transposed, no identity) and skip the factorisation.
 // Returns false if J is not finite or M singular.
-template <typename MT, bool kJacOnly, bool kX>
+template <typename MT, bool kJacOnly, bool kX, int NS>
 __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uint64_t* tab, MT* A, int ld,
                                       double gamma, double P, const double* y, const double* ftemp,
                                       double* v1, double* v2, double* tempv, int* piv, double* dinv,
@@ -456,12 +496,12 @@ __device__ __noinline__ bool devSetup(const DevMech& mm, double* base, const uin
     ok = __all_sync(0xffffffffu, ok && fin);
     if (!ok) return false;
     if (kJacOnly) return true;
-    return devLuStaged<MT>(A, N, ld, piv, dinv, lane, pool);
+    return devLuStaged<MT, NS>(A, N, ld, piv, dinv, lane, pool);
 }
 
 // A = M^T = I - gamma J^T from a kept Jacobian (stored transposed, FP64), then the LU
 // factorisation of A.
-template <typename MT>
+template <typename MT, int NS>
 __device__ __noinline__ bool devFormLU(MT* M, const double* J, int N, int ld, double gamma, int* piv, double* dinv,
                                        int lane, LuPool pool) {
     bool fin = true;
@@ -477,7 +517,7 @@ __device__ __noinline__ bool devFormLU(MT* M, const double* J, int N, int ld, do
     }
     __syncwarp();
     if (!__all_sync(0xffffffffu, fin)) return false;
-    return devLuStaged<MT>(M, N, ld, piv, dinv, lane, pool);
+    return devLuStaged<MT, NS>(M, N, ld, piv, dinv, lane, pool);
 }
 
 // Solve (P^T L U) x = b in place.  The vector lives in registers (element i in lane
@@ -485,11 +525,11 @@ __device__ __noinline__ bool devFormLU(MT* M, const double* J, int N, int ld, do
 template <typename MT, int S>
 __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, const int* piv, const double* dinv,
                                         int lane) {
-    // a holds the factors of A = M^T: P A = L U (row i of P A is row piv[i] of A), so
-    // M = U^T L^T P and M x = b is solved by U^T w = b (forward), L^T z = w (backward),
-    // x[piv[i]] = z[i].  Step k of either sweep reads row k of a (coalesced); rows k+1 and
-    // k+2 are in flight meanwhile.  The vector lives in registers: element i in lane i % 32,
-    // slot i / 32.
+    // a holds the factors of A = M^T: P A = L U with row k of P A stored in row piv[k] of a
+    // (and coming from row piv[k] of A), so M = U^T L^T P and M x = b is solved by U^T w = b
+    // (forward), L^T z = w (backward), x[piv[i]] = z[i].  Step k of either sweep reads stored
+    // row piv[k] (coalesced); the rows of steps k+1 and k+2 are in flight meanwhile.  The
+    // vector lives in registers: element i in lane i % 32, slot i / 32.
     MT x[S];
 #pragma unroll
     for (int t = 0; t < S; t++) {
@@ -498,11 +538,13 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
     }
     MT n1[S], n2[S];
     // forward: U^T w = b; w_k = b_k / U_kk, then b_i -= U[k][i] w_k for i > k
+    const MT* r1 = a + (size_t)piv[0] * ld;
+    const MT* r2 = a + (size_t)piv[N > 1 ? 1 : 0] * ld;
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        n1[t] = (i < N) ? a[i] : (MT)0;
-        n2[t] = (i < N && N > 1) ? a[(size_t)ld + i] : (MT)0;
+        n1[t] = (i < N) ? r1[i] : (MT)0;
+        n2[t] = (i < N && N > 1) ? r2[i] : (MT)0;
     }
     MT nd1 = (MT)dinv[0];
     MT nd2 = (N > 1) ? (MT)dinv[1] : (MT)0;
@@ -514,12 +556,13 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
             const MT dk = nd1;
             nd1 = nd2;
             if (k + 2 < N) nd2 = (MT)dinv[k + 2];
+            const MT* rn = a + (size_t)piv[k + 2 < N ? k + 2 : 0] * ld;
 #pragma unroll
             for (int t = 0; t < S; t++) {
                 cur[t] = n1[t];
                 n1[t] = n2[t];
                 const int i = lane + 32 * t;
-                if (i < N && k + 2 < N) n2[t] = a[(size_t)(k + 2) * ld + i];
+                if (i < N && k + 2 < N) n2[t] = rn[i];
             }
             if (lane == (k & 31)) x[tk] = x[tk] * dk;
             const MT wk = __shfl_sync(0xffffffffu, x[tk], k & 31);
@@ -531,23 +574,26 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
         }
     }
     // backward: L^T z = w (unit diagonal); w_i -= L[k][i] z_k for i < k
+    const MT* b1 = a + (size_t)piv[N - 1] * ld;
+    const MT* b2 = a + (size_t)piv[N > 1 ? N - 2 : 0] * ld;
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        n1[t] = (i < N) ? a[(size_t)(N - 1) * ld + i] : (MT)0;
-        n2[t] = (i < N && N > 1) ? a[(size_t)(N - 2) * ld + i] : (MT)0;
+        n1[t] = (i < N) ? b1[i] : (MT)0;
+        n2[t] = (i < N && N > 1) ? b2[i] : (MT)0;
     }
 #pragma unroll
     for (int tk = S - 1; tk >= 0; tk--) {
         const int kbeg = min(N, 32 * (tk + 1)) - 1;
         for (int k = kbeg; k >= 32 * tk; k--) {
             MT cur[S];
+            const MT* rp = a + (size_t)piv[k > 1 ? k - 2 : 0] * ld;
 #pragma unroll
             for (int t = 0; t < S; t++) {
                 cur[t] = n1[t];
                 n1[t] = n2[t];
                 const int i = lane + 32 * t;
-                if (i < N && k > 1) n2[t] = a[(size_t)(k - 2) * ld + i];
+                if (i < N && k > 1) n2[t] = rp[i];
             }
             const MT zk = __shfl_sync(0xffffffffu, x[tk], k & 31);
 #pragma unroll
@@ -604,12 +650,12 @@ struct BdfWarp {
     // and a small change of gamma, or a failure of the previous step); otherwise M is formed
     // from the kept one.  convfail: 0 none, 1 retry after a failure with a stale Jacobian,
     // 2 the previous attempt at this step failed.  fresh: a new Jacobian was evaluated.
-    template <typename MT>
+    template <typename MT, int NS>
     __device__ bool setup(MT* M, BdfScal& S, int convfail, bool& fresh) {
         if (!Jsv) {
             if (lane == 0) { aux->nje++; aux->nsetups++; aux->nrhs++; }   // nrhs: the difference in T
             fresh = true;
-            return devSetup<MT, false, kX>(*m, base, tab, M, ld, S.gamma, P, y, ftemp, v1, v2, tempv, piv, dinv, lane, pool);
+            return devSetup<MT, false, kX, NS>(*m, base, tab, M, ld, S.gamma, P, y, ftemp, v1, v2, tempv, piv, dinv, lane, pool);
         }
         const double dgamma = fabs(ddiv(S.gamma, S.gammap) - 1.0);
         fresh = !S.haveJ || S.nst == 0 || S.nst >= S.nstlj + MSBJ || (convfail == 1 && dgamma < DGMAX_JBAD) ||
@@ -617,13 +663,13 @@ struct BdfWarp {
         if (lane == 0) aux->nsetups++;
         if (fresh) {
             if (lane == 0) { aux->nje++; aux->nrhs++; }
-            const bool ok = devSetup<double, true, kX>(*m, base, tab, Jsv, ld, -1.0, P, y, ftemp, v1, v2, tempv, piv, dinv,
+            const bool ok = devSetup<double, true, kX, NS>(*m, base, tab, Jsv, ld, -1.0, P, y, ftemp, v1, v2, tempv, piv, dinv,
                                                    lane, LuPool{nullptr, nullptr, 0, 0});
             S.nstlj = S.nst;
             S.haveJ = ok;
             if (!ok) return false;
         }
-        return devFormLU<MT>(M, Jsv, N, ld, S.gamma, piv, dinv, lane, pool);
+        return devFormLU<MT, NS>(M, Jsv, N, ld, S.gamma, piv, dinv, lane, pool);
     }
 
     template <typename MT, int S>
@@ -729,7 +775,7 @@ struct BdfWarp {
             if (callSetup) {
                 callSetup = false;
                 bool fresh = true;
-                bool ok = setup<MT>(M, S, convfail, fresh);
+                bool ok = setup<MT, NS>(M, S, convfail, fresh);
                 S.gammap = S.gamma;
                 S.gamrat = 1.0;
                 S.crate = 1.0;
