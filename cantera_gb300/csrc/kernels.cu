@@ -344,11 +344,79 @@ __device__ __forceinline__ bool luLeft(MT* a, int N, int ld, int* piv, double* d
     return true;
 }
 
-// NS: register slots per lane of the integrator instantiation (N <= 32 NS)
+// Right-looking LU with partial pivoting and physical row interchanges (row k of P A stored
+// in row k): for the larger matrices, where the trailing updates' parallel work beats the
+// left-looking form's sequential chain of N^2 / 2 shuffles (n-dodecane, N = 101: 646 against
+// 514 reactors/s).
+template <typename MT>
+__device__ __forceinline__ bool luRight(MT* a, int N, int ld, int* piv, double* dinv, int lane) {
+    bool nonsingular = true;
+    if (lane == 0)
+        for (int i = 0; i < N; i++) piv[i] = i;
+    __syncwarp();
+    for (int k = 0; k < N; k++) {
+        // pivot search on the integer pipe: for finite values |x| orders like the bits of
+        // x with the sign cleared (the caller has checked that M is finite)
+        unsigned long long bv = 0ULL;
+        int bi = N;
+        for (int i = k + lane; i < N; i += 32) {
+            const unsigned long long v = absKey(a[(size_t)i * ld + k]);
+            if (v > bv || bi == N) { bv = v; bi = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+        }
+        if (bv == 0ULL) { nonsingular = false; break; }
+        if (bi != k) {
+            for (int j = lane; j < N; j += 32) {
+                MT t = a[(size_t)k * ld + j];
+                a[(size_t)k * ld + j] = a[(size_t)bi * ld + j];
+                a[(size_t)bi * ld + j] = t;
+            }
+            if (lane == 0) { int t = piv[k]; piv[k] = piv[bi]; piv[bi] = t; }
+        }
+        __syncwarp();
+        const MT inv = (MT)1 / a[(size_t)k * ld + k];
+        if (lane == 0) dinv[k] = (double)inv;
+        for (int i = k + 1 + lane; i < N; i += 32) a[(size_t)i * ld + k] *= inv;
+        __syncwarp();
+        // trailing update, eight rows at a time with all loads issued before the stores
+        for (int j = k + 1 + lane; j < N; j += 32) {
+            const MT u = a[(size_t)k * ld + j];
+            int i = k + 1;
+            for (; i + 8 <= N; i += 8) {
+                MT l[8], v[8];
+#pragma unroll
+                for (int r = 0; r < 8; r++) {
+                    l[r] = a[(size_t)(i + r) * ld + k];
+                    v[r] = a[(size_t)(i + r) * ld + j];
+                }
+#pragma unroll
+                for (int r = 0; r < 8; r++) a[(size_t)(i + r) * ld + j] = v[r] - l[r] * u;
+            }
+            for (; i < N; i++) a[(size_t)i * ld + j] -= a[(size_t)i * ld + k] * u;
+        }
+        __syncwarp();
+    }
+    return nonsingular;
+}
+
+// The factorisation of an integrator instantiation with NS register slots per lane (N <= 32
+// NS): left-looking up to 64 components (h2o2 +5 %, gri30 +0.7 % FP64 / +3.7 % FP32 reactors/s
+// over the right-looking form), right-looking beyond.  kLazyRows<NS> tells the solve which
+// layout the factors have.
+template <int NS>
+constexpr bool kLazyRows = NS <= 2;
+
 template <typename MT, int NS>
 __device__ __noinline__ bool devLuFactor(MT* a, int N, int ld, int* piv, double* dinv, int lane) {
     __syncwarp();
-    const bool ok = luLeft<MT, NS>(a, N, ld, piv, dinv, lane);
+    bool ok;
+    if constexpr (kLazyRows<NS>) ok = luLeft<MT, NS>(a, N, ld, piv, dinv, lane);
+    else ok = luRight<MT>(a, N, ld, piv, dinv, lane);
     __syncwarp();
     return ok;
 }
@@ -525,11 +593,13 @@ __device__ __noinline__ bool devFormLU(MT* M, const double* J, int N, int ld, do
 template <typename MT, int S>
 __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, const int* piv, const double* dinv,
                                         int lane) {
-    // a holds the factors of A = M^T: P A = L U with row k of P A stored in row piv[k] of a
-    // (and coming from row piv[k] of A), so M = U^T L^T P and M x = b is solved by U^T w = b
-    // (forward), L^T z = w (backward), x[piv[i]] = z[i].  Step k of either sweep reads stored
-    // row piv[k] (coalesced); the rows of steps k+1 and k+2 are in flight meanwhile.  The
-    // vector lives in registers: element i in lane i % 32, slot i / 32.
+    // a holds the factors of A = M^T: P A = L U, row k of P A coming from row piv[k] of A and
+    // stored in row piv[k] of a (left-looking form) or in row k (right-looking form), so
+    // M = U^T L^T P and M x = b is solved by U^T w = b (forward), L^T z = w (backward),
+    // x[piv[i]] = z[i].  Step k of either sweep reads the stored row of k (coalesced); the rows
+    // of steps k+1 and k+2 are in flight meanwhile.  The vector lives in registers: element i
+    // in lane i % 32, slot i / 32.
+    auto row = [&](int k) -> const MT* { return a + (size_t)(kLazyRows<S> ? piv[k] : k) * ld; };
     MT x[S];
 #pragma unroll
     for (int t = 0; t < S; t++) {
@@ -538,8 +608,8 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
     }
     MT n1[S], n2[S];
     // forward: U^T w = b; w_k = b_k / U_kk, then b_i -= U[k][i] w_k for i > k
-    const MT* r1 = a + (size_t)piv[0] * ld;
-    const MT* r2 = a + (size_t)piv[N > 1 ? 1 : 0] * ld;
+    const MT* r1 = row(0);
+    const MT* r2 = row(N > 1 ? 1 : 0);
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
@@ -556,7 +626,7 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
             const MT dk = nd1;
             nd1 = nd2;
             if (k + 2 < N) nd2 = (MT)dinv[k + 2];
-            const MT* rn = a + (size_t)piv[k + 2 < N ? k + 2 : 0] * ld;
+            const MT* rn = row(k + 2 < N ? k + 2 : 0);
 #pragma unroll
             for (int t = 0; t < S; t++) {
                 cur[t] = n1[t];
@@ -574,8 +644,8 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
         }
     }
     // backward: L^T z = w (unit diagonal); w_i -= L[k][i] z_k for i < k
-    const MT* b1 = a + (size_t)piv[N - 1] * ld;
-    const MT* b2 = a + (size_t)piv[N > 1 ? N - 2 : 0] * ld;
+    const MT* b1 = row(N - 1);
+    const MT* b2 = row(N > 1 ? N - 2 : 0);
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
@@ -587,7 +657,7 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
         const int kbeg = min(N, 32 * (tk + 1)) - 1;
         for (int k = kbeg; k >= 32 * tk; k--) {
             MT cur[S];
-            const MT* rp = a + (size_t)piv[k > 1 ? k - 2 : 0] * ld;
+            const MT* rp = row(k > 1 ? k - 2 : 0);
 #pragma unroll
             for (int t = 0; t < S; t++) {
                 cur[t] = n1[t];
