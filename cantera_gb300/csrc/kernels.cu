@@ -257,13 +257,6 @@ __device__ __forceinline__ unsigned long long absKey(float x) {
     return (unsigned long long)((unsigned)__float_as_int(x) & 0x7FFFFFFFu);
 }
 
-// Fetch the line holding p into L1 ahead of its use (no register is tied up)
-template <typename MT>
-__device__ __forceinline__ void prefetchL1(const MT* p) {
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-constexpr int kPrefetchRows = 8;   // rows of the factors fetched ahead of a substitution step
-
 // Left-looking LU with partial pivoting and lazy row interchanges: P A = L U with row k of
 // P A being the stored (physical) row piv[k].  Column j is computed in registers (lane l holds
 // rows l, l + 32, ... of it): the eliminations of the earlier pivots are applied in pivot order
@@ -298,9 +291,6 @@ __device__ __forceinline__ bool luLeft(MT* a, int N, int ld, int* piv, double* d
                 m1[t] = m2[t];
                 const int r = lane + 32 * t;
                 if (r < N && k + 2 < j) m2[t] = a[(size_t)r * ld + k + 2];
-                // the next line of the row's multipliers (16 doubles or 32 floats per line)
-                if (r < N && ((k + kPrefetchRows) & 15) == 0 && k + kPrefetchRows < j)
-                    prefetchL1(a + (size_t)r * ld + k + kPrefetchRows);
             }
             const int pk = p1;
             if (k + 1 < j) p1 = piv[k + 1];
@@ -637,14 +627,12 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
             nd1 = nd2;
             if (k + 2 < N) nd2 = (MT)dinv[k + 2];
             const MT* rn = row(k + 2 < N ? k + 2 : 0);
-            const MT* rf = row(k + kPrefetchRows < N ? k + kPrefetchRows : 0);
 #pragma unroll
             for (int t = 0; t < S; t++) {
                 cur[t] = n1[t];
                 n1[t] = n2[t];
                 const int i = lane + 32 * t;
                 if (i < N && k + 2 < N) n2[t] = rn[i];
-                if (i < N && k + kPrefetchRows < N) prefetchL1(rf + i);
             }
             if (lane == (k & 31)) x[tk] = x[tk] * dk;
             const MT wk = __shfl_sync(0xffffffffu, x[tk], k & 31);
@@ -670,14 +658,12 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
         for (int k = kbeg; k >= 32 * tk; k--) {
             MT cur[S];
             const MT* rp = row(k > 1 ? k - 2 : 0);
-            const MT* rf = row(k >= kPrefetchRows ? k - kPrefetchRows : 0);
 #pragma unroll
             for (int t = 0; t < S; t++) {
                 cur[t] = n1[t];
                 n1[t] = n2[t];
                 const int i = lane + 32 * t;
                 if (i < N && k > 1) n2[t] = rp[i];
-                if (i < N && k >= kPrefetchRows) prefetchL1(rf + i);
             }
             const MT zk = __shfl_sync(0xffffffffu, x[tk], k & 31);
 #pragma unroll
