@@ -226,77 +226,6 @@ __device__ __forceinline__ void epilogueChunk(const UmmaArgs& g, int row, int n,
     }
 }
 
-// A warp's 32 x 32 block of outputs (lane l holds row row0 + l, columns n..n+31 in v) written
-// row by row through the warp's staging buffer (32 rows of 33 floats: conflict-free both
-// ways), so that each store instruction writes 32 consecutive elements of one row.
-template <typename T>
-__device__ __forceinline__ void storeBlockStaged(T* out, long long ld, int row0, int n, const float* v,
-                                                 float* stage, int lane) {
-#pragma unroll
-    for (int i = 0; i < 32; i++) stage[lane * 33 + i] = v[i];
-    __syncwarp();
-#pragma unroll 4
-    for (int rr = 0; rr < 32; rr++) {
-        const float x = stage[rr * 33 + lane];
-        if constexpr (sizeof(T) == 4) out[(size_t)(row0 + rr) * ld + n + lane] = x;
-        else out[(size_t)(row0 + rr) * ld + n + lane] = __float2bfloat16(x);
-    }
-    __syncwarp();
-}
-
-// epilogueChunk with the row-major stores (Z, C) staged: for the persistent kernel, whose
-// epilogue warps have a staging buffer each.  The split-K atomics and the transposed copy
-// (already one run per column) are as in epilogueChunk.
-__device__ __forceinline__ void epilogueChunkStaged(const UmmaArgs& g, int row0, int lane, int n, float* v,
-                                                    float* stage) {
-    const int row = row0 + lane;
-    if (g.splitK) {
-        epilogueChunk(g, row, n, v);
-        return;
-    }
-#pragma unroll
-    for (int i = 0; i < 32; i++) {
-        float x = g.alpha * v[i];
-        if (g.bias) x += g.bias[n + i];
-        v[i] = x;
-    }
-    if (g.act == 1) {
-        if (g.Z) {
-            if (g.zFloat) storeBlockStaged((float*)g.Z, g.ldz, row0, n, v, stage, lane);
-            else storeBlockStaged((__nv_bfloat16*)g.Z, g.ldz, row0, n, v, stage, lane);
-        }
-#pragma unroll
-        for (int i = 0; i < 32; i++) v[i] = gelu(v[i]);
-    } else if (g.act == 2) {
-        if (g.zFloat) {
-            const float4* Z = (const float4*)((const float*)g.Z + (size_t)row * g.ldz + n);
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const float4 z = Z[i];
-                v[4 * i] *= geluGrad(z.x);
-                v[4 * i + 1] *= geluGrad(z.y);
-                v[4 * i + 2] *= geluGrad(z.z);
-                v[4 * i + 3] *= geluGrad(z.w);
-            }
-        } else {
-            const __nv_bfloat162* Z = (const __nv_bfloat162*)((const __nv_bfloat16*)g.Z + (size_t)row * g.ldz + n);
-#pragma unroll
-            for (int i = 0; i < 16; i++) {
-                const float2 z = __bfloat1622float2(Z[i]);
-                v[2 * i] *= geluGrad(z.x);
-                v[2 * i + 1] *= geluGrad(z.y);
-            }
-        }
-    }
-    if (g.cFloat) storeBlockStaged((float*)g.C, g.ldc, row0, n, v, stage, lane);
-    else storeBlockStaged((__nv_bfloat16*)g.C, g.ldc, row0, n, v, stage, lane);
-    if (g.CT) {
-        __nv_bfloat16* CT = (__nv_bfloat16*)g.CT;
-#pragma unroll
-        for (int i = 0; i < 32; i++) CT[(size_t)(n + i) * g.ldct + row] = __float2bfloat16(v[i]);
-    }
-}
-
 template <int BN>
 __global__ void __launch_bounds__(kUmmaThreads, 2)
 k_umma_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, UmmaArgs g) {
@@ -412,8 +341,7 @@ struct UmmaPCfg {
     static constexpr int kBBytes = BN * kBK * 2;
     static constexpr int kStageBytes = kABytes + kBBytes;
     static constexpr int kTmemCols = 2 * BN;                      // two accumulators (<= 512)
-    static constexpr int kStageOut = 32 * 33 * 4;                 // an epilogue warp's staging buffer
-    static constexpr int kSmem = 1024 + kStages * kStageBytes + 256 + 4 * kStageOut;
+    static constexpr int kSmem = 1024 + kStages * kStageBytes + 256;
 };
 
 __device__ __forceinline__ void mbarArrive(uint32_t mbar) {
@@ -512,7 +440,6 @@ k_umma_gemm_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_co
         }
     } else {
         const int ew = warp & 3;                       // TMEM lanes 32 ew .. 32 ew + 31
-        float* stage = (float*)(base + S * Cfg::kStageBytes + 256 + (warp - 2) * Cfg::kStageOut);
         int i = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
             const int b = i & 1;
@@ -521,13 +448,13 @@ k_umma_gemm_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_co
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int z = t / (gx * gy), r = t - z * gx * gy;
             const int m0 = (r / gx) * 128, n0 = (r % gx) * BN;
-            const int row0 = m0 + ew * 32;
+            const int row = m0 + ew * 32 + lane;
             const uint32_t tbase = tmem + ((uint32_t)(ew * 32) << 16) + (uint32_t)(b * BN);
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 32) {
                 float v[32];
                 tmemLoad32(tbase + (uint32_t)c0, v);
-                epilogueChunkStaged(g, row0, lane, n0 + c0, v, stage);
+                epilogueChunk(g, row, n0 + c0, v);
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
