@@ -46,7 +46,8 @@ class NetOptions(ctypes.Structure):
                 ("max_time_step", ctypes.c_double), ("lu_precision", ctypes.c_int32),
                 ("warps_per_block", ctypes.c_int32), ("use_graph", ctypes.c_int32),
                 ("matrix_placement", ctypes.c_int32), ("mechanism_in_shared", ctypes.c_int32),
-                ("jacobian_reuse", ctypes.c_int32), ("lu_staging", ctypes.c_int32)]
+                ("jacobian_reuse", ctypes.c_int32), ("lu_staging", ctypes.c_int32),
+                ("linear_solver", ctypes.c_int32)]
 
 
 _lib = None
@@ -95,6 +96,8 @@ def library():
         "gb_net_get_status": (I32, [I32, P]),
         "gb_net_solver_stats": (I32, [I32, P]),
         "gb_net_ignition_times": (I32, [I32, P]),
+        "gb_net_krylov_stats": (I32, [I32, P]),
+        "gb_precond_ilut": (I32, [I32, I32, P, P]),
         "gb_net_launch_info": (I32, [I32, P]),
         "gb_reactor_rhs": (I32, [I32, I32, P, P, P, P, P, I32]),
         "gb_mech_n_elements": (I32, [I32]),
@@ -294,13 +297,25 @@ class Solution:
             pass
 
 
+LINEAR_SOLVERS = {"DENSE": 0, "GMRES": 1}
+
+
 class ReactorNet:
-    """n independent constant-pressure ideal-gas reactors advanced together."""
+    """n independent constant-pressure ideal-gas reactors advanced together.
+
+    linear_solver "DENSE" (default): the mass-fraction reactor with the analytic Jacobian and
+    a dense LU.  "GMRES": the reference's preconditioned Krylov path, the mole reactor
+    (IdealGasConstPressureMoleReactor) with GMRES and the adaptive preconditioner (ILUT of an
+    approximate Jacobian); its per-reactor counters are in krylov_stats."""
 
     def __init__(self, solution, T, P, Y, rtol=1e-9, atol=1e-15, max_steps=20000, max_order=5,
                  max_time_step=0.0, lu_precision=64, warps_per_block=0, use_graph=False,
-                 matrix_placement=0, mechanism_in_shared=0, jacobian_reuse=False, lu_staging=0):
+                 matrix_placement=0, mechanism_in_shared=0, jacobian_reuse=False, lu_staging=0,
+                 linear_solver="DENSE"):
         L = library()
+        if str(linear_solver).upper() not in LINEAR_SOLVERS:
+            raise ValueError("linear_solver must be one of %s" % sorted(LINEAR_SOLVERS))
+        self.linear_solver = str(linear_solver).upper()
         self.solution = solution
         o = NetOptions()
         L.gb_net_default_options(ctypes.byref(o))
@@ -311,6 +326,7 @@ class ReactorNet:
         o.mechanism_in_shared = mechanism_in_shared
         o.jacobian_reuse = int(jacobian_reuse)
         o.lu_staging = int(lu_staging)
+        o.linear_solver = LINEAR_SOLVERS[self.linear_solver]
         n = T.shape[0] if _is_torch_cuda(T) else np.asarray(T).shape[0]
         self.n = n
         self._rtol, self._atol, self._max_steps, self._max_time_step = rtol, atol, max_steps, max_time_step
@@ -438,6 +454,14 @@ class ReactorNet:
         return {k: st[:, i] for i, k in enumerate(STAT_NAMES)}
 
     @property
+    def krylov_stats(self):
+        """Per-reactor counters of the GMRES path: lin_iters, prec_solves, jt_vec_prod_evals
+        (CVodesIntegrator::solverStats names)."""
+        st = np.empty((self.n, 3), dtype=np.int64)
+        _check(library().gb_net_krylov_stats(self._h, _ptr(st)))
+        return {k: st[:, i] for i, k in enumerate(("lin_iters", "prec_solves", "jt_vec_prod_evals"))}
+
+    @property
     def ignition_times(self):
         t = np.empty(self.n)
         _check(library().gb_net_ignition_times(self._h, _ptr(t)))
@@ -449,3 +473,19 @@ class ReactorNet:
                 _lib.gb_net_del(self._h)
         except Exception:
             pass
+
+
+def precond_ilut(P):
+    """ILUT factors of the adaptive preconditioner (AdaptivePreconditioner::factorize) for a
+    batch of matrices P [n, N, N] (or one [N, N]), factored on the GPU one warp per matrix:
+    L (unit diagonal, strictly lower part) and U in place, the same shape as P."""
+    A = np.ascontiguousarray(P, dtype=np.float64)
+    one = A.ndim == 2
+    if one:
+        A = A[None]
+    n, N, N2 = A.shape
+    if N != N2:
+        raise ValueError("square matrices expected")
+    F = np.empty_like(A)
+    _check(library().gb_precond_ilut(n, N, _ptr(A), _ptr(F)))
+    return F[0] if one else F

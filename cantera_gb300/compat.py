@@ -19,14 +19,18 @@ The names and semantics follow the reference's Python interface:
 thermo.py: ``TP``, ``TPX``, ``TPY``, ``X``, ``Y``, ``set_equivalence_ratio``,
 ``density``, ``mean_molecular_weight``, ``concentrations``), ``Kinetics``
 (interfaces/cython/cantera/kinetics.py:456-461,928-940: ``net_production_rates``,
-``net_production_rates_ddCi`` as a scipy CSC matrix), ``IdealGasConstPressureReactor``
-and ``ReactorNet`` (interfaces/cython/cantera/reactor.py:1781-2100: ``advance``, ``time``,
-``initial_time``, ``reinitialize``, ``rtol``, ``atol``, ``max_steps``, ``max_time_step``,
-``solver_stats``).  One ``ReactorNet`` over many reactors is one batched GPU network: every
-reactor is independent (no walls or inlets), shares the network's mechanism and tolerances,
-and reaches each ``advance`` time together.  What the batched engine does not do raises:
-``ReactorNet.step`` (one internal step of a batch has no single meaning), reactors of
-different mechanisms in one network, thermodynamic properties beyond the state.
+``net_production_rates_ddCi`` as a scipy CSC matrix), ``IdealGasConstPressureReactor``,
+``IdealGasConstPressureMoleReactor``, ``AdaptivePreconditioner`` (interfaces/cython/cantera/
+jacobians.py:120-200) and ``ReactorNet`` (interfaces/cython/cantera/reactor.py:1781-2100,
+2396-2415: ``advance``, ``step``, ``time``, ``initial_time``, ``reinitialize``, ``rtol``,
+``atol``, ``max_steps``, ``max_time_step``, ``solver_stats``, ``preconditioner``,
+``linear_solver_type``).  One ``ReactorNet`` over many reactors is one batched GPU network:
+every reactor is independent (no walls or inlets), shares the network's mechanism and
+tolerances, and reaches each ``advance`` time together.  A network of mole reactors with an
+``AdaptivePreconditioner`` runs the engine's GMRES path (the mole-reactor state, the
+preconditioner's ILUT, J v products); without one it runs the dense path.  What the batched
+engine does not do raises: reactors of different mechanisms in one network, preconditioner
+settings other than the reference's defaults, thermodynamic properties beyond the state.
 """
 import numpy as np
 
@@ -36,8 +40,8 @@ one_atm = 101325.0
 avogadro = 6.02214076e26
 gas_constant = avogadro * 1.380649e-23   # J/kmol/K
 
-__all__ = ["Solution", "IdealGasConstPressureReactor", "ReactorNet", "one_atm", "avogadro",
-           "gas_constant", "CanteraError"]
+__all__ = ["Solution", "IdealGasConstPressureReactor", "IdealGasConstPressureMoleReactor",
+           "AdaptivePreconditioner", "ReactorNet", "one_atm", "avogadro", "gas_constant", "CanteraError"]
 CanteraError = GBError
 
 
@@ -250,11 +254,55 @@ class IdealGasConstPressureReactor:
         self._thermo = gas._copy()
 
 
+class IdealGasConstPressureMoleReactor(IdealGasConstPressureReactor):
+    """A constant-pressure ideal-gas reactor whose integrator state is T and the species
+    amounts (IdealGasConstPressureMoleReactor); the one reactor type that supports the
+    adaptive preconditioner."""
+
+
+class AdaptivePreconditioner:
+    """The reference's preconditioner for GMRES (interfaces/cython/cantera/jacobians.py:
+    120-200, src/numerics/AdaptivePreconditioner.cpp): an approximate Jacobian of the mole
+    reactors, factored by ILUT.  The engine runs it with the reference's defaults (no
+    pruning threshold, drop tolerance 1e-12, fill factor 10); other settings raise."""
+    linear_solver_type = "GMRES"
+    _defaults = {"threshold": 0.0, "ilut_fill_factor": 10, "ilut_drop_tol": 1e-12}
+
+    def _check(self, name, v):
+        if float(v) != float(self._defaults[name]):
+            raise NotImplementedError("the engine's preconditioner uses %s = %g" % (name, self._defaults[name]))
+
+    @property
+    def threshold(self):
+        return self._defaults["threshold"]
+
+    @threshold.setter
+    def threshold(self, v):
+        self._check("threshold", v)
+
+    @property
+    def ilut_fill_factor(self):
+        return self._defaults["ilut_fill_factor"]
+
+    @ilut_fill_factor.setter
+    def ilut_fill_factor(self, v):
+        self._check("ilut_fill_factor", v)
+
+    @property
+    def ilut_drop_tol(self):
+        return self._defaults["ilut_drop_tol"]
+
+    @ilut_drop_tol.setter
+    def ilut_drop_tol(self, v):
+        self._check("ilut_drop_tol", v)
+
+
 class ReactorNet:
     """Independent reactors advanced together as one batched GPU network."""
 
     def __init__(self, reactors=(), **engine_options):
         self._reactors = []
+        self._precon = None
         self._opts = dict(engine_options)
         self._rtol, self._atol = 1e-9, 1e-15
         self._max_steps, self._max_time_step = 20000, 0.0
@@ -284,8 +332,14 @@ class ReactorNet:
         T = np.array([s.T for s in g])
         P = np.array([s.P for s in g])
         Y = np.array([s._Y for s in g]).T.copy()
+        opts = dict(self._opts)
+        if self._precon is not None:
+            # ReactorNet::initialize: every reactor must support the preconditioner
+            if not all(isinstance(r, IdealGasConstPressureMoleReactor) for r in self._reactors):
+                raise CanteraError("the AdaptivePreconditioner needs IdealGasConstPressureMoleReactor reactors")
+            opts["linear_solver"] = "GMRES"
         self._engine = _Net(g[0]._m, T, P, Y, rtol=self._rtol, atol=self._atol, max_steps=self._max_steps,
-                            max_time_step=self._max_time_step, **self._opts)
+                            max_time_step=self._max_time_step, **opts)
         self._t0 = self._t
 
     def reinitialize(self):
@@ -390,9 +444,30 @@ class ReactorNet:
         return self._engine.status if self._engine is not None else np.zeros(len(self._reactors), dtype=np.int32)
 
     @property
+    def preconditioner(self):
+        return self._precon
+
+    @preconditioner.setter
+    def preconditioner(self, precon):
+        """ReactorNet.preconditioner: an AdaptivePreconditioner switches the network to GMRES
+        (applied at the next initialisation, as in the reference)."""
+        if precon is not None and not isinstance(precon, AdaptivePreconditioner):
+            raise NotImplementedError("the engine supports the AdaptivePreconditioner only")
+        self._precon = precon
+        self._engine = None
+
+    @property
+    def linear_solver_type(self):
+        return "GMRES" if self._precon is not None else "DENSE"
+
+    @property
     def solver_stats(self):
         """Integrator counters (CVodesIntegrator::solverStats names) as arrays over the
-        reactors, summed since the last (re)initialisation."""
+        reactors, summed since the last (re)initialisation; with GMRES also lin_iters,
+        prec_solves and jt_vec_prod_evals."""
         if self._engine is None:
             return {}
-        return self._engine.solver_stats
+        st = dict(self._engine.solver_stats)
+        if self._engine.linear_solver == "GMRES":
+            st.update(self._engine.krylov_stats)
+        return st

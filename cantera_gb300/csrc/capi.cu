@@ -96,7 +96,8 @@ struct NetEntry {
     gb_net_options opts;
     double time = 0.0;
     int warpsPerBlock = 0, blocks = 0, ld = 0, warpDoubles = 0, recStride = 0;
-    DBuf dP, dT, dY, dRec, dStats, dStatus, dTign, dCounter, dOrder, dM, dJ, dJS, dTnow;
+    DBuf dP, dT, dY, dRec, dStats, dStatus, dTign, dCounter, dOrder, dM, dJ, dJS, dTnow, dKStats;
+    bool krylov = false;  // the mole reactor with GMRES and the adaptive preconditioner
     size_t JSstride = 0;  // bytes per Jacobian-scratch slot in dJS (with global matrices)
     size_t Jstride = 0;   // bytes per kept-Jacobian slot in dJ (0: no Jacobian reuse)
     size_t Mstride = 0;   // bytes per Newton-matrix slot in dM (0: matrices in shared memory)
@@ -557,8 +558,9 @@ int32_t runRates(int32_t h, int32_t n, const double* T, const double* P, const d
 void chooseBdfLaunch(const MechEntry& me, const gb_net_options& o, int n, bool fp32, int ld, NetEntry& ne) {
     const DevMech& d = me.dm;
     const int budget = maxSmemPerBlock();
-    const int wdShared = bdfWarpDoubles(d, ld, fp32);
-    const int wdGlobal = bdfWarpDoublesNoMatrix(d);
+    const int kry = ne.krylov ? bdfKrylovDoubles(d.N) : 0;   // the Krylov basis and GMRES scalars
+    const int wdShared = bdfWarpDoubles(d, ld, fp32) + kry;
+    const int wdGlobal = bdfWarpDoublesNoMatrix(d) + kry;
     const int maxW = o.warps_per_block > 0 ? std::min(o.warps_per_block, kBdfMaxThreads / 32) : kBdfMaxThreads / 32;
     auto mechBytes = [&](int level) {
         return level == 4 ? d.sideBytes : (level == 3 ? d.jacBytes : (level == 2 ? d.hotBytes : 0));
@@ -597,13 +599,14 @@ void chooseBdfLaunch(const MechEntry& me, const gb_net_options& o, int n, bool f
     // automatic: none - on gri30 every staging buffer cost more in L1 capacity (the global
     // matrices' cache) than it saved in the factorisation (8 warps/SM: 5,942 reactors/s with
     // none, 5,689 / 5,560 / 5,419 with 1 / 2 / 3 buffers)
-    if (ne.matGlobal && o.lu_staging > 0) {
+    if (ne.matGlobal && o.lu_staging > 0 && !ne.krylov) {
         const int room = (budget - ne.mechSmem - ne.warpDoubles * 8 * bestFit) / ne.luSlotBytes;
         const int cap = std::min(o.lu_staging, kMaxLuSlots);
         ne.luSlots = std::max(0, std::min(room, cap));
     }
     const int perBlock = ne.mechSmem + ne.warpDoubles * 8 * bestFit + ne.luSlots * ne.luSlotBytes;
-    const int blocksPerSm = bdfBlocksPerSm(d.N, fp32, bestFit, (size_t)perBlock, d.NX > 0);
+    const int blocksPerSm = ne.krylov ? bdfBlocksPerSmKrylov(d.N, d.NX > 0, bestFit, (size_t)perBlock)
+                                      : bdfBlocksPerSm(d.N, fp32, bestFit, (size_t)perBlock, d.NX > 0);
     ne.blocks = std::min(me.smCount * blocksPerSm, (n + bestFit - 1) / bestFit);
 }
 
@@ -625,8 +628,10 @@ void netLaunch(NetEntry& ne, MechEntry& me, double t0, double tout, bool oneStep
     p.JSbuf = ne.JSstride ? ne.dJS.p : nullptr; p.JSstride = (long long)ne.JSstride;
     p.mechSmem = ne.mechSmem;
     p.luSlots = ne.luSlots; p.luSlotBytes = ne.luSlotBytes;
+    p.kstats = ne.krylov ? ne.dKStats.as<long long>() : nullptr;
     ck(cudaMemsetAsync(ne.dCounter.p, 0, sizeof(int), me.stream), "memset");
-    ck(launchBdf(p, ne.blocks, ne.warpsPerBlock, ne.opts.lu_precision == 32, me.stream), "integrator launch");
+    if (ne.krylov) ck(launchBdfKrylov(p, ne.blocks, ne.warpsPerBlock, me.stream), "integrator launch (Krylov)");
+    else ck(launchBdf(p, ne.blocks, ne.warpsPerBlock, ne.opts.lu_precision == 32, me.stream), "integrator launch");
 }
 
 
@@ -878,6 +883,7 @@ void gb_net_default_options(gb_net_options* o) {
     o->mechanism_in_shared = 0;
     o->jacobian_reuse = 0;
     o->lu_staging = 0;
+    o->linear_solver = 0;
 }
 
 int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
@@ -894,6 +900,11 @@ int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
             throw std::runtime_error("lu_precision must be 32 or 64");
         if (ne->opts.max_order < 1 || ne->opts.max_order > 5) throw std::runtime_error("max_order must be 1..5");
         if (!(ne->opts.rtol > 0) || !(ne->opts.atol > 0)) throw std::runtime_error("tolerances must be positive");
+        if (ne->opts.linear_solver != 0 && ne->opts.linear_solver != 1)
+            throw std::runtime_error("linear_solver must be 0 (dense) or 1 (GMRES with the adaptive preconditioner)");
+        ne->krylov = ne->opts.linear_solver == 1;
+        if (ne->krylov && ne->opts.lu_precision != 64)
+            throw std::runtime_error("the GMRES path factors its preconditioner in FP64: lu_precision must be 64");
         const int N = me.dm.N;
         const bool fp32 = ne->opts.lu_precision == 32;
         ne->ld = fp32 ? (N % 2 == 0 ? N + 1 : N) : (N % 2 == 0 ? N + 1 : N);
@@ -912,9 +923,13 @@ int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
             ne->JSstride = (((size_t)2 * me.m.R + bdfNordsieckDoubles(N)) * 8 + 255) & ~size_t(255);
             ne->dJS.ensure(ne->JSstride * (size_t)ne->blocks * wpb);
         }
-        if (ne->opts.jacobian_reuse) {
+        if (ne->opts.jacobian_reuse || ne->krylov) {   // the Krylov path keeps the preconditioner's Jacobian
             ne->Jstride = ((size_t)N * ne->ld * 8 + 255) & ~size_t(255);
             ne->dJ.ensure(ne->Jstride * (size_t)ne->blocks * wpb);
+        }
+        if (ne->krylov) {
+            ne->dKStats.ensure((size_t)n * 3 * 8);
+            ck(cudaMemset(ne->dKStats.p, 0, (size_t)n * 24), "memset");
         }
         const int K = me.m.K;
         ne->dP.ensure((size_t)n * 8);
@@ -969,6 +984,7 @@ int32_t gb_net_set_state(int32_t h, const double* T, const double* P, const doub
         ck(cudaMemcpyAsync(ne.dY.p, Y, (size_t)K * n * 8, kind, s), "copy Y");
         ck(cudaMemsetAsync(ne.dRec.p, 0, (size_t)n * ne.recStride * 8, s), "reset records");
         ck(cudaMemsetAsync(ne.dStats.p, 0, (size_t)n * 64, s), "reset stats");
+        if (ne.krylov) ck(cudaMemsetAsync(ne.dKStats.p, 0, (size_t)n * 24, s), "reset Krylov stats");
         ck(cudaMemsetAsync(ne.dStatus.p, 0, (size_t)n * 4, s), "reset status");
         // queue order: hottest reactors first (they take the most steps), so the
         // longest integrations start early and the tail of the queue is short
@@ -1104,7 +1120,7 @@ namespace {
 constexpr int64_t kCkptMagic = 0x4B43504B43424747LL;   // "GGBCKPCK"
 constexpr int64_t kCkptVersion = 1;
 struct CkptLayout {
-    size_t header, rec, stats, status, tign, T, P, Y, total;
+    size_t header, rec, stats, status, tign, T, P, Y, kstats, total;
 };
 CkptLayout ckptLayout(const NetEntry& ne, int K) {
     CkptLayout L{};
@@ -1118,7 +1134,8 @@ CkptLayout ckptLayout(const NetEntry& ne, int K) {
     L.T = L.tign + n * 8;
     L.P = L.T + n * 8;
     L.Y = L.P + n * 8;
-    L.total = L.Y + (size_t)K * n * 8;
+    L.kstats = L.Y + (size_t)K * n * 8;                // the Krylov path's counters (its networks only)
+    L.total = L.kstats + (ne.krylov ? n * 24 : 0);
     return L;
 }
 }  // namespace
@@ -1142,7 +1159,7 @@ int32_t gb_net_checkpoint(int32_t h, void* buf, int64_t bytes) {
         const CkptLayout L = ckptLayout(ne, K);
         if (!buf || bytes < (int64_t)L.total) throw std::runtime_error("checkpoint buffer smaller than gb_net_checkpoint_bytes");
         char* b = (char*)buf;
-        int64_t hd[8] = {kCkptMagic, kCkptVersion, ne.n, me.dm.N, ne.recStride, K, 0, 0};
+        int64_t hd[8] = {kCkptMagic, kCkptVersion, ne.n, me.dm.N, ne.recStride, K, ne.krylov ? 1 : 0, 0};
         std::memcpy(b, hd, sizeof(hd));
         std::memcpy(b + 64, &ne.time, 8);
         const size_t n = (size_t)ne.n;
@@ -1154,6 +1171,7 @@ int32_t gb_net_checkpoint(int32_t h, void* buf, int64_t bytes) {
         ck(cudaMemcpy(b + L.T, ne.dT.p, n * 8, cudaMemcpyDeviceToHost), "checkpoint T");
         ck(cudaMemcpy(b + L.P, ne.dP.p, n * 8, cudaMemcpyDeviceToHost), "checkpoint P");
         ck(cudaMemcpy(b + L.Y, ne.dY.p, (size_t)K * n * 8, cudaMemcpyDeviceToHost), "checkpoint Y");
+        if (ne.krylov) ck(cudaMemcpy(b + L.kstats, ne.dKStats.p, n * 24, cudaMemcpyDeviceToHost), "checkpoint Krylov stats");
         return 0;
     });
 }
@@ -1165,13 +1183,16 @@ int32_t gb_net_restore(int32_t h, const void* buf, int64_t bytes) {
         requireMechDevice(me);
         const int K = me.m.K;
         const CkptLayout L = ckptLayout(ne, K);
-        if (!buf || bytes < (int64_t)L.total) throw std::runtime_error("checkpoint buffer too small for this network");
+        if (!buf || bytes < (int64_t)L.header) throw std::runtime_error("checkpoint buffer too small for this network");
         const char* b = (const char*)buf;
         int64_t hd[8];
         std::memcpy(hd, b, sizeof(hd));
         if (hd[0] != kCkptMagic || hd[1] != kCkptVersion) throw std::runtime_error("not a reactor-network checkpoint");
         if (hd[2] != ne.n || hd[3] != me.dm.N || hd[4] != ne.recStride || hd[5] != K)
             throw std::runtime_error("checkpoint of a network of another size or mechanism");
+        if (hd[6] != (ne.krylov ? 1 : 0))
+            throw std::runtime_error("checkpoint of a network with the other linear solver (its records hold other state variables)");
+        if (bytes < (int64_t)L.total) throw std::runtime_error("checkpoint buffer too small for this network");
         double t = 0.0;
         std::memcpy(&t, b + 64, 8);
         if (!std::isfinite(t) || t < 0.0) throw std::runtime_error("checkpoint time is not valid");
@@ -1185,6 +1206,7 @@ int32_t gb_net_restore(int32_t h, const void* buf, int64_t bytes) {
         ck(cudaMemcpy(ne.dT.p, b + L.T, n * 8, cudaMemcpyHostToDevice), "restore T");
         ck(cudaMemcpy(ne.dP.p, b + L.P, n * 8, cudaMemcpyHostToDevice), "restore P");
         ck(cudaMemcpy(ne.dY.p, b + L.Y, (size_t)K * n * 8, cudaMemcpyHostToDevice), "restore Y");
+        if (ne.krylov) ck(cudaMemcpy(ne.dKStats.p, b + L.kstats, n * 24, cudaMemcpyHostToDevice), "restore Krylov stats");
         // queue order as gb_net_set_state makes it (hottest first); it only schedules
         std::vector<double> hT(n);
         std::memcpy(hT.data(), b + L.T, n * 8);
@@ -1273,6 +1295,42 @@ int32_t gb_net_solver_stats(int32_t h, int64_t* stats) {
     });
 }
 
+int32_t gb_net_krylov_stats(int32_t h, int64_t* stats) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        if (!stats) throw std::runtime_error("null array argument");
+        if (!ne.krylov) throw std::runtime_error("the network uses the dense linear solver (linear_solver 0)");
+        ck(cudaMemcpy(stats, ne.dKStats.p, (size_t)ne.n * 24, cudaMemcpyDeviceToHost), "copy Krylov stats");
+        return 0;
+    });
+}
+
+int32_t gb_precond_ilut(int32_t n, int32_t N, const double* P, double* F) {
+    return guarded([&]() -> int32_t {
+        if (n <= 0 || N <= 0 || N > 256) throw std::runtime_error("need n > 0 matrices of order 1..256");
+        if (!P || !F) throw std::runtime_error("null array argument");
+        int dev = -1;
+        ck(cudaGetDevice(&dev), "cudaGetDevice");
+        const int ld = (N % 2 == 0) ? N + 1 : N;
+        const size_t per = (size_t)N * ld;
+        std::vector<double> h((size_t)n * per, 0.0);
+        for (int r = 0; r < n; r++)   // transposed: row j holds column j
+            for (int i = 0; i < N; i++)
+                for (int j = 0; j < N; j++) h[r * per + (size_t)j * ld + i] = P[((size_t)r * N + i) * N + j];
+        DBuf a, dinv, rn;
+        a.ensure(h.size() * 8);
+        dinv.ensure((size_t)n * N * 8);
+        rn.ensure((size_t)n * N * 8);
+        ck(cudaMemcpy(a.p, h.data(), h.size() * 8, cudaMemcpyHostToDevice), "copy matrices");
+        ck(launchIlut(n, N, ld, a.as<double>(), dinv.as<double>(), rn.as<double>(), nullptr), "ILUT launch");
+        ck(cudaMemcpy(h.data(), a.p, h.size() * 8, cudaMemcpyDeviceToHost), "copy factors");
+        for (int r = 0; r < n; r++)
+            for (int i = 0; i < N; i++)
+                for (int j = 0; j < N; j++) F[((size_t)r * N + i) * N + j] = h[r * per + (size_t)j * ld + i];
+        return 0;
+    });
+}
+
 int32_t gb_net_ignition_times(int32_t h, double* tign) {
     return guarded([&]() -> int32_t {
         NetEntry& ne = net(h);
@@ -1296,6 +1354,8 @@ int32_t gb_reactors_advance_noalloc(int32_t h, int32_t n, double t_end, double* 
         if (o.lu_precision != 32 && o.lu_precision != 64) throw std::runtime_error("lu_precision must be 32 or 64");
         if (o.max_order < 1 || o.max_order > 5) throw std::runtime_error("max_order must be 1..5");
         if (!(o.rtol > 0) || !(o.atol > 0)) throw std::runtime_error("tolerances must be positive");
+        if (o.linear_solver != 0)
+            throw std::runtime_error("the allocation-free advance runs the dense linear solver only (linear_solver 0)");
         const int N = me.dm.N;
         const int cap = noallocCapacity(N);
         if (n > cap)

@@ -28,10 +28,10 @@
 #include <stdint.h>
 #include <string.h>
 
-// Non-inline functions of these headers have internal linkage in the second kernel module
-// (kernels_x.cu), which compiles the same code again: their host-side stubs must not collide
-// at link time.
-#ifdef GB_KERNELS_EXTRA
+// Non-inline functions of these headers have internal linkage in the kernel modules that
+// compile the same code again (kernels_x.cu, krylov.cu): their host-side stubs must not
+// collide at link time.
+#if defined(GB_KERNELS_EXTRA) || defined(GB_KERNELS_KRYLOV)
 #define GB_TU_LOCAL static
 #else
 #define GB_TU_LOCAL

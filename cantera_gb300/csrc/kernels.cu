@@ -166,6 +166,7 @@ struct BdfScal {
 struct WarpAux {
     double ls_t, ls_v, pv_t, pv_v, bs_t, bs_v, nx_t, nx_v;
     long long nrhs, nni, nsetups, nje, netf, ncfn;
+    long long nli, nps, njtv;   // Krylov path: linear iterations, preconditioner solves, J v products
     int nsamp, flags;
 };
 constexpr int kAuxDoubles = (int)((sizeof(WarpAux) + 7) / 8);
@@ -214,14 +215,17 @@ __device__ __forceinline__ void loadState(const double* base, KinState& st) {
 
 // reactor right-hand side at z = [T, Y]; returns true when every derivative is finite
 // (with forJac the kinetics scratch also keeps what d(wdot)/dc needs: the right-hand side
-// that precedes a Jacobian evaluation)
-template <bool kX>
+// that precedes a Jacobian evaluation).  kMole: the state is z = [T, n_1..n_K] of
+// IdealGasConstPressureMoleReactor (src/zeroD/IdealGasConstPressureMoleReactor.cpp:53-104):
+// dn_k/dt = wdot_k V with V = mass / rho, and m cp dT/dt = -sum_k h_k wdot_k V, which is the
+// same dT/dt as the mass-fraction form.
+template <bool kX, bool kMole = false>
 __device__ __noinline__ bool devRhs(const DevMech& m, double* base, const uint64_t* tab, double P,
                                     const double* z, double* zdot, int lane, bool forJac) {
     KinScratch s;
     carveScratch(m, base, tab, s);
     KinState st;
-    warpState(m, z[0], P, z + 1, s, st, lane);
+    warpState<kMole>(m, z[0], P, z + 1, s, st, lane);
     __syncwarp();
     warpRates<kX>(m, s, st, lane, forJac);
     if (lane == 0) storeState(base, st);
@@ -237,11 +241,24 @@ __device__ __noinline__ bool devRhs(const DevMech& m, double* base, const uint64
     bool ok = finiteBits(dTdt);
     if (lane == 0) zdot[0] = dTdt;
     const double rrho = st.rrho;
+    if (kMole) {
+        double pm = 0.0;
 #pragma unroll 1
-    for (int k = lane; k < m.K; k += 32) {
-        const double v = s.wdot[k] * m.mw[k] * rrho;
-        zdot[1 + k] = v;
-        ok = ok && finiteBits(v);
+        for (int k = lane; k < m.K; k += 32) pm += z[1 + k] * m.mw[k];
+        const double vol = warpSum(pm) * rrho;
+#pragma unroll 1
+        for (int k = lane; k < m.K; k += 32) {
+            const double v = s.wdot[k] * vol;
+            zdot[1 + k] = v;
+            ok = ok && finiteBits(v);
+        }
+    } else {
+#pragma unroll 1
+        for (int k = lane; k < m.K; k += 32) {
+            const double v = s.wdot[k] * m.mw[k] * rrho;
+            zdot[1 + k] = v;
+            ok = ok && finiteBits(v);
+        }
     }
     __syncwarp();
     return __all_sync(0xffffffffu, ok);
@@ -683,7 +700,361 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
 }
 
 
+// =============================================================================
+// Krylov linear solver: GMRES preconditioned by an incomplete LU of I - gamma Jp, where Jp
+// is the adaptive preconditioner's approximate Jacobian of the mole reactor
+// (IdealGasConstPressureMoleReactor::getJacobianElements,
+// src/zeroD/IdealGasConstPressureMoleReactor.cpp:106-221; AdaptivePreconditioner,
+// src/numerics/AdaptivePreconditioner.cpp:17-81; the solver CVODE runs for it,
+// src/numerics/CVodesIntegrator.cpp:67-80).  The matrices are stored transposed (row j holds
+// column j), so that the factorisation's updates and both triangular sweeps read and write
+// whole rows (coalesced).
+// =============================================================================
+constexpr int kMaxl = 5;               // Krylov vectors (CVODE's default)
+constexpr double kEplifac = 0.05;      // linear tolerance factor (CVODE's default)
+constexpr double kIlutTau = 1e-12;     // drop tolerance the adaptive preconditioner gives ILUT
+constexpr int kIlutFillFactor = 10;    // ILUT's fill factor (the library default it keeps)
+// GMRES scalars per warp: H[(kMaxl + 1)][kMaxl], cs[kMaxl], sn[kMaxl], g[kMaxl + 1], y[kMaxl],
+// rho (padded to an even count)
+constexpr int kGmresScalars = ((kMaxl + 1) * kMaxl + 2 * kMaxl + (kMaxl + 1) + kMaxl + 1 + 1) & ~1;
+
+// The preconditioner's Jacobian Jp at the state y, its components clipped below at atol
+// (AdaptivePreconditioner::stateAdjustment), into Jt = Jp^T (FP64, leading dimension ld):
+// the T column by a one-sided difference with dT = T sqrt(eps) (perturbed state first, as the
+// reference), the species block d(dn_k/dt)/dn_j = d(wdot_k)/dc_j (ddCi; the -n_i/(V N) terms of
+// the exact derivative are left out, as there), and the T row
+// d(dT/dt)/dn_j = (cp_j qdot - m cp sum_k h_k d(dn_k/dt)/dn_j) / (m cp)^2, qdot = sum_k h_k dn_k/dt.
+// Scratch: four N-vectors at w.  Returns false when a right-hand side is not finite.
 template <bool kX>
+__device__ __noinline__ bool devPrecJac(const DevMech& mm, double* base, const uint64_t* tab, double* Jt, int ld,
+                                        double P, double atol, const double* y, double* w, int lane) {
+    const int K = mm.K, N = mm.N;
+    double* zc = w;
+    double* zp = w + N;
+    double* fc = w + 2 * N;
+    double* fp = w + 3 * N;
+#pragma unroll 1
+    for (int i = lane; i < N; i += 32) {
+        const double v = fmax(y[i], atol);
+        zc[i] = v;
+        zp[i] = v;
+    }
+    __syncwarp();
+    const double dT = zc[0] * sqrt(UROUND);
+    if (lane == 0) zp[0] = zc[0] + dT;
+    __syncwarp();
+    bool ok = devRhs<kX, true>(mm, base, tab, P, zp, fp, lane, false);
+    ok = devRhs<kX, true>(mm, base, tab, P, zc, fc, lane, true) && ok;
+    if (!ok) return false;
+#pragma unroll 1
+    for (int q = lane; q < N * ld; q += 32) Jt[q] = 0.0;
+    __syncwarp();
+    // T column of Jp = row 0 of Jt
+#pragma unroll 1
+    for (int j = lane; j < N; j += 32) Jt[j] = (fp[j] - fc[j]) / dT;
+    KinScratch s;
+    carveScratch(mm, base, tab, s);
+    KinState st;
+    loadState(base, st);
+    // species block: d(wdot_k)/dc_j at Jt[(1 + j) ld + 1 + k], then the default-efficiency part
+    // g_k that every column shares
+    double* Jsp = Jt + ld + 1;
+    warpJacC<double, true>(mm, s, Jsp, ld, lane);
+    double* g = fp;
+    warpDenseG(mm, s, g, lane);
+    bool anyG = false;
+#pragma unroll 1
+    for (int k = lane; k < K; k += 32) anyG = anyG || g[k] != 0.0;
+    if (__any_sync(0xffffffffu, anyG)) {
+#pragma unroll 1
+        for (int j = 0; j < K; j++) {
+            double* row = Jsp + (size_t)j * ld;
+#pragma unroll 1
+            for (int k = lane; k < K; k += 32) row[k] += g[k];
+        }
+    }
+    __syncwarp();
+    // T row: h_k = (h_k/RT) RT, qdot = sum_k h_k wdot_k V, m cp = V R sum_k c_k cp_k/R
+    double pm = 0.0, pq = 0.0, pc = 0.0;
+#pragma unroll 1
+    for (int k = lane; k < K; k += 32) {
+        pm += zc[1 + k] * mm.mw[k];
+        pq += s.hRT[k] * s.wdot[k];
+        pc += s.c[k] * s.cpR[k];
+    }
+    const double vol = warpSum(pm) * st.rrho;
+    const double qdot = warpSum(pq) * st.RT * vol;
+    const double mcp = vol * mm.Rgas * warpSum(pc);
+    const double denom = 1.0 / (mcp * mcp);
+#pragma unroll 1
+    for (int j = lane; j < K; j += 32) {
+        const double* row = Jsp + (size_t)j * ld;
+        double hs = 0.0;
+#pragma unroll 1
+        for (int k = 0; k < K; k++) hs += row[k] * (s.hRT[k] * st.RT);
+        const double cpj = s.cpR[j] * mm.Rgas;
+        Jt[(size_t)(1 + j) * ld] = (cpj * qdot - mcp * hs) * denom;
+    }
+    __syncwarp();
+    return true;
+}
+
+// Keep the `fill` largest entries (by magnitude) among those of w[] that `part` selects and
+// clear the others (ILUT's fill limit): the fill-th largest magnitude is found bit by bit on
+// the magnitudes' bit patterns; entries equal to it are kept in index order.
+template <int S>
+__device__ __forceinline__ void ilutFillLimit(double (&w)[S], const bool (&part)[S], int fill, int lane) {
+    unsigned long long key[S];
+#pragma unroll
+    for (int t = 0; t < S; t++) key[t] = part[t] ? absKey(w[t]) : 0ULL;
+    auto countGe = [&](unsigned long long v) {
+        int c = 0;
+#pragma unroll
+        for (int t = 0; t < S; t++) c += __popc(__ballot_sync(0xffffffffu, part[t] && key[t] >= v));
+        return c;
+    };
+    unsigned long long T = 0;
+#pragma unroll 1
+    for (int b = 62; b >= 0; b--) {
+        const unsigned long long cand = T | (1ULL << b);
+        if (countGe(cand) >= fill) T = cand;
+    }
+    int need = fill - (T == ~0ULL ? 0 : countGe(T + 1));
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int t = 0; t < S; t++) {
+        const unsigned eq = __ballot_sync(0xffffffffu, part[t] && key[t] == T);
+        const int rank = __popc(eq & lt);
+        if (part[t] && (key[t] < T || (key[t] == T && rank >= need))) w[t] = 0.0;
+        need -= __popc(eq);
+    }
+}
+
+// ILUT(p, tau) of P in place, P stored transposed (a[j ld + i] = P[i][j]), with the rules of
+// Saad's dual-threshold incomplete LU as the adaptive preconditioner uses it: row by row, a
+// multiplier at or below tau is dropped, then the entries of the finished row below tau times
+// its 2-norm (of the row before elimination), then all but the p largest of its L part and of
+// its U part, p = 10 nnz(P) / N + 1, and a zero pivot becomes sqrt(tau) times the row norm.
+// Carried out right-looking: at step k row k has received every update it gets in the
+// row-by-row (IKJ) order, in the same order, so it is finished and dropped before its U part
+// updates the rows below.  Afterwards a holds L (unit diagonal, strictly lower part) and U,
+// dinv[] the reciprocal diagonal of U.  rn: N doubles of scratch.
+template <int S>
+__device__ __noinline__ void devIlut(double* a, int N, int ld, double* dinv, double* rn, int lane) {
+    int cnt = 0;
+#pragma unroll 1
+    for (int j = 0; j < N; j++) {
+        const double* row = a + (size_t)j * ld;
+#pragma unroll 1
+        for (int i = lane; i < N; i += 32) cnt += row[i] != 0.0;
+    }
+    const long long nnz = __reduce_add_sync(0xffffffffu, cnt);
+    const int fill = (int)(nnz * kIlutFillFactor / N) + 1;
+    // 2-norms of the rows of P (columns of a)
+#pragma unroll 1
+    for (int i = lane; i < N; i += 32) {
+        double q = 0.0;
+#pragma unroll 1
+        for (int j = 0; j < N; j++) {
+            const double v = a[(size_t)j * ld + i];
+            q += v * v;
+        }
+        rn[i] = sqrt(q);
+    }
+    __syncwarp();
+    const double sqrtTau = sqrt(kIlutTau);
+#pragma unroll 1
+    for (int k = 0; k < N; k++) {
+        // finish row k of P (column k of a): threshold drops, fill limits, zero pivot
+        double w[S];
+        bool inL[S], inU[S];
+        const double rnk = rn[k];
+        const double thr = kIlutTau * rnk;
+        int cL = 0, cU = 0;
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            const int j = lane + 32 * t;
+            double v = (j < N) ? a[(size_t)j * ld + k] : 0.0;
+            if (j != k && !(fabs(v) > thr)) v = 0.0;
+            w[t] = v;
+            inL[t] = j < k;
+            inU[t] = j > k && j < N;
+            cL += __popc(__ballot_sync(0xffffffffu, inL[t] && v != 0.0));
+            cU += __popc(__ballot_sync(0xffffffffu, inU[t] && v != 0.0));
+        }
+        if (cL > fill) ilutFillLimit<S>(w, inL, fill, lane);
+        if (cU > fill) ilutFillLimit<S>(w, inU, fill, lane);
+        double dk = 0.0;
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            const int j = lane + 32 * t;
+            if (j == k && w[t] == 0.0) w[t] = sqrtTau * rnk;
+            if (j < N) a[(size_t)j * ld + k] = w[t];
+            if (t == (k >> 5)) dk = w[t];
+        }
+        dk = __shfl_sync(0xffffffffu, dk, k & 31);
+        if (lane == 0) dinv[k] = 1.0 / dk;
+        // multipliers of column k (row k of a): f_i = P[i][k] / P[k][k], dropped at or below tau
+        double f[S];
+        bool anyF[S];
+        double* rk = a + (size_t)k * ld;
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            const int i = lane + 32 * t;
+            double v = 0.0;
+            if (i > k && i < N) {
+                const double p = rk[i];
+                if (p != 0.0) {
+                    v = p / dk;
+                    if (fabs(v) <= kIlutTau) v = 0.0;
+                    rk[i] = v;
+                }
+            }
+            f[t] = v;
+            anyF[t] = __any_sync(0xffffffffu, v != 0.0);
+        }
+        // rows i > k: P[i][j] -= f_i P[k][j] for the kept entries P[k][j], j > k (row j of a),
+        // walking the set bits of the kept entries' mask four rows at a time: the four rows'
+        // loads are issued before any store (the rows are distinct, so the order of the updates
+        // of each element is unchanged)
+#pragma unroll
+        for (int tj = 0; tj < S; tj++) {
+            if (32 * tj + 31 <= k) continue;
+            const int j0 = 32 * tj;
+            unsigned msk = __ballot_sync(0xffffffffu, w[tj] != 0.0 && j0 + lane > k && j0 + lane < N);
+#pragma unroll 1
+            while (msk) {
+                int jq[4];
+                double u[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    jq[q] = msk ? __ffs(msk) - 1 : -1;
+                    if (msk) msk &= msk - 1;
+                    u[q] = __shfl_sync(0xffffffffu, w[tj], jq[q] < 0 ? 0 : jq[q]);
+                }
+                double v[S][4];
+#pragma unroll
+                for (int t = 0; t < S; t++) {
+                    const int i = lane + 32 * t;
+                    const bool act = anyF[t] && i > k && i < N;
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        v[t][q] = (act && jq[q] >= 0) ? a[(size_t)(j0 + jq[q]) * ld + i] : 0.0;
+                }
+#pragma unroll
+                for (int t = 0; t < S; t++) {
+                    const int i = lane + 32 * t;
+                    const bool act = anyF[t] && i > k && i < N;
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (act && jq[q] >= 0) a[(size_t)(j0 + jq[q]) * ld + i] = fma(-f[t], u[q], v[t][q]);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Solve (L U) x = b in place with the factors of devIlut: L w = b forward (unit lower; column
+// k of L is row k of a), then U x = w backward (column j of U is row j of a, its diagonal
+// from dinv).  The vector lives in registers (element i in lane i % 32, slot i / 32); every
+// substitution step broadcasts one element by a shuffle.  The factors are usually in L2 (one
+// matrix per resident warp), so the rows of the next kIluAhead steps are in flight meanwhile.
+constexpr int kIluAhead = 4;
+template <int S>
+__device__ __noinline__ void devIluSolve(const double* a, double* b, int N, int ld, const double* dinv, int lane) {
+    double x[S], nr[kIluAhead][S];
+#pragma unroll
+    for (int t = 0; t < S; t++) {
+        const int i = lane + 32 * t;
+        x[t] = (i < N) ? b[i] : 0.0;
+    }
+#pragma unroll
+    for (int p = 0; p < kIluAhead; p++) {
+        const double* r = a + (size_t)(p < N ? p : 0) * ld;
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            const int i = lane + 32 * t;
+            nr[p][t] = (i < N && p < N) ? r[i] : 0.0;
+        }
+    }
+#pragma unroll
+    for (int tk = 0; tk < S; tk++) {
+        const int kend = min(N, 32 * (tk + 1));
+        for (int k = 32 * tk; k < kend; k++) {
+            double cur[S];
+            const int kn = k + kIluAhead;
+            const double* rn = a + (size_t)(kn < N ? kn : 0) * ld;
+#pragma unroll
+            for (int t = 0; t < S; t++) {
+                cur[t] = nr[0][t];
+#pragma unroll
+                for (int p = 0; p + 1 < kIluAhead; p++) nr[p][t] = nr[p + 1][t];
+                const int i = lane + 32 * t;
+                if (i < N && kn < N) nr[kIluAhead - 1][t] = rn[i];
+            }
+            const double wk = __shfl_sync(0xffffffffu, x[tk], k & 31);
+            if (wk == 0.0) continue;
+#pragma unroll
+            for (int t = tk; t < S; t++) {
+                const int i = lane + 32 * t;
+                if (i > k && i < N) x[t] -= cur[t] * wk;
+            }
+        }
+    }
+    double nd[kIluAhead];
+#pragma unroll
+    for (int p = 0; p < kIluAhead; p++) {
+        const int k = N - 1 - p;
+        const double* r = a + (size_t)(k >= 0 ? k : 0) * ld;
+        nd[p] = (k >= 0) ? dinv[k] : 0.0;
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            const int i = lane + 32 * t;
+            nr[p][t] = (i < N && k >= 0) ? r[i] : 0.0;
+        }
+    }
+#pragma unroll
+    for (int tk = S - 1; tk >= 0; tk--) {
+        const int kbeg = min(N, 32 * (tk + 1)) - 1;
+        for (int k = kbeg; k >= 32 * tk; k--) {
+            double cur[S];
+            const int kn = k - kIluAhead;
+            const double dk = nd[0];
+#pragma unroll
+            for (int p = 0; p + 1 < kIluAhead; p++) nd[p] = nd[p + 1];
+            if (kn >= 0) nd[kIluAhead - 1] = dinv[kn];
+            const double* rp = a + (size_t)(kn >= 0 ? kn : 0) * ld;
+#pragma unroll
+            for (int t = 0; t < S; t++) {
+                cur[t] = nr[0][t];
+#pragma unroll
+                for (int p = 0; p + 1 < kIluAhead; p++) nr[p][t] = nr[p + 1][t];
+                const int i = lane + 32 * t;
+                if (i < N && kn >= 0) nr[kIluAhead - 1][t] = rp[i];
+            }
+            if (lane == (k & 31)) x[tk] = x[tk] * dk;
+            const double zk = __shfl_sync(0xffffffffu, x[tk], k & 31);
+            if (zk == 0.0) continue;
+#pragma unroll
+            for (int t = 0; t <= tk; t++) {
+                const int i = lane + 32 * t;
+                if (i < k) x[t] -= cur[t] * zk;
+            }
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < S; t++) {
+        const int i = lane + 32 * t;
+        if (i < N) b[i] = x[t];
+    }
+    __syncwarp();
+}
+
+// One reactor per warp.  kKry: the mole reactor with GMRES and the adaptive preconditioner
+// (the Krylov path) instead of the mass-fraction reactor with a dense LU.
+template <bool kX, bool kKry = false>
 struct BdfWarp {
     const DevMech* m;
     int N, Nnorm, lane, ld;
@@ -696,6 +1067,8 @@ struct BdfWarp {
     LuPool pool;             // shared-memory staging buffers for the factorisation
     double *zn, *ewt, *acor, *y, *ftemp, *tempv, *v1, *v2, *dinv;
     int* piv;
+    double* V;               // Krylov path: the Krylov basis, (kMaxl + 1) N-vectors
+    double* Hs;              // Krylov path: the GMRES scalars (kGmresScalars)
 
     __device__ double wrms(const double* v) const {
         double a = 0.0;
@@ -713,7 +1086,7 @@ struct BdfWarp {
     }
     __device__ bool rhs(const double* z, double* zdot, BdfScal& S, bool forJac = false) {
         if (lane == 0) aux->nrhs++;
-        return devRhs<kX>(*m, base, tab, P, z, zdot, lane, forJac);
+        return devRhs<kX, kKry>(*m, base, tab, P, z, zdot, lane, forJac);
     }
     // Linear-solver setup.  With a kept Jacobian, CVODE's policy decides when to evaluate a
     // new one (first step, 51 steps since the last, a convergence failure with a stale one
@@ -722,6 +1095,38 @@ struct BdfWarp {
     // 2 the previous attempt at this step failed.  fresh: a new Jacobian was evaluated.
     template <typename MT, int NS>
     __device__ bool setup(MT* M, BdfScal& S, int convfail, bool& fresh) {
+        if constexpr (kKry) {
+            // preconditioner setup as CVODE's linear-solver interface drives it for a
+            // matrix-free solver (cvLsSetup): the preconditioner's Jacobian is evaluated anew on
+            // the same conditions as a kept dense one, otherwise only gamma changes; then the
+            // incomplete factorisation of I - gamma Jp
+            const double dgamma = fabs(ddiv(S.gamma, S.gammap) - 1.0);
+            fresh = !S.haveJ || S.nst == 0 || S.nst >= S.nstlj + MSBJ || (convfail == 1 && dgamma < DGMAX_JBAD) ||
+                    convfail == 2;
+            if (lane == 0) aux->nsetups++;
+            if (fresh) {
+                if (lane == 0) { aux->nje++; aux->nrhs += 2; }
+                const bool ok = devPrecJac<kX>(*m, base, tab, Jsv, ld, P, atol, y, V, lane);
+                S.nstlj = S.nst;
+                S.haveJ = ok;
+                if (!ok) return false;
+            }
+            const double g = S.gamma;
+#pragma unroll 1
+            for (int j = 0; j < N; j++) {
+                const double* src = Jsv + (size_t)j * ld;
+                MT* dst = M + (size_t)j * ld;
+#pragma unroll 1
+                for (int i = lane; i < N; i += 32) {
+                    double v = -g * src[i];
+                    if (i == j) v += 1.0;
+                    dst[i] = (MT)v;
+                }
+            }
+            __syncwarp();
+            devIlut<NS>((double*)M, N, ld, dinv, V, lane);
+            return true;
+        }
         if (!Jsv) {
             if (lane == 0) { aux->nje++; aux->nsetups++; aux->nrhs++; }   // nrhs: the difference in T
             fresh = true;
@@ -744,6 +1149,186 @@ struct BdfWarp {
 
     template <typename MT, int S>
     __device__ void luSolve(const MT* a, double* b) { devLuSolve<MT, S>(a, b, N, ld, piv, dinv, lane); }
+
+    // J v by the difference quotient (f(y + sig v) - f(y)) / sig, sig = 1 / ||v||_wrms, shrunk by
+    // 1/4 (at most three tries) when f is not finite (CVODE's default Jacobian-times-vector
+    // product); y and f(y) are the current Newton iterate.  work: an N-vector of scratch.
+    __device__ bool jtimes(const double* v, double* Jv, double* work, BdfScal& S) {
+        double sig = ddiv(1.0, wrms(v));
+        bool ok = false;
+        for (int it = 0; it < 3; it++) {
+#pragma unroll 1
+            for (int i = lane; i < N; i += 32) work[i] = y[i] + sig * v[i];
+            __syncwarp();
+            if (lane == 0) aux->njtv++;
+            ok = rhs(work, Jv, S);
+            if (ok) break;
+            sig *= 0.25;
+        }
+        if (!ok) return false;
+        const double siginv = ddiv(1.0, sig);
+#pragma unroll 1
+        for (int i = lane; i < N; i += 32) Jv[i] = (Jv[i] - ftemp[i]) * siginv;
+        __syncwarp();
+        return true;
+    }
+    template <int NS>
+    __device__ void precSolve(const double* Ft, double* x) {
+        if (lane == 0) aux->nps++;
+        devIluSolve<NS>(Ft, x, N, ld, dinv, lane);
+    }
+    // (I - gamma J) x = b in place by right-preconditioned GMRES, as CVODE's iterative
+    // linear-solver interface runs SUNDIALS' SPGMR for the reference's preconditioned solver
+    // (src/numerics/CVodesIntegrator.cpp:67-80; cvLsSolve): tolerance eplifac tq[4] in the
+    // weighted RMS norm (sqrt(N) times it in the scaled 2-norm), the error weights as both
+    // scaling vectors, zero initial guess, at most kMaxl Krylov vectors, no restarts, modified
+    // Gram-Schmidt with one reorthogonalisation when the new vector's norm collapses by the
+    // factor 1000, Givens rotations for the least-squares problem (lane 0 holds it).  A
+    // right-hand side already below the tolerance is the solution on the first Newton
+    // iteration and zero afterwards.  Returns 0, or 1 (recoverable: not converged and, after
+    // the first Newton iteration, only reduced).
+    template <int NS>
+    __device__ int gmres(const double* Ft, double* b, BdfScal& S, int mnewt) {
+        const double deltar = kEplifac * S.tq[4];
+        if (wrms(b) <= deltar) {
+            if (mnewt > 0) {
+#pragma unroll 1
+                for (int i = lane; i < N; i += 32) b[i] = 0.0;
+                __syncwarp();
+            }
+            return 0;
+        }
+        const double delta = deltar * dsqrt((double)N);
+        double* H = Hs;                              // H[i][l] at H[i * kMaxl + l]
+        double* cs = Hs + (kMaxl + 1) * kMaxl;
+        double* sn = cs + kMaxl;
+        double* g = sn + kMaxl;
+        double* yv = g + kMaxl + 1;
+        double* z = v1;
+        double* Az = v2;
+        double q = 0.0;
+#pragma unroll 1
+        for (int i = lane; i < N; i += 32) {
+            const double x = ewt[i] * b[i];
+            V[i] = x;
+            q += x * x;
+        }
+        const double beta = dsqrt(warpSum(q));
+#pragma unroll 1
+        for (int i = lane; i < N; i += 32) V[i] = V[i] / beta;
+        if (lane == 0) {
+            g[0] = beta;
+#pragma unroll 1
+            for (int j = 1; j <= kMaxl; j++) g[j] = 0.0;
+        }
+        __syncwarp();
+        double rho = beta;
+        bool converged = false;
+        int mv = 0;
+        while (mv < kMaxl) {
+            const int l = mv;
+            const double* vl = V + (size_t)l * N;
+            double* vn = V + (size_t)(l + 1) * N;
+#pragma unroll 1
+            for (int i = lane; i < N; i += 32) z[i] = vl[i] / ewt[i];
+            __syncwarp();
+            precSolve<NS>(Ft, z);
+            if (!jtimes(z, Az, b, S)) return 1;
+            double pk = 0.0;
+#pragma unroll 1
+            for (int i = lane; i < N; i += 32) {
+                const double x = ewt[i] * (z[i] - S.gamma * Az[i]);
+                vn[i] = x;
+                pk += x * x;
+            }
+            const double vk = dsqrt(warpSum(pk));
+#pragma unroll 1
+            for (int i2 = 0; i2 <= l; i2++) {
+                const double* vi = V + (size_t)i2 * N;
+                double pd = 0.0;
+#pragma unroll 1
+                for (int i = lane; i < N; i += 32) pd += vi[i] * vn[i];
+                const double h = warpSum(pd);
+#pragma unroll 1
+                for (int i = lane; i < N; i += 32) vn[i] -= h * vi[i];
+                if (lane == 0) H[i2 * kMaxl + l] = h;
+            }
+            double pn = 0.0;
+#pragma unroll 1
+            for (int i = lane; i < N; i += 32) pn += vn[i] * vn[i];
+            double vnorm = dsqrt(warpSum(pn));
+            const double fac = 1000.0 * vk;
+            if (fac + vnorm == fac) {
+#pragma unroll 1
+                for (int i2 = 0; i2 <= l; i2++) {
+                    const double* vi = V + (size_t)i2 * N;
+                    double pd = 0.0;
+#pragma unroll 1
+                    for (int i = lane; i < N; i += 32) pd += vi[i] * vn[i];
+                    const double pr = warpSum(pd);
+#pragma unroll 1
+                    for (int i = lane; i < N; i += 32) vn[i] -= pr * vi[i];
+                    if (lane == 0) H[i2 * kMaxl + l] += pr;
+                }
+                pn = 0.0;
+#pragma unroll 1
+                for (int i = lane; i < N; i += 32) pn += vn[i] * vn[i];
+                vnorm = dsqrt(warpSum(pn));
+            }
+            double rl = 0.0;
+            if (lane == 0) {
+                H[(l + 1) * kMaxl + l] = vnorm;
+#pragma unroll 1
+                for (int i2 = 0; i2 < l; i2++) {
+                    const double t1 = H[i2 * kMaxl + l], t2 = H[(i2 + 1) * kMaxl + l];
+                    H[i2 * kMaxl + l] = cs[i2] * t1 + sn[i2] * t2;
+                    H[(i2 + 1) * kMaxl + l] = -sn[i2] * t1 + cs[i2] * t2;
+                }
+                const double hl = H[l * kMaxl + l], hl1 = H[(l + 1) * kMaxl + l];
+                const double d = hypot(hl, hl1);
+                cs[l] = hl / d;
+                sn[l] = hl1 / d;
+                H[l * kMaxl + l] = d;
+                H[(l + 1) * kMaxl + l] = 0.0;
+                g[l + 1] = -sn[l] * g[l];
+                g[l] = cs[l] * g[l];
+                rl = fabs(g[l + 1]);
+            }
+            rho = __shfl_sync(0xffffffffu, rl, 0);
+            mv++;
+            if (rho <= delta) { converged = true; break; }
+            if (vnorm == 0.0) break;
+#pragma unroll 1
+            for (int i = lane; i < N; i += 32) vn[i] = vn[i] / vnorm;
+            __syncwarp();
+        }
+        if (lane == 0) {
+            aux->nli += mv;
+#pragma unroll 1
+            for (int i2 = mv - 1; i2 >= 0; i2--) {
+                double sacc = g[i2];
+#pragma unroll 1
+                for (int j = i2 + 1; j < mv; j++) sacc -= H[i2 * kMaxl + j] * yv[j];
+                yv[i2] = sacc / H[i2 * kMaxl + i2];
+            }
+        }
+        __syncwarp();
+#pragma unroll 1
+        for (int i = lane; i < N; i += 32) {
+            double sacc = 0.0;
+#pragma unroll 1
+            for (int j = 0; j < mv; j++) sacc += yv[j] * V[(size_t)j * N + i];
+            z[i] = sacc / ewt[i];
+        }
+        __syncwarp();
+        precSolve<NS>(Ft, z);
+#pragma unroll 1
+        for (int i = lane; i < N; i += 32) b[i] = z[i];
+        __syncwarp();
+        if (converged) return 0;
+        if (rho < beta && mnewt == 0) return 0;
+        return 1;
+    }
 
     __device__ void predict(BdfScal& S) {
         S.tn += S.h;
@@ -863,12 +1448,17 @@ struct BdfWarp {
 #pragma unroll 1
                 for (int i = lane; i < N; i += 32) tempv[i] = S.gamma * ftemp[i] - (rl1 * z1[i] + acor[i]);
                 __syncwarp();
-                luSolve<MT, NS>(M, tempv);
-                if (S.gamrat != 1.0) {
-                    double f = ddiv(2.0, 1.0 + S.gamrat);
+                if constexpr (kKry) {
+                    // an iterative solve uses the current gamma: no correction for its change
+                    if (gmres<NS>((const double*)M, tempv, S, mm) != 0) { retry = !jcur; break; }
+                } else {
+                    luSolve<MT, NS>(M, tempv);
+                    if (S.gamrat != 1.0) {
+                        double f = ddiv(2.0, 1.0 + S.gamrat);
 #pragma unroll 1
-                    for (int i = lane; i < N; i += 32) tempv[i] *= f;
-                    __syncwarp();
+                        for (int i = lane; i < N; i += 32) tempv[i] *= f;
+                        __syncwarp();
+                    }
                 }
                 del = wrms(tempv);
 #pragma unroll 1
@@ -1173,7 +1763,7 @@ struct BdfWarp {
     }
 };
 
-template <typename MT, int NS, bool kX>
+template <typename MT, int NS, bool kX, bool kKry>
 __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     extern __shared__ __align__(128) double smem[];
     __shared__ uint64_t s_tab[kGbxTableWords];
@@ -1186,10 +1776,12 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     double* base = smem + p.mechSmem / 8 + (size_t)warp * p.warpDoubles;
-    BdfWarp<kX> W;
+    BdfWarp<kX, kKry> W;
     W.m = &m;
     W.N = m.N;
-    W.Nnorm = m.N + 1;
+    // error-norm divisor: the reference's state has the mass as well for the mass-fraction
+    // reactor (K + 2 components), T and the K amounts for the mole reactor
+    W.Nnorm = kKry ? m.N : m.N + 1;
     W.lane = lane;
     W.ld = p.ld;
     W.rtol = p.rtol;
@@ -1220,6 +1812,12 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     W.v2 = q; q += N;
     W.dinv = q; q += N;
     W.piv = (int*)q; q += (N + 1) / 2;
+    if (kKry) {
+        W.V = q; q += (kMaxl + 1) * N;
+        W.Hs = q; q += kGmresScalars;
+    } else {
+        W.V = W.Hs = nullptr;
+    }
     MT* M = p.Mbuf ? (MT*)((char*)p.Mbuf + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * p.Mstride)
                    : (MT*)q;
     W.Jsv = p.Jbuf ? (double*)((char*)p.Jbuf + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * p.Jstride) : nullptr;
@@ -1238,15 +1836,27 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
         double* rec = p.rec + (size_t)r * p.recStride;
         const double* rs = rec + (QMAX + 1) * N;
         long long* stt = p.stats + (size_t)r * 8;
+        long long* kst = kKry ? p.kstats + (size_t)r * 3 : nullptr;
         W.P = p.P[r];
         BdfScal S;
         const bool fresh = !(((int)rs[R_FLAGS]) & F_INIT);
         if (fresh) {
             // zn[0] = state, zn[1] = h*f(state)
             double* z0 = W.zn;
-            if (lane == 0) z0[0] = p.T[r];
+            const double T0 = p.T[r];
+            if (lane == 0) z0[0] = T0;
+            if (kKry) {
+                // amounts in an initial volume of 1 m^3: n_k = rho Y_k / W_k
+                double py = 0.0;
 #pragma unroll 1
-            for (int k = lane; k < m.K; k += 32) z0[1 + k] = p.Y[(size_t)k * p.n + r];
+                for (int k = lane; k < m.K; k += 32) py += p.Y[(size_t)k * p.n + r] * m.rmw[k];
+                const double rho = (W.P / (m.Rgas * T0)) / warpSum(py);
+#pragma unroll 1
+                for (int k = lane; k < m.K; k += 32) z0[1 + k] = rho * p.Y[(size_t)k * p.n + r] * m.rmw[k];
+            } else {
+#pragma unroll 1
+                for (int k = lane; k < m.K; k += 32) z0[1 + k] = p.Y[(size_t)k * p.n + r];
+            }
 #pragma unroll 1
             for (int j = 1; j <= QMAX; j++)
 #pragma unroll 1
@@ -1256,6 +1866,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
             if (lane == 0) {
                 WarpAux& A = *W.aux;
                 A.nrhs = A.nni = A.nsetups = A.nje = A.netf = A.ncfn = 0;
+                A.nli = A.nps = A.njtv = 0;
                 A.flags = F_INIT; A.nsamp = 0;
                 A.ls_t = A.ls_v = A.pv_t = A.pv_v = A.bs_t = A.bs_v = A.nx_t = A.nx_v = 0.0;
             }
@@ -1307,6 +1918,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
                 A.nsamp = (int)rs[R_NSAMP];
                 A.flags = (int)rs[R_FLAGS];
                 A.nrhs = stt[1]; A.nni = stt[2]; A.nsetups = stt[3]; A.nje = stt[4]; A.netf = stt[5]; A.ncfn = stt[6];
+                if (kKry) { A.nli = kst[0]; A.nps = kst[1]; A.njtv = kst[2]; }
             }
             S.q = (int)rs[R_Q]; S.qprime = (int)rs[R_QPRIME]; S.qwait = (int)rs[R_QWAIT];
             S.nst = (int)rs[R_NST]; S.nstlp = (int)rs[R_NSTLP];
@@ -1328,14 +1940,36 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
         // output: interpolate to tout (or the last state on failure; the state at the new
         // internal time after one step)
         const double sfac = (status == ST_OK && S.h != 0.0 && !p.oneStep) ? ddiv(p.tout - S.tn, S.h) : 0.0;
+        if (kKry) {
+            // the state at tout, then mass fractions from the amounts: Y_k = n_k W_k / mass
+            double pm = 0.0;
 #pragma unroll 1
-        for (int i = lane; i < N; i += 32) {
-            double v = W.zn[(size_t)S.q * N + i];
+            for (int i = lane; i < N; i += 32) {
+                double v = W.zn[(size_t)S.q * N + i];
 #pragma unroll 1
-            for (int j = S.q - 1; j >= 0; j--) v = W.zn[(size_t)j * N + i] + sfac * v;
-            if (status != ST_OK) v = W.zn[i];
-            if (i == 0) p.T[r] = v;
-            else p.Y[(size_t)(i - 1) * p.n + r] = v;
+                for (int j = S.q - 1; j >= 0; j--) v = W.zn[(size_t)j * N + i] + sfac * v;
+                if (status != ST_OK) v = W.zn[i];
+                W.tempv[i] = v;
+                if (i > 0) pm += v * m.mw[i - 1];
+            }
+            const double rmass = 1.0 / warpSum(pm);
+#pragma unroll 1
+            for (int i = lane; i < N; i += 32) {
+                const double v = W.tempv[i];
+                if (i == 0) p.T[r] = v;
+                else p.Y[(size_t)(i - 1) * p.n + r] = v * m.mw[i - 1] * rmass;
+            }
+            __syncwarp();
+        } else {
+#pragma unroll 1
+            for (int i = lane; i < N; i += 32) {
+                double v = W.zn[(size_t)S.q * N + i];
+#pragma unroll 1
+                for (int j = S.q - 1; j >= 0; j--) v = W.zn[(size_t)j * N + i] + sfac * v;
+                if (status != ST_OK) v = W.zn[i];
+                if (i == 0) p.T[r] = v;
+                else p.Y[(size_t)(i - 1) * p.n + r] = v;
+            }
         }
         // save the integrator record
 #pragma unroll 1
@@ -1358,6 +1992,7 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
             o[R_NSTLP] = S.nstlp; o[R_NSAMP] = A.nsamp; o[R_FLAGS] = A.flags | F_INIT; o[R_STATUS] = status;
             stt[0] = S.nst; stt[1] = A.nrhs; stt[2] = A.nni; stt[3] = A.nsetups; stt[4] = A.nje;
             stt[5] = A.netf; stt[6] = A.ncfn; stt[7] = S.q;
+            if (kKry) { kst[0] = A.nli; kst[1] = A.nps; kst[2] = A.njtv; }
             p.status[r] = status;
             p.tign[r] = W.ignitionTime();
             if (p.tnow) p.tnow[r] = S.tn;
@@ -1407,18 +2042,18 @@ cudaError_t launchReactorRhsT(const RhsParams& p, int blocks, int warpsPerBlock,
     return cudaGetLastError();
 }
 
-template <typename MT, int NS, bool kX>
+template <typename MT, int NS, bool kX, bool kKry = false>
 cudaError_t launchBdfT(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
     size_t smem = (size_t)p.mechSmem + (size_t)p.warpDoubles * 8 * warpsPerBlock +
                   (size_t)(p.Mbuf ? p.luSlots : 0) * p.luSlotBytes;
-    cudaError_t e = cudaFuncSetAttribute(k_bdf<MT, NS, kX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_bdf<MT, NS, kX, kKry>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     // the rest of the SM's 256 KB of L1/shared storage is L1: ask for the smallest carveout
     // that holds the block (static tables and the per-block reservation included)
     const int pct = (int)std::min<size_t>(100, ((smem + 4096 + 1024) * 100 + 233471) / 233472);
-    e = cudaFuncSetAttribute(k_bdf<MT, NS, kX>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+    e = cudaFuncSetAttribute(k_bdf<MT, NS, kX, kKry>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
     if (e != cudaSuccess) return e;
-    k_bdf<MT, NS, kX><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
+    k_bdf<MT, NS, kX, kKry><<<blocks, 32 * warpsPerBlock, smem, stream>>>(p);
     return cudaGetLastError();
 }
 
@@ -1431,12 +2066,12 @@ cudaError_t launchRatesT(const RatesParams& p, int blocks, int warpsPerBlock, cu
     return cudaGetLastError();
 }
 
-template <typename MT, int NS, bool kX>
+template <typename MT, int NS, bool kX, bool kKry = false>
 int bdfBlocksPerSmT(int warpsPerBlock, size_t smem) {
     int nb = 0;
-    if (cudaFuncSetAttribute(k_bdf<MT, NS, kX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_bdf<MT, NS, kX, kKry>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bdf<MT, NS, kX>, 32 * warpsPerBlock, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bdf<MT, NS, kX, kKry>, 32 * warpsPerBlock, smem) != cudaSuccess)
         return 1;
     return nb > 0 ? nb : 1;
 }
@@ -1459,6 +2094,40 @@ cudaError_t launchBdfX(const BdfParams& p, int blocks, int warpsPerBlock, bool f
 int bdfBlocksPerSmX(bool fp32, int warpsPerBlock, size_t smem) {
     return fp32 ? bdfBlocksPerSmT<float, 8, true>(warpsPerBlock, smem)
                 : bdfBlocksPerSmT<double, 8, true>(warpsPerBlock, smem);
+}
+#elif defined(GB_KERNELS_KRYLOV)
+// The Krylov path's instantiations (krylov.cu): FP64 throughout, the preconditioner's factors
+// in the matrix slot; mechanisms with the less common rate forms use the widest register slots.
+cudaError_t launchBdfKrylov(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
+    if (p.m.NX) return launchBdfT<double, 8, true, true>(p, blocks, warpsPerBlock, stream);
+    const int N = p.m.N;
+    if (N <= 64) return launchBdfT<double, 2, false, true>(p, blocks, warpsPerBlock, stream);
+    if (N <= 128) return launchBdfT<double, 4, false, true>(p, blocks, warpsPerBlock, stream);
+    return launchBdfT<double, 8, false, true>(p, blocks, warpsPerBlock, stream);
+}
+int bdfBlocksPerSmKrylov(int N, bool extra, int warpsPerBlock, size_t smem) {
+    if (extra) return bdfBlocksPerSmT<double, 8, true, true>(warpsPerBlock, smem);
+    if (N <= 64) return bdfBlocksPerSmT<double, 2, false, true>(warpsPerBlock, smem);
+    if (N <= 128) return bdfBlocksPerSmT<double, 4, false, true>(warpsPerBlock, smem);
+    return bdfBlocksPerSmT<double, 8, false, true>(warpsPerBlock, smem);
+}
+
+// Batched incomplete factorisation: one warp per matrix (grid-stride), each stored transposed
+// in a[m][N][ld] and factored in place, its reciprocal pivots to dinv[m][N]; rn[m][N] scratch.
+template <int S>
+__global__ void __launch_bounds__(256) k_ilut(int n, int N, int ld, double* a, double* dinv, double* rn) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int r = blockIdx.x * wpb + (threadIdx.x >> 5); r < n; r += gridDim.x * wpb)
+        devIlut<S>(a + (size_t)r * N * ld, N, ld, dinv + (size_t)r * N, rn + (size_t)r * N, lane);
+}
+cudaError_t launchIlut(int n, int N, int ld, double* a, double* dinv, double* rn, cudaStream_t stream) {
+    const int blocks = std::max(1, std::min((n + 7) / 8, 4096));
+    if (N <= 64) k_ilut<2><<<blocks, 256, 0, stream>>>(n, N, ld, a, dinv, rn);
+    else if (N <= 128) k_ilut<4><<<blocks, 256, 0, stream>>>(n, N, ld, a, dinv, rn);
+    else if (N <= 256) k_ilut<8><<<blocks, 256, 0, stream>>>(n, N, ld, a, dinv, rn);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
 }
 #else
 int rhsWarpDoubles(const DevMech& m) {
@@ -1489,6 +2158,8 @@ int bdfWarpDoublesNoMatrix(const DevMech& m) {
     int vec = 8 * N + (N + 1) / 2 + kAuxDoubles;   // the Nordsieck array is in the global slot
     return (kinD + vec + 1) & ~1;
 }
+
+int bdfKrylovDoubles(int N) { return (((kMaxl + 1) * N + kGmresScalars) + 1) & ~1; }
 
 int ratesWarpDoubles(const DevMech& m, bool jac) {
     int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);

@@ -75,6 +75,8 @@ struct BdfParams {
     int oneStep;          // 1: each reactor takes one internal step (its state at the new
                           // internal time is written, no interpolation); 0: step past tout
     double* tnow;         // [n] internal time of each reactor after the launch (or null)
+    long long* kstats;    // Krylov path: [n][3] linear iterations, preconditioner solves,
+                          // J v products (null otherwise)
 };
 
 constexpr int kBdfMaxThreads = 256;   // at most 8 warps per block
@@ -94,6 +96,15 @@ cudaError_t launchReactorRhsX(const RhsParams& p, int blocks, int warpsPerBlock,
 cudaError_t launchRatesX(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
 cudaError_t launchBdfX(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream);
 int bdfBlocksPerSmX(bool fp32, int warpsPerBlock, size_t smem);
+// the Krylov path (krylov.cu): the mole reactor with GMRES and the adaptive preconditioner;
+// its per-warp slice adds bdfKrylovDoubles(N) doubles (the Krylov basis and GMRES scalars),
+// Jbuf (the preconditioner's Jacobian) is required and the matrix slot holds its factors
+int bdfKrylovDoubles(int N);
+cudaError_t launchBdfKrylov(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
+int bdfBlocksPerSmKrylov(int N, bool extra, int warpsPerBlock, size_t smem);
+// batched ILUT of n matrices stored transposed in a[n][N][ld] (in place), reciprocal pivots
+// to dinv[n][N], rn[n][N] scratch (device pointers)
+cudaError_t launchIlut(int n, int N, int ld, double* a, double* dinv, double* rn, cudaStream_t stream);
 // FP64 throughput probe: returns {GFLOP/s of FMA, exp cost, log cost in FMA-equivalents}
 cudaError_t measureFp64(double* results, int smCount);
 cudaError_t checkExp(int n, const double* x, double* mine, double* lib);

@@ -332,14 +332,31 @@ GB_TU_LOCAL __device__ __noinline__ double rateExtra(const DevMech& m, int4 info
 // argument per lane (1/T, 1/sum(Y/W), 1/RT, 1/P and ln T, ln P, ln RT, ln Pref), then
 // broadcast: a double division costs the FP64 pipe the same whether one lane or all 32
 // need it.  The logarithm runs on the integer pipe (fastexp.h).
+// kMoles: the third argument holds species amounts n_k (kmol) instead of mass fractions, as
+// the state of IdealGasConstPressureMoleReactor (src/zeroD/IdealGasConstPressureMoleReactor.cpp:
+// 34-51: the mass from the amounts, then the mixture at T, P); Y_k/W_k = n_k / mass.
+template <bool kMoles = false>
 __device__ __forceinline__ void warpState(const DevMech& m, double T, double P, const double* Y,
                                           KinScratch& s, KinState& st, int lane) {
     double part = 0.0;
+    if (kMoles) {
+        double pm = 0.0;
 #pragma unroll 1
-    for (int k = lane; k < m.K; k += 32) {
-        double ym = Y[k] * m.rmw[k];
-        s.c[k] = ym;
-        part += ym;
+        for (int k = lane; k < m.K; k += 32) pm += Y[k] * m.mw[k];
+        const double rmass = 1.0 / warpSum(pm);
+#pragma unroll 1
+        for (int k = lane; k < m.K; k += 32) {
+            const double ym = Y[k] * rmass;
+            s.c[k] = ym;
+            part += ym;
+        }
+    } else {
+#pragma unroll 1
+        for (int k = lane; k < m.K; k += 32) {
+            double ym = Y[k] * m.rmw[k];
+            s.c[k] = ym;
+            part += ym;
+        }
     }
     const double sum = warpSum(part);
     const double RT = T * m.Rgas;

@@ -108,6 +108,18 @@ typedef struct {
                                shared-memory buffers a block keeps for that (a warp that finds
                                none free factors in place): 0 = automatic (none: the buffers
                                take L1 capacity the global matrices need), k > 0 = at most k */
+    int32_t linear_solver;  /* 0 (default): the mass-fraction reactor [T, Y] with the analytic
+                               Jacobian and a dense LU of I - gamma*J.  1: the reference's
+                               preconditioned Krylov path - IdealGasConstPressureMoleReactor
+                               (state T and the species amounts in kmol, an initial volume of
+                               1 m^3; src/zeroD/IdealGasConstPressureMoleReactor.cpp:34-104)
+                               with ReactorNet's GMRES solver and the AdaptivePreconditioner
+                               (src/zeroD/ReactorNet.cpp:881-908, src/numerics/
+                               AdaptivePreconditioner.cpp:17-81; Python: net.preconditioner =
+                               AdaptivePreconditioner()): an approximate Jacobian (ddCi species
+                               block, difference T column, enthalpy T row) factored by ILUT,
+                               J v by difference quotients.  Needs lu_precision 64; the state
+                               handed in and out stays T and mass fractions. */
 } gb_net_options;
 
 void gb_net_default_options(gb_net_options* opts);
@@ -170,6 +182,19 @@ int32_t gb_net_get_status(int32_t net, int32_t* status);
 enum { GB_STAT_STEPS = 0, GB_STAT_RHS, GB_STAT_NEWTON, GB_STAT_SETUPS, GB_STAT_JACS,
        GB_STAT_ERRFAIL, GB_STAT_CONVFAIL, GB_STAT_ORDER, GB_NSTAT };
 int32_t gb_net_solver_stats(int32_t net, int64_t* stats);
+
+/* Counters of the Krylov path per reactor, stats[s*3 + i]: linear (GMRES) iterations,
+ * preconditioner solves, Jacobian-times-vector products (CVodesIntegrator::solverStats
+ * lin_iters, prec_solves, jt_vec_prod_evals; src/numerics/CVodesIntegrator.cpp:572-621).
+ * GB_ERR for a network with the dense solver. */
+int32_t gb_net_krylov_stats(int32_t net, int64_t* stats);
+
+/* Batched incomplete factorisation of the adaptive preconditioner (AdaptivePreconditioner::
+ * factorize, src/numerics/AdaptivePreconditioner.cpp:42-55, with the ILUT parameters it sets,
+ * :24-38): n matrices P[n][N][N] (row-major, host) are factored by ILUT(p, tau) with
+ * tau = 1e-12 and p = 10 nnz(P)/N + 1, one warp per matrix on the current device; F[n][N][N]
+ * (host) receives L (unit diagonal, strictly lower part) and U in place.  N <= 256. */
+int32_t gb_precond_ilut(int32_t n, int32_t N, const double* P, double* F);
 
 /* Time of the largest dT/dt seen at accepted steps since gb_net_set_state, refined by the
  * vertex of the parabola through that step and its accepted neighbours. */

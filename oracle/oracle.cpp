@@ -673,6 +673,54 @@ constexpr double DGMAX_JBAD = 0.2;
 
 enum { ST_OK = 0, ST_MAX_STEPS = 1, ST_ERR_FAIL = 2, ST_CONV_FAIL = 3, ST_NONFINITE = 4, ST_H_TOO_SMALL = 5 };
 
+// ILUT(p, tau), the dual-threshold incomplete LU of Saad (1994), row by row, with the
+// parameters the reference's AdaptivePreconditioner leaves Eigen's IncompleteLUT
+// (AdaptivePreconditioner.cpp:24-38: drop tolerance 1e-12; its fill factor is set only when
+// no drop tolerance was, so Eigen's default of 10 holds): a multiplier at or below tau is
+// dropped, then the entries of the row below tau times its 2-norm, then all but the p
+// largest of its L and of its U part, p = 10 nnz(P) / N + 1.  A zero pivot becomes a small
+// multiple of the row norm.  Eigen's fill-reducing ordering ahead of the factorisation is
+// left out (it changes what is dropped, not what the preconditioner approximates).
+void ilutFactor(int N, double* a) {
+    const double tau = 1e-12;
+    long nnz = 0;
+    for (size_t i = 0; i < (size_t)N * N; i++) nnz += a[i] != 0.0;
+    const int fill = (int)(nnz * 10 / N) + 1;
+    std::vector<double> w(N);
+    std::vector<std::pair<double, int>> e;
+    for (int i = 0; i < N; i++) {
+        double rn = 0.0;
+        for (int j = 0; j < N; j++) { w[j] = a[(size_t)i * N + j]; rn += w[j] * w[j]; }
+        rn = std::sqrt(rn);
+        for (int k = 0; k < i; k++) {
+            if (w[k] == 0.0) continue;
+            const double f = w[k] / a[(size_t)k * N + k];
+            if (std::fabs(f) <= tau) { w[k] = 0.0; continue; }
+            w[k] = f;
+            for (int j = k + 1; j < N; j++) {
+                const double u = a[(size_t)k * N + j];
+                if (u != 0.0) w[j] -= f * u;
+            }
+        }
+        auto keep = [&](int j0, int j1) {
+            e.clear();
+            for (int j = j0; j < j1; j++) {
+                if (std::fabs(w[j]) > tau * rn) e.push_back({std::fabs(w[j]), j});
+                else w[j] = 0.0;
+            }
+            if ((int)e.size() > fill) {
+                std::nth_element(e.begin(), e.begin() + fill, e.end(),
+                                 [](const std::pair<double, int>& x, const std::pair<double, int>& y) { return x.first > y.first; });
+                for (size_t q = fill; q < e.size(); q++) w[e[q].second] = 0.0;
+            }
+        };
+        keep(0, i);
+        keep(i + 1, N);
+        if (w[i] == 0.0) w[i] = std::sqrt(tau) * rn;
+        for (int j = 0; j < N; j++) a[(size_t)i * N + j] = w[j];
+    }
+}
+
 struct Bdf {
     System* r = nullptr;
     int N = 0;            // integrated components (K+1)
@@ -900,53 +948,7 @@ struct Bdf {
         return 0;
     }
 
-    // ILUT(p, tau), the dual-threshold incomplete LU of Saad (1994), row by row, with the
-    // parameters the reference's AdaptivePreconditioner leaves Eigen's IncompleteLUT
-    // (AdaptivePreconditioner.cpp:24-38: drop tolerance 1e-12; its fill factor is set only when
-    // no drop tolerance was, so Eigen's default of 10 holds): a multiplier at or below tau is
-    // dropped, then the entries of the row below tau times its 2-norm, then all but the p
-    // largest of its L and of its U part, p = 10 nnz(P) / N + 1.  A zero pivot becomes a small
-    // multiple of the row norm.  Eigen's fill-reducing ordering ahead of the factorisation is
-    // left out (it changes what is dropped, not what the preconditioner approximates).
-    void ilut(double* a) const {
-        const double tau = 1e-12;
-        long nnz = 0;
-        for (size_t i = 0; i < (size_t)N * N; i++) nnz += a[i] != 0.0;
-        const int fill = (int)(nnz * 10 / N) + 1;
-        std::vector<double> w(N);
-        std::vector<std::pair<double, int>> e;
-        for (int i = 0; i < N; i++) {
-            double rn = 0.0;
-            for (int j = 0; j < N; j++) { w[j] = a[(size_t)i * N + j]; rn += w[j] * w[j]; }
-            rn = std::sqrt(rn);
-            for (int k = 0; k < i; k++) {
-                if (w[k] == 0.0) continue;
-                const double f = w[k] / a[(size_t)k * N + k];
-                if (std::fabs(f) <= tau) { w[k] = 0.0; continue; }
-                w[k] = f;
-                for (int j = k + 1; j < N; j++) {
-                    const double u = a[(size_t)k * N + j];
-                    if (u != 0.0) w[j] -= f * u;
-                }
-            }
-            auto keep = [&](int j0, int j1) {
-                e.clear();
-                for (int j = j0; j < j1; j++) {
-                    if (std::fabs(w[j]) > tau * rn) e.push_back({std::fabs(w[j]), j});
-                    else w[j] = 0.0;
-                }
-                if ((int)e.size() > fill) {
-                    std::nth_element(e.begin(), e.begin() + fill, e.end(),
-                                     [](const std::pair<double, int>& x, const std::pair<double, int>& y) { return x.first > y.first; });
-                    for (size_t q = fill; q < e.size(); q++) w[e[q].second] = 0.0;
-                }
-            };
-            keep(0, i);
-            keep(i + 1, N);
-            if (w[i] == 0.0) w[i] = std::sqrt(tau) * rn;
-            for (int j = 0; j < N; j++) a[(size_t)i * N + j] = w[j];
-        }
-    }
+    void ilut(double* a) const { ilutFactor(N, a); }
     void precSolve(double* x) {
         nps++;
         const double* a = Pf.data();
@@ -1689,6 +1691,12 @@ int32_t or_mole_reactor_rhs(int32_t h, double P, const double* z, double* zdot) 
     if (!k) return -1;
     MoleReactor r(k, P);
     return r.rhs(z, zdot);
+}
+
+int32_t or_ilut(int32_t N, double* a) {
+    if (N <= 0 || !a) return -1;
+    ilutFactor(N, a);
+    return 0;
 }
 
 int32_t or_mole_precond_jacobian(int32_t h, double P, const double* z, double atol, double* J) {

@@ -101,6 +101,9 @@ int32_t or_reactor_rhs(int32_t h, double P, const double* y, double* ydot);
 // preconditioner's Jacobian elements J[(K+1)^2] (row-major) at z clipped below at atol.
 int32_t or_mole_reactor_rhs(int32_t h, double P, const double* z, double* zdot);
 int32_t or_mole_precond_jacobian(int32_t h, double P, const double* z, double atol, double* J);
+/* The adaptive preconditioner's ILUT (the factorisation the Krylov path uses) of one N x N
+ * row-major matrix, in place: L (unit diagonal, strictly lower) and U. */
+int32_t or_ilut(int32_t N, double* a);
 
 // Advance n independent constant-pressure reactors from t=0 to t_end.
 //  T0[n], P[n], Y0[n][K] (reactor-major); outputs T[n], Y[n][K], stats[n][OR_NSTAT],

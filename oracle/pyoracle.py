@@ -98,6 +98,8 @@ def lib(fast=False):
         L.or_reactor_rhs.argtypes = [I32, ctypes.c_double, D, D]
         L.or_mole_reactor_rhs.argtypes = [I32, ctypes.c_double, D, D]
         L.or_mole_precond_jacobian.argtypes = [I32, ctypes.c_double, D, ctypes.c_double, D]
+        L.or_ilut.argtypes = [I32, D]
+        L.or_ilut.restype = I32
         L.or_equivalence_ratio.argtypes = [I32, ctypes.c_double, D, D, D]
         L.or_mole_to_mass.argtypes = [I32, D, D]
         L.or_molecular_weights.argtypes = [I32, D]
@@ -251,3 +253,13 @@ class Mech:
                                         ctypes.byref(t),
                                         st.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
         return t.value, st, rc
+
+
+def ilut(A, fast=False):
+    """The adaptive preconditioner's ILUT of one N x N matrix (row-major copy): L (unit
+    diagonal, strictly lower part) and U in one array."""
+    a = np.array(A, dtype=np.float64, order="C", copy=True)
+    n = a.shape[0]
+    if lib(fast).or_ilut(n, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) != 0:
+        raise RuntimeError("or_ilut failed")
+    return a
