@@ -542,8 +542,8 @@ def variant_ndodecane(dev, torch, flush, threads, n=16384, sample=64):
     Td, Pd, Yd = (torch.tensor(a, device=dev) for a in (T0, P, np.ascontiguousarray(Y0.T)))
     idx = cpu_sample_indices(n, sample, 20261203 + 3)
     res, gpu = {}, {}
-    for name, lu in (("fp64", 64), ("fp32_lu", 32)):
-        net = gb.ReactorNet(sol, Td, Pd, Yd, rtol=rtol, atol=atol, lu_precision=lu)
+    for name, lu, solver in (("fp64", 64, "DENSE"), ("fp32_lu", 32, "DENSE"), ("gmres", 64, "GMRES")):
+        net = gb.ReactorNet(sol, Td, Pd, Yd, rtol=rtol, atol=atol, lu_precision=lu, linear_solver=solver)
         net.advance(1e-7)          # untimed first launch (module load, attributes)
         bad, ms, wall = time_advance(net, Td, Pd, Yd, t_end, flush, torch)
         Tg, Yg = net.get_state()
@@ -552,6 +552,10 @@ def variant_ndodecane(dev, torch, flush, threads, n=16384, sample=64):
                      "failed_reactors": int(bad), "launch": net.launch_info,
                      "newton_iters_mean": float(st["newton_iters"].mean()), "steps_mean": float(st["steps"].mean()),
                      "solver_stats_mean": {k: float(v.mean()) for k, v in st.items()}}
+        if solver == "GMRES":
+            res[name]["solver_stats_mean"].update({k: float(v.mean()) for k, v in net.krylov_stats.items()})
+            res[name]["method"] = ("IdealGasConstPressureMoleReactor with GMRES and the adaptive preconditioner "
+                                   "(ILUT of I - gamma Jp), FP64")
         gpu[name] = (Tg[idx], Yg[:, idx].T, net.ignition_times[idx])
         del net
     m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "nDodecane_Reitz.yaml"), "nDodecane_IG")
@@ -560,7 +564,7 @@ def variant_ndodecane(dev, torch, flush, threads, n=16384, sample=64):
     t0 = time.perf_counter()
     mf.advance_batch(T0[idx], P[idx], Y0[idx], t_end, oracle_opts(po, rtol, atol), threads=threads)
     cpu = len(idx) / (time.perf_counter() - t0)
-    return dict(res["fp64"], variants={"fp32_lu": res["fp32_lu"]},
+    return dict(res["fp64"], variants={"fp32_lu": res["fp32_lu"], "gmres": res["gmres"]},
                 config={"workload": "nDodecane_IG (K=100, R=553), %d reactors, T0 U[700,1400] K, P log-U[10,60] atm, "
                                     "phi U[0.5,2.0], to 5e-3 s" % n, "rtol": rtol, "atol": atol,
                         "seed": 20261206, "l2": "flushed (256 MB write) before the timed advance"},
@@ -639,6 +643,8 @@ def main():
                     help="states or reactors of the workload (default: the workload's own size)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-gmres", action="store_true",
+                    help="skip the Krylov-path variant (mole reactor, GMRES, adaptive preconditioner)")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-workloads", action="store_true",
                     help="skip the other workloads (h2o2, rates, n-dodecane) of the default run")
@@ -696,13 +702,13 @@ def main():
         from cantera_gb300.tuning import autotune
         tuned, tune_log = autotune(sol, dT, dP, dY, WL["t_end"] / 10)
     results = {}
-    for variant, lu in (("fp64", 64), ("fp32_lu", 32)):
-        if variant == "fp32_lu" and args.no_fp32:
+    for variant, lu, solver in (("fp64", 64, "DENSE"), ("fp32_lu", 32, "DENSE"), ("gmres", 64, "GMRES")):
+        if (variant == "fp32_lu" and args.no_fp32) or (variant == "gmres" and args.no_gmres):
             continue
-        shape = dict(tuned) if lu == 64 else {}
+        shape = dict(tuned) if variant == "fp64" else {}
         shape.setdefault("matrix_placement", args.matrix_placement)
         net = gb.ReactorNet(sol, dT, dP, dY, rtol=WL["rtol"], atol=WL["atol"], lu_precision=lu, use_graph=True,
-                            lu_staging=args.lu_staging, **shape)
+                            lu_staging=args.lu_staging, linear_solver=solver, **shape)
         launch = net.launch_info
         for _ in range(args.warmup if variant == "fp64" else 1):
             net.set_state(dT, dP, dY)
@@ -732,6 +738,8 @@ def main():
                             "f64": f64, "f32": f32, "clocks": clk.summary(), "T": Tg, "Y": Yg,
                             "tign": net.ignition_times,
                             "stats": {k: float(v.mean()) for k, v in stats.items()}}
+        if solver == "GMRES":
+            results[variant]["stats"].update({k: float(v.mean()) for k, v in net.krylov_stats.items()})
         del net
 
     # end to end through the public API with host buffers: every step the H2D copy of the
@@ -798,12 +806,16 @@ def main():
             "solver_stats_mean": r64["stats"], "failed_reactors": r64["failed"],
             "e2e": {"value": n_all * e2e_steps / (e2e_ms / 1e3), "unit": "reactors/s", "steps": e2e_steps,
                     "h2d_bytes_per_step": n * (2 + K) * 8, "d2h_bytes_per_step": n * (1 + K) * 8}}
-    if "fp32_lu" in results:
-        r32 = results["fp32_lu"]
-        line["variants"] = {"fp32_lu": {"value": n_all * r32["steps"] / (r32["ms"] / 1e3), "unit": "reactors/s",
-                                        "ms_per_step": r32["ms"] / r32["steps"],
-                                        "solver_stats_mean": r32["stats"], "failed_reactors": r32["failed"],
-                                        "clocks": r32["clocks"]}}
+    for vname in ("fp32_lu", "gmres"):
+        if vname in results:
+            rv = results[vname]
+            line.setdefault("variants", {})[vname] = {
+                "value": n_all * rv["steps"] / (rv["ms"] / 1e3), "unit": "reactors/s",
+                "ms_per_step": rv["ms"] / rv["steps"], "solver_stats_mean": rv["stats"],
+                "failed_reactors": rv["failed"], "launch": rv["launch"], "clocks": rv["clocks"]}
+    if "gmres" in results:
+        line["variants"]["gmres"]["method"] = ("IdealGasConstPressureMoleReactor with GMRES and the adaptive "
+                                              "preconditioner (ILUT of I - gamma Jp), FP64")
     threads = os.cpu_count()
     # the other workloads of the hot path (their own configurations), each with its errors
     # and its CPU baseline

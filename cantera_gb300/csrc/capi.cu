@@ -440,6 +440,8 @@ void packDevMech(MechEntry& e) {
     size_t o_spPtr = a.add(spPtr), o_tbRxn = a.add(tbRxn), o_tbMA = a.add(tbMA);
     size_t o_jcPtr = a.add(jcPtr), o_jrIdx = a.add(jrIdx), o_jpCol = a.add(jpCol);
     size_t o_pdep = a.add(pdep);
+    const std::vector<int32_t> precOrder = preconditionerOrdering(m);
+    size_t o_precOrder = a.add(precOrder);
     e.arena.ensure(a.data.size());
     ck(cudaMemcpy(e.arena.p, a.data.data(), a.data.size(), cudaMemcpyHostToDevice), "upload mechanism");
     char* b = e.arena.as<char>();
@@ -470,6 +472,7 @@ void packDevMech(MechEntry& e) {
     d.jcPtr = (const int*)(b + o_jcPtr); d.jrIdx = (const int*)(b + o_jrIdx); d.jpCol = (const int*)(b + o_jpCol);
     d.pdep = (const double*)(b + o_pdep);
     d.colSlotStart = (const int*)(b + o_colSlotStart); d.colSlot = (const int*)(b + o_colSlot);
+    d.precOrder = (const int*)(b + o_precOrder);
 }
 
 // dynamic shared memory a block may use: the opt-in maximum less the kernels' static

@@ -113,6 +113,9 @@ struct DevMech {
     // jcPtr/jrIdx, or -1
     const int* colSlotStart;     // [K+1]
     const int* colSlot;
+    // fill-reducing ordering of the Krylov path's preconditioner over z = [T, n]: precOrder[new]
+    // = old, N entries (preconditionerOrdering)
+    const int* precOrder;
     // bounds-check record of the checked build (GBCHEM_CHECKED): first failing site, its
     // index, its bound; written only by the checked build's kernels
     int* chk;
@@ -156,7 +159,7 @@ enum { GB_SITE_SPECIES = 1, GB_SITE_SIDE = 2, GB_SITE_TB_SPECIES = 3, GB_SITE_TB
     X(rsPtr) X(rsK) X(rsNu) X(fo1) X(fo2) X(tbRxn) X(tbDef) X(tbMA) X(tbPtr) X(tbK) X(tbE) \
     X(spPtr) X(spRxn) X(spNu) X(taskPtr) X(laneTaskPtr) X(laneTasks) X(spTaskPtr) X(spTasks) \
     X(colPtr) X(colRxn) X(colE) X(laneColPtr) X(laneCols) X(gsPtr) X(gsTb) X(gsCoef) \
-    X(jcPtr) X(jrIdx) X(jpCol) X(pdep) X(colSlotStart) X(colSlot)
+    X(jcPtr) X(jrIdx) X(jpCol) X(pdep) X(colSlotStart) X(colSlot) X(precOrder)
 
 #ifdef __CUDACC__
 // Point the arrays that lie in the first `bytes` of the arena at a copy of that prefix

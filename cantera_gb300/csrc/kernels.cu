@@ -955,19 +955,23 @@ __device__ __noinline__ void devIlut(double* a, int N, int ld, double* dinv, dou
     }
 }
 
-// Solve (L U) x = b in place with the factors of devIlut: L w = b forward (unit lower; column
-// k of L is row k of a), then U x = w backward (column j of U is row j of a, its diagonal
-// from dinv).  The vector lives in registers (element i in lane i % 32, slot i / 32); every
+// Solve (L U) x' = b' in place with the factors of devIlut of the reordered matrix, b'[i] =
+// b[q[i]] and b[q[i]] = x'[i] (q: the fill-reducing order): L w = b' forward (unit lower;
+// column k of L is row k of a), then U x' = w backward (column j of U is row j of a, its
+// diagonal from dinv).  The vector lives in registers (element i in lane i % 32, slot i / 32); every
 // substitution step broadcasts one element by a shuffle.  The factors are usually in L2 (one
 // matrix per resident warp), so the rows of the next kIluAhead steps are in flight meanwhile.
 constexpr int kIluAhead = 4;
 template <int S>
-__device__ __noinline__ void devIluSolve(const double* a, double* b, int N, int ld, const double* dinv, int lane) {
+__device__ __noinline__ void devIluSolve(const double* a, double* b, int N, int ld, const double* dinv, const int* q,
+                                         int lane) {
     double x[S], nr[kIluAhead][S];
+    int qi[S];
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        x[t] = (i < N) ? b[i] : 0.0;
+        qi[t] = (i < N) ? q[i] : 0;
+        x[t] = (i < N) ? b[qi[t]] : 0.0;
     }
 #pragma unroll
     for (int p = 0; p < kIluAhead; p++) {
@@ -1047,7 +1051,7 @@ __device__ __noinline__ void devIluSolve(const double* a, double* b, int N, int 
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        if (i < N) b[i] = x[t];
+        if (i < N) b[qi[t]] = x[t];
     }
     __syncwarp();
 }
@@ -1111,16 +1115,22 @@ struct BdfWarp {
                 S.haveJ = ok;
                 if (!ok) return false;
             }
+            // P' = Q P Q^T in the fill-reducing order (Eigen's IncompleteLUT orders the matrix
+            // before the factorisation), stored transposed: M[b][a] = P[q[a]][q[b]] =
+            // delta - gamma Jp^T[q[b]][q[a]]
             const double g = S.gamma;
+            const int* q = m->precOrder;
 #pragma unroll 1
-            for (int j = 0; j < N; j++) {
-                const double* src = Jsv + (size_t)j * ld;
-                MT* dst = M + (size_t)j * ld;
+            for (int b = 0; b < N; b++) {
+                const int jb = q[b];
+                const double* src = Jsv + (size_t)jb * ld;
+                MT* dst = M + (size_t)b * ld;
 #pragma unroll 1
-                for (int i = lane; i < N; i += 32) {
-                    double v = -g * src[i];
-                    if (i == j) v += 1.0;
-                    dst[i] = (MT)v;
+                for (int a = lane; a < N; a += 32) {
+                    const int ia = q[a];
+                    double v = -g * src[ia];
+                    if (ia == jb) v += 1.0;
+                    dst[a] = (MT)v;
                 }
             }
             __syncwarp();
@@ -1175,7 +1185,7 @@ struct BdfWarp {
     template <int NS>
     __device__ void precSolve(const double* Ft, double* x) {
         if (lane == 0) aux->nps++;
-        devIluSolve<NS>(Ft, x, N, ld, dinv, lane);
+        devIluSolve<NS>(Ft, x, N, ld, dinv, m->precOrder, lane);
     }
     // (I - gamma J) x = b in place by right-preconditioned GMRES, as CVODE's iterative
     // linear-solver interface runs SUNDIALS' SPGMR for the reference's preconditioned solver

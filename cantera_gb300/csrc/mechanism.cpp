@@ -1012,6 +1012,44 @@ void equivalenceRatioMassFractions(const Mechanism& m, double phi, const double*
     for (int k = 0; k < K; k++) Y[k] /= tot;
 }
 
+std::vector<int32_t> preconditionerOrdering(const Mechanism& m) {
+    const int K = m.K, N = K + 1;
+    std::vector<int32_t> cp, ri;
+    jacobianPattern(m, cp, ri);
+    // symmetric structure of Jp + Jp^T over z = [T, n_1..n_K]: the species block's pattern, the
+    // dense T row and column
+    std::vector<std::vector<char>> adj(N, std::vector<char>(N, 0));
+    for (int i = 1; i < N; i++) adj[0][i] = adj[i][0] = 1;
+    for (int c = 0; c < K; c++)
+        for (int q = cp[c]; q < cp[c + 1]; q++) {
+            const int r = ri[q];
+            if (r != c) adj[1 + r][1 + c] = adj[1 + c][1 + r] = 1;
+        }
+    // greedy minimum degree: eliminate the remaining node of least degree (ties: the lowest
+    // index), joining its remaining neighbours into a clique (the fill its elimination makes)
+    std::vector<char> alive(N, 1);
+    std::vector<int32_t> order;
+    order.reserve(N);
+    for (int step = 0; step < N; step++) {
+        int best = -1, bestDeg = N + 1;
+        for (int v = 0; v < N; v++) {
+            if (!alive[v]) continue;
+            int d = 0;
+            for (int u = 0; u < N; u++) d += alive[u] && adj[v][u];
+            if (d < bestDeg) { bestDeg = d; best = v; }
+        }
+        std::vector<int> nb;
+        for (int u = 0; u < N; u++)
+            if (alive[u] && adj[best][u]) nb.push_back(u);
+        for (int a : nb)
+            for (int b : nb)
+                if (a != b) adj[a][b] = 1;
+        alive[best] = 0;
+        order.push_back(best);
+    }
+    return order;
+}
+
 void jacobianPattern(const Mechanism& m, std::vector<int32_t>& colPtr, std::vector<int32_t>& rowIdx) {
     std::vector<std::set<int>> cols(m.K);
     for (int i = 0; i < m.R; i++) {

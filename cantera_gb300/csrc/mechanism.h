@@ -133,4 +133,10 @@ void equivalenceRatioMassFractions(const Mechanism& m, double phi, const double*
 // returned as compressed sparse columns: colPtr[K+1], rowIdx[nnz], rows ascending.
 void jacobianPattern(const Mechanism& m, std::vector<int32_t>& colPtr, std::vector<int32_t>& rowIdx);
 
+// Fill-reducing ordering of the Krylov path's preconditioner I - gamma Jp over z = [T, n_1..n_K]
+// (the reference factors it with Eigen's IncompleteLUT, which orders the matrix first): a
+// greedy minimum-degree ordering of the symmetric structure of Jp + Jp^T (species block from
+// jacobianPattern, dense T row and column), ties to the lowest index.  order[new] = old.
+std::vector<int32_t> preconditionerOrdering(const Mechanism& m);
+
 }  // namespace gbchem

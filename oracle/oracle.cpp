@@ -140,6 +140,7 @@ struct Kin {
     std::vector<double> rmw;    // 1/mw
     std::vector<int> revIndex, irrev;
     double R_gas;
+    std::vector<int32_t> precOrder;   // fill-reducing ordering of the Krylov path's preconditioner
 };
 
 struct Work {  // per-thread scratch for one state
@@ -679,8 +680,10 @@ enum { ST_OK = 0, ST_MAX_STEPS = 1, ST_ERR_FAIL = 2, ST_CONV_FAIL = 3, ST_NONFIN
 // no drop tolerance was, so Eigen's default of 10 holds): a multiplier at or below tau is
 // dropped, then the entries of the row below tau times its 2-norm, then all but the p
 // largest of its L and of its U part, p = 10 nnz(P) / N + 1.  A zero pivot becomes a small
-// multiple of the row norm.  Eigen's fill-reducing ordering ahead of the factorisation is
-// left out (it changes what is dropped, not what the preconditioner approximates).
+// multiple of the row norm.  The integrator factors its preconditioner in a fill-reducing
+// order, as Eigen's IncompleteLUT orders the matrix first (there AMD; here the greedy minimum
+// degree of preconditionerOrdering, which the engine uses too): the drops are below 1e-12 of a
+// row's norm, so the order changes the factorisation's cost, not the preconditioner.
 void ilutFactor(int N, double* a) {
     const double tau = 1e-12;
     long nnz = 0;
@@ -740,6 +743,7 @@ struct Bdf {
     bool haveJ = false;
     // GMRES with the adaptive preconditioner (linear_solver = 1)
     std::vector<double> Jp, Pf;        // preconditioner Jacobian (kept between setups), factors of I - gamma Jp
+    const int32_t* qord = nullptr;     // the preconditioner's ordering (order[new] = old), or null
     long nli = 0, nps = 0, njtv = 0;    // linear iterations, preconditioner solves, J v products
     bool jcur = false, haveLU = false;
     // ignition tracking (see recordSample)
@@ -937,8 +941,13 @@ struct Bdf {
             jcur = false;
         }
         nsetups++;
-        for (size_t i = 0; i < (size_t)N * N; i++) Pf[i] = -gamma * Jp[i];
-        for (int i = 0; i < N; i++) Pf[(size_t)i * N + i] += 1.0;
+        // P' = Q P Q^T in the fill-reducing order (Eigen's IncompleteLUT, which the reference's
+        // preconditioner uses, orders the matrix before the factorisation)
+        for (int a = 0; a < N; a++)
+            for (int b = 0; b < N; b++) {
+                const int i = qord ? qord[a] : a, j = qord ? qord[b] : b;
+                Pf[(size_t)a * N + b] = -gamma * Jp[(size_t)i * N + j] + (i == j ? 1.0 : 0.0);
+            }
         ilut(Pf.data());
         gammap = gamma;
         gamrat = 1.0;
@@ -949,9 +958,12 @@ struct Bdf {
     }
 
     void ilut(double* a) const { ilutFactor(N, a); }
-    void precSolve(double* x) {
+    void precSolve(double* xo) {
         nps++;
         const double* a = Pf.data();
+        std::vector<double> xv(N);
+        for (int i = 0; i < N; i++) xv[i] = xo[qord ? qord[i] : i];
+        double* x = xv.data();
         for (int i = 0; i < N; i++) {
             double s = x[i];
             for (int k = 0; k < i; k++) s -= a[(size_t)i * N + k] * x[k];
@@ -962,6 +974,7 @@ struct Bdf {
             for (int j = i + 1; j < N; j++) s -= a[(size_t)i * N + j] * x[j];
             x[i] = s / a[(size_t)i * N + i];
         }
+        for (int i = 0; i < N; i++) xo[qord ? qord[i] : i] = x[i];
     }
     // J v by the difference quotient (f(y + sig v) - f(y)) / sig, sig = 1 / ||v||_wrms, sig
     // shrunk by 1/4 (at most three tries) when f fails recoverably (CVODE's default
@@ -1487,6 +1500,7 @@ Kin* buildKin(const std::string& path, const std::string& phase) {
         if (m.reversible[i]) { kn->revIndex.push_back(i); kn->revProd.add(i, pk, pnu, pnu); }
         else kn->irrev.push_back(i);
     }
+    kn->precOrder = preconditionerOrdering(m);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     g_kins.push_back(std::move(kn));
     return g_kins.back().get();
@@ -1536,6 +1550,7 @@ int runReactor(const Kin* kn, double T0, double P, const double* Y0, double t_en
         for (int k = 0; k < K; k++) z0[1 + k] = Y0[k];
     }
     Bdf b;
+    if (o.linear_solver == 1) b.qord = kn->precOrder.data();
     b.init(o.mole_reactor ? (System*)&mr : (System*)&r, z0.data(), o, t_end);
     long steps = 0;
     int st = b.advance(t_end, zout.data(), steps);
@@ -1739,6 +1754,7 @@ int32_t or_advance_trajectory(int32_t h, double T0, double P, const double* Y0, 
         for (int i = 0; i < K; i++) z0[1 + i] = Y0[i];
     }
     Bdf b;
+    if (opts->linear_solver == 1) b.qord = k->precOrder.data();
     b.init(opts->mole_reactor ? (System*)&mr : (System*)&r, z0.data(), *opts, times[nt - 1]);
     long steps = 0;
     int st = ST_OK;

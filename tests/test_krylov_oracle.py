@@ -129,3 +129,31 @@ def test_gmres_needs_the_mole_reactor():
     assert st[0, 8] != 0
     with pytest.raises(ValueError):
         po.opts(gmres=True, analytic=True)
+
+
+def test_ilut_rules():
+    """The oracle's ILUT (the adaptive preconditioner's factorisation, checked here on the CPU
+    and against the GPU's in the GPU tests): a matrix with no entry near the thresholds is
+    factored exactly (L U = A); a row with more entries than the fill limit p = 10 nnz / N + 1
+    keeps its p largest; a zero pivot becomes sqrt(tau) times the row norm."""
+    from oracle import pyoracle as po
+    rng = np.random.default_rng(11)
+    N = 30
+    A = np.eye(N) * 4 + 0.1 * rng.standard_normal((N, N))
+    F = po.ilut(A)
+    L, U = np.tril(F, -1) + np.eye(N), np.triu(F)
+    assert np.allclose(L @ U, A, rtol=0, atol=1e-13)
+    # an arrow matrix: diagonal plus one dense last row; nnz = 2N - 1, p = 10 (2N - 1) // N + 1 = 20
+    B = np.eye(N) * 2.0
+    B[-1, :] = np.arange(1, N + 1, dtype=float)
+    Fb = po.ilut(B)
+    p = (np.count_nonzero(B) * 10) // N + 1
+    kept = np.nonzero(Fb[-1, :-1])[0]
+    assert len(kept) == p
+    # the multipliers are B[-1, j] / 2, so the largest p are the last p columns of the L part
+    assert np.array_equal(kept, np.arange(N - 1 - p, N - 1))
+    # a zero pivot in row 0 (no L part): sqrt(1e-12) times the row's 2-norm
+    C = np.eye(N) + 0.01 * np.ones((N, N))
+    C[0, 0] = 0.0
+    Fc = po.ilut(C)
+    assert Fc[0, 0] == pytest.approx(1e-6 * np.linalg.norm(C[0]), rel=1e-15)
