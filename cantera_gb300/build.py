@@ -14,7 +14,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgbchem.so")
 OUT_CHECKED = os.path.join(HERE, "_build_checked")
 LIB_CHECKED = os.path.join(OUT_CHECKED, "libgbchem.so")
-SOURCES = ["capi.cu", "kernels.cu", "kernels_x.cu", "krylov.cu", "surrogate.cu", "umma.cu", "mechanism.cpp", "yaml_lite.cpp"]
+SOURCES = ["capi.cu", "kernels.cu", "kernels_x.cu", "krylov.cu", "krylov32.cu", "surrogate.cu", "umma.cu", "mechanism.cpp", "yaml_lite.cpp"]
 HEADERS = ["devmech.h", "fastexp.h", "kernels.h", "kinetics.cuh", "mechanism.h", "nnmath.cuh", "surrogate.h",
            "yaml_lite.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -608,7 +608,8 @@ void chooseBdfLaunch(const MechEntry& me, const gb_net_options& o, int n, bool f
         ne.luSlots = std::max(0, std::min(room, cap));
     }
     const int perBlock = ne.mechSmem + ne.warpDoubles * 8 * bestFit + ne.luSlots * ne.luSlotBytes;
-    const int blocksPerSm = ne.krylov ? bdfBlocksPerSmKrylov(d.N, d.NX > 0, bestFit, (size_t)perBlock)
+    const int blocksPerSm = ne.krylov ? (fp32 ? bdfBlocksPerSmKrylov32(d.N, d.NX > 0, bestFit, (size_t)perBlock)
+                                              : bdfBlocksPerSmKrylov64(d.N, d.NX > 0, bestFit, (size_t)perBlock))
                                       : bdfBlocksPerSm(d.N, fp32, bestFit, (size_t)perBlock, d.NX > 0);
     ne.blocks = std::min(me.smCount * blocksPerSm, (n + bestFit - 1) / bestFit);
 }
@@ -633,7 +634,10 @@ void netLaunch(NetEntry& ne, MechEntry& me, double t0, double tout, bool oneStep
     p.luSlots = ne.luSlots; p.luSlotBytes = ne.luSlotBytes;
     p.kstats = ne.krylov ? ne.dKStats.as<long long>() : nullptr;
     ck(cudaMemsetAsync(ne.dCounter.p, 0, sizeof(int), me.stream), "memset");
-    if (ne.krylov) ck(launchBdfKrylov(p, ne.blocks, ne.warpsPerBlock, me.stream), "integrator launch (Krylov)");
+    if (ne.krylov)
+        ck(ne.opts.lu_precision == 32 ? launchBdfKrylov32(p, ne.blocks, ne.warpsPerBlock, me.stream)
+                                      : launchBdfKrylov64(p, ne.blocks, ne.warpsPerBlock, me.stream),
+           "integrator launch (Krylov)");
     else ck(launchBdf(p, ne.blocks, ne.warpsPerBlock, ne.opts.lu_precision == 32, me.stream), "integrator launch");
 }
 
@@ -906,8 +910,6 @@ int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
         if (ne->opts.linear_solver != 0 && ne->opts.linear_solver != 1)
             throw std::runtime_error("linear_solver must be 0 (dense) or 1 (GMRES with the adaptive preconditioner)");
         ne->krylov = ne->opts.linear_solver == 1;
-        if (ne->krylov && ne->opts.lu_precision != 64)
-            throw std::runtime_error("the GMRES path factors its preconditioner in FP64: lu_precision must be 64");
         const int N = me.dm.N;
         const bool fp32 = ne->opts.lu_precision == 32;
         ne->ld = fp32 ? (N % 2 == 0 ? N + 1 : N) : (N % 2 == 0 ? N + 1 : N);

@@ -29,7 +29,7 @@
 #include <string.h>
 
 // Non-inline functions of these headers have internal linkage in the kernel modules that
-// compile the same code again (kernels_x.cu, krylov.cu): their host-side stubs must not
+// compile the same code again (kernels_x.cu, krylov.cu, krylov32.cu): their host-side stubs must not
 // collide at link time.
 #if defined(GB_KERNELS_EXTRA) || defined(GB_KERNELS_KRYLOV)
 #define GB_TU_LOCAL static

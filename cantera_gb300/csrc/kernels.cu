@@ -802,8 +802,8 @@ __device__ __noinline__ bool devPrecJac(const DevMech& mm, double* base, const u
 // Keep the `fill` largest entries (by magnitude) among those of w[] that `part` selects and
 // clear the others (ILUT's fill limit): the fill-th largest magnitude is found bit by bit on
 // the magnitudes' bit patterns; entries equal to it are kept in index order.
-template <int S>
-__device__ __forceinline__ void ilutFillLimit(double (&w)[S], const bool (&part)[S], int fill, int lane) {
+template <typename MT, int S>
+__device__ __forceinline__ void ilutFillLimit(MT (&w)[S], const bool (&part)[S], int fill, int lane) {
     unsigned long long key[S];
 #pragma unroll
     for (int t = 0; t < S; t++) key[t] = part[t] ? absKey(w[t]) : 0ULL;
@@ -825,7 +825,7 @@ __device__ __forceinline__ void ilutFillLimit(double (&w)[S], const bool (&part)
     for (int t = 0; t < S; t++) {
         const unsigned eq = __ballot_sync(0xffffffffu, part[t] && key[t] == T);
         const int rank = __popc(eq & lt);
-        if (part[t] && (key[t] < T || (key[t] == T && rank >= need))) w[t] = 0.0;
+        if (part[t] && (key[t] < T || (key[t] == T && rank >= need))) w[t] = (MT)0;
         need -= __popc(eq);
     }
 }
@@ -838,15 +838,16 @@ __device__ __forceinline__ void ilutFillLimit(double (&w)[S], const bool (&part)
 // Carried out right-looking: at step k row k has received every update it gets in the
 // row-by-row (IKJ) order, in the same order, so it is finished and dropped before its U part
 // updates the rows below.  Afterwards a holds L (unit diagonal, strictly lower part) and U,
-// dinv[] the reciprocal diagonal of U.  rn: N doubles of scratch.
-template <int S>
-__device__ __noinline__ void devIlut(double* a, int N, int ld, double* dinv, double* rn, int lane) {
+// dinv[] the reciprocal diagonal of U.  rn: N doubles of scratch.  MT: the element type of the
+// factors (double; float for the FP32 preconditioner, whose arithmetic is FP32 too).
+template <typename MT, int S>
+__device__ __noinline__ void devIlut(MT* a, int N, int ld, double* dinv, double* rn, int lane) {
     int cnt = 0;
 #pragma unroll 1
     for (int j = 0; j < N; j++) {
-        const double* row = a + (size_t)j * ld;
+        const MT* row = a + (size_t)j * ld;
 #pragma unroll 1
-        for (int i = lane; i < N; i += 32) cnt += row[i] != 0.0;
+        for (int i = lane; i < N; i += 32) cnt += row[i] != (MT)0;
     }
     const long long nnz = __reduce_add_sync(0xffffffffu, cnt);
     const int fill = (int)(nnz * kIlutFillFactor / N) + 1;
@@ -856,7 +857,7 @@ __device__ __noinline__ void devIlut(double* a, int N, int ld, double* dinv, dou
         double q = 0.0;
 #pragma unroll 1
         for (int j = 0; j < N; j++) {
-            const double v = a[(size_t)j * ld + i];
+            const double v = (double)a[(size_t)j * ld + i];
             q += v * v;
         }
         rn[i] = sqrt(q);
@@ -866,7 +867,7 @@ __device__ __noinline__ void devIlut(double* a, int N, int ld, double* dinv, dou
 #pragma unroll 1
     for (int k = 0; k < N; k++) {
         // finish row k of P (column k of a): threshold drops, fill limits, zero pivot
-        double w[S];
+        MT w[S];
         bool inL[S], inU[S];
         const double rnk = rn[k];
         const double thr = kIlutTau * rnk;
@@ -874,44 +875,44 @@ __device__ __noinline__ void devIlut(double* a, int N, int ld, double* dinv, dou
 #pragma unroll
         for (int t = 0; t < S; t++) {
             const int j = lane + 32 * t;
-            double v = (j < N) ? a[(size_t)j * ld + k] : 0.0;
-            if (j != k && !(fabs(v) > thr)) v = 0.0;
+            MT v = (j < N) ? a[(size_t)j * ld + k] : (MT)0;
+            if (j != k && !(fabs((double)v) > thr)) v = (MT)0;
             w[t] = v;
             inL[t] = j < k;
             inU[t] = j > k && j < N;
-            cL += __popc(__ballot_sync(0xffffffffu, inL[t] && v != 0.0));
-            cU += __popc(__ballot_sync(0xffffffffu, inU[t] && v != 0.0));
+            cL += __popc(__ballot_sync(0xffffffffu, inL[t] && v != (MT)0));
+            cU += __popc(__ballot_sync(0xffffffffu, inU[t] && v != (MT)0));
         }
-        if (cL > fill) ilutFillLimit<S>(w, inL, fill, lane);
-        if (cU > fill) ilutFillLimit<S>(w, inU, fill, lane);
-        double dk = 0.0;
+        if (cL > fill) ilutFillLimit<MT, S>(w, inL, fill, lane);
+        if (cU > fill) ilutFillLimit<MT, S>(w, inU, fill, lane);
+        MT dk = (MT)0;
 #pragma unroll
         for (int t = 0; t < S; t++) {
             const int j = lane + 32 * t;
-            if (j == k && w[t] == 0.0) w[t] = sqrtTau * rnk;
+            if (j == k && w[t] == (MT)0) w[t] = (MT)(sqrtTau * rnk);
             if (j < N) a[(size_t)j * ld + k] = w[t];
             if (t == (k >> 5)) dk = w[t];
         }
         dk = __shfl_sync(0xffffffffu, dk, k & 31);
-        if (lane == 0) dinv[k] = 1.0 / dk;
+        if (lane == 0) dinv[k] = 1.0 / (double)dk;
         // multipliers of column k (row k of a): f_i = P[i][k] / P[k][k], dropped at or below tau
-        double f[S];
+        MT f[S];
         bool anyF[S];
-        double* rk = a + (size_t)k * ld;
+        MT* rk = a + (size_t)k * ld;
 #pragma unroll
         for (int t = 0; t < S; t++) {
             const int i = lane + 32 * t;
-            double v = 0.0;
+            MT v = (MT)0;
             if (i > k && i < N) {
-                const double p = rk[i];
-                if (p != 0.0) {
+                const MT p = rk[i];
+                if (p != (MT)0) {
                     v = p / dk;
-                    if (fabs(v) <= kIlutTau) v = 0.0;
+                    if (fabs((double)v) <= kIlutTau) v = (MT)0;
                     rk[i] = v;
                 }
             }
             f[t] = v;
-            anyF[t] = __any_sync(0xffffffffu, v != 0.0);
+            anyF[t] = __any_sync(0xffffffffu, v != (MT)0);
         }
         // rows i > k: P[i][j] -= f_i P[k][j] for the kept entries P[k][j], j > k (row j of a),
         // walking the set bits of the kept entries' mask four rows at a time: the four rows'
@@ -921,25 +922,25 @@ __device__ __noinline__ void devIlut(double* a, int N, int ld, double* dinv, dou
         for (int tj = 0; tj < S; tj++) {
             if (32 * tj + 31 <= k) continue;
             const int j0 = 32 * tj;
-            unsigned msk = __ballot_sync(0xffffffffu, w[tj] != 0.0 && j0 + lane > k && j0 + lane < N);
+            unsigned msk = __ballot_sync(0xffffffffu, w[tj] != (MT)0 && j0 + lane > k && j0 + lane < N);
 #pragma unroll 1
             while (msk) {
                 int jq[4];
-                double u[4];
+                MT u[4];
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     jq[q] = msk ? __ffs(msk) - 1 : -1;
                     if (msk) msk &= msk - 1;
                     u[q] = __shfl_sync(0xffffffffu, w[tj], jq[q] < 0 ? 0 : jq[q]);
                 }
-                double v[S][4];
+                MT v[S][4];
 #pragma unroll
                 for (int t = 0; t < S; t++) {
                     const int i = lane + 32 * t;
                     const bool act = anyF[t] && i > k && i < N;
 #pragma unroll
                     for (int q = 0; q < 4; q++)
-                        v[t][q] = (act && jq[q] >= 0) ? a[(size_t)(j0 + jq[q]) * ld + i] : 0.0;
+                        v[t][q] = (act && jq[q] >= 0) ? a[(size_t)(j0 + jq[q]) * ld + i] : (MT)0;
                 }
 #pragma unroll
                 for (int t = 0; t < S; t++) {
@@ -962,33 +963,33 @@ __device__ __noinline__ void devIlut(double* a, int N, int ld, double* dinv, dou
 // substitution step broadcasts one element by a shuffle.  The factors are usually in L2 (one
 // matrix per resident warp), so the rows of the next kIluAhead steps are in flight meanwhile.
 constexpr int kIluAhead = 4;
-template <int S>
-__device__ __noinline__ void devIluSolve(const double* a, double* b, int N, int ld, const double* dinv, const int* q,
+template <typename MT, int S>
+__device__ __noinline__ void devIluSolve(const MT* a, double* b, int N, int ld, const double* dinv, const int* q,
                                          int lane) {
-    double x[S], nr[kIluAhead][S];
+    MT x[S], nr[kIluAhead][S];
     int qi[S];
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
         qi[t] = (i < N) ? q[i] : 0;
-        x[t] = (i < N) ? b[qi[t]] : 0.0;
+        x[t] = (i < N) ? (MT)b[qi[t]] : (MT)0;
     }
 #pragma unroll
     for (int p = 0; p < kIluAhead; p++) {
-        const double* r = a + (size_t)(p < N ? p : 0) * ld;
+        const MT* r = a + (size_t)(p < N ? p : 0) * ld;
 #pragma unroll
         for (int t = 0; t < S; t++) {
             const int i = lane + 32 * t;
-            nr[p][t] = (i < N && p < N) ? r[i] : 0.0;
+            nr[p][t] = (i < N && p < N) ? r[i] : (MT)0;
         }
     }
 #pragma unroll
     for (int tk = 0; tk < S; tk++) {
         const int kend = min(N, 32 * (tk + 1));
         for (int k = 32 * tk; k < kend; k++) {
-            double cur[S];
+            MT cur[S];
             const int kn = k + kIluAhead;
-            const double* rn = a + (size_t)(kn < N ? kn : 0) * ld;
+            const MT* rn = a + (size_t)(kn < N ? kn : 0) * ld;
 #pragma unroll
             for (int t = 0; t < S; t++) {
                 cur[t] = nr[0][t];
@@ -997,8 +998,8 @@ __device__ __noinline__ void devIluSolve(const double* a, double* b, int N, int 
                 const int i = lane + 32 * t;
                 if (i < N && kn < N) nr[kIluAhead - 1][t] = rn[i];
             }
-            const double wk = __shfl_sync(0xffffffffu, x[tk], k & 31);
-            if (wk == 0.0) continue;
+            const MT wk = __shfl_sync(0xffffffffu, x[tk], k & 31);
+            if (wk == (MT)0) continue;
 #pragma unroll
             for (int t = tk; t < S; t++) {
                 const int i = lane + 32 * t;
@@ -1006,29 +1007,29 @@ __device__ __noinline__ void devIluSolve(const double* a, double* b, int N, int 
             }
         }
     }
-    double nd[kIluAhead];
+    MT nd[kIluAhead];
 #pragma unroll
     for (int p = 0; p < kIluAhead; p++) {
         const int k = N - 1 - p;
-        const double* r = a + (size_t)(k >= 0 ? k : 0) * ld;
-        nd[p] = (k >= 0) ? dinv[k] : 0.0;
+        const MT* r = a + (size_t)(k >= 0 ? k : 0) * ld;
+        nd[p] = (k >= 0) ? (MT)dinv[k] : (MT)0;
 #pragma unroll
         for (int t = 0; t < S; t++) {
             const int i = lane + 32 * t;
-            nr[p][t] = (i < N && k >= 0) ? r[i] : 0.0;
+            nr[p][t] = (i < N && k >= 0) ? r[i] : (MT)0;
         }
     }
 #pragma unroll
     for (int tk = S - 1; tk >= 0; tk--) {
         const int kbeg = min(N, 32 * (tk + 1)) - 1;
         for (int k = kbeg; k >= 32 * tk; k--) {
-            double cur[S];
+            MT cur[S];
             const int kn = k - kIluAhead;
-            const double dk = nd[0];
+            const MT dk = nd[0];
 #pragma unroll
             for (int p = 0; p + 1 < kIluAhead; p++) nd[p] = nd[p + 1];
-            if (kn >= 0) nd[kIluAhead - 1] = dinv[kn];
-            const double* rp = a + (size_t)(kn >= 0 ? kn : 0) * ld;
+            if (kn >= 0) nd[kIluAhead - 1] = (MT)dinv[kn];
+            const MT* rp = a + (size_t)(kn >= 0 ? kn : 0) * ld;
 #pragma unroll
             for (int t = 0; t < S; t++) {
                 cur[t] = nr[0][t];
@@ -1038,8 +1039,8 @@ __device__ __noinline__ void devIluSolve(const double* a, double* b, int N, int 
                 if (i < N && kn >= 0) nr[kIluAhead - 1][t] = rp[i];
             }
             if (lane == (k & 31)) x[tk] = x[tk] * dk;
-            const double zk = __shfl_sync(0xffffffffu, x[tk], k & 31);
-            if (zk == 0.0) continue;
+            const MT zk = __shfl_sync(0xffffffffu, x[tk], k & 31);
+            if (zk == (MT)0) continue;
 #pragma unroll
             for (int t = 0; t <= tk; t++) {
                 const int i = lane + 32 * t;
@@ -1051,7 +1052,7 @@ __device__ __noinline__ void devIluSolve(const double* a, double* b, int N, int 
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        if (i < N) b[qi[t]] = x[t];
+        if (i < N) b[qi[t]] = (double)x[t];
     }
     __syncwarp();
 }
@@ -1134,7 +1135,7 @@ struct BdfWarp {
                 }
             }
             __syncwarp();
-            devIlut<NS>((double*)M, N, ld, dinv, V, lane);
+            devIlut<MT, NS>(M, N, ld, dinv, V, lane);
             return true;
         }
         if (!Jsv) {
@@ -1182,10 +1183,10 @@ struct BdfWarp {
         __syncwarp();
         return true;
     }
-    template <int NS>
-    __device__ void precSolve(const double* Ft, double* x) {
+    template <typename MT, int NS>
+    __device__ void precSolve(const MT* Ft, double* x) {
         if (lane == 0) aux->nps++;
-        devIluSolve<NS>(Ft, x, N, ld, dinv, m->precOrder, lane);
+        devIluSolve<MT, NS>(Ft, x, N, ld, dinv, m->precOrder, lane);
     }
     // (I - gamma J) x = b in place by right-preconditioned GMRES, as CVODE's iterative
     // linear-solver interface runs SUNDIALS' SPGMR for the reference's preconditioned solver
@@ -1197,8 +1198,8 @@ struct BdfWarp {
     // right-hand side already below the tolerance is the solution on the first Newton
     // iteration and zero afterwards.  Returns 0, or 1 (recoverable: not converged and, after
     // the first Newton iteration, only reduced).
-    template <int NS>
-    __device__ int gmres(const double* Ft, double* b, BdfScal& S, int mnewt) {
+    template <typename MT, int NS>
+    __device__ int gmres(const MT* Ft, double* b, BdfScal& S, int mnewt) {
         const double deltar = kEplifac * S.tq[4];
         if (wrms(b) <= deltar) {
             if (mnewt > 0) {
@@ -1242,7 +1243,7 @@ struct BdfWarp {
 #pragma unroll 1
             for (int i = lane; i < N; i += 32) z[i] = vl[i] / ewt[i];
             __syncwarp();
-            precSolve<NS>(Ft, z);
+            precSolve<MT, NS>(Ft, z);
             if (!jtimes(z, Az, b, S)) return 1;
             double pk = 0.0;
 #pragma unroll 1
@@ -1331,7 +1332,7 @@ struct BdfWarp {
             z[i] = sacc / ewt[i];
         }
         __syncwarp();
-        precSolve<NS>(Ft, z);
+        precSolve<MT, NS>(Ft, z);
 #pragma unroll 1
         for (int i = lane; i < N; i += 32) b[i] = z[i];
         __syncwarp();
@@ -1460,7 +1461,7 @@ struct BdfWarp {
                 __syncwarp();
                 if constexpr (kKry) {
                     // an iterative solve uses the current gamma: no correction for its change
-                    if (gmres<NS>((const double*)M, tempv, S, mm) != 0) { retry = !jcur; break; }
+                    if (gmres<MT, NS>(M, tempv, S, mm) != 0) { retry = !jcur; break; }
                 } else {
                     luSolve<MT, NS>(M, tempv);
                     if (S.gamrat != 1.0) {
@@ -2106,21 +2107,35 @@ int bdfBlocksPerSmX(bool fp32, int warpsPerBlock, size_t smem) {
                 : bdfBlocksPerSmT<double, 8, true>(warpsPerBlock, smem);
 }
 #elif defined(GB_KERNELS_KRYLOV)
-// The Krylov path's instantiations (krylov.cu): FP64 throughout, the preconditioner's factors
-// in the matrix slot; mechanisms with the less common rate forms use the widest register slots.
-cudaError_t launchBdfKrylov(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
-    if (p.m.NX) return launchBdfT<double, 8, true, true>(p, blocks, warpsPerBlock, stream);
+// The Krylov path's instantiations (krylov.cu with FP64 preconditioner factors, krylov32.cu
+// with FP32 ones; everything else FP64): the factors in the matrix slot; mechanisms with the
+// less common rate forms use the widest register slots.
+#if GB_KERNELS_KRYLOV == 32
+#define GB_KMT float
+#define GB_KLAUNCH launchBdfKrylov32
+#define GB_KBLOCKS bdfBlocksPerSmKrylov32
+#else
+#define GB_KMT double
+#define GB_KLAUNCH launchBdfKrylov64
+#define GB_KBLOCKS bdfBlocksPerSmKrylov64
+#endif
+cudaError_t GB_KLAUNCH(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream) {
+    if (p.m.NX) return launchBdfT<GB_KMT, 8, true, true>(p, blocks, warpsPerBlock, stream);
     const int N = p.m.N;
-    if (N <= 64) return launchBdfT<double, 2, false, true>(p, blocks, warpsPerBlock, stream);
-    if (N <= 128) return launchBdfT<double, 4, false, true>(p, blocks, warpsPerBlock, stream);
-    return launchBdfT<double, 8, false, true>(p, blocks, warpsPerBlock, stream);
+    if (N <= 64) return launchBdfT<GB_KMT, 2, false, true>(p, blocks, warpsPerBlock, stream);
+    if (N <= 128) return launchBdfT<GB_KMT, 4, false, true>(p, blocks, warpsPerBlock, stream);
+    return launchBdfT<GB_KMT, 8, false, true>(p, blocks, warpsPerBlock, stream);
 }
-int bdfBlocksPerSmKrylov(int N, bool extra, int warpsPerBlock, size_t smem) {
-    if (extra) return bdfBlocksPerSmT<double, 8, true, true>(warpsPerBlock, smem);
-    if (N <= 64) return bdfBlocksPerSmT<double, 2, false, true>(warpsPerBlock, smem);
-    if (N <= 128) return bdfBlocksPerSmT<double, 4, false, true>(warpsPerBlock, smem);
-    return bdfBlocksPerSmT<double, 8, false, true>(warpsPerBlock, smem);
+int GB_KBLOCKS(int N, bool extra, int warpsPerBlock, size_t smem) {
+    if (extra) return bdfBlocksPerSmT<GB_KMT, 8, true, true>(warpsPerBlock, smem);
+    if (N <= 64) return bdfBlocksPerSmT<GB_KMT, 2, false, true>(warpsPerBlock, smem);
+    if (N <= 128) return bdfBlocksPerSmT<GB_KMT, 4, false, true>(warpsPerBlock, smem);
+    return bdfBlocksPerSmT<GB_KMT, 8, false, true>(warpsPerBlock, smem);
 }
+#undef GB_KMT
+#undef GB_KLAUNCH
+#undef GB_KBLOCKS
+#if GB_KERNELS_KRYLOV != 32
 
 // Batched incomplete factorisation: one warp per matrix (grid-stride), each stored transposed
 // in a[m][N][ld] and factored in place, its reciprocal pivots to dinv[m][N]; rn[m][N] scratch.
@@ -2129,7 +2144,7 @@ __global__ void __launch_bounds__(256) k_ilut(int n, int N, int ld, double* a, d
     const int lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
     for (int r = blockIdx.x * wpb + (threadIdx.x >> 5); r < n; r += gridDim.x * wpb)
-        devIlut<S>(a + (size_t)r * N * ld, N, ld, dinv + (size_t)r * N, rn + (size_t)r * N, lane);
+        devIlut<double, S>(a + (size_t)r * N * ld, N, ld, dinv + (size_t)r * N, rn + (size_t)r * N, lane);
 }
 cudaError_t launchIlut(int n, int N, int ld, double* a, double* dinv, double* rn, cudaStream_t stream) {
     const int blocks = std::max(1, std::min((n + 7) / 8, 4096));
@@ -2139,6 +2154,7 @@ cudaError_t launchIlut(int n, int N, int ld, double* a, double* dinv, double* rn
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
+#endif  // GB_KERNELS_KRYLOV != 32
 #else
 int rhsWarpDoubles(const DevMech& m) {
     const int tot = kStateSlots + KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT) + 2 * m.N;

@@ -100,8 +100,12 @@ int bdfBlocksPerSmX(bool fp32, int warpsPerBlock, size_t smem);
 // its per-warp slice adds bdfKrylovDoubles(N) doubles (the Krylov basis and GMRES scalars),
 // Jbuf (the preconditioner's Jacobian) is required and the matrix slot holds its factors
 int bdfKrylovDoubles(int N);
-cudaError_t launchBdfKrylov(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
-int bdfBlocksPerSmKrylov(int N, bool extra, int warpsPerBlock, size_t smem);
+// FP64 preconditioner factors (krylov.cu) or FP32 ones (krylov32.cu; the ILUT and the
+// triangular solves in FP32, everything else FP64)
+cudaError_t launchBdfKrylov64(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
+cudaError_t launchBdfKrylov32(const BdfParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
+int bdfBlocksPerSmKrylov64(int N, bool extra, int warpsPerBlock, size_t smem);
+int bdfBlocksPerSmKrylov32(int N, bool extra, int warpsPerBlock, size_t smem);
 // batched ILUT of n matrices stored transposed in a[n][N][ld] (in place), reciprocal pivots
 // to dinv[n][N], rn[n][N] scratch (device pointers)
 cudaError_t launchIlut(int n, int N, int ld, double* a, double* dinv, double* rn, cudaStream_t stream);

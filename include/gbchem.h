@@ -118,8 +118,10 @@ typedef struct {
                                AdaptivePreconditioner.cpp:17-81; Python: net.preconditioner =
                                AdaptivePreconditioner()): an approximate Jacobian (ddCi species
                                block, difference T column, enthalpy T row) factored by ILUT,
-                               J v by difference quotients.  Needs lu_precision 64; the state
-                               handed in and out stays T and mass fractions. */
+                               J v by difference quotients.  With lu_precision 32 the ILUT
+                               factors and their triangular solves are FP32 (J v, GMRES and step
+                               control stay FP64).  The state handed in and out stays T and mass
+                               fractions. */
 } gb_net_options;
 
 void gb_net_default_options(gb_net_options* opts);

@@ -86,18 +86,20 @@ def _ignition_cases():
     return m, T0, P, np.tile(Y0, (4, 1))
 
 
-def test_gmres_ignition_matches_oracle_and_direct_solvers():
-    """gri30 ignition at four initial states to 0.1 s: the GPU's GMRES path, the oracle's
-    GMRES path, the oracle's dense mass-fraction reactor and the GPU's dense path agree within
-    the reference test's bars; the GPU takes the oracle's step and iteration counts (to the
-    rounding of a different arithmetic order) and its Krylov counters have the same
-    structure (one J v product per linear iteration, more preconditioner solves)."""
+@pytest.mark.parametrize("lu", [64, 32])
+def test_gmres_ignition_matches_oracle_and_direct_solvers(lu):
+    """gri30 ignition at four initial states to 0.1 s: the GPU's GMRES path (FP64 or FP32
+    preconditioner factors), the oracle's GMRES path, the oracle's dense mass-fraction reactor
+    and the GPU's dense path agree within the reference test's bars; with FP64 factors the GPU
+    takes the oracle's step and iteration counts (to the rounding of a different arithmetic
+    order); the Krylov counters have the same structure (one J v product per linear
+    iteration, more preconditioner solves)."""
     import cantera_gb300 as gb
     from oracle import pyoracle as po
     m, T0, P, Y0 = _ignition_cases()
     sol = gpu_solution("gri30")
     t_end, atol = 0.1, 1e-16
-    net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=RTOL, atol=atol, linear_solver="GMRES")
+    net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=RTOL, atol=atol, linear_solver="GMRES", lu_precision=lu)
     assert net.advance(t_end) == 0
     Tg, Yg = net.get_state()
     Yg = Yg.T
@@ -113,12 +115,14 @@ def test_gmres_ignition_matches_oracle_and_direct_solvers():
         assert np.all(np.abs(Yg - Yr) <= 5e-4 * np.abs(Yr) + 1e-6)
         assert np.all(np.abs(tg - tr) <= 1e-3 * tr)
     assert np.all(tg < 0.09)
-    # the same algorithm: counts within a few per cent of the oracle's
+    # the same algorithm: counts within a few per cent of the oracle's (with FP32 factors the
+    # preconditioner differs at the 1e-7 level, and so can the linear iterations)
+    tol = 0.1 if lu == 64 else 0.2
     for i, k in ((0, "steps"), (1, "rhs_evals"), (2, "newton_iters")):
-        assert np.all(np.abs(stg[k] - sto[:, i]) <= 0.1 * sto[:, i] + 5), (k, stg[k], sto[:, i])
+        assert np.all(np.abs(stg[k] - sto[:, i]) <= tol * sto[:, i] + 5), (k, stg[k], sto[:, i])
     lin, ps, jtv = kst["lin_iters"], kst["prec_solves"], kst["jt_vec_prod_evals"]
     assert np.all(lin > 0) and np.all(jtv == lin) and np.all(ps > lin)
-    assert np.all(np.abs(lin - sto[:, 9]) <= 0.15 * sto[:, 9] + 10)
+    assert np.all(np.abs(lin - sto[:, 9]) <= (0.15 if lu == 64 else 0.3) * sto[:, 9] + 10)
 
 
 def test_gmres_kin1_blessed_trajectory(goldens):
@@ -164,16 +168,18 @@ def _ndodecane(n, seed):
     return m, T0[idx], P[idx], Y0
 
 
-def test_gmres_ndodecane_against_oracle_and_dense():
+@pytest.mark.parametrize("lu", [64, 32])
+def test_gmres_ndodecane_against_oracle_and_dense(lu):
     """64 reactors of the n-dodecane workload to 5e-3 s at its tolerances: the GPU's GMRES path
-    against the oracle's GMRES path and the GPU's dense path (the reference test's bars,
-    ignition delays within 1e-3), with the oracle's step counts."""
+    (FP64 or FP32 preconditioner factors) against the oracle's GMRES path and the GPU's dense
+    path (the reference test's bars, ignition delays within 1e-3), with the oracle's step
+    counts."""
     import cantera_gb300 as gb
     from oracle import pyoracle as po
     sol = gpu_solution("nDodecane")
     m, T0, P, Y0 = _ndodecane(64, 41)
     t_end, atol = 5e-3, 1e-15
-    net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=RTOL, atol=atol, linear_solver="GMRES")
+    net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=RTOL, atol=atol, linear_solver="GMRES", lu_precision=lu)
     assert net.advance(t_end) == 0
     Tg, Yg = net.get_state()
     Yg = Yg.T
@@ -199,8 +205,8 @@ def test_gmres_ndodecane_against_oracle_and_dense():
 
 def test_gmres_step_checkpoint_and_errors():
     """ReactorNet.step and checkpoint / restore on the GMRES path (bit-identical continuation,
-    Krylov counters included); a dense network's checkpoint is refused; FP32 factorisation,
-    Krylov counters of a dense network and the allocation-free advance with GMRES are errors."""
+    Krylov counters included); a dense network's checkpoint is refused; Krylov counters of a
+    dense network and the allocation-free advance with GMRES are errors."""
     import cantera_gb300 as gb
     sol = gpu_solution("gri30")
     m, T0, P, Y0 = _ignition_cases()
@@ -227,8 +233,6 @@ def test_gmres_step_checkpoint_and_errors():
         b.restore(dense.checkpoint())
     with pytest.raises(gb.GBError, match="dense linear solver"):
         dense.krylov_stats
-    with pytest.raises(gb.GBError, match="lu_precision must be 64"):
-        gb.ReactorNet(sol, T0, P, Y0.T.copy(), lu_precision=32, linear_solver="GMRES")
     import torch
     L = gb.library()
     o = gb.NetOptions()
