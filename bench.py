@@ -356,12 +356,15 @@ def tight_run(m, po, T0, P, Y0, t_end, threads):
     return Tt, Yt, stt, tit, rerun, stt[:, 8] != 0
 
 
-def error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, gpu, threads):
+def error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, gpu, threads, extra_oracles=None):
     """Error protocol of the integrator workloads on one sample: (i) against the CPU oracle
     configured as the reference's ReactorNet at the same tolerances, (ii) against a tight
     run of it (rtol 1e-12, atol 1e-20), with the oracle's own error against (ii) beside the
     GPU's, and the ignition-delay (time of the largest dT/dt) error of every igniting
-    reactor.  gpu: {variant: (T [n], Y [n][K], tign [n])} on the same sample."""
+    reactor.  gpu: {variant: (T [n], Y [n][K], tign [n])} on the same sample.
+    extra_oracles: {name: (oracle options, [variants])}: further configurations of the oracle
+    (the reference's other linear solver), each with its own error against (ii) and, for the
+    listed GPU variants, the ratio of their error to it."""
     t0 = time.perf_counter()
     To, Yo, sto, tio = m.advance_batch(T0, P, Y0, t_end, oracle_opts(po, rtol, atol), threads=threads)
     Tt, Yt, stt, tit, rerun, tfail = tight_run(m, po, T0, P, Y0, t_end, threads)
@@ -397,6 +400,28 @@ def error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, gpu, threads):
         if ign.any():
             e["ignition_within_1e-3"] = e["ignition_delay_max_rel_vs_oracle"] <= 1e-3
         out[name] = e
+    for oname, (oopts, variants) in (extra_oracles or {}).items():
+        Tx, Yx, stx, tix = m.advance_batch(T0, P, Y0, t_end, oopts, threads=threads)
+        ok = use & (stx[:, 8] == 0)
+        ex = {"failed": int(np.sum(stx[:, 8] != 0)),
+              "vs_tight": {"all": state_errors(Tx[ok], Yx[ok], Tt[ok], Yt[ok]),
+                           "settled": state_errors(Tx[ok & settled], Yx[ok & settled], Tt[ok & settled],
+                                                   Yt[ok & settled])}}
+        ig = ign & ok
+        if ig.any():
+            ex["ignition_delay_max_rel_vs_tight"] = float(np.max(np.abs(tix[ig] - tit[ig]) / tit[ig]))
+        out["oracle_" + oname] = ex
+        for v in variants:
+            if v not in gpu:
+                continue
+            Tg, Yg, tg = gpu[v]
+            a = state_errors(Tg[ok], Yg[ok], Tt[ok], Yt[ok])
+            o_ = ex["vs_tight"]["all"]
+            out[v]["T_error_ratio_to_oracle_" + oname] = a["T_max_rel"] / max(o_["T_max_rel"], 1e-300)
+            out[v]["T_within_3x_oracle_" + oname] = a["T_max_rel"] <= max(bar, 3 * o_["T_max_rel"])
+            out[v]["vs_oracle_" + oname] = state_errors(Tg[ok], Yg[ok], Tx[ok], Yx[ok])
+            if ig.any():
+                out[v]["ignition_delay_max_rel_vs_oracle_" + oname] = float(np.max(np.abs(tg[ig] - tix[ig]) / tix[ig]))
     return out
 
 
@@ -563,7 +588,8 @@ def variant_ndodecane(dev, torch, flush, threads, n=16384, sample=64):
         gpu[name] = (Tg[idx], Yg[:, idx].T, net.ignition_times[idx])
         del net
     m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "nDodecane_Reitz.yaml"), "nDodecane_IG")
-    errs = error_protocol(m, po, T0[idx], P[idx], Y0[idx], t_end, rtol, atol, gpu, threads)
+    errs = error_protocol(m, po, T0[idx], P[idx], Y0[idx], t_end, rtol, atol, gpu, threads,
+                          extra_oracles={"gmres": (po.opts(rtol=rtol, atol=atol, gmres=True), ["gmres", "gmres_fp32"])})
     mf = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "nDodecane_Reitz.yaml"), "nDodecane_IG", fast=True)
     t0 = time.perf_counter()
     mf.advance_batch(T0[idx], P[idx], Y0[idx], t_end, oracle_opts(po, rtol, atol), threads=threads)

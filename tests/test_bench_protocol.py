@@ -50,6 +50,24 @@ def test_error_protocol_flags_a_shifted_result():
     assert e["off"]["ignition_delay_max_rel_vs_oracle"] > 9e-3 and not e["off"]["ignition_within_1e-3"]
 
 
+def test_error_protocol_extra_oracle_configuration():
+    """A further oracle configuration (the Krylov path): its own error against the tight run,
+    and for the listed variant the comparison with it - zero when the variant is that
+    configuration's own result."""
+    m, T0, P, Y0 = h2o2_sample(4)
+    t_end, rtol, atol = 1e-3, 1e-8, 1e-15
+    og = po.opts(rtol=rtol, atol=atol, gmres=True)
+    Tg, Yg, stg, tig = m.advance_batch(T0, P, Y0, t_end, og, threads=2)
+    assert np.all(stg[:, 8] == 0)
+    e = bench.error_protocol(m, po, T0, P, Y0, t_end, rtol, atol, {"kry": (Tg, Yg, tig)}, threads=2,
+                             extra_oracles={"gmres": (og, ["kry"])})
+    ex = e["oracle_gmres"]
+    assert ex["failed"] == 0 and ex["vs_tight"]["all"] == e["kry"]["vs_tight"]["all"]
+    assert e["kry"]["T_error_ratio_to_oracle_gmres"] == 1.0 and e["kry"]["T_within_3x_oracle_gmres"]
+    assert e["kry"]["vs_oracle_gmres"]["T_max_rel"] == 0.0
+    assert e["kry"]["ignition_delay_max_rel_vs_oracle_gmres"] == 0.0
+
+
 def test_flop_model_and_roofline_arithmetic():
     st = {"K": 53, "R": 325, "reversible": 309, "falloff": 29, "troe": 26, "three_body": 41,
           "tb_entries": 300, "gather_entries": 1500, "jac_col_entries": 2000, "jac_scatter_entries": 3000}
