@@ -157,3 +157,63 @@ def test_ilut_rules():
     C[0, 0] = 0.0
     Fc = po.ilut(C)
     assert Fc[0, 0] == pytest.approx(1e-6 * np.linalg.norm(C[0]), rel=1e-15)
+
+
+def _ilut_right_looking(P, tau=1e-12):
+    """The GPU kernel's elimination order (devIlut), restated: right-looking, row k finished
+    (threshold drops against its original 2-norm, fill limits, zero pivot) when step k reaches
+    it, then its kept U entries update the rows below.  Row norms summed in index order and no
+    fused multiply-adds, as the oracle's checker build computes."""
+    N = P.shape[0]
+    a = P.copy()
+    fill = np.count_nonzero(a) * 10 // N + 1
+    rn = np.zeros(N)
+    for i in range(N):
+        q = 0.0
+        for v in a[i]:
+            q += v * v
+        rn[i] = np.sqrt(q)
+    for k in range(N):
+        w = a[k].copy()
+        for j in range(N):
+            if j != k and not (abs(w[j]) > tau * rn[k]):
+                w[j] = 0.0
+        for part in (np.arange(N) < k, np.arange(N) > k):
+            idx = np.nonzero(part & (w != 0))[0]
+            if len(idx) > fill:
+                keep = set(sorted(idx, key=lambda j: (-abs(w[j]), j))[:fill])
+                for j in idx:
+                    if j not in keep:
+                        w[j] = 0.0
+        if w[k] == 0.0:
+            w[k] = np.sqrt(tau) * rn[k]
+        a[k] = w
+        for i in range(k + 1, N):
+            if a[i, k] != 0.0:
+                f = a[i, k] / w[k]
+                if abs(f) <= tau:
+                    f = 0.0
+                a[i, k] = f
+                if f != 0.0:
+                    for j in range(k + 1, N):
+                        if w[j] != 0.0:
+                            a[i, j] -= f * w[j]
+    return a
+
+
+def test_ilut_right_looking_order_equals_row_by_row():
+    """The GPU's right-looking ILUT gives the oracle's row-by-row (IKJ) factors bit for bit:
+    each row receives the same updates in the same order before it is finished.  Random sparse
+    matrices with entries around the drop thresholds, rows past the fill limit, zero pivots."""
+    from oracle import pyoracle as po
+    rng = np.random.default_rng(3)
+    for trial in range(40):
+        N = int(rng.integers(2, 24))
+        A = rng.standard_normal((N, N)) * (rng.uniform(size=(N, N)) < rng.uniform(0.05, 0.9))
+        A *= 10.0 ** rng.uniform(-14, 2, size=(N, N))
+        if trial % 3 == 0:
+            A[rng.integers(N)] = rng.standard_normal(N)
+        A += np.diag(rng.uniform(0.5, 2, N) * (rng.uniform(size=N) < 0.8))
+        with np.errstate(all="ignore"):
+            F1, F2 = po.ilut(A), _ilut_right_looking(A)
+        assert np.array_equal(F1, F2, equal_nan=True), trial
