@@ -170,14 +170,14 @@ def _ndodecane(n, seed):
 
 @pytest.mark.parametrize("lu", [64, 32])
 def test_gmres_ndodecane_against_oracle_and_dense(lu):
-    """64 reactors of the n-dodecane workload to 5e-3 s at its tolerances: the GPU's GMRES path
+    """256 reactors of the n-dodecane workload to 5e-3 s at its tolerances: the GPU's GMRES path
     (FP64 or FP32 preconditioner factors) against the oracle's GMRES path and the GPU's dense
-    path (the reference test's bars, ignition delays within 1e-3), with the oracle's step
-    counts."""
+    path (the reference test's bars on the reactors not in mid-ignition at 5e-3 s, ignition
+    delays within 1e-3), with the oracle's step counts."""
     import cantera_gb300 as gb
     from oracle import pyoracle as po
     sol = gpu_solution("nDodecane")
-    m, T0, P, Y0 = _ndodecane(64, 41)
+    m, T0, P, Y0 = _ndodecane(256, 41)
     t_end, atol = 5e-3, 1e-15
     net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=RTOL, atol=atol, linear_solver="GMRES", lu_precision=lu)
     assert net.advance(t_end) == 0
@@ -192,12 +192,12 @@ def test_gmres_ndodecane_against_oracle_and_dense(lu):
     # ignition delay; the others by the reference test's bars
     from test_gpu_workloads import settled
     ok = settled(m, P, To, Yo, t_end)
-    assert ok.sum() >= 48
+    assert ok.sum() >= 192
     for Tr, Yr in ((To, Yo), (Td, Yd.T)):
         assert np.all(np.abs(Tg - Tr)[ok] <= 1e-5 * Tr[ok])
         assert np.all((np.abs(Yg - Yr) <= 5e-4 * np.abs(Yr) + 1e-6)[ok])
     ign = (To > T0 + 400) & (tio > 0) & (tio < t_end)
-    assert ign.sum() >= 5
+    assert ign.sum() >= 20
     assert np.max(np.abs(net.ignition_times[ign] - tio[ign]) / tio[ign]) < 1e-3
     steps = net.solver_stats["steps"]
     assert abs(steps.mean() - sto[:, 0].mean()) <= 0.1 * sto[:, 0].mean()
