@@ -93,18 +93,21 @@ def _subset(T, P, Y, idx_stride, count):
 
 
 def autotune(solution, T, P, Y, t_probe, waves=3, pool=8192, rtol=1e-8, atol=1e-15, lu_precision=64,
-             repeat=1, margin=0.03, use_cache=True):
+             repeat=1, margin=0.03, use_cache=True, linear_solver="DENSE"):
     """Options dict (matrix_placement, warps_per_block) of the fastest launch shape for
-    advancing these reactors (host or device arrays; Y species-major [K, n]) to t_probe.
-    Each candidate advances `waves` full waves of its resident capacity, drawn with a stride
-    from the caller's reactors (at most `pool` of them).  Also returns every candidate's
-    timing (seconds per reactor)."""
-    key = (solution._h, lu_precision, waves, pool, float(t_probe), rtol, atol)
+    advancing these reactors (host or device arrays; Y species-major [K, n]) to t_probe with
+    the given linear solver ("DENSE" or "GMRES", the Krylov path).  Each candidate advances
+    `waves` full waves of its resident capacity, drawn with a stride from the caller's
+    reactors (at most `pool` of them).  Also returns every candidate's timing (seconds per
+    reactor)."""
+    linear_solver = str(linear_solver).upper()
+    key = (solution._h, lu_precision, waves, pool, float(t_probe), rtol, atol, linear_solver)
     if use_cache and key in _cache:
         return _cache[key]
     path = cache_path() if use_cache else None
     pkey = "|".join([mechanism_key(solution), gpu_key(), "lu%d" % lu_precision, "w%d" % waves, "p%d" % pool,
-                     "t%.6g" % t_probe, "r%.3g" % rtol, "a%.3g" % atol])
+                     "t%.6g" % t_probe, "r%.3g" % rtol, "a%.3g" % atol]
+                    + ([] if linear_solver == "DENSE" else [linear_solver]))
     if path:
         hit = _load(path).get(pkey)
         if hit:
@@ -117,7 +120,8 @@ def autotune(solution, T, P, Y, t_probe, waves=3, pool=8192, rtol=1e-8, atol=1e-
     timings = []
     seen = set()
     for c in candidates():
-        probe = ReactorNet(solution, Tp, Pp, Yp, rtol=rtol, atol=atol, lu_precision=lu_precision, **c)
+        probe = ReactorNet(solution, Tp, Pp, Yp, rtol=rtol, atol=atol, lu_precision=lu_precision,
+                           linear_solver=linear_solver, **c)
         info = probe.launch_info
         del probe
         shape = tuple(sorted(info.items()))
@@ -126,7 +130,8 @@ def autotune(solution, T, P, Y, t_probe, waves=3, pool=8192, rtol=1e-8, atol=1e-
         seen.add(shape)
         m = min(npool, waves * info["blocks"] * info["warps_per_block"])
         Ts, Ps, Ys = _subset(Tp, Pp, Yp, max(1, npool // m), m)
-        net = ReactorNet(solution, Ts, Ps, Ys, rtol=rtol, atol=atol, lu_precision=lu_precision, **c)
+        net = ReactorNet(solution, Ts, Ps, Ys, rtol=rtol, atol=atol, lu_precision=lu_precision,
+                         linear_solver=linear_solver, **c)
         net.advance(t_probe)       # warm-up (module load, first launch)
         best = float("inf")
         for _ in range(repeat):

@@ -222,6 +222,10 @@ def test_autotune_picks_a_measured_candidate():
     assert pick["seconds"] <= log[0]["seconds"] * 1.03
     cap = lambda e: e["shape"]["blocks"] * e["shape"]["warps_per_block"]
     assert all(cap(e) <= cap(pick) for e in log if e["seconds"] <= log[0]["seconds"] * 1.03)
+    # the Krylov path is tuned the same way
+    best_k, log_k = autotune(sol, T0, P, Y0.T.copy(), 1e-4, waves=1, pool=256, use_cache=False,
+                             linear_solver="GMRES")
+    assert best_k in list(candidates()) and len(log_k) >= 2
 
 
 def test_settings_of_a_network():

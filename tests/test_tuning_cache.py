@@ -41,6 +41,14 @@ def test_cache_hit_and_miss(tmp_path, monkeypatch):
         raise AssertionError("expected a measurement attempt")
     except AttributeError:
         pass
+    # the Krylov path's shapes are stored under their own key: the dense entry is not taken
+    tuning._cache.clear()
+    mech.write_text("phases: []\n")
+    try:
+        tuning.autotune(sol, None, None, None, 1e-3, linear_solver="gmres")
+        raise AssertionError("expected a measurement attempt")
+    except AttributeError:
+        pass
     # an empty setting turns the file off
     monkeypatch.setenv("GBCHEM_TUNING_CACHE", "")
     assert tuning.cache_path() is None
