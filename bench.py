@@ -875,8 +875,10 @@ def main():
         m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", WL["mechanism"]), WL["phase"])
         tidx = cpu_sample_indices(n_all, TIGHT_SAMPLE, WL["seed"] + 7)
         gpu = {v: (r["T"][tidx], r["Y"][:, tidx].T, r["tign"][tidx]) for v, r in results.items()}
+        extra = ({"gmres": (po.opts(rtol=WL["rtol"], atol=WL["atol"], gmres=True), ["gmres"])}
+                 if "gmres" in results else None)
         line["error_protocol"] = error_protocol(m, po, T0[tidx], P[tidx], Y0[tidx], WL["t_end"], WL["rtol"],
-                                                WL["atol"], gpu, threads)
+                                                WL["atol"], gpu, threads, extra_oracles=extra)
     if not args.no_surrogate and ws == 1:
         try:
             line.setdefault("variants", {})["surrogate"] = surrogate_leg(sol, dev, torch)
