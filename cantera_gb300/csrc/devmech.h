@@ -151,7 +151,8 @@ __device__ __forceinline__ int4 gbCheckIx4(const DevMech& m, int4 e, int n, int 
 #endif
 enum { GB_SITE_SPECIES = 1, GB_SITE_SIDE = 2, GB_SITE_TB_SPECIES = 3, GB_SITE_TB = 4, GB_SITE_FALLOFF = 5,
        GB_SITE_GATHER_RXN = 6, GB_SITE_TASK = 7, GB_SITE_COLUMN = 8, GB_SITE_COL_RXN = 9, GB_SITE_SLOT = 10,
-       GB_SITE_NET_SPECIES = 11, GB_SITE_DENSE_TB = 12, GB_SITE_PATTERN_ROW = 13, GB_SITE_QUEUE = 14 };
+       GB_SITE_NET_SPECIES = 11, GB_SITE_DENSE_TB = 12, GB_SITE_PATTERN_ROW = 13, GB_SITE_QUEUE = 14,
+       GB_SITE_PREC_ORDER = 15 };
 
 // every array of a DevMech
 #define GB_DEVMECH_ARRAYS(X) \

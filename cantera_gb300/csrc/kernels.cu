@@ -964,14 +964,15 @@ __device__ __noinline__ void devIlut(MT* a, int N, int ld, double* dinv, double*
 // matrix per resident warp), so the rows of the next kIluAhead steps are in flight meanwhile.
 constexpr int kIluAhead = 4;
 template <typename MT, int S>
-__device__ __noinline__ void devIluSolve(const MT* a, double* b, int N, int ld, const double* dinv, const int* q,
+__device__ __noinline__ void devIluSolve(const MT* a, double* b, int N, int ld, const double* dinv, const DevMech& m,
                                          int lane) {
+    const int* q = m.precOrder;
     MT x[S], nr[kIluAhead][S];
     int qi[S];
 #pragma unroll
     for (int t = 0; t < S; t++) {
         const int i = lane + 32 * t;
-        qi[t] = (i < N) ? q[i] : 0;
+        qi[t] = (i < N) ? GB_IX(m, q[i], N, GB_SITE_PREC_ORDER) : 0;
         x[t] = (i < N) ? (MT)b[qi[t]] : (MT)0;
     }
 #pragma unroll
@@ -1123,12 +1124,12 @@ struct BdfWarp {
             const int* q = m->precOrder;
 #pragma unroll 1
             for (int b = 0; b < N; b++) {
-                const int jb = q[b];
+                const int jb = GB_IX(*m, q[b], N, GB_SITE_PREC_ORDER);
                 const double* src = Jsv + (size_t)jb * ld;
                 MT* dst = M + (size_t)b * ld;
 #pragma unroll 1
                 for (int a = lane; a < N; a += 32) {
-                    const int ia = q[a];
+                    const int ia = GB_IX(*m, q[a], N, GB_SITE_PREC_ORDER);
                     double v = -g * src[ia];
                     if (ia == jb) v += 1.0;
                     dst[a] = (MT)v;
@@ -1186,7 +1187,7 @@ struct BdfWarp {
     template <typename MT, int NS>
     __device__ void precSolve(const MT* Ft, double* x) {
         if (lane == 0) aux->nps++;
-        devIluSolve<MT, NS>(Ft, x, N, ld, dinv, m->precOrder, lane);
+        devIluSolve<MT, NS>(Ft, x, N, ld, dinv, *m, lane);
     }
     // (I - gamma J) x = b in place by right-preconditioned GMRES, as CVODE's iterative
     // linear-solver interface runs SUNDIALS' SPGMR for the reference's preconditioned solver

@@ -171,3 +171,34 @@ def test_integrator_with_rate_forms_matches_oracle(tmp_path, form):
     w_base = base.net_production_rates(Tr, Pr, Yr)
     assert not np.allclose(w_var, w_base, rtol=1e-6, atol=0)
     assert math.isfinite(float(np.sum(T)))
+
+
+@pytest.mark.parametrize("form,lu", [("plog_cheb_sri", 64), ("plog_cheb_sri", 32), ("tsang", 64), ("chemact", 64)])
+def test_krylov_path_with_rate_forms_matches_oracle(tmp_path, form, lu):
+    """The Krylov path (mole reactor, GMRES, adaptive preconditioner) on mechanisms with the
+    less common rate forms (their own kernel instantiation) against the oracle's GMRES path,
+    with the bars of the reference's test of that solver (T 1e-5, Y 5e-4 relative + 1e-6)."""
+    import cantera_gb300 as gb
+    from oracle import pyoracle as po
+    path = h2o2_variant(tmp_path, form)
+    sol, m = gb.Solution(path, "ohmech"), po.Mech(path, "ohmech")
+    rtol, atol = 1e-8, 1e-15
+    rng = np.random.default_rng(37)
+    n = 48
+    T0 = rng.uniform(1000, 1600, n)
+    P = 101325.0 * 10 ** rng.uniform(-0.5, 1.0, n)
+    phi = rng.uniform(0.5, 2.0, n)
+    Y0 = np.array([m.equivalence_ratio(p, "H2:1", "O2:1, N2:3.76") for p in phi])
+    net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=rtol, atol=atol, linear_solver="GMRES", lu_precision=lu)
+    assert net.advance(1e-3) == 0
+    T, Y = net.get_state()
+    To, Yo, sto, tio = m.advance_batch(T0, P, Y0, 1e-3, po.opts(rtol=rtol, atol=atol, gmres=True))
+    assert np.all(sto[:, 8] == 0)
+    assert np.all(np.abs(T - To) <= 1e-5 * To)
+    assert np.all(np.abs(Y.T - Yo) <= 5e-4 * np.abs(Yo) + 1e-6)
+    # ignition delays of the reactors that ignite (a reactor that warms by a few K has its
+    # largest dT/dt at the last step, wherever the step sequence puts it)
+    ign = (To > T0 + 400) & (tio > 0) & (tio < 1e-3)
+    assert ign.sum() >= 40
+    assert np.max(np.abs(net.ignition_times[ign] - tio[ign]) / tio[ign]) < 1e-3
+    assert np.all(net.krylov_stats["lin_iters"] > 0)
