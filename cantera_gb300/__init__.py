@@ -153,6 +153,15 @@ def _is_torch_cuda(a):
     return type(a).__module__.startswith("torch") and getattr(a, "is_cuda", False)
 
 
+def _after_torch_stream(a):
+    """The engine orders its reads of device arrays after the default stream's work; a tensor
+    written on another torch stream is waited for here."""
+    import torch
+    s = torch.cuda.current_stream(a.device)
+    if s.cuda_stream != torch.cuda.default_stream(a.device).cuda_stream:
+        s.synchronize()
+
+
 def _ptr(a):
     if a is None:
         return None
@@ -240,6 +249,7 @@ class Solution:
 
     def _args(self, T, P, Y):
         if _is_torch_cuda(T):
+            _after_torch_stream(T)
             n = T.shape[0]
             return n, T, P, Y, GB_DEVICE_POINTERS
         T = _host(T)
@@ -288,6 +298,19 @@ class Solution:
             for p in range(self.jac_colptr[c], self.jac_colptr[c + 1]):
                 J[self.jac_rowidx[p], c] = v[p]
         return J
+
+    def reactor_rhs(self, T, P, Y):
+        """dT/dt [n] and dY/dt [K, n] of constant-pressure ideal-gas reactors at these states
+        (IdealGasConstPressureReactor::eval, batched; numpy or torch CUDA arrays)."""
+        n, T, P, Y, flags = self._args(T, P, Y)
+        if flags:
+            import torch
+            dT = torch.empty(n, dtype=torch.float64, device=T.device)
+            dY = torch.empty((self.n_species, n), dtype=torch.float64, device=T.device)
+        else:
+            dT, dY = np.empty(n), np.empty((self.n_species, n))
+        _check(library().gb_reactor_rhs(self._h, n, _ptr(T), _ptr(P), _ptr(Y), _ptr(dT), _ptr(dY), flags))
+        return dT, dY
 
     def __del__(self):
         try:

@@ -82,13 +82,28 @@ struct MechEntry {
     DBuf dT, dP, dY, dW, dJ, dCounter;
     DBuf dChk;                                  // bounds-check record (checked build)
     cudaEvent_t evA = nullptr, evB = nullptr;   // around the last kinetics kernel launch
+    cudaEvent_t evCaller = nullptr;             // the caller's default-stream work (afterCallerWork)
     double lastMs = 0.0;
     ~MechEntry() {
         if (evA) cudaEventDestroy(evA);
         if (evB) cudaEventDestroy(evB);
+        if (evCaller) cudaEventDestroy(evCaller);
         if (stream) cudaStreamDestroy(stream);
     }
 };
+
+// Device arrays a caller hands in (GB_DEVICE_POINTERS) have usually just been written by its
+// kernels on the default stream, and the engine's stream is a non-blocking one, which does not
+// wait for the default stream by itself: make it wait for the work already issued to the legacy
+// and the per-thread default streams before it reads them (an event dependency, no host
+// synchronisation).  Arrays written on another stream must be synchronised by the caller.
+void afterCallerWork(MechEntry& e) {
+    if (!e.evCaller) ck(cudaEventCreateWithFlags(&e.evCaller, cudaEventDisableTiming), "event");
+    ck(cudaEventRecord(e.evCaller, cudaStreamLegacy), "record the default stream's work");
+    ck(cudaStreamWaitEvent(e.stream, e.evCaller, 0), "wait for the default stream's work");
+    ck(cudaEventRecord(e.evCaller, cudaStreamPerThread), "record the per-thread stream's work");
+    ck(cudaStreamWaitEvent(e.stream, e.evCaller, 0), "wait for the per-thread stream's work");
+}
 
 struct NetEntry {
     int mech;
@@ -501,6 +516,7 @@ int32_t runRates(int32_t h, int32_t n, const double* T, const double* P, const d
     const bool dev = (flags & GB_DEVICE_POINTERS) != 0;
     const int K = e.m.K;
     cudaStream_t s = e.stream;
+    if (dev) afterCallerWork(e);
     const double* dT = stage(T, n, e.dT, dev, s);
     const double* dP = stage(P, n, e.dP, dev, s);
     const double* dY = stage(Y, (size_t)K * n, e.dY, dev, s);
@@ -984,6 +1000,7 @@ int32_t gb_net_set_state(int32_t h, const double* T, const double* P, const doub
         const int K = me.m.K, n = ne.n;
         auto kind = (flags & GB_DEVICE_POINTERS) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
         cudaStream_t s = me.stream;
+        if (flags & GB_DEVICE_POINTERS) afterCallerWork(me);
         ck(cudaMemcpyAsync(ne.dT.p, T, (size_t)n * 8, kind, s), "copy T");
         ck(cudaMemcpyAsync(ne.dP.p, P, (size_t)n * 8, kind, s), "copy P");
         ck(cudaMemcpyAsync(ne.dY.p, Y, (size_t)K * n * 8, kind, s), "copy Y");
@@ -1432,6 +1449,7 @@ int32_t gb_reactor_rhs(int32_t h, int32_t n, const double* T, const double* P, c
         const bool dev = (flags & GB_DEVICE_POINTERS) != 0;
         const int K = e.m.K;
         cudaStream_t s = e.stream;
+        if (dev) afterCallerWork(e);
         const double* dT = stage(T, n, e.dT, dev, s);
         const double* dP = stage(P, n, e.dP, dev, s);
         const double* dY = stage(Y, (size_t)K * n, e.dY, dev, s);

@@ -10,7 +10,9 @@
  * Array layout: state batches are species-major, Y[k*n + s] for species k of state s
  * (T[s], P[s] one value per state).  Pointers are host pointers unless `flags` has
  * GB_DEVICE_POINTERS, in which case they are CUDA device pointers on the engine's
- * device.  Every call returns after the GPU work it starts has finished.
+ * device; the engine reads them after the work already issued to the legacy and the
+ * per-thread default streams (arrays written on another stream must be synchronised by the
+ * caller first).  Every call returns after the GPU work it starts has finished.
  *
  * Threading: a handle is used by one host thread at a time; distinct handles may be
  * used from distinct threads.  The last error message is kept per host thread.
