@@ -3,7 +3,8 @@ has already queued on the default stream.  The engine runs on a non-blocking str
 own, so without that ordering a call can read an input that the caller's last kernels have
 not written yet.  Each test queues a few tens of milliseconds of work on torch's default
 stream, writes the input only after it (replacing a sentinel), calls the engine at once and
-compares with the same call on host arrays."""
+compares with the same call on host arrays.  (Without the ordering the set_state and reactor
+right-hand-side tests read the sentinel; the rates call happened to order itself.)"""
 import numpy as np
 import pytest
 
@@ -13,11 +14,11 @@ pytestmark = pytest.mark.gpu
 
 
 def _queue_work_then_write(dst, src):
-    """Queue about 20 ms of kernels on the current (default) stream, then write src into dst
+    """Queue about 25 ms of kernels on the current (default) stream, then write src into dst
     with a kernel that runs after them; returns without waiting."""
     import torch
     big = torch.ones(1 << 26, device=dst.device)
-    for _ in range(100):
+    for _ in range(300):
         big.mul_(1.0000001)
     dst.copy_(src + 0.0 * big[:1].double())
 
@@ -30,9 +31,12 @@ def test_rates_read_inputs_after_the_default_streams_work():
     ref = sol.net_production_rates(T, P, Y)
     Ts, Pd, Yd = (torch.tensor(a, device="cuda") for a in (T, P, Y))
     Td = torch.full((n,), 5000.0, dtype=torch.float64, device="cuda")     # the sentinel
+    # the output allocated up front: an allocation inside the timed window could call
+    # cudaMalloc, whose implicit device synchronisation would hide a missing ordering
+    w = torch.empty((sol.n_species, n), dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
     _queue_work_then_write(Td, Ts)
-    w = sol.net_production_rates(Td, Pd, Yd)
+    sol.net_production_rates(Td, Pd, Yd, out=w)
     assert np.array_equal(w.cpu().numpy(), ref)
 
 
