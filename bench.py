@@ -180,7 +180,7 @@ def read_traffic():
     return read_profile_value("traffic_bytes_per_launch")
 
 
-SUR = dict(dt=1e-6, train_reactors=65536, held_reactors=65536, hidden=512, layers=4, epochs=6, batch=16384,
+SUR = dict(dt=1e-6, train_reactors=65536, held_reactors=65536, hidden=512, layers=4, epochs=12, batch=16384,
            lr=1e-3, times=tuple([0.0] + [float(t) for t in np.logspace(-6, -2, 63)]),
            held_times=(0.0, 2e-5, 5e-5, 2e-4, 5e-4, 1e-3, 1.5e-3, 2.5e-3, 3e-3, 3.5e-3, 4.5e-3, 5e-3, 6.5e-3, 7e-3,
                        9e-3, 1e-2))
