@@ -111,7 +111,7 @@ struct NetEntry {
     gb_net_options opts;
     double time = 0.0;
     int warpsPerBlock = 0, blocks = 0, ld = 0, warpDoubles = 0, recStride = 0;
-    DBuf dP, dT, dY, dRec, dStats, dStatus, dTign, dCounter, dOrder, dM, dJ, dJS, dTnow, dKStats;
+    DBuf dP, dT, dY, dRec, dStats, dStatus, dTign, dCounter, dOrder, dM, dJ, dJS, dTnow, dKStats, dKz;
     bool krylov = false;  // the mole reactor with GMRES and the adaptive preconditioner
     size_t JSstride = 0;  // bytes per Jacobian-scratch slot in dJS (with global matrices)
     size_t Jstride = 0;   // bytes per kept-Jacobian slot in dJ (0: no Jacobian reuse)
@@ -649,6 +649,7 @@ void netLaunch(NetEntry& ne, MechEntry& me, double t0, double tout, bool oneStep
     p.mechSmem = ne.mechSmem;
     p.luSlots = ne.luSlots; p.luSlotBytes = ne.luSlotBytes;
     p.kstats = ne.krylov ? ne.dKStats.as<long long>() : nullptr;
+    p.kzBuf = ne.krylov ? ne.dKz.as<double>() : nullptr;
     ck(cudaMemsetAsync(ne.dCounter.p, 0, sizeof(int), me.stream), "memset");
     if (ne.krylov)
         ck(ne.opts.lu_precision == 32 ? launchBdfKrylov32(p, ne.blocks, ne.warpsPerBlock, me.stream)
@@ -951,6 +952,7 @@ int32_t gb_net_new(int32_t h, int32_t n, const gb_net_options* opts) {
         if (ne->krylov) {
             ne->dKStats.ensure((size_t)n * 3 * 8);
             ck(cudaMemset(ne->dKStats.p, 0, (size_t)n * 24), "memset");
+            ne->dKz.ensure((size_t)kKrylovMaxl * N * 8 * ne->blocks * wpb);   // preconditioned vectors per warp
         }
         const int K = me.m.K;
         ne->dP.ensure((size_t)n * 8);

@@ -710,7 +710,7 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
 // column j), so that the factorisation's updates and both triangular sweeps read and write
 // whole rows (coalesced).
 // =============================================================================
-constexpr int kMaxl = 5;               // Krylov vectors (CVODE's default)
+constexpr int kMaxl = kKrylovMaxl;     // Krylov vectors (CVODE's default)
 constexpr double kEplifac = 0.05;      // linear tolerance factor (CVODE's default)
 constexpr double kIlutTau = 1e-12;     // drop tolerance the adaptive preconditioner gives ILUT
 constexpr int kIlutFillFactor = 10;    // ILUT's fill factor (the library default it keeps)
@@ -1075,6 +1075,7 @@ struct BdfWarp {
     int* piv;
     double* V;               // Krylov path: the Krylov basis, (kMaxl + 1) N-vectors
     double* Hs;              // Krylov path: the GMRES scalars (kGmresScalars)
+    double* Zs;              // Krylov path: the preconditioned basis vectors, kMaxl N-vectors (global)
 
     __device__ double wrms(const double* v) const {
         double a = 0.0;
@@ -1245,6 +1246,10 @@ struct BdfWarp {
             for (int i = lane; i < N; i += 32) z[i] = vl[i] / ewt[i];
             __syncwarp();
             precSolve<MT, NS>(Ft, z);
+            // keep z_l = P^-1 S^-1 v_l: the solution P^-1 S^-1 (V y) is sum_l y_l z_l
+            double* zl = Zs + (size_t)l * N;
+#pragma unroll 1
+            for (int i = lane; i < N; i += 32) zl[i] = z[i];
             if (!jtimes(z, Az, b, S)) return 1;
             double pk = 0.0;
 #pragma unroll 1
@@ -1325,17 +1330,16 @@ struct BdfWarp {
             }
         }
         __syncwarp();
+        // x = P^-1 S^-1 (V y) = sum_j y_j z_j: the preconditioned vectors kept during the
+        // iterations (the reference's SPGMR forms V y and applies the preconditioner once more;
+        // the same vector by linearity, one solve fewer)
 #pragma unroll 1
         for (int i = lane; i < N; i += 32) {
             double sacc = 0.0;
 #pragma unroll 1
-            for (int j = 0; j < mv; j++) sacc += yv[j] * V[(size_t)j * N + i];
-            z[i] = sacc / ewt[i];
+            for (int j = 0; j < mv; j++) sacc += yv[j] * Zs[(size_t)j * N + i];
+            b[i] = sacc;
         }
-        __syncwarp();
-        precSolve<MT, NS>(Ft, z);
-#pragma unroll 1
-        for (int i = lane; i < N; i += 32) b[i] = z[i];
         __syncwarp();
         if (converged) return 0;
         if (rho < beta && mnewt == 0) return 0;
@@ -1827,8 +1831,9 @@ __global__ void __launch_bounds__(kBdfMaxThreads, 1) k_bdf(BdfParams p) {
     if (kKry) {
         W.V = q; q += (kMaxl + 1) * N;
         W.Hs = q; q += kGmresScalars;
+        W.Zs = p.kzBuf + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * kMaxl * N;
     } else {
-        W.V = W.Hs = nullptr;
+        W.V = W.Hs = W.Zs = nullptr;
     }
     MT* M = p.Mbuf ? (MT*)((char*)p.Mbuf + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * p.Mstride)
                    : (MT*)q;

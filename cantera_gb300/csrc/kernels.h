@@ -77,9 +77,12 @@ struct BdfParams {
     double* tnow;         // [n] internal time of each reactor after the launch (or null)
     long long* kstats;    // Krylov path: [n][3] linear iterations, preconditioner solves,
                           // J v products (null otherwise)
+    double* kzBuf;        // Krylov path: the preconditioned basis vectors, kKrylovMaxl N-vectors
+                          // per resident warp (null otherwise)
 };
 
 constexpr int kBdfMaxThreads = 256;   // at most 8 warps per block
+constexpr int kKrylovMaxl = 5;         // Krylov path: at most 5 Krylov vectors (CVODE's default)
 constexpr int kMaxLuSlots = 4;         // shared-memory factorisation buffers per block
 int bdfRecordStride(int N);
 int bdfNordsieckDoubles(int N);

@@ -93,7 +93,7 @@ def test_gmres_ignition_matches_oracle_and_direct_solvers(lu):
     and the GPU's dense path agree within the reference test's bars; with FP64 factors the GPU
     takes the oracle's step and iteration counts (to the rounding of a different arithmetic
     order); the Krylov counters have the same structure (one J v product per linear
-    iteration, more preconditioner solves)."""
+    iteration)."""
     import cantera_gb300 as gb
     from oracle import pyoracle as po
     m, T0, P, Y0 = _ignition_cases()
@@ -121,7 +121,10 @@ def test_gmres_ignition_matches_oracle_and_direct_solvers(lu):
     for i, k in ((0, "steps"), (1, "rhs_evals"), (2, "newton_iters")):
         assert np.all(np.abs(stg[k] - sto[:, i]) <= tol * sto[:, i] + 5), (k, stg[k], sto[:, i])
     lin, ps, jtv = kst["lin_iters"], kst["prec_solves"], kst["jt_vec_prod_evals"]
-    assert np.all(lin > 0) and np.all(jtv == lin) and np.all(ps > lin)
+    # one J v product and one preconditioner solve per linear iteration (the engine keeps the
+    # preconditioned vectors; the reference solves once more at the end of each GMRES call)
+    assert np.all(lin > 0) and np.all(jtv == lin) and np.all(ps == lin)
+    assert np.all(sto[:, 10] > sto[:, 9])
     assert np.all(np.abs(lin - sto[:, 9]) <= (0.15 if lu == 64 else 0.3) * sto[:, 9] + 10)
 
 
