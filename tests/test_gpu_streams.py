@@ -13,7 +13,7 @@ from conftest import gpu_solution, random_states
 pytestmark = pytest.mark.gpu
 
 
-def _queue_work_then_write(dst, src):
+def _queue_kernels_then_write(dst, src):
     """Queue about 25 ms of kernels on the current (default) stream, then write src into dst
     with a kernel that runs after them; returns without waiting."""
     import torch
@@ -35,7 +35,7 @@ def test_rates_read_inputs_after_the_default_streams_work():
     # cudaMalloc, whose implicit device synchronisation would hide a missing ordering
     w = torch.empty((sol.n_species, n), dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
-    _queue_work_then_write(Td, Ts)
+    _queue_kernels_then_write(Td, Ts)
     sol.net_production_rates(Td, Pd, Yd, out=w)
     assert np.array_equal(w.cpu().numpy(), ref)
 
@@ -57,7 +57,7 @@ def test_set_state_reads_inputs_after_the_default_streams_work():
     Td = torch.full((n,), 300.0, dtype=torch.float64, device="cuda")      # the sentinel
     net = gb.ReactorNet(sol, Td, Pd, Yd, rtol=1e-8, atol=1e-15)
     torch.cuda.synchronize()
-    _queue_work_then_write(Td, Ts)
+    _queue_kernels_then_write(Td, Ts)
     net.set_state(Td, Pd, Yd)
     assert net.advance(1e-4) == 0
     Tg, Yg = net.get_state()
@@ -74,6 +74,6 @@ def test_reactor_rhs_reads_inputs_after_the_default_streams_work():
     Ts, Pd, Yd = (torch.tensor(a, device="cuda") for a in (T, P, Y))
     Td = torch.full((n,), 5000.0, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
-    _queue_work_then_write(Td, Ts)
+    _queue_kernels_then_write(Td, Ts)
     dT, dY = sol.reactor_rhs(Td, Pd, Yd)
     assert np.array_equal(dT.cpu().numpy(), dT_ref) and np.array_equal(dY.cpu().numpy(), dY_ref)
