@@ -70,3 +70,30 @@ def test_copies_are_independent(gas):
     assert r.mass == pytest.approx(r.thermo.density * 2.0)
     with pytest.raises(NotImplementedError):
         IdealGasConstPressureReactor(gas, energy="off")
+
+
+def test_preconditioner_settings_without_engine(gas):
+    """The facade's Krylov-path switch (no engine needed until the first advance): an
+    AdaptivePreconditioner makes the network's linear solver GMRES, holds the reference's
+    defaults and refuses other settings; mass-fraction reactors with it are refused when the
+    network is built."""
+    import cantera_gb300.compat as ct
+    p = ct.AdaptivePreconditioner()
+    assert p.linear_solver_type == "GMRES"
+    assert (p.threshold, p.ilut_fill_factor, p.ilut_drop_tol) == (0.0, 10, 1e-12)
+    p.ilut_drop_tol = 1e-12          # the default is accepted
+    with pytest.raises(NotImplementedError):
+        p.ilut_fill_factor = 2
+    with pytest.raises(NotImplementedError):
+        p.threshold = 1e-8
+    gas.TPX = 1200.0, ct.one_atm, "H2:2, O2:1, N2:4"
+    net = ct.ReactorNet([ct.IdealGasConstPressureMoleReactor(gas), ct.IdealGasConstPressureMoleReactor(gas)])
+    assert net.linear_solver_type == "DENSE" and net.preconditioner is None
+    net.preconditioner = p
+    assert net.linear_solver_type == "GMRES" and net.preconditioner is p
+    with pytest.raises(NotImplementedError):
+        net.preconditioner = object()
+    mixed = ct.ReactorNet([ct.IdealGasConstPressureReactor(gas)])
+    mixed.preconditioner = ct.AdaptivePreconditioner()
+    with pytest.raises(ct.CanteraError, match="IdealGasConstPressureMoleReactor"):
+        mixed.advance(1e-3)
