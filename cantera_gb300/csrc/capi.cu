@@ -79,7 +79,7 @@ struct MechEntry {
     int smCount = 0;
     int device = -1;      // the CUDA device the mechanism's arena and stream live on
     // kinetics workspace
-    DBuf dT, dP, dY, dW, dJ, dCounter;
+    DBuf dT, dP, dY, dW, dJ, dCounter, dExt;
     DBuf dChk;                                  // bounds-check record (checked build)
     cudaEvent_t evA = nullptr, evB = nullptr;   // around the last kinetics kernel launch
     cudaEvent_t evCaller = nullptr;             // the caller's default-stream work (afterCallerWork)
@@ -549,6 +549,10 @@ int32_t runRates(int32_t h, int32_t n, const double* T, const double* P, const d
     // wdot alone: a tile of 32 states per block at a time; with the Jacobian: a state per warp
     const long long units = dJ ? ((long long)n + wpb - 1) / wpb : ((long long)n + kRatesTile - 1) / kRatesTile;
     int blocks = (int)std::min<long long>((long long)e.smCount * blocksPerSm, units);
+    if (dJ) {   // kfe and rkc of each resident warp (the Jacobian's per-reaction data)
+        e.dExt.ensure((size_t)blocks * wpb * 2 * e.dm.R * 8);
+        p.ext = e.dExt.as<double>();
+    }
     if (!e.evA) {
         ck(cudaEventCreate(&e.evA), "event");
         ck(cudaEventCreate(&e.evB), "event");

@@ -48,8 +48,9 @@ __global__ void __launch_bounds__(256, 1) k_rates(RatesParams p) {
     double* tile = smem + p.mechSmem / 8;     // rows: T, P, then Y_k / wdot_k, each LD doubles
     double* base = tile + p.tileDoubles + (size_t)warp * p.warpDoubles;
     KinScratch s;
-    const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
-    s.carve(base, m.K, m.R, m.NTB, m.NF, m.NT);
+    double* ext = p.ext ? p.ext + (size_t)(blockIdx.x * W + warp) * 2 * m.R : nullptr;
+    const int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT, ext != nullptr);
+    s.carve(base, m.K, m.R, m.NTB, m.NF, m.NT, ext);
     s.tab = s_tab;
     double* Yl = base + kinD;
     double* gk = Yl + K;
@@ -2194,7 +2195,7 @@ int bdfWarpDoublesNoMatrix(const DevMech& m) {
 int bdfKrylovDoubles(int N) { return (((kMaxl + 1) * N + kGmresScalars) + 1) & ~1; }
 
 int ratesWarpDoubles(const DevMech& m, bool jac) {
-    int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT);
+    int kinD = KinScratch::doubles(m.K, m.R, m.NTB, m.NF, m.NT, jac);
     int tot = kinD + 2 * m.K + (jac ? m.nnz : 0);
     return (tot + 1) & ~1;
 }

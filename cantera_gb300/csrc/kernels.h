@@ -21,6 +21,9 @@ struct RatesParams {
     int warpDoubles;      // shared-memory doubles per warp
     int mechSmem;         // bytes of the mechanism arena copied into shared memory
     int tileDoubles;      // the block's state tile (wdot alone; 0 with the Jacobian)
+    double* ext;          // with the Jacobian: kfe and rkc (2R doubles) of each resident warp in
+                          // global memory (block b, warp w at ext + (b * warps + w) * 2R), so
+                          // that more warps fit in shared memory; null: in the warp's slice
 };
 constexpr int kRatesTile = 32;   // consecutive states per block tile of the rates kernel
 // the block's state tile in shared memory: rows T, P, Y_0..Y_{K-1} of kRatesTile + 1 doubles
@@ -89,7 +92,8 @@ int bdfNordsieckDoubles(int N);
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32);
 int bdfWarpDoublesNoMatrix(const DevMech& m);   // the slice when the matrix (and the Jacobian
                                                  // scratch kfe, rkc) are in global memory
-int ratesWarpDoubles(const DevMech& m, bool jac);   // the pattern-sized Jacobian only with jac
+int ratesWarpDoubles(const DevMech& m, bool jac);   // the pattern-sized Jacobian only with jac;
+                                                     // with jac, kfe and rkc in RatesParams::ext
 cudaError_t launchRates(const RatesParams& p, int blocks, int warpsPerBlock, cudaStream_t stream);
 cudaError_t launchBdf(const BdfParams& p, int blocks, int warpsPerBlock, bool fp32, cudaStream_t stream);
 // resident blocks per SM of the integrator kernel for this launch shape (registers included)
