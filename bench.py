@@ -161,6 +161,27 @@ def algorithmic_flops(stats, fm, fp32_lu):
     return float(f64), float(f32)
 
 
+def integrator_roofline(f64, f32, n, fp32_lu, kernel_ms, fp, sms):
+    """Roofline of one integrator launch of n reactors under the operation model: the model's
+    FP64 FLOPs of the advance (f64, from that advance's per-reactor counters) over the launch's
+    CUDA-event time, against the FP64 FMA rate measured by this run.  With the FP32 Newton
+    matrix, the factorisations and solves are FP32 work (f32); the model's time is then
+    F64 / peak64 + F32 / peak32, with peak32 the nominal FP32 rate (SMs x 128 lanes x 2 x
+    2.07 GHz)."""
+    s = kernel_ms / 1e3
+    peak = fp["gflops"] / 1e3
+    out = {"bound": "fp64", "achieved": f64 / s / 1e12, "peak": peak, "unit": "TFLOP/s",
+           "frac": f64 / s / 1e12 / peak, "flops_per_reactor": f64 / n,
+           "ceiling_reactors_per_s": peak * 1e12 / (f64 / n),
+           "peak_source": "FP64 FMA rate measured live by this run"}
+    if fp32_lu:
+        peak32 = sms * 128 * 2 * 2.07e9 / 1e12
+        t_model = f64 / (peak * 1e12) + f32 / (peak32 * 1e12)
+        out.update({"fp32_flops_per_reactor": f32 / n, "fp32_peak_nominal": peak32,
+                    "model_time_frac": t_model / s, "ceiling_reactors_per_s": n / t_model})
+    return out
+
+
 def read_profile_value(key, name="k_bdf_gri30_uneven.md"):
     """A `key: value ...` figure of a committed ncu summary (None if absent)."""
     path = os.path.join(ROOT, "profiles", name)
@@ -437,13 +458,16 @@ def time_advance(net, T, P, Y, t_end, flush, torch):
     return bad, net.last_kernel_ms, 1e3 * (time.perf_counter() - t0)
 
 
-def variant_h2o2(dev, torch, flush, threads):
+def variant_h2o2(dev, torch, flush, threads, fp):
     """Plain method, small: h2o2, 1,024 reactors, T0 U[1000,1600] K, 1 atm, H2/air phi
     U[0.5,2.0] (seed 20261203), to 1e-3 s at rtol 1e-8, atol 1e-15, every reactor compared
-    with the oracle (reference configuration and tight run)."""
+    with the oracle (reference configuration and tight run).  fp: the FP64 rate measured by
+    this run (the roofline's peak)."""
     import cantera_gb300 as gb
     from oracle import pyoracle as po
     sol = gb.Solution("h2o2.yaml", "ohmech")
+    fm = flop_model(sol.structure(), sol.n_species + 1)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
     n, t_end, rtol, atol = 1024, 1e-3, 1e-8, 1e-15
     rng = np.random.default_rng(20261203 + 0)
     T0 = rng.uniform(1000.0, 1600.0, n)
@@ -460,9 +484,12 @@ def variant_h2o2(dev, torch, flush, threads):
         runs = [time_advance(net, Td, Pd, Yd, t_end, flush, torch) for _ in range(5)]
         ms = float(np.median([r[1] for r in runs]))
         Tg, Yg = net.get_state()
+        st = net.solver_stats           # the last advance's counters (set_state resets them)
         res[name] = {"value": n / (ms / 1e3), "unit": "reactors/s", "kernel_ms": ms,
                      "failed_reactors": int(runs[-1][0]),
-                     "solver_stats_mean": {k: float(v.mean()) for k, v in net.solver_stats.items()}}
+                     "solver_stats_mean": {k: float(v.mean()) for k, v in st.items()},
+                     "roofline": integrator_roofline(*algorithmic_flops(st, fm, lu == 32), n, lu == 32,
+                                                     runs[-1][1], fp, sms)}
         gpu[name] = (Tg, Yg.T, net.ignition_times)
         del net
     m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", "h2o2.yaml"), "ohmech")
@@ -551,15 +578,18 @@ def variant_rates(dev, torch, flush, threads, n=1 << 20, peaks=None):
                                                        % (ns, po.FLAGS[True])}}
 
 
-def variant_ndodecane(dev, torch, flush, threads, n=16384, sample=64):
+def variant_ndodecane(dev, torch, flush, threads, fp, n=16384, sample=64):
     """Mixed-precision Newton and the Krylov path: nDodecane_IG (K=100, R=553), 16,384 reactors,
     T0 U[700,1400] K, P log-U[10,60] atm, n-dodecane/air phi U[0.5,2.0] (seed 20261206), to
-    5e-3 s at rtol 1e-8: the dense path with FP64 and FP32 Newton matrices, the mole reactor
-    with GMRES and the adaptive preconditioner (FP64 and FP32 factors), with Newton counts and
-    the error protocol on a sample."""
+    5e-3 s at rtol 1e-8: the dense path with FP64 and FP32 Newton matrices (each with its
+    roofline; fp: the FP64 rate measured by this run), the mole reactor with GMRES and the
+    adaptive preconditioner (FP64 and FP32 factors), with Newton counts and the error protocol
+    on a sample."""
     import cantera_gb300 as gb
     from oracle import pyoracle as po
     sol = gb.Solution("nDodecane_Reitz.yaml", "nDodecane_IG")
+    fm = flop_model(sol.structure(), sol.n_species + 1)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
     t_end, rtol, atol = 5e-3, 1e-8, 1e-15
     rng = np.random.default_rng(20261203 + 3)
     T0 = rng.uniform(700.0, 1400.0, n)
@@ -580,6 +610,9 @@ def variant_ndodecane(dev, torch, flush, threads, n=16384, sample=64):
                      "failed_reactors": int(bad), "launch": net.launch_info,
                      "newton_iters_mean": float(st["newton_iters"].mean()), "steps_mean": float(st["steps"].mean()),
                      "solver_stats_mean": {k: float(v.mean()) for k, v in st.items()}}
+        if solver == "DENSE":
+            res[name]["roofline"] = integrator_roofline(*algorithmic_flops(st, fm, lu == 32), n, lu == 32, ms,
+                                                        fp, sms)
         if solver == "GMRES":
             res[name]["solver_stats_mean"].update({k: float(v.mean()) for k, v in net.krylov_stats.items()})
             res[name]["method"] = ("IdealGasConstPressureMoleReactor with GMRES and the adaptive preconditioner "
@@ -620,8 +653,8 @@ def run_workload(args):
     torch.cuda.set_device(0)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     threads = os.cpu_count()
+    import cantera_gb300 as gb
     if args.workload == "gemm":
-        import cantera_gb300 as gb
         from cantera_gb300.surrogate import Surrogate
         sur = Surrogate(gb.Solution("gri30.yaml", "gri30"), hidden=SUR["hidden"], layers=SUR["layers"], seed=0,
                         device=str(dev))
@@ -631,8 +664,8 @@ def run_workload(args):
         return
     fn = {"rates": lambda: variant_rates(dev, torch, flush, threads, n=args.n or 1 << 20,
                                          peaks=measured_peaks()),
-          "ndodecane": lambda: variant_ndodecane(dev, torch, flush, threads, n=args.n or 16384),
-          "h2o2": lambda: variant_h2o2(dev, torch, flush, threads)}[args.workload]
+          "ndodecane": lambda: variant_ndodecane(dev, torch, flush, threads, gb.measure_fp64(), n=args.n or 16384),
+          "h2o2": lambda: variant_h2o2(dev, torch, flush, threads, gb.measure_fp64())}[args.workload]
     line = dict(workload=args.workload, n_gpus=1, dtype="f64", data="synthetic", higher_is_better=True)
     line.update(fn())
     print(json.dumps(line))
@@ -852,6 +885,11 @@ def main():
                 "value": n_all * rv["steps"] / (rv["ms"] / 1e3), "unit": "reactors/s",
                 "ms_per_step": rv["ms"] / rv["steps"], "solver_stats_mean": rv["stats"],
                 "failed_reactors": rv["failed"], "launch": rv["launch"], "clocks": rv["clocks"]}
+    if "fp32_lu" in results:
+        rv = results["fp32_lu"]
+        line["variants"]["fp32_lu"]["roofline"] = integrator_roofline(
+            rv["f64"], rv["f32"], n, True, rv["kernel_ms"] / rv["steps"], fp,
+            torch.cuda.get_device_properties(dev).multi_processor_count)
     if "gmres" in results:
         line["variants"]["gmres"]["method"] = ("IdealGasConstPressureMoleReactor with GMRES and the adaptive "
                                               "preconditioner (ILUT of I - gamma Jp in a minimum-degree order), FP64")
@@ -860,9 +898,9 @@ def main():
     # and its CPU baseline
     if not args.no_workloads and ws == 1:
         wl = {}
-        for name, fn in (("h2o2_1024", lambda: variant_h2o2(dev, torch, flush, threads)),
+        for name, fn in (("h2o2_1024", lambda: variant_h2o2(dev, torch, flush, threads, fp)),
                          ("rates_gri30_2p20", lambda: variant_rates(dev, torch, flush, threads, peaks=measured_peaks())),
-                         ("ndodecane_16384", lambda: variant_ndodecane(dev, torch, flush, threads))):
+                         ("ndodecane_16384", lambda: variant_ndodecane(dev, torch, flush, threads, fp))):
             try:
                 t0 = time.perf_counter()
                 wl[name] = fn()
