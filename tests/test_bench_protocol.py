@@ -82,6 +82,19 @@ def test_flop_model_and_roofline_arithmetic():
     assert abs(f64 - expect) <= 1e-9 * expect and f32 == 0.0
     f64b, f32b = bench.algorithmic_flops(stats, fm, True)
     assert abs(f64b + f32b - f64) <= 1e-9 * f64 and f32b > 0
+    # the roofline of one launch: FP64 model FLOPs over the launch time against the measured
+    # rate; with the FP32 matrix the model's time adds the FP32 part at the nominal FP32 rate
+    fp = {"gflops": 1250.0}
+    r = bench.integrator_roofline(f64, f32, n, False, 2.0, fp, 152)
+    assert abs(r["achieved"] - f64 / 2e-3 / 1e12) <= 1e-12 * r["achieved"]
+    assert abs(r["frac"] - r["achieved"] / 1.25) <= 1e-12 and r["unit"] == "TFLOP/s"
+    assert abs(r["ceiling_reactors_per_s"] - 1.25e12 / (f64 / n)) <= 1e-9 * r["ceiling_reactors_per_s"]
+    r32 = bench.integrator_roofline(f64b, f32b, n, True, 2.0, fp, 152)
+    peak32 = 152 * 128 * 2 * 2.07e9
+    t_model = f64b / 1.25e12 + f32b / peak32
+    assert abs(r32["model_time_frac"] - t_model / 2e-3) <= 1e-12 * r32["model_time_frac"]
+    assert abs(r32["ceiling_reactors_per_s"] - n / t_model) <= 1e-9 * r32["ceiling_reactors_per_s"]
+    assert r32["frac"] < r["frac"]          # the FP64 part alone is smaller
 
 
 def test_timing_build_agrees_with_checker():
