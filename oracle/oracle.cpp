@@ -1714,6 +1714,27 @@ int32_t or_ilut(int32_t N, double* a) {
     return 0;
 }
 
+// The fill-reducing order the Krylov path factors its preconditioner in (K + 1 entries over
+// z = [T, n_1..n_K], order[new] = old), and the structural pattern of d(wdot)/dc it is built
+// on (CSC: colptr K + 1 entries, rowidx up to cap; returns nnz, or -1 when cap is too small).
+int32_t or_prec_order(int32_t h, int32_t* order) {
+    Kin* k = getKin(h);
+    if (!k || !order) return -1;
+    std::copy(k->precOrder.begin(), k->precOrder.end(), order);
+    return (int32_t)k->precOrder.size();
+}
+
+int32_t or_jac_pattern(int32_t h, int32_t cap, int32_t* colptr, int32_t* rowidx) {
+    Kin* k = getKin(h);
+    if (!k) return -1;
+    std::vector<int32_t> cp, ri;
+    jacobianPattern(k->m, cp, ri);
+    if ((int32_t)ri.size() > cap || !colptr || !rowidx) { g_err = "pattern buffer too small"; return -1; }
+    std::copy(cp.begin(), cp.end(), colptr);
+    std::copy(ri.begin(), ri.end(), rowidx);
+    return (int32_t)ri.size();
+}
+
 int32_t or_mole_precond_jacobian(int32_t h, double P, const double* z, double atol, double* J) {
     Kin* k = getKin(h);
     if (!k) return -1;

@@ -104,6 +104,8 @@ int32_t or_mole_precond_jacobian(int32_t h, double P, const double* z, double at
 /* The adaptive preconditioner's ILUT (the factorisation the Krylov path uses) of one N x N
  * row-major matrix, in place: L (unit diagonal, strictly lower) and U. */
 int32_t or_ilut(int32_t N, double* a);
+int32_t or_prec_order(int32_t h, int32_t* order);
+int32_t or_jac_pattern(int32_t h, int32_t cap, int32_t* colptr, int32_t* rowidx);
 
 // Advance n independent constant-pressure reactors from t=0 to t_end.
 //  T0[n], P[n], Y0[n][K] (reactor-major); outputs T[n], Y[n][K], stats[n][OR_NSTAT],

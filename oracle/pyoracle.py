@@ -100,6 +100,10 @@ def lib(fast=False):
         L.or_mole_precond_jacobian.argtypes = [I32, ctypes.c_double, D, ctypes.c_double, D]
         L.or_ilut.argtypes = [I32, D]
         L.or_ilut.restype = I32
+        L.or_prec_order.argtypes = [I32, ctypes.POINTER(I32)]
+        L.or_prec_order.restype = I32
+        L.or_jac_pattern.argtypes = [I32, I32, ctypes.POINTER(I32), ctypes.POINTER(I32)]
+        L.or_jac_pattern.restype = I32
         L.or_equivalence_ratio.argtypes = [I32, ctypes.c_double, D, D, D]
         L.or_mole_to_mass.argtypes = [I32, D, D]
         L.or_molecular_weights.argtypes = [I32, D]
@@ -220,6 +224,23 @@ class Mech:
         J = np.zeros((self.K + 1, self.K + 1))
         st = self.L.or_mole_precond_jacobian(self.h, P, _p(_c(z)), atol, _p(J))
         return J, st
+
+    def prec_order(self):
+        """The Krylov path's fill-reducing order of z = [T, n_1..n_K] (order[new] = old)."""
+        o = np.zeros(self.K + 1, dtype=np.int32)
+        if self.L.or_prec_order(self.h, o.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))) != self.K + 1:
+            raise RuntimeError(self.L.or_last_error().decode())
+        return o
+
+    def jac_pattern(self):
+        """The structural pattern of d(wdot)/dc (CSC colptr [K+1], rowidx [nnz])."""
+        cp = np.zeros(self.K + 1, dtype=np.int32)
+        ri = np.zeros(self.K * self.K, dtype=np.int32)
+        I = ctypes.POINTER(ctypes.c_int32)
+        nnz = self.L.or_jac_pattern(self.h, len(ri), cp.ctypes.data_as(I), ri.ctypes.data_as(I))
+        if nnz < 0:
+            raise RuntimeError(self.L.or_last_error().decode())
+        return cp, ri[:nnz].copy()
 
     def advance_batch(self, T0, P, Y0, t_end, o=None, threads=None):
         """Reactor-major Y0 [n][K].  Returns T [n], Y [n][K], stats [n][9], tign [n]."""

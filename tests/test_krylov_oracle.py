@@ -217,3 +217,74 @@ def test_ilut_right_looking_order_equals_row_by_row():
         with np.errstate(all="ignore"):
             F1, F2 = po.ilut(A), _ilut_right_looking(A)
         assert np.array_equal(F1, F2, equal_nan=True), trial
+
+
+def _symmetric_structure(K, cp, ri):
+    """Adjacency of Jp + Jp^T over z = [T, n_1..n_K]: the species block's pattern and the
+    dense T row and column (no diagonal)."""
+    N = K + 1
+    adj = np.zeros((N, N), dtype=bool)
+    adj[0, 1:] = adj[1:, 0] = True
+    for c in range(K):
+        for r in ri[cp[c]:cp[c + 1]]:
+            if r != c:
+                adj[1 + r, 1 + c] = adj[1 + c, 1 + r] = True
+    return adj
+
+
+def _elimination_fill(adj, order):
+    """Edges the symbolic elimination adds when the nodes are eliminated in `order`."""
+    adj = adj.copy()
+    alive = np.ones(len(adj), dtype=bool)
+    fill = 0
+    for v in order:
+        nb = np.flatnonzero(alive & adj[v])
+        sub = adj[np.ix_(nb, nb)]
+        fill += int((~sub).sum()) - len(nb)          # missing off-diagonal pairs
+        adj[np.ix_(nb, nb)] = True
+        adj[nb, nb] = False
+        alive[v] = False
+    return fill // 2
+
+
+@pytest.mark.parametrize("name", ["h2o2", "gri30", "nDodecane"])
+def test_preconditioner_order_is_greedy_minimum_degree(name):
+    """The Krylov path factors I - gamma Jp in a fill-reducing order that the engine and the
+    oracle share.  Restated here: the pattern covers every nonzero of the numeric Jp at a
+    generic state; the order eliminates, at every step, a remaining node of least degree in
+    the elimination graph (ties to the lowest index); it makes no more fill than the natural
+    order (for n-dodecane far less)."""
+    m = oracle_mech(name)
+    K, N = m.K, m.K + 1
+    cp, ri = m.jac_pattern()
+    assert cp[0] == 0 and cp[-1] == len(ri) and np.all(np.diff(cp) >= 0)
+    # pattern soundness against the numeric preconditioner Jacobian (all species present)
+    T, P = 1400.0, 5 * 101325.0
+    Y = np.random.default_rng(11).dirichlet(np.ones(K))
+    J, st = m.mole_precond_jacobian(P, mole_state(m, T, P, Y))
+    assert st == 0
+    inpat = np.zeros((K, K), dtype=bool)
+    for c in range(K):
+        inpat[ri[cp[c]:cp[c + 1]], c] = True
+    off = (J[1:, 1:] != 0.0) & ~np.eye(K, dtype=bool)
+    assert not np.any(off & ~inpat)
+    # greedy minimum degree, restated
+    adj0 = _symmetric_structure(K, cp, ri)
+    adj = adj0.copy()
+    alive = np.ones(N, dtype=bool)
+    expect = []
+    for _ in range(N):
+        deg = np.where(alive, (adj & alive[None, :]).sum(axis=1), N + 1)
+        v = int(np.argmin(deg))
+        nb = np.flatnonzero(alive & adj[v])
+        adj[np.ix_(nb, nb)] = True
+        adj[nb, nb] = False
+        alive[v] = False
+        expect.append(v)
+    order = m.prec_order()
+    assert sorted(order.tolist()) == list(range(N))
+    assert order.tolist() == expect
+    f_order, f_natural = _elimination_fill(adj0, order), _elimination_fill(adj0, range(N))
+    assert f_order <= f_natural
+    if name == "nDodecane":
+        assert f_order < 0.5 * f_natural
