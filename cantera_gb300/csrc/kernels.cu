@@ -365,7 +365,8 @@ __device__ __forceinline__ bool luLeft(MT* a, int N, int ld, int* piv, double* d
 // Right-looking LU with partial pivoting and physical row interchanges (row k of P A stored
 // in row k): for the larger matrices, where the trailing updates' parallel work beats the
 // left-looking form's sequential chain of N^2 / 2 shuffles (n-dodecane, N = 101: 646 against
-// 514 reactors/s).
+// 514 reactors/s).  The integrator runs its panel form (luRightPanel4), which gives the same
+// factors; this one states the order of operations that form keeps.
 template <typename MT>
 __device__ __forceinline__ bool luRight(MT* a, int N, int ld, int* piv, double* dinv, int lane) {
     bool nonsingular = true;
@@ -422,10 +423,112 @@ __device__ __forceinline__ bool luRight(MT* a, int N, int ld, int* piv, double* 
     return nonsingular;
 }
 
+// The right-looking LU above, blocked by panels of four columns: the panel's columns are
+// factored with the same pivot searches, full-row interchanges and scalings, and only then
+// are its four pivots applied to the rest of the matrix, each trailing entry loaded and stored
+// once per panel instead of once per pivot (a global store goes to L2).  Every entry receives
+// the same fused multiply-adds in the same pivot order as in luRight, with the same operands
+// (a row interchange inside the panel moves a row's multipliers with its not-yet-updated
+// trailing part), so the factors are bit for bit those of luRight.
+template <typename MT>
+__device__ __forceinline__ bool luRightPanel4(MT* a, int N, int ld, int* piv, double* dinv, int lane) {
+    constexpr int B = 4;
+    if (lane == 0)
+        for (int i = 0; i < N; i++) piv[i] = i;
+    __syncwarp();
+#pragma unroll 1
+    for (int k0 = 0; k0 < N; k0 += B) {
+        const int kend = min(k0 + B, N);
+        // the panel: columns k0 .. kend - 1
+#pragma unroll 1
+        for (int k = k0; k < kend; k++) {
+            unsigned long long bv = 0ULL;
+            int bi = N;
+            for (int i = k + lane; i < N; i += 32) {
+                const unsigned long long v = absKey(a[(size_t)i * ld + k]);
+                if (v > bv || bi == N) { bv = v; bi = i; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+            }
+            if (bv == 0ULL) return false;
+            if (bi != k) {
+                for (int j = lane; j < N; j += 32) {
+                    MT t = a[(size_t)k * ld + j];
+                    a[(size_t)k * ld + j] = a[(size_t)bi * ld + j];
+                    a[(size_t)bi * ld + j] = t;
+                }
+                if (lane == 0) { int t = piv[k]; piv[k] = piv[bi]; piv[bi] = t; }
+            }
+            __syncwarp();
+            const MT inv = (MT)1 / a[(size_t)k * ld + k];
+            if (lane == 0) dinv[k] = (double)inv;
+            // multipliers of column k, then pivot k applied to the panel's later columns
+#pragma unroll 1
+            for (int i = k + 1 + lane; i < N; i += 32) {
+                MT* r = a + (size_t)i * ld;
+                const MT l = r[k] * inv;
+                r[k] = l;
+                for (int j = k + 1; j < kend; j++) r[j] = fma(-l, a[(size_t)k * ld + j], r[j]);
+            }
+            __syncwarp();
+        }
+        const int nb = kend - k0;
+        // the trailing columns: the panel's rows first (row k0 + p receives pivots k0 .. k0 + p - 1
+        // in order), then the rows below (all the panel's pivots in order), lanes over columns
+#pragma unroll 1
+        for (int j = kend + lane; j < N; j += 32) {
+            MT u[B];
+#pragma unroll
+            for (int p = 0; p < B; p++) u[p] = p < nb ? a[(size_t)(k0 + p) * ld + j] : (MT)0;
+#pragma unroll
+            for (int p = 1; p < B; p++) {
+                if (p >= nb) break;
+                const MT* r = a + (size_t)(k0 + p) * ld + k0;
+#pragma unroll
+                for (int q = 0; q < p; q++) u[p] = fma(-r[q], u[q], u[p]);
+                a[(size_t)(k0 + p) * ld + j] = u[p];
+            }
+            int i = kend;
+            for (; i + 4 <= N; i += 4) {
+                MT l[4][B], v[4];
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    const MT* row = a + (size_t)(i + r) * ld;
+#pragma unroll
+                    for (int p = 0; p < B; p++) l[r][p] = p < nb ? row[k0 + p] : (MT)0;
+                    v[r] = row[j];
+                }
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+#pragma unroll
+                    for (int p = 0; p < B; p++)
+                        if (p < nb) v[r] = fma(-l[r][p], u[p], v[r]);
+                    a[(size_t)(i + r) * ld + j] = v[r];
+                }
+            }
+            for (; i < N; i++) {
+                MT* row = a + (size_t)i * ld;
+                MT v = row[j];
+#pragma unroll
+                for (int p = 0; p < B; p++)
+                    if (p < nb) v = fma(-row[k0 + p], u[p], v);
+                row[j] = v;
+            }
+        }
+        __syncwarp();
+    }
+    return true;
+}
+
 // The factorisation of an integrator instantiation with NS register slots per lane (N <= 32
 // NS): left-looking up to 64 components (h2o2 +5 %, gri30 +0.7 % FP64 / +3.7 % FP32 reactors/s
-// over the right-looking form), right-looking beyond.  kLazyRows<NS> tells the solve which
-// layout the factors have.
+// over the right-looking form), right-looking in panels of four beyond (n-dodecane, same factors
+// as the unblocked form: +9 % FP64, +14 % FP32 reactors/s).  kLazyRows<NS> tells the solve
+// which layout the factors have.
 template <int NS>
 constexpr bool kLazyRows = NS <= 2;
 
@@ -434,7 +537,7 @@ __device__ __noinline__ bool devLuFactor(MT* a, int N, int ld, int* piv, double*
     __syncwarp();
     bool ok;
     if constexpr (kLazyRows<NS>) ok = luLeft<MT, NS>(a, N, ld, piv, dinv, lane);
-    else ok = luRight<MT>(a, N, ld, piv, dinv, lane);
+    else ok = luRightPanel4<MT>(a, N, ld, piv, dinv, lane);
     __syncwarp();
     return ok;
 }
