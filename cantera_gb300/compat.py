@@ -23,8 +23,11 @@ thermo.py: ``TP``, ``TPX``, ``TPY``, ``X``, ``Y``, ``set_equivalence_ratio``,
 ``IdealGasConstPressureMoleReactor``, ``AdaptivePreconditioner`` (interfaces/cython/cantera/
 jacobians.py:120-200) and ``ReactorNet`` (interfaces/cython/cantera/reactor.py:1781-2100,
 2396-2415: ``advance``, ``step``, ``time``, ``initial_time``, ``reinitialize``, ``rtol``,
-``atol``, ``max_steps``, ``max_time_step``, ``solver_stats``, ``preconditioner``,
-``linear_solver_type``).  One ``ReactorNet`` over many reactors is one batched GPU network:
+``atol``, ``max_steps``, ``max_time_step``, ``max_order``, ``solver_stats``,
+``preconditioner``, ``linear_solver_type``, ``initialize``, ``verbose``, ``n_vars``,
+``get_state``, ``component_name``, ``global_component_index``; the integrator limits
+``max_err_test_fails``, ``max_nonlinear_iterations``, ``max_nonlinear_convergence_failures``
+at CVODE's defaults).  One ``ReactorNet`` over many reactors is one batched GPU network:
 every reactor is independent (no walls or inlets), shares the network's mechanism and
 tolerances, and reaches each ``advance`` time together.  A network of mole reactors with an
 ``AdaptivePreconditioner`` runs the engine's GMRES path (the mole-reactor state, the
@@ -222,15 +225,24 @@ class Solution:
 
 
 class IdealGasConstPressureReactor:
-    """A constant-pressure ideal-gas reactor holding its own copy of the gas state."""
+    """A constant-pressure ideal-gas reactor holding its own copy of the gas state.  Its
+    state vector is [mass, temperature, Y_1..Y_K] (src/zeroD/IdealGasConstPressureReactor.cpp:
+    16-26,133-155): the mass is fixed when a network initialises the reactor (as
+    density x volume) and conserved, the volume follows as mass / density."""
+    _components = ("mass", "temperature")
 
     def __init__(self, contents, *, name="", volume=1.0, energy="on"):
         if energy != "on":
             raise NotImplementedError("only the energy equation 'on' is supported")
         self.name = name
-        self.volume = float(volume)
+        self._volume = float(volume)
+        self._mass = None
         self._thermo = contents._copy()
         self._net = None
+
+    @property
+    def type(self):
+        return type(self).__name__
 
     @property
     def thermo(self):
@@ -247,17 +259,66 @@ class IdealGasConstPressureReactor:
 
     @property
     def mass(self):
-        return self._thermo.density * self.volume
+        return self._thermo.density * self._volume if self._mass is None else self._mass
+
+    @property
+    def volume(self):
+        return self._volume if self._mass is None else self._mass / self._thermo.density
+
+    @volume.setter
+    def volume(self, v):
+        self._volume = float(v)
+        self._mass = None
+
+    def _initialize(self):
+        self._mass = self._thermo.density * self.volume
 
     def insert(self, gas):
-        """Replace the contents (and state) of the reactor."""
+        """Replace the contents (and state) of the reactor; its volume is kept."""
+        self._volume = self.volume
+        self._mass = None
         self._thermo = gas._copy()
+
+    @property
+    def n_vars(self):
+        """Number of components of the reactor's state vector."""
+        return len(self._components) + self._thermo.n_species
+
+    def component_index(self, name):
+        """Index of a state component: a state variable's name or a species name."""
+        if name in self._components:
+            return self._components.index(name)
+        try:
+            k = self._thermo.species_index(name)
+        except (ValueError, KeyError, GBError):
+            k = -1
+        if k is None or k < 0:
+            raise CanteraError("%s::componentIndex: Component '%s' not found" % (self.type, name))
+        return len(self._components) + int(k)
+
+    def component_name(self, k):
+        """Name of the k-th component of the reactor's state vector."""
+        nc = len(self._components)
+        if 0 <= k < nc:
+            return self._components[k]
+        if nc <= k < self.n_vars:
+            return self._thermo.species_names[k - nc]
+        raise IndexError("%s::componentName: component %d outside [0, %d)" % (self.type, k, self.n_vars))
+
+    def get_state(self):
+        """The reactor's state vector."""
+        return np.concatenate([[self.mass, self.T], self._thermo.Y])
 
 
 class IdealGasConstPressureMoleReactor(IdealGasConstPressureReactor):
     """A constant-pressure ideal-gas reactor whose integrator state is T and the species
-    amounts (IdealGasConstPressureMoleReactor); the one reactor type that supports the
-    adaptive preconditioner."""
+    amounts (IdealGasConstPressureMoleReactor): [temperature, n_1..n_K] in kmol
+    (src/zeroD/IdealGasConstPressureMoleReactor.cpp:22-30,274-295); the one reactor type
+    that supports the adaptive preconditioner."""
+    _components = ("temperature",)
+
+    def get_state(self):
+        return np.concatenate([[self.T], self.mass * self._thermo.Y / self._thermo.molecular_weights])
 
 
 class AdaptivePreconditioner:
@@ -300,12 +361,21 @@ class AdaptivePreconditioner:
 class ReactorNet:
     """Independent reactors advanced together as one batched GPU network."""
 
+    # the integrator's fixed limits (CVODE's defaults, which the reference's CVODES keeps unless
+    # set): error-test failures per step, Newton iterations per solve, convergence failures
+    # per step
+    _fixed_limits = {"max_err_test_fails": 7, "max_nonlinear_iterations": 3,
+                     "max_nonlinear_convergence_failures": 10}
+
     def __init__(self, reactors=(), **engine_options):
         self._reactors = []
         self._precon = None
         self._opts = dict(engine_options)
         self._rtol, self._atol = 1e-9, 1e-15
         self._max_steps, self._max_time_step = 20000, 0.0
+        self._max_order = int(self._opts.pop("max_order", 5))
+        self._verbose = False
+        self._counts = {}
         self._t0 = 0.0
         self._t = 0.0
         self._engine = None
@@ -318,8 +388,102 @@ class ReactorNet:
         if r._net is not None and r._net is not self:
             raise ValueError("reactor already belongs to another network")
         r._net = self
+        # reproducible names for unnamed reactors, "<type>_<count>" (ReactorNet::updateNames,
+        # ReactorBase::setDefaultName: src/zeroD/ReactorNet.cpp:572-575, ReactorBase.cpp:54-65)
+        if r.name in ("", "(none)"):
+            r.name = "%s_%d" % (r.type, self._counts.get(r.type, 0))
+        self._counts[r.type] = self._counts.get(r.type, 0) + 1
         self._reactors.append(r)
         self._engine = None
+
+    def initialize(self):
+        """Initialise the integration now (otherwise the first advance or step does)."""
+        if self._engine is None:
+            self._build()
+
+    @property
+    def verbose(self):
+        """With True, (re)initialisations print the network's configuration."""
+        return self._verbose
+
+    @verbose.setter
+    def verbose(self, v):
+        self._verbose = bool(v)
+
+    @property
+    def max_order(self):
+        """Maximum order of the BDF method (1..5), applied at the next (re)initialisation as
+        the reference's CVODES does (CVodesIntegrator::applyOptions)."""
+        return self._max_order
+
+    @max_order.setter
+    def max_order(self, n):
+        n = int(n)
+        if not 1 <= n <= 5:
+            raise ValueError("max_order must be in 1..5")
+        self._max_order = n
+
+    def _limit(self, name, n):
+        if int(n) != self._fixed_limits[name]:
+            raise NotImplementedError("the engine's integrator uses %s = %d" % (name, self._fixed_limits[name]))
+
+    @property
+    def max_err_test_fails(self):
+        raise AttributeError("unreadable attribute 'max_err_test_fails'")
+
+    @max_err_test_fails.setter
+    def max_err_test_fails(self, n):
+        self._limit("max_err_test_fails", n)
+
+    @property
+    def max_nonlinear_iterations(self):
+        return self._fixed_limits["max_nonlinear_iterations"]
+
+    @max_nonlinear_iterations.setter
+    def max_nonlinear_iterations(self, n):
+        self._limit("max_nonlinear_iterations", n)
+
+    @property
+    def max_nonlinear_convergence_failures(self):
+        return self._fixed_limits["max_nonlinear_convergence_failures"]
+
+    @max_nonlinear_convergence_failures.setter
+    def max_nonlinear_convergence_failures(self, n):
+        self._limit("max_nonlinear_convergence_failures", n)
+
+    @property
+    def n_vars(self):
+        """Number of state variables of the network: the reactors' state vectors together."""
+        return sum(r.n_vars for r in self._reactors)
+
+    def _locate(self, i):
+        if i < 0:
+            raise IndexError("component %d outside [0, %d)" % (i, self.n_vars))
+        for r in self._reactors:
+            if i < r.n_vars:
+                return r, i
+            i -= r.n_vars
+        raise IndexError("component outside [0, %d)" % self.n_vars)
+
+    def component_name(self, i):
+        """Name of the i-th component of the network's state vector, 'reactor: component'
+        (ReactorNet::componentName, src/zeroD/ReactorNet.cpp:781-794)."""
+        r, k = self._locate(int(i))
+        return "%s: %s" % (r.name, r.component_name(k))
+
+    def global_component_index(self, name, reactor):
+        """Index in the network's state vector of component `name` of the reactor with index
+        `reactor` (ReactorNet::globalComponentIndex, src/zeroD/ReactorNet.cpp:774-779)."""
+        offset = sum(r.n_vars for r in self._reactors[:reactor])
+        return offset + self._reactors[reactor].component_index(name)
+
+    def get_state(self):
+        """The network's state vector: the reactors' state vectors one after another
+        (ReactorNet::getState, src/zeroD/ReactorNet.cpp:754-759)."""
+        if not self._reactors:
+            raise CanteraError("ReactorNet empty or not initialized.")
+        self.initialize()
+        return np.concatenate([r.get_state() for r in self._reactors])
 
     @property
     def reactors(self):
@@ -339,8 +503,14 @@ class ReactorNet:
                 raise CanteraError("the AdaptivePreconditioner needs IdealGasConstPressureMoleReactor reactors")
             opts["linear_solver"] = "GMRES"
         self._engine = _Net(g[0]._m, T, P, Y, rtol=self._rtol, atol=self._atol, max_steps=self._max_steps,
-                            max_time_step=self._max_time_step, **opts)
+                            max_time_step=self._max_time_step, max_order=self._max_order, **opts)
         self._t0 = self._t
+        for r in self._reactors:
+            r._initialize()
+        if self._verbose:
+            print("ReactorNet: %d %s reactor(s), %d species, %s linear solver, rtol %g, atol %g, max order %d, "
+                  "t0 = %g" % (len(self._reactors), self._reactors[0].type, g[0].n_species, self.linear_solver_type,
+                               self._rtol, self._atol, self._max_order, self._t0))
 
     def reinitialize(self):
         """Restart the integration from the reactors' current states at the current time."""

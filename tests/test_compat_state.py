@@ -97,3 +97,78 @@ def test_preconditioner_settings_without_engine(gas):
     mixed.preconditioner = ct.AdaptivePreconditioner()
     with pytest.raises(ct.CanteraError, match="IdealGasConstPressureMoleReactor"):
         mixed.advance(1e-3)
+
+
+def test_reactor_components_names_and_mass(gas):
+    """The reactors' state vectors and names as the reference defines them: [mass,
+    temperature, Y] for IdealGasConstPressureReactor, [temperature, n] for the mole reactor;
+    unnamed reactors get '<type>_<count>' when added to a network; the mass is fixed at
+    initialisation and conserved, the volume follows the density."""
+    import cantera_gb300.compat as ct
+    gas.TPX = 1200.0, 1e5, "H2:2, O2:1, N2:4"
+    a = ct.IdealGasConstPressureReactor(gas, volume=2.0)
+    b = ct.IdealGasConstPressureReactor(gas, name="hot")
+    c = ct.IdealGasConstPressureMoleReactor(gas)
+    net = ct.ReactorNet([a, b])
+    assert (a.name, b.name) == ("IdealGasConstPressureReactor_0", "hot")
+    assert a.n_vars == 6 and c.n_vars == 5 and net.n_vars == 12
+    assert [a.component_name(k) for k in range(6)] == ["mass", "temperature", "H2", "O2", "H2O", "N2"]
+    assert [c.component_name(k) for k in range(5)] == ["temperature", "H2", "O2", "H2O", "N2"]
+    assert a.component_index("temperature") == 1 and a.component_index("H2O") == 4
+    assert c.component_index("temperature") == 0 and c.component_index("H2O") == 3
+    with pytest.raises(ct.CanteraError, match="not found"):
+        a.component_index("CH4")
+    with pytest.raises(IndexError):
+        a.component_name(6)
+    assert net.component_name(0) == "IdealGasConstPressureReactor_0: mass"
+    assert net.component_name(7) == "hot: temperature"
+    with pytest.raises(IndexError):
+        net.component_name(12)
+    assert net.global_component_index("O2", 1) == 6 + 3
+    # mass and volume: density x volume until initialised, then the mass is kept
+    rho0 = a.density
+    assert a.mass == pytest.approx(2.0 * rho0) and a.volume == 2.0
+    a._initialize()
+    a.thermo.TP = 2400.0, 1e5                      # as an advance would heat it
+    assert a.mass == pytest.approx(2.0 * rho0)
+    assert a.volume == pytest.approx(4.0) and a.mass == pytest.approx(a.density * a.volume)
+    state = a.get_state()
+    assert state[0] == pytest.approx(2.0 * rho0) and state[1] == 2400.0
+    assert np.allclose(state[2:], a.thermo.Y)
+    n = c.get_state()[1:]
+    assert np.allclose(n * gas.molecular_weights, c.mass * c.thermo.Y)
+    a.insert(gas)                                  # new contents keep the current volume
+    assert a.volume == pytest.approx(4.0) and a.mass == pytest.approx(4.0 * gas.density)
+    m2 = ct.ReactorNet([ct.IdealGasConstPressureMoleReactor(gas), ct.IdealGasConstPressureReactor(gas)])
+    assert [r.name for r in m2.reactors] == ["IdealGasConstPressureMoleReactor_0", "IdealGasConstPressureReactor_0"]
+
+
+def test_network_integrator_settings_without_engine(gas):
+    """max_order is kept for the next initialisation (1..5); the integrator's fixed limits
+    (CVODE's defaults) are readable where the reference's are and refuse other values;
+    verbose is a flag."""
+    import cantera_gb300.compat as ct
+    gas.TPX = 1200.0, 1e5, "H2:2, O2:1, N2:4"
+    net = ct.ReactorNet([ct.IdealGasConstPressureReactor(gas)])
+    assert net.max_order == 5
+    net.max_order = 3
+    assert net.max_order == 3
+    with pytest.raises(ValueError):
+        net.max_order = 6
+    assert ct.ReactorNet(max_order=2).max_order == 2
+    with pytest.raises(AttributeError):
+        net.max_err_test_fails
+    net.max_err_test_fails = 7
+    with pytest.raises(NotImplementedError):
+        net.max_err_test_fails = 10
+    assert net.max_nonlinear_iterations == 3 and net.max_nonlinear_convergence_failures == 10
+    net.max_nonlinear_iterations = 3
+    with pytest.raises(NotImplementedError):
+        net.max_nonlinear_iterations = 5
+    with pytest.raises(NotImplementedError):
+        net.max_nonlinear_convergence_failures = 20
+    assert net.verbose is False
+    net.verbose = 1
+    assert net.verbose is True
+    with pytest.raises(ct.CanteraError, match="empty"):
+        ct.ReactorNet().get_state()

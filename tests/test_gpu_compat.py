@@ -139,3 +139,33 @@ def test_failures_raise(ct):
     other = ct.Solution("h2o2.yaml", "ohmech")
     with pytest.raises(NotImplementedError):
         ct.ReactorNet([ct.IdealGasConstPressureReactor(gas), ct.IdealGasConstPressureReactor(other)])
+
+
+def test_network_state_vector_and_max_order(ct):
+    """get_state after an advance: [mass, T, Y] per reactor with the initial mass conserved
+    (the volume follows the density), [T, n] for mole reactors; global_component_index into
+    it; max_order reaches the integrator at the next (re)initialisation."""
+    gas = ct.Solution("h2o2.yaml", "ohmech")
+    gas.TPX = 1200.0, ct.one_atm, "H2:2, O2:1, N2:4"
+    rho0 = gas.density
+    a, b = ct.IdealGasConstPressureReactor(gas, volume=0.5), ct.IdealGasConstPressureReactor(gas)
+    net = ct.ReactorNet([a, b])
+    net.advance(1e-3)
+    y = net.get_state()
+    assert y.shape == (net.n_vars,) and net.n_vars == 2 * (gas.n_species + 2)
+    assert y[0] == pytest.approx(0.5 * rho0, rel=1e-12) and a.mass == pytest.approx(0.5 * rho0, rel=1e-12)
+    assert a.T > 2000.0 and a.volume == pytest.approx(a.mass / a.density, rel=1e-12) and a.volume > 0.75
+    i = net.global_component_index("temperature", 1)
+    assert y[i] == b.T and net.component_name(i).endswith(": temperature")
+    assert np.array_equal(y[net.global_component_index("H2O", 0):][:1], a.thermo.Y[gas.species_index("H2O"):][:1])
+    m = ct.IdealGasConstPressureMoleReactor(gas)
+    mnet = ct.ReactorNet([m])
+    mnet.advance(1e-3)
+    z = mnet.get_state()
+    assert z[0] == m.T and np.allclose(z[1:] * gas.molecular_weights, m.mass * m.thermo.Y, rtol=1e-14)
+    # max order: a new value applies at the next initialisation
+    net.max_order = 2
+    net.reinitialize()
+    net.advance(2e-3)
+    assert np.all(net.solver_stats["last_order"] <= 2)
+    assert a.mass == pytest.approx(0.5 * rho0, rel=1e-12)
