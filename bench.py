@@ -20,8 +20,9 @@ against its tight run at rtol 1e-12, atol 1e-20, with ignition delays).
 
 Usage:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
         python bench.py --workload rates|ndodecane|h2o2|gemm (one workload's line alone)
-Under torchrun each rank takes a contiguous shard of the reactors (no collective on the
-data path); the time is the maximum over ranks.
+Under torchrun each rank advances its own 65,536 reactors, a contiguous shard of the N x 65,536
+drawn from the workload's distributions (weak scaling, no collective on the data path); the
+time is the maximum over ranks and the value counts the reactors of all ranks.
 """
 import argparse
 import json
@@ -682,10 +683,11 @@ def run_reference(args):
         return
     from oracle import pyoracle as po
     m = po.Mech(os.path.join(ROOT, "cantera_gb300", "data", WL["mechanism"]), WL["phase"], fast=True)
-    T0, P, Y0 = workload_arrays(WL["n"], WL["seed"],
+    n_all = (args.n or WL["n"]) * ws          # the workload of the GPU arm at this world size
+    T0, P, Y0 = workload_arrays(n_all, WL["seed"],
                                 lambda p: m.equivalence_ratio(p, WL["fuel"], WL["oxidizer"]))
     threads = os.cpu_count()
-    idx = cpu_sample_indices(WL["n"], CPU_SAMPLE, WL["seed"])
+    idx = cpu_sample_indices(n_all, CPU_SAMPLE, WL["seed"])
     times = []
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
@@ -699,7 +701,7 @@ def run_reference(args):
             "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "gri30 uneven stiffness: %d reactors to %g s (bounded sample of %d per step)"
-                       % (WL["n"], WL["t_end"], len(idx)), "rtol": WL["rtol"], "atol": WL["atol"]},
+                       % (n_all, WL["t_end"], len(idx)), "rtol": WL["rtol"], "atol": WL["atol"]},
             "cpu_baseline": dict(cb, value=value),
             "e2e": {"value": value, "unit": "reactors/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -712,7 +714,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=None,
-                    help="states or reactors of the workload (default: the workload's own size)")
+                    help="states or reactors of the workload, per GPU for the headline (default: the "
+                         "workload's own size)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-gmres", action="store_true",
@@ -745,7 +748,9 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
         pg = dist
-    n_all = args.n or WL["n"]
+    # weak scaling: every rank advances its own n reactors (default 65,536), a contiguous shard
+    # of ws x n reactors drawn from the workload's distributions
+    n_all = (args.n or WL["n"]) * ws
     sol = gb.Solution(WL["mechanism"], WL["phase"])
     K = sol.n_species
     T0, P, Y0 = workload_arrays(n_all, WL["seed"],
