@@ -93,6 +93,7 @@ def library():
         "gb_check_status": (I32, [I32, P]),
         "gb_net_last_advance_ms": (D, [I32]),
         "gb_net_get_state": (I32, [I32, P, P, I32]),
+        "gb_net_get_derivative": (I32, [I32, I32, P, I32]),
         "gb_net_get_status": (I32, [I32, P]),
         "gb_net_solver_stats": (I32, [I32, P]),
         "gb_net_ignition_times": (I32, [I32, P]),
@@ -454,6 +455,17 @@ class ReactorNet:
             Y = np.empty((self.solution.n_species, self.n))
         _check(library().gb_net_get_state(self._h, _ptr(T), _ptr(Y), flags))
         return T, Y
+
+    def get_derivative(self, k, out=None):
+        """The k-th time derivative (0..5) of every reactor's integrator state at its output
+        time, from the integrator's step history (ReactorNet.get_derivative): [K + 1, n], row 0
+        temperature, then the mass fractions (dense solver) or the species amounts in kmol per
+        m^3 of initial volume (GMRES).  out: a numpy array or a torch CUDA tensor to fill."""
+        flags = GB_DEVICE_POINTERS if _is_torch_cuda(out) else 0
+        if out is None:
+            out = np.empty((self.solution.n_species + 1, self.n))
+        _check(library().gb_net_get_derivative(self._h, int(k), _ptr(out), flags))
+        return out
 
     @property
     def T(self):

@@ -25,8 +25,9 @@ jacobians.py:120-200) and ``ReactorNet`` (interfaces/cython/cantera/reactor.py:1
 2396-2415: ``advance``, ``step``, ``time``, ``initial_time``, ``reinitialize``, ``rtol``,
 ``atol``, ``max_steps``, ``max_time_step``, ``max_order``, ``solver_stats``,
 ``preconditioner``, ``linear_solver_type``, ``initialize``, ``verbose``, ``n_vars``,
-``get_state``, ``component_name``, ``global_component_index``; the integrator limits
-``max_err_test_fails``, ``max_nonlinear_iterations``, ``max_nonlinear_convergence_failures``
+``get_state``, ``get_derivative``, ``component_name``, ``global_component_index``; the
+integrator limits ``max_err_test_fails``, ``max_nonlinear_iterations``,
+``max_nonlinear_convergence_failures``
 at CVODE's defaults).  One ``ReactorNet`` over many reactors is one batched GPU network:
 every reactor is independent (no walls or inlets), shares the network's mechanism and
 tolerances, and reaches each ``advance`` time together.  A network of mole reactors with an
@@ -271,7 +272,8 @@ class IdealGasConstPressureReactor:
         self._mass = None
 
     def _initialize(self):
-        self._mass = self._thermo.density * self.volume
+        self._v_init = self.volume
+        self._mass = self._thermo.density * self._v_init
 
     def insert(self, gas):
         """Replace the contents (and state) of the reactor; its volume is kept."""
@@ -484,6 +486,28 @@ class ReactorNet:
             raise CanteraError("ReactorNet empty or not initialized.")
         self.initialize()
         return np.concatenate([r.get_state() for r in self._reactors])
+
+    def get_derivative(self, k):
+        """The k-th time derivative of the network's state vector at the current time, from
+        the integrator's step history (ReactorNet::getDerivative, src/zeroD/ReactorNet.cpp:
+        721-726): per reactor [mass (0 for k > 0, the mass being conserved), T, Y], or [T, n]
+        for a mole reactor.  After step() each reactor's derivative is at its own time."""
+        if not self._reactors:
+            raise CanteraError("ReactorNet empty or not initialized.")
+        if self._engine is None:
+            raise CanteraError("the network has not been integrated yet")
+        d = self._engine.get_derivative(int(k))
+        amounts = self._engine.linear_solver == "GMRES"
+        parts = []
+        for i, r in enumerate(self._reactors):
+            dT, dz = d[0, i], d[1:, i]
+            if isinstance(r, IdealGasConstPressureMoleReactor):
+                # the GMRES engine integrates the amounts per m^3 of the volume at initialisation
+                dn = dz * r._v_init if amounts else r.mass * dz / r.thermo.molecular_weights
+                parts.append(np.concatenate([[dT], dn]))
+            else:
+                parts.append(np.concatenate([[r.mass if k == 0 else 0.0, dT], dz]))
+        return np.concatenate(parts)
 
     @property
     def reactors(self):

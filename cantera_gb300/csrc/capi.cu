@@ -1307,6 +1307,54 @@ int32_t gb_net_get_state(int32_t h, double* T, double* Y, int32_t flags) {
     });
 }
 
+int32_t gb_net_get_derivative(int32_t h, int32_t k, double* out, int32_t flags) {
+    return guarded([&]() -> int32_t {
+        NetEntry& ne = net(h);
+        MechEntry& me = mech(ne.mech);
+        requireMechDevice(me);
+        const BdfRecordLayout L = bdfRecordLayout();
+        if (!out) throw std::runtime_error("null array argument");
+        if (k < 0 || k > L.qmax) throw std::runtime_error("derivative order k must be in 0.." + std::to_string(L.qmax));
+        const int N = me.m.K + 1, n = ne.n;
+        const size_t stride = (size_t)ne.recStride;
+        std::vector<double> rec((size_t)n * stride);
+        ck(cudaStreamSynchronize(me.stream), "integrator");
+        ck(cudaMemcpy(rec.data(), ne.dRec.p, rec.size() * 8, cudaMemcpyDeviceToHost), "copy records");
+        // c[j] = j! / (j - k)! for j >= k
+        double c[16] = {0.0};
+        for (int j = k; j <= L.qmax; j++) {
+            double v = 1.0;
+            for (int i = j - k + 1; i <= j; i++) v *= i;
+            c[j] = v;
+        }
+        std::vector<double> res((size_t)N * n);
+        for (int r = 0; r < n; r++) {
+            const double* z = rec.data() + (size_t)r * stride;
+            const double* o = z + (size_t)(L.qmax + 1) * N;
+            if (!(((int)o[L.flags]) & L.initFlag))
+                throw std::runtime_error("reactor " + std::to_string(r) + " has not been integrated since its state was set");
+            const double tn = o[L.tn], hh = o[L.h];
+            const int q = (int)o[L.q];
+            // the reactor's output time: the network's time after an advance (within the last
+            // step, tn >= t), its own internal time after a step or a failure (tn <= t)
+            const double t = std::min(ne.time, tn);
+            const double s = hh != 0.0 ? (t - tn) / hh : 0.0;
+            const double hk = (k == 0) ? 1.0 : (hh != 0.0 ? std::pow(hh, -k) : 0.0);
+            for (int i = 0; i < N; i++) {
+                double v = 0.0;
+                if (q >= k) {
+                    v = c[q] * z[(size_t)q * N + i];
+                    for (int j = q - 1; j >= k; j--) v = c[j] * z[(size_t)j * N + i] + s * v;
+                }
+                res[(size_t)i * n + r] = v * hk;
+            }
+        }
+        auto kind = (flags & GB_DEVICE_POINTERS) ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+        ck(cudaMemcpy(out, res.data(), res.size() * 8, kind), "copy derivative");
+        return 0;
+    });
+}
+
 int32_t gb_net_get_status(int32_t h, int32_t* status) {
     return guarded([&]() -> int32_t {
         NetEntry& ne = net(h);

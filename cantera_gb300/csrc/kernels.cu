@@ -2278,6 +2278,7 @@ cudaError_t launchReactorRhs(const RhsParams& p, int blocks, int warpsPerBlock, 
 
 int bdfRecordStride(int N) { return (QMAX + 1) * N + R_NSCAL; }
 int bdfNordsieckDoubles(int N) { return (QMAX + 1) * N; }
+BdfRecordLayout bdfRecordLayout() { return {QMAX, R_TN, R_H, R_Q, R_FLAGS, F_INIT}; }
 
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32) {
     int N = m.N;

@@ -89,6 +89,12 @@ constexpr int kKrylovMaxl = 5;         // Krylov path: at most 5 Krylov vectors 
 constexpr int kMaxLuSlots = 4;         // shared-memory factorisation buffers per block
 int bdfRecordStride(int N);
 int bdfNordsieckDoubles(int N);
+// Where the host finds a reactor's step history in its integrator record: rec[j N + i] =
+// h^j y_i^(j) / j! (the Nordsieck array, j = 0..qmax, scaled by the current step size h), then
+// the step scalars at (qmax + 1) N + {tn, h, q, flags}; flags & initFlag: integrated at least
+// once since the last reset.
+struct BdfRecordLayout { int qmax, tn, h, q, flags, initFlag; };
+BdfRecordLayout bdfRecordLayout();
 int bdfWarpDoubles(const DevMech& m, int ld, bool fp32);
 int bdfWarpDoublesNoMatrix(const DevMech& m);   // the slice when the matrix (and the Jacobian
                                                  // scratch kfe, rkc) are in global memory

@@ -158,6 +158,17 @@ double gb_net_time(int32_t net);
  * the engine's stream around the launch). */
 double gb_net_last_advance_ms(int32_t net);
 int32_t gb_net_get_state(int32_t net, double* T, double* Y, int32_t flags);
+/* The k-th time derivative (0 <= k <= 5) of every reactor's integrator state at its output
+ * time - the network's time after gb_net_advance, the reactor's own time after gb_net_step or
+ * a failed step - from its Nordsieck history (ReactorNet::getDerivative,
+ * src/zeroD/ReactorNet.cpp:721-726, through CVodesIntegrator::derivative and CVodeGetDky,
+ * src/numerics/CVodesIntegrator.cpp:551-556).  out[N][n], species-major, N = K + 1: row 0 the
+ * temperature, rows 1..K the mass fractions (linear_solver 0) or the species amounts in kmol
+ * per m^3 of initial volume (linear_solver 1).  The interpolating polynomial of a reactor at
+ * order q < k gives 0 (CVODES refuses k > q for its one system).  Host array, or device with
+ * GB_DEVICE_POINTERS.  Returns 0, or GB_ERR before the first integration after a state was
+ * set. */
+int32_t gb_net_get_derivative(int32_t net, int32_t k, double* out, int32_t flags);
 
 /* Checkpoint of a network (no counterpart in the reference, whose CVODES state cannot be
  * saved; the nearest is ReactorNet::reinitialize from the reactors' states,

@@ -169,3 +169,36 @@ def test_network_state_vector_and_max_order(ct):
     net.advance(2e-3)
     assert np.all(net.solver_stats["last_order"] <= 2)
     assert a.mass == pytest.approx(0.5 * rho0, rel=1e-12)
+
+
+def test_network_get_derivative(ct):
+    """ReactorNet.get_derivative in the reference's layouts: [0, dT, dY] per mass-fraction
+    reactor (the mass being conserved), [dT, dn] per mole reactor, the amounts' derivatives
+    scaled to the reactor's size on either linear solver."""
+    gas = ct.Solution("h2o2.yaml", "ohmech")
+    gas.TPX = 1100.0, ct.one_atm, "H2:2, O2:1, N2:4"
+    a = ct.IdealGasConstPressureReactor(gas, volume=0.5)
+    net = ct.ReactorNet([a])
+    with pytest.raises(ct.CanteraError):
+        net.get_derivative(1)
+    net.rtol, net.atol = 1e-10, 1e-16
+    net.advance(1e-4)
+    d = net.get_derivative(1)
+    assert d.shape == (net.n_vars,) and d[0] == 0.0
+    y0 = net.get_derivative(0)
+    assert y0[0] == pytest.approx(a.mass, rel=1e-14) and y0[1] == pytest.approx(a.T, rel=1e-14)
+    moles = {}
+    for solver in ("DENSE", "GMRES"):
+        m = ct.IdealGasConstPressureMoleReactor(gas, volume=0.5)
+        mnet = ct.ReactorNet([m])
+        if solver == "GMRES":
+            mnet.preconditioner = ct.AdaptivePreconditioner()
+        mnet.rtol, mnet.atol = 1e-10, 1e-20
+        mnet.advance(1e-4)
+        dm = mnet.get_derivative(1)
+        assert dm.shape == (mnet.n_vars,)
+        # the derivative of the amounts is that of m Y / W
+        assert np.allclose(dm[1:] * gas.molecular_weights / m.mass, d[2:], rtol=1e-3, atol=1e-3 * np.max(np.abs(d[2:])))
+        assert dm[0] == pytest.approx(d[1], rel=1e-3)
+        moles[solver] = mnet.get_derivative(0)[1:]
+        assert np.allclose(moles[solver], m.get_state()[1:], rtol=1e-12, atol=1e-30)

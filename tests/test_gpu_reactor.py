@@ -249,3 +249,38 @@ def test_settings_of_a_network():
         c.max_steps = 0
     with pytest.raises(gb.GBError):
         c.max_time_step = -1.0
+
+
+def _rhs_close(d1, T, P, Y, sol, tol):
+    """The interpolated first derivative against the reactor right-hand side at the same
+    states: within tol of each reactor's largest rate (integration error, not a formula's)."""
+    dT, dY = sol.reactor_rhs(T, P, Y)
+    sT = np.maximum(np.abs(dT), 1.0)
+    assert np.all(np.abs(d1[0] - dT) <= tol * sT), np.max(np.abs(d1[0] - dT) / sT)
+    sY = np.maximum(np.max(np.abs(dY), axis=0), 1e-3)
+    assert np.all(np.max(np.abs(d1[1:] - dY), axis=0) <= tol * sY), np.max(np.max(np.abs(d1[1:] - dY), axis=0) / sY)
+
+
+def test_get_derivative_from_the_step_history():
+    """ReactorNet.get_derivative: k = 0 is the state gb_net_get_state returns; k = 1 is the
+    reactor right-hand side at that state to within the integration error, after an advance
+    (interpolated inside the last step) and after one internal step (at the step's end); the
+    order range and the not-yet-integrated state are refused."""
+    import cantera_gb300 as gb
+    sol = gpu_solution("h2o2")
+    T0, P, Y0 = h2o2_batch(64, seed=17)
+    net = gb.ReactorNet(sol, T0, P, Y0.T.copy(), rtol=1e-10, atol=1e-16)
+    with pytest.raises(gb.GBError, match="not been integrated"):
+        net.get_derivative(1)
+    assert net.advance(2e-4) == 0               # some of the reactors mid-ignition
+    T, Y = net.get_state()
+    d0 = net.get_derivative(0)
+    assert np.allclose(d0[0], T, rtol=1e-14, atol=0) and np.allclose(d0[1:], Y, rtol=1e-12, atol=1e-18)
+    _rhs_close(net.get_derivative(1), T, P, Y, sol, 1e-4)
+    assert np.all(np.isfinite(net.get_derivative(2)))
+    with pytest.raises(gb.GBError, match="0..5"):
+        net.get_derivative(6)
+    times = net.step()
+    T, Y = net.get_state()
+    assert np.all(times > 2e-4)
+    _rhs_close(net.get_derivative(1), T, P, Y, sol, 1e-4)
