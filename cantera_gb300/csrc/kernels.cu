@@ -363,73 +363,19 @@ __device__ __forceinline__ bool luLeft(MT* a, int N, int ld, int* piv, double* d
 }
 
 // Right-looking LU with partial pivoting and physical row interchanges (row k of P A stored
-// in row k): for the larger matrices, where the trailing updates' parallel work beats the
+// in row k), for the larger matrices, where the trailing updates' parallel work beats the
 // left-looking form's sequential chain of N^2 / 2 shuffles (n-dodecane, N = 101: 646 against
-// 514 reactors/s).  The integrator runs its panel form (luRightPanel4), which gives the same
-// factors; this one states the order of operations that form keeps.
-template <typename MT>
-__device__ __forceinline__ bool luRight(MT* a, int N, int ld, int* piv, double* dinv, int lane) {
-    bool nonsingular = true;
-    if (lane == 0)
-        for (int i = 0; i < N; i++) piv[i] = i;
-    __syncwarp();
-    for (int k = 0; k < N; k++) {
-        // pivot search on the integer pipe: for finite values |x| orders like the bits of
-        // x with the sign cleared (the caller has checked that M is finite)
-        unsigned long long bv = 0ULL;
-        int bi = N;
-        for (int i = k + lane; i < N; i += 32) {
-            const unsigned long long v = absKey(a[(size_t)i * ld + k]);
-            if (v > bv || bi == N) { bv = v; bi = i; }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-        }
-        if (bv == 0ULL) { nonsingular = false; break; }
-        if (bi != k) {
-            for (int j = lane; j < N; j += 32) {
-                MT t = a[(size_t)k * ld + j];
-                a[(size_t)k * ld + j] = a[(size_t)bi * ld + j];
-                a[(size_t)bi * ld + j] = t;
-            }
-            if (lane == 0) { int t = piv[k]; piv[k] = piv[bi]; piv[bi] = t; }
-        }
-        __syncwarp();
-        const MT inv = (MT)1 / a[(size_t)k * ld + k];
-        if (lane == 0) dinv[k] = (double)inv;
-        for (int i = k + 1 + lane; i < N; i += 32) a[(size_t)i * ld + k] *= inv;
-        __syncwarp();
-        // trailing update, eight rows at a time with all loads issued before the stores
-        for (int j = k + 1 + lane; j < N; j += 32) {
-            const MT u = a[(size_t)k * ld + j];
-            int i = k + 1;
-            for (; i + 8 <= N; i += 8) {
-                MT l[8], v[8];
-#pragma unroll
-                for (int r = 0; r < 8; r++) {
-                    l[r] = a[(size_t)(i + r) * ld + k];
-                    v[r] = a[(size_t)(i + r) * ld + j];
-                }
-#pragma unroll
-                for (int r = 0; r < 8; r++) a[(size_t)(i + r) * ld + j] = v[r] - l[r] * u;
-            }
-            for (; i < N; i++) a[(size_t)i * ld + j] -= a[(size_t)i * ld + k] * u;
-        }
-        __syncwarp();
-    }
-    return nonsingular;
-}
-
-// The right-looking LU above, blocked by panels of four columns: the panel's columns are
-// factored with the same pivot searches, full-row interchanges and scalings, and only then
-// are its four pivots applied to the rest of the matrix, each trailing entry loaded and stored
-// once per panel instead of once per pivot (a global store goes to L2).  Every entry receives
-// the same fused multiply-adds in the same pivot order as in luRight, with the same operands
-// (a row interchange inside the panel moves a row's multipliers with its not-yet-updated
-// trailing part), so the factors are bit for bit those of luRight.
+// 514 reactors/s), blocked by panels of four columns.  Step k of the unblocked form: the
+// pivot is the largest |a[i][k]|, i >= k (integer compare of the bits with the sign cleared;
+// the caller has checked that the matrix is finite; lowest row on ties); rows k and the
+// pivot's are interchanged in full; the multipliers a[i][k] *= 1 / a[k][k]; every trailing
+// entry a[i][j] (i, j > k) = fma(-a[i][k], a[k][j], a[i][j]).  Here a panel's four columns are
+// factored first (those steps restricted to the panel's columns), and only then are its four
+// pivots applied to the rest of the matrix, each trailing entry loaded and stored once per
+// panel instead of once per pivot (a global store goes to L2).  Every entry receives the same
+// fused multiply-adds in the same pivot order, with the same operands (a row interchange inside
+// the panel moves a row's multipliers with its not-yet-updated trailing part), so the factors
+// are bit for bit those of the unblocked form.
 template <typename MT>
 __device__ __forceinline__ bool luRightPanel4(MT* a, int N, int ld, int* piv, double* dinv, int lane) {
     constexpr int B = 4;

@@ -1,5 +1,5 @@
 // The integrator's dense LU beyond 64 components (kernels.cu) in two orders of the same
-// operations: unblocked right-looking (luRight) and in panels of four (luRightPanel4), with
+// operations: unblocked right-looking (luRight here) and in panels of four (luRightPanel4), with
 // explicit fused multiply-adds as the device code has them.  The two must give the same
 // factors, pivots and reciprocal diagonals bit for bit on random matrices (sizes 1-128,
 // sparse and dense, row interchanges, rank-deficient ones).  Exit status 0: identical.
