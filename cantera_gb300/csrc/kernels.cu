@@ -761,9 +761,9 @@ __device__ __noinline__ void devLuSolve(const MT* a, double* b, int N, int ld, c
 // whole rows (coalesced).
 // =============================================================================
 constexpr int kMaxl = kKrylovMaxl;     // Krylov vectors (CVODE's default)
-constexpr double kEplifac = 0.05;      // linear tolerance factor (CVODE's default)
-constexpr double kIlutTau = 1e-12;     // drop tolerance the adaptive preconditioner gives ILUT
-constexpr int kIlutFillFactor = 10;    // ILUT's fill factor (the library default it keeps)
+[[maybe_unused]] constexpr double kEplifac = 0.05;     // linear tolerance factor (CVODE's default)
+[[maybe_unused]] constexpr double kIlutTau = 1e-12;    // drop tolerance the adaptive preconditioner gives ILUT
+[[maybe_unused]] constexpr int kIlutFillFactor = 10;   // ILUT's fill factor (the library default it keeps)
 // GMRES scalars per warp: H[(kMaxl + 1)][kMaxl], cs[kMaxl], sn[kMaxl], g[kMaxl + 1], y[kMaxl],
 // rho (padded to an even count)
 constexpr int kGmresScalars = ((kMaxl + 1) * kMaxl + 2 * kMaxl + (kMaxl + 1) + kMaxl + 1 + 1) & ~1;
@@ -1012,7 +1012,7 @@ __device__ __noinline__ void devIlut(MT* a, int N, int ld, double* dinv, double*
 // diagonal from dinv).  The vector lives in registers (element i in lane i % 32, slot i / 32); every
 // substitution step broadcasts one element by a shuffle.  The factors are usually in L2 (one
 // matrix per resident warp), so the rows of the next kIluAhead steps are in flight meanwhile.
-constexpr int kIluAhead = 4;
+[[maybe_unused]] constexpr int kIluAhead = 4;
 template <typename MT, int S>
 __device__ __noinline__ void devIluSolve(const MT* a, double* b, int N, int ld, const double* dinv, const DevMech& m,
                                          int lane) {

@@ -311,7 +311,7 @@ private:
                 l.indent = indent + extra;
                 l.text = rest;
                 n.elems.push_back(parseMap(pos, l.indent));
-            } else if (isSeqLine(LLine{0, rest, 0})) {
+            } else if (isSeqLine(LLine{0, rest, 0, false, {}})) {
                 l.indent = indent + extra;
                 l.text = rest;
                 n.elems.push_back(parseSeq(pos, l.indent));
@@ -394,7 +394,7 @@ std::vector<LLine> logicalLines(const std::string& src) {
                 }
             }
         }
-        LLine L{ind, body, (int)i + 1};
+        LLine L{ind, body, (int)i + 1, false, {}};
         out.push_back(L);
         // block scalar indicator at the end of "key: |" or "- |"
         std::string value;
@@ -424,7 +424,7 @@ std::vector<LLine> logicalLines(const std::string& src) {
                 payload += content[c];
             }
             if (!strip && !payload.empty()) payload += "\n";
-            LLine B{ind + 1, payload, (int)j + 2};
+            LLine B{ind + 1, payload, (int)j + 2, false, {}};
             B.isBlockScalar = true;
             out.push_back(B);
             j = k - 1;
