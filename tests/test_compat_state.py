@@ -172,3 +172,43 @@ def test_network_integrator_settings_without_engine(gas):
     assert net.verbose is True
     with pytest.raises(ct.CanteraError, match="empty"):
         ct.ReactorNet().get_state()
+
+
+class StandInEngine:
+    """The part of cantera_gb300.ReactorNet the facade's get_derivative reads."""
+
+    def __init__(self, d, linear_solver):
+        self._d, self.linear_solver = d, linear_solver
+
+    def get_derivative(self, k):
+        return self._d * (k + 1)
+
+
+def test_get_derivative_layouts_without_engine(gas):
+    """The facade turns the engine's [T, Y] (dense) or [T, n per m^3 of initial volume] (GMRES)
+    derivatives into the reference's per-reactor layouts: [mass or 0, T, Y] for mass-fraction
+    reactors, [T, n] for mole reactors (n = m Y / W, or the engine's amounts times the volume
+    at initialisation)."""
+    import cantera_gb300.compat as ct
+    gas.TPX = 1200.0, 1e5, "H2:2, O2:1, N2:4"
+    a = ct.IdealGasConstPressureReactor(gas, volume=2.0)
+    m = ct.IdealGasConstPressureMoleReactor(gas, volume=3.0)
+    net = ct.ReactorNet([a, m])
+    with pytest.raises(ct.CanteraError, match="not been integrated"):
+        net.get_derivative(1)
+    for r in (a, m):
+        r._initialize()
+    K = gas.n_species
+    d = np.arange(2.0 * (K + 1)).reshape(K + 1, 2) + 1.0      # [K + 1, 2 reactors]
+    net._engine = StandInEngine(d, "DENSE")
+    y1 = net.get_derivative(1)                                 # the stand-in doubles d for k = 1
+    assert y1.shape == (net.n_vars,)
+    assert y1[0] == 0.0 and y1[1] == 2 * d[0, 0] and np.array_equal(y1[2:2 + K], 2 * d[1:, 0])
+    mo = 2 + K
+    assert y1[mo] == 2 * d[0, 1]
+    assert np.allclose(y1[mo + 1:], m.mass * 2 * d[1:, 1] / gas.molecular_weights, rtol=1e-15)
+    y0 = net.get_derivative(0)
+    assert y0[0] == a.mass                                     # k = 0: the state, mass included
+    net._engine = StandInEngine(d, "GMRES")
+    y1 = net.get_derivative(1)
+    assert np.allclose(y1[mo + 1:], 3.0 * 2 * d[1:, 1], rtol=1e-15)   # amounts of 1 m^3 x 3 m^3
