@@ -120,6 +120,8 @@ def library():
         "gb_get_error": (I32, [I32, ctypes.c_char_p]),
         "gb_mech_structure": (I32, [I32, I32, P]),
         "gb_mech_equivalence_ratio": (I32, [I32, D, P, P, I32, P]),
+        "gb_mech_species_thermo": (I32, [I32, I32, P, P, P, P]),
+        "gb_mech_reference_pressure": (D, [I32]),
         "gb_measure_fp64": (I32, [P]),
         "gb_check_exp": (I32, [I32, P, P, P]),
         "gb_check_log": (I32, [I32, P, P, P]),
@@ -231,6 +233,24 @@ class Solution:
     def mole_to_mass(self, X):
         y = np.asarray(X, dtype=np.float64) * self.molecular_weights
         return y / y.sum()
+
+    def species_thermo(self, T):
+        """cp/R, h/RT and s/R of every species at temperature(s) T (NASA7, host-evaluated):
+        arrays [K] for a scalar T, [K, n] for n temperatures."""
+        scalar = np.ndim(T) == 0
+        Ta = np.ascontiguousarray(np.atleast_1d(np.asarray(T, dtype=np.float64)))
+        out = [np.empty((self.n_species, Ta.size)) for _ in range(3)]
+        _check(library().gb_mech_species_thermo(self._h, Ta.size, _ptr(Ta), _ptr(out[0]), _ptr(out[1]),
+                                                _ptr(out[2])))
+        return tuple(o[:, 0].copy() for o in out) if scalar else tuple(out)
+
+    @property
+    def reference_pressure(self):
+        """Reference pressure of the species' thermodynamic data, Pa."""
+        v = library().gb_mech_reference_pressure(self._h)
+        if v == -999.999:
+            _check(GB_ERR)
+        return v
 
     def equivalence_ratio_mass_fractions(self, phi, fuel, oxidizer):
         """Mass fractions of the fuel/oxidizer mixture with equivalence ratio phi

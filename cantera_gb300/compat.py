@@ -17,7 +17,10 @@
 The names and semantics follow the reference's Python interface:
 ``Solution`` / ``ThermoPhase`` state setters and getters (interfaces/cython/cantera/
 thermo.py: ``TP``, ``TPX``, ``TPY``, ``X``, ``Y``, ``set_equivalence_ratio``,
-``density``, ``mean_molecular_weight``, ``concentrations``), ``Kinetics``
+``density``, ``mean_molecular_weight``, ``concentrations``; the ideal-gas properties
+``cp``/``cv``/``h``/``u``/``s``/``g`` on mass and mole bases, ``partial_molar_*``,
+``chemical_potentials`` and the ``standard_*`` reference-state arrays, from the species' NASA7
+data), ``Kinetics``
 (interfaces/cython/cantera/kinetics.py:456-461,928-940: ``net_production_rates``,
 ``net_production_rates_ddCi`` as a scipy CSC matrix), ``IdealGasConstPressureReactor``,
 ``IdealGasConstPressureMoleReactor``, ``AdaptivePreconditioner`` (interfaces/cython/cantera/
@@ -27,14 +30,14 @@ jacobians.py:120-200) and ``ReactorNet`` (interfaces/cython/cantera/reactor.py:1
 ``preconditioner``, ``linear_solver_type``, ``initialize``, ``verbose``, ``n_vars``,
 ``get_state``, ``get_derivative``, ``component_name``, ``global_component_index``; the
 integrator limits ``max_err_test_fails``, ``max_nonlinear_iterations``,
-``max_nonlinear_convergence_failures``
-at CVODE's defaults).  One ``ReactorNet`` over many reactors is one batched GPU network:
+``max_nonlinear_convergence_failures`` at CVODE's defaults).  One ``ReactorNet`` over many reactors is one batched GPU network:
 every reactor is independent (no walls or inlets), shares the network's mechanism and
 tolerances, and reaches each ``advance`` time together.  A network of mole reactors with an
 ``AdaptivePreconditioner`` runs the engine's GMRES path (the mole-reactor state, the
 preconditioner's ILUT, J v products); without one it runs the dense path.  What the batched
 engine does not do raises: reactors of different mechanisms in one network, preconditioner
-settings other than the reference's defaults, thermodynamic properties beyond the state.
+settings other than the reference's defaults; transport properties and other phase models
+are not there.
 """
 import numpy as np
 
@@ -201,6 +204,105 @@ class Solution:
     @property
     def concentrations(self):
         return self.density * self._Y / self._m.molecular_weights
+
+    # ---- ideal-gas properties of this state (src/thermo/IdealGasPhase.cpp:25-96,
+    # include/cantera/thermo/IdealGasPhase.h:294-296; the NASA7 species data evaluated on the host)
+    def _ref(self):
+        return self._m.species_thermo(self._T)
+
+    @property
+    def standard_cp_R(self):
+        return self._ref()[0]
+
+    @property
+    def standard_enthalpies_RT(self):
+        return self._ref()[1]
+
+    @property
+    def standard_entropies_R(self):
+        return self._ref()[2]
+
+    @property
+    def standard_gibbs_RT(self):
+        _, h, s = self._ref()
+        return h - s
+
+    @property
+    def standard_int_energies_RT(self):
+        return self._ref()[1] - 1.0
+
+    def _ym(self):
+        return self._Y / self._m.molecular_weights
+
+    def _log_x(self):
+        """ln max(X_k, 1e-300) (the reference's SmallNumber floor)."""
+        return np.log(np.maximum(self._ym() * self.mean_molecular_weight, 1e-300))
+
+    @property
+    def partial_molar_enthalpies(self):
+        return self._ref()[1] * gas_constant * self._T
+
+    @property
+    def partial_molar_int_energies(self):
+        return (self._ref()[1] - 1.0) * gas_constant * self._T
+
+    @property
+    def partial_molar_cp(self):
+        return self._ref()[0] * gas_constant
+
+    @property
+    def partial_molar_entropies(self):
+        logp = np.log(self._P / self._m.reference_pressure)
+        return gas_constant * (self._ref()[2] - logp - self._log_x())
+
+    @property
+    def standard_chemical_potentials(self):
+        _, h, s = self._ref()
+        RT = gas_constant * self._T
+        return (h - s) * RT + RT * np.log(self._P / self._m.reference_pressure)
+
+    @property
+    def chemical_potentials(self):
+        return self.standard_chemical_potentials + gas_constant * self._T * self._log_x()
+
+    def _mean_x(self, v):
+        return self.mean_molecular_weight * np.sum(self._ym() * v)
+
+    @property
+    def cp_mole(self):
+        return gas_constant * self._mean_x(self._ref()[0])
+
+    @property
+    def cv_mole(self):
+        return self.cp_mole - gas_constant
+
+    @property
+    def enthalpy_mole(self):
+        return gas_constant * self._T * self._mean_x(self._ref()[1])
+
+    @property
+    def int_energy_mole(self):
+        return gas_constant * self._T * (self._mean_x(self._ref()[1]) - 1.0)
+
+    @property
+    def entropy_mole(self):
+        ym, mmw = self._ym(), self.mean_molecular_weight
+        sum_xlogx = mmw * np.sum(ym * np.log(np.maximum(ym, 1e-300))) + np.log(mmw)
+        return gas_constant * (self._mean_x(self._ref()[2]) - sum_xlogx
+                               - np.log(self._P / self._m.reference_pressure))
+
+    @property
+    def gibbs_mole(self):
+        return self.enthalpy_mole - self._T * self.entropy_mole
+
+    cp_mass = property(lambda self: self.cp_mole / self.mean_molecular_weight)
+    cv_mass = property(lambda self: self.cv_mole / self.mean_molecular_weight)
+    enthalpy_mass = property(lambda self: self.enthalpy_mole / self.mean_molecular_weight)
+    int_energy_mass = property(lambda self: self.int_energy_mole / self.mean_molecular_weight)
+    entropy_mass = property(lambda self: self.entropy_mole / self.mean_molecular_weight)
+    gibbs_mass = property(lambda self: self.gibbs_mole / self.mean_molecular_weight)
+    # the reference's default basis is mass
+    cp, cv, h, u, s, g = cp_mass, cv_mass, enthalpy_mass, int_energy_mass, entropy_mass, gibbs_mass
 
     # ---- kinetics (one state through the batched GPU kernels) ----
     def _one(self):

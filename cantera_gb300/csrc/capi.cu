@@ -802,6 +802,38 @@ int32_t gb_mech_equivalence_ratio(int32_t h, double phi, const double* fuelX, co
     });
 }
 
+int32_t gb_mech_species_thermo(int32_t h, int32_t n, const double* T, double* cp_R, double* h_RT, double* s_R) {
+    return guarded([&]() -> int32_t {
+        MechEntry& e = mech(h);
+        const Mechanism& m = e.m;
+        if (n < 0) throw std::runtime_error("negative number of temperatures");
+        if (!T || !cp_R || !h_RT || !s_R) throw std::runtime_error("null array argument");
+        for (int s = 0; s < n; s++) {
+            const double t = T[s];
+            if (!(t > 0.0)) throw std::runtime_error("temperature must be positive");
+            const double lt = std::log(t), rt = 1.0 / t;
+            for (int k = 0; k < m.K; k++) {
+                // NASA7: the low range up to and including the midpoint temperature
+                const double* a = (t <= m.nasaTmid[k] ? m.nasaLow.data() : m.nasaHigh.data()) + 7 * (size_t)k;
+                const size_t o = (size_t)k * n + s;
+                cp_R[o] = a[0] + t * (a[1] + t * (a[2] + t * (a[3] + t * a[4])));
+                h_RT[o] = a[0] + t * (a[1] / 2 + t * (a[2] / 3 + t * (a[3] / 4 + t * a[4] / 5))) + a[5] * rt;
+                s_R[o] = a[0] * lt + t * (a[1] + t * (a[2] / 2 + t * (a[3] / 3 + t * a[4] / 4))) + a[6];
+            }
+        }
+        return 0;
+    });
+}
+
+double gb_mech_reference_pressure(int32_t h) {
+    try {
+        return mech(h).m.Pref;
+    } catch (std::exception& ex) {
+        g_error = ex.what();
+        return -999.999;
+    }
+}
+
 int32_t gb_kin_net_production_rates(int32_t h, int32_t n, const double* T, const double* P, const double* Y,
                                     int32_t bufLen, double* wdot, int32_t flags) {
     return guarded([&]() -> int32_t {

@@ -51,6 +51,17 @@ int32_t gb_mech_molecular_weights(int32_t mech, int32_t buflen, double* mw);
  * src/thermo/ThermoPhase.cpp:879-910). */
 int32_t gb_mech_equivalence_ratio(int32_t mech, double phi, const double* fuelX, const double* oxX,
                                   int32_t buflen, double* Y);
+/* Reference-state species properties at n temperatures, host arrays [K][n] (species-major):
+ * cp/R, h/RT and s/R of the NASA7 polynomials, the low range up to and including the midpoint
+ * temperature (NasaPoly1::updateProperties, include/cantera/thermo/NasaPoly1.h:83-122;
+ * NasaPoly2::updateProperties, NasaPoly2.h:105-112; MultiSpeciesThermo::update,
+ * src/thermo/MultiSpeciesThermo.cpp:94-107).  Evaluated on the host, for single states and
+ * setup (the kernels evaluate their own); every temperature must be positive. */
+int32_t gb_mech_species_thermo(int32_t mech, int32_t n, const double* T, double* cp_R, double* h_RT,
+                               double* s_R);
+/* The reference pressure of the species' thermodynamic data in Pa (ThermoPhase::refPressure),
+ * or -999.999 with an invalid handle. */
+double gb_mech_reference_pressure(int32_t mech);
 
 /* ---- kinetics ----------------------------------------------------------------------
  * Batched Kinetics::getNetProductionRates (src/kinetics/Kinetics.cpp:447-457; CLib

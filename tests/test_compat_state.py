@@ -212,3 +212,51 @@ def test_get_derivative_layouts_without_engine(gas):
     net._engine = StandInEngine(d, "GMRES")
     y1 = net.get_derivative(1)
     assert np.allclose(y1[mo + 1:], 3.0 * 2 * d[1:, 1], rtol=1e-15)   # amounts of 1 m^3 x 3 m^3
+
+
+class OracleThermoMech(StandInMech):
+    """A stand-in whose species data come from the oracle's NASA7 evaluation (h2o2)."""
+
+    def __init__(self):
+        from conftest import oracle_mech
+        self._o = oracle_mech("h2o2")
+        self.n_species = self._o.K
+        self.species_names = ["s%d" % k for k in range(self._o.K)]
+        self.molecular_weights = self._o.mw.copy()
+        self.reference_pressure = 101325.0
+
+    def species_thermo(self, T):
+        return self._o.thermo(T)
+
+
+def test_ideal_gas_properties_identities():
+    """The facade's ideal-gas properties satisfy the thermodynamic identities: cp = dh/dT and
+    s = -dg/dT at constant P and composition (central differences), g = sum X_k mu_k,
+    h = sum X_k hbar_k, u = h - RT, cp - cv = R; a species at zero mole fraction enters the
+    entropy and chemical potentials through the 1e-300 floor, as in the reference."""
+    from cantera_gb300.compat import Solution, gas_constant
+    gas = Solution(None, _mech=OracleThermoMech())
+    rng = np.random.default_rng(3)
+    for T in (600.0, 999.9, 1000.1, 1700.0, 2500.0):        # both NASA7 ranges
+        Y = rng.dirichlet(np.ones(gas.n_species))
+        Y[2] = 0.0
+        gas.TPY = T, 3e5, Y
+        X = gas.X
+        d = 1e-3
+        def at(t, prop):
+            gas.TP = t, None
+            v = getattr(gas, prop)
+            gas.TP = T, None
+            return v
+        cp_fd = (at(T + d, "enthalpy_mass") - at(T - d, "enthalpy_mass")) / (2 * d)
+        assert gas.cp_mass == pytest.approx(cp_fd, rel=1e-7)
+        s_fd = -(at(T + d, "gibbs_mole") - at(T - d, "gibbs_mole")) / (2 * d)
+        assert gas.entropy_mole == pytest.approx(s_fd, rel=1e-6)
+        assert gas.gibbs_mole == pytest.approx(np.sum(X * gas.chemical_potentials), rel=1e-10, abs=1e-3)
+        assert gas.enthalpy_mole == pytest.approx(np.sum(X * gas.partial_molar_enthalpies), rel=1e-12)
+        assert gas.int_energy_mole == pytest.approx(gas.enthalpy_mole - gas_constant * T, rel=1e-12)
+        assert gas.cp_mole - gas.cv_mole == pytest.approx(gas_constant, rel=1e-12)
+        assert gas.cp == gas.cp_mass and gas.s == gas.entropy_mass
+        mu0 = gas.standard_chemical_potentials
+        assert gas.chemical_potentials[2] == pytest.approx(mu0[2] + gas_constant * T * np.log(1e-300), rel=1e-12)
+        assert np.all(np.isfinite(gas.partial_molar_entropies))

@@ -3,7 +3,7 @@ kinetics and reactor networks built from reactor objects, against the oracle."""
 import numpy as np
 import pytest
 
-from conftest import oracle_mech
+from conftest import gpu_solution, oracle_mech
 
 pytestmark = pytest.mark.gpu
 
@@ -202,3 +202,33 @@ def test_network_get_derivative(ct):
         assert dm[0] == pytest.approx(d[1], rel=1e-3)
         moles[solver] = mnet.get_derivative(0)[1:]
         assert np.allclose(moles[solver], m.get_state()[1:], rtol=1e-12, atol=1e-30)
+
+
+def test_species_thermo_and_ideal_gas_properties(ct):
+    """The host NASA7 evaluation behind the facade's properties against the oracle's
+    (every species of gri30 and n-dodecane, both ranges and the midpoint itself), the reference
+    pressure, and the facade's mixture properties from them."""
+    import cantera_gb300 as gb
+    for name in ("gri30", "nDodecane"):
+        sol = gpu_solution(name)
+        m = oracle_mech(name)
+        T = np.array([300.0, 999.999, 1000.0, 1000.001, 1500.0, 2999.0])
+        cp, h, s = sol.species_thermo(T)
+        for j, t in enumerate(T):
+            co, ho, so = m.thermo(t)
+            assert np.allclose(cp[:, j], co, rtol=1e-13, atol=1e-13)
+            assert np.allclose(h[:, j], ho, rtol=1e-13, atol=1e-13)
+            assert np.allclose(s[:, j], so, rtol=1e-13, atol=1e-13)
+        assert sol.reference_pressure == 101325.0
+        with pytest.raises(gb.GBError):
+            sol.species_thermo(-1.0)
+    gas = ct.Solution("gri30.yaml", "gri30")
+    gas.TPX = 1400.0, 2 * ct.one_atm, "CH4:1, O2:2, N2:7.52"
+    co, ho, so = oracle_mech("gri30").thermo(1400.0)
+    X = gas.X
+    assert gas.cp_mole == pytest.approx(ct.gas_constant * np.sum(X * co), rel=1e-12)
+    assert gas.enthalpy_mass == pytest.approx(ct.gas_constant * 1400.0 * np.sum(X * ho) / gas.mean_molecular_weight,
+                                              rel=1e-12)
+    nz = X > 0
+    s_ref = ct.gas_constant * (np.sum(X * so) - np.sum(X[nz] * np.log(X[nz])) - np.log(2.0))
+    assert gas.entropy_mole == pytest.approx(s_ref, rel=1e-12)
