@@ -378,10 +378,14 @@ class IdealGasConstPressureReactor:
         self._mass = self._thermo.density * self._v_init
 
     def insert(self, gas):
-        """Replace the contents (and state) of the reactor; its volume is kept."""
+        """Replace the contents (and state) of the reactor; its volume is kept, and a network
+        holding it restarts from its reactors' states at the next advance (as the reference's
+        ReactorBase::setSolution asks its network to reinitialise)."""
         self._volume = self.volume
         self._mass = None
         self._thermo = gas._copy()
+        if self._net is not None:
+            self._net._engine = None
 
     @property
     def n_vars(self):

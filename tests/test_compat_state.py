@@ -260,3 +260,17 @@ def test_ideal_gas_properties_identities():
         mu0 = gas.standard_chemical_potentials
         assert gas.chemical_potentials[2] == pytest.approx(mu0[2] + gas_constant * T * np.log(1e-300), rel=1e-12)
         assert np.all(np.isfinite(gas.partial_molar_entropies))
+
+
+def test_insert_restarts_the_network(gas):
+    """New contents in a reactor of a running network make it restart from the reactors'
+    states at the next advance, keeping its time."""
+    import cantera_gb300.compat as ct
+    gas.TPX = 1200.0, 1e5, "H2:2, O2:1, N2:4"
+    r = ct.IdealGasConstPressureReactor(gas)
+    net = ct.ReactorNet([r])
+    net._engine = StandInEngine(np.zeros((gas.n_species + 1, 1)), "DENSE")
+    net._t = 1e-3
+    gas.TPX = 900.0, 1e5, "N2:1"
+    r.insert(gas)
+    assert net._engine is None and net.time == 1e-3 and r.T == 900.0
